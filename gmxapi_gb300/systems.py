@@ -1,0 +1,257 @@
+"""Seeded synthetic systems for the short-range nonbonded path.
+
+These stand in for the reference's own benchmark input (the 3000-atom SPC/E
+box of ``src/gromacs/nbnxm/benchmark/bench_coords.h`` used by
+``gmx nonbonded-benchmark``): SPC water at the same number density
+(~100 atoms/nm^3), built from a jittered lattice with random orientations,
+plus a random multi-type LJ + Coulomb liquid for force matching.
+
+Everything uses ``numpy.random.default_rng`` (PCG64), which gives the same
+stream on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+#: SPC water (rigid): LJ on oxygen only, q_O = -0.82, q_H = +0.41.
+SPC_SIGMA = 0.3166
+SPC_EPSILON = 0.650
+SPC_Q_O = -0.82
+SPC_Q_H = 0.41
+OH_LENGTH = 0.1
+HOH_ANGLE_DEG = 109.47
+
+
+@dataclasses.dataclass
+class System:
+    """One periodic rectangular system in nblib terms.
+
+    ``nbfp`` holds ``ntypes*ntypes`` pairs ``{6*C6, 12*C12}`` like
+    nblib's non-bonded parameter array (api/nblib/gmxsetup.cpp:143-166);
+    exclusions are a CSR list per atom that includes the atom itself
+    (gmx::ListOfLists as built by nblib's Topology).
+    """
+
+    x: np.ndarray  # (N, 3) float32
+    box: np.ndarray  # (3,) float32
+    q: np.ndarray  # (N,) float32
+    type: np.ndarray  # (N,) int32
+    ntypes: int
+    nbfp: np.ndarray  # (ntypes*ntypes*2,) float32
+    excl_index: np.ndarray  # (N+1,) int32
+    excl_list: np.ndarray  # (nnz,) int32
+    name: str = ""
+    # per-type LJ parameters when the system was built from sigma/epsilon
+    sigma: np.ndarray | None = None
+    epsilon: np.ndarray | None = None
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+
+def lj_c6_c12(sigma: float, epsilon: float) -> tuple[float, float]:
+    s6 = sigma**6
+    return 4.0 * epsilon * s6, 4.0 * epsilon * s6 * s6
+
+
+def nbfp_from_c6c12(c6: np.ndarray, c12: np.ndarray) -> np.ndarray:
+    """(nt, nt) C6/C12 matrices -> nblib's flat {6*C6, 12*C12} array."""
+    nt = c6.shape[0]
+    out = np.empty((nt, nt, 2), dtype=np.float64)
+    out[..., 0] = 6.0 * c6
+    out[..., 1] = 12.0 * c12
+    return out.reshape(-1).astype(np.float32)
+
+
+def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform random rotation matrices (Shoemake's unit-quaternion method)."""
+    u1, u2, u3 = rng.random((3, n))
+    a = np.sqrt(1.0 - u1)
+    b = np.sqrt(u1)
+    qx = a * np.sin(2 * np.pi * u2)
+    qy = a * np.cos(2 * np.pi * u2)
+    qz = b * np.sin(2 * np.pi * u3)
+    qw = b * np.cos(2 * np.pi * u3)
+    r = np.empty((n, 3, 3))
+    r[:, 0, 0] = 1 - 2 * (qy * qy + qz * qz)
+    r[:, 0, 1] = 2 * (qx * qy - qz * qw)
+    r[:, 0, 2] = 2 * (qx * qz + qy * qw)
+    r[:, 1, 0] = 2 * (qx * qy + qz * qw)
+    r[:, 1, 1] = 1 - 2 * (qx * qx + qz * qz)
+    r[:, 1, 2] = 2 * (qy * qz - qx * qw)
+    r[:, 2, 0] = 2 * (qx * qz - qy * qw)
+    r[:, 2, 1] = 2 * (qy * qz + qx * qw)
+    r[:, 2, 2] = 1 - 2 * (qx * qx + qy * qy)
+    return r
+
+
+def spc_water(n_molecules: int, box_edge: float, seed: int, jitter: float = 0.03) -> System:
+    """SPC water box: oxygens on a jittered cubic lattice, random orientations.
+
+    The lattice has m^3 >= n_molecules sites of spacing box_edge/m; when
+    m^3 > n_molecules a seeded subset of sites is used.  Each oxygen gets a
+    uniform jitter in [-jitter, jitter] per coordinate.
+    """
+    rng = np.random.default_rng(seed)
+    m = int(math.ceil(n_molecules ** (1.0 / 3.0) - 1e-9))
+    while m**3 < n_molecules:
+        m += 1
+    spacing = box_edge / m
+    g = np.arange(m, dtype=np.float64)
+    sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
+    if sites.shape[0] > n_molecules:
+        pick = np.sort(rng.choice(sites.shape[0], size=n_molecules, replace=False))
+        sites = sites[pick]
+    o = (sites + 0.5) * spacing + rng.uniform(-jitter, jitter, size=(n_molecules, 3))
+    half = math.radians(HOH_ANGLE_DEG) / 2.0
+    body = np.array(
+        [
+            [OH_LENGTH * math.sin(half), 0.0, OH_LENGTH * math.cos(half)],
+            [-OH_LENGTH * math.sin(half), 0.0, OH_LENGTH * math.cos(half)],
+        ]
+    )
+    rot = _random_rotations(rng, n_molecules)
+    h = o[:, None, :] + np.einsum("nij,kj->nki", rot, body)
+    x = np.empty((n_molecules, 3, 3))
+    x[:, 0] = o
+    x[:, 1:] = h
+    x = x.reshape(-1, 3)
+    n = 3 * n_molecules
+    q = np.tile(np.array([SPC_Q_O, SPC_Q_H, SPC_Q_H], dtype=np.float32), n_molecules)
+    types = np.tile(np.array([0, 1, 1], dtype=np.int32), n_molecules)
+    c6o, c12o = lj_c6_c12(SPC_SIGMA, SPC_EPSILON)
+    c6 = np.array([[c6o, 0.0], [0.0, 0.0]])
+    c12 = np.array([[c12o, 0.0], [0.0, 0.0]])
+    # every atom excludes its own molecule (itself included)
+    excl_index = np.arange(0, 3 * n + 1, 3, dtype=np.int32)
+    mol = np.arange(n) // 3
+    excl_list = (3 * mol[:, None] + np.arange(3)[None, :]).reshape(-1).astype(np.int32)
+    return System(
+        x=x.astype(np.float32),
+        box=np.full(3, box_edge, dtype=np.float32),
+        q=q,
+        type=types,
+        ntypes=2,
+        nbfp=nbfp_from_c6c12(c6, c12),
+        excl_index=excl_index,
+        excl_list=excl_list,
+        name=f"spc{n_molecules}",
+    )
+
+
+def water_small(seed: int = 1) -> System:
+    """1,000 SPC waters (3,000 atoms) in a 3.104 nm cubic box."""
+    return spc_water(1000, 3.104, seed)
+
+
+def water_large(seed: int = 2) -> System:
+    """96,000 SPC waters (288,000 atoms) in a 14.21 nm cubic box."""
+    return spc_water(96000, 14.21, seed)
+
+
+def uneven_ensemble(
+    num_systems: int = 256, seed: int = 3, n_min: int = 500, n_max: int = 20000
+) -> list[System]:
+    """Independent SPC water boxes with atom counts log-uniform in [n_min, n_max].
+
+    N_i = 3*round(exp(U(ln n_min, ln n_max))/3); edge = (N_i/3 * 0.0299)^(1/3).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(num_systems):
+        n = 3 * int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max))) / 3.0))
+        nmol = n // 3
+        edge = (nmol * 0.0299) ** (1.0 / 3.0)
+        sysx = spc_water(nmol, edge, seed * 100003 + s)
+        sysx.name = f"ens{s}_n{n}"
+        out.append(sysx)
+    return out
+
+
+def perturb(x: np.ndarray, rng: np.random.Generator, sigma: float = 0.002) -> np.ndarray:
+    """Gaussian displacement of every coordinate (the per-step drift of the MD-like run)."""
+    return (x + rng.normal(0.0, sigma, size=x.shape)).astype(np.float32)
+
+
+def lj_liquid(
+    n: int = 24000,
+    ntypes: int = 8,
+    density: float = 100.0,
+    seed: int = 4,
+    min_dist_fraction: float = 0.5,
+    q_sigma: float = 0.4,
+    sigma_range: tuple[float, float] = (0.25, 0.40),
+    epsilon_range: tuple[float, float] = (0.1, 1.0),
+) -> System:
+    """Random multi-type LJ + Coulomb liquid with Lorentz-Berthelot mixing.
+
+    Types are drawn uniformly per atom; sigma_t ~ U(sigma_range),
+    epsilon_t ~ U(epsilon_range); charges ~ N(0, q_sigma) shifted to a zero
+    total.  Positions are uniform in a cubic box at ``density`` with pairs
+    closer than ``min_dist_fraction * sigma_ij`` rejected and redrawn
+    (random sequential addition on a cell grid).  At 100 atoms/nm^3 a
+    fraction of 0.8 packs beyond random close packing, so it cannot finish;
+    0.5 is the default (packing fraction ~0.22).
+    """
+    rng = np.random.default_rng(seed)
+    edge = (n / density) ** (1.0 / 3.0)
+    sig_t = rng.uniform(*sigma_range, size=ntypes)
+    eps_t = rng.uniform(*epsilon_range, size=ntypes)
+    types = rng.integers(0, ntypes, size=n).astype(np.int32)
+    q = rng.normal(0.0, q_sigma, size=n)
+    q = (q - q.mean()).astype(np.float32)
+    sig_ij = 0.5 * (sig_t[:, None] + sig_t[None, :])
+    eps_ij = np.sqrt(eps_t[:, None] * eps_t[None, :])
+    dmin = min_dist_fraction * sig_ij
+    cell = float(dmin.max())
+    nc = max(1, int(edge / cell))
+    cs = edge / nc
+    cells: dict[tuple[int, int, int], list[int]] = {}
+    x = np.empty((n, 3))
+    for i in range(n):
+        ti = types[i]
+        for _attempt in range(100000):
+            p = rng.uniform(0.0, edge, size=3)
+            c = tuple((p / cs).astype(int) % nc)
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        key = ((c[0] + dx) % nc, (c[1] + dy) % nc, (c[2] + dz) % nc)
+                        for j in cells.get(key, ()):
+                            d = p - x[j]
+                            d -= edge * np.round(d / edge)
+                            if d @ d < dmin[ti, types[j]] ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                x[i] = p
+                cells.setdefault(c, []).append(i)
+                break
+        else:
+            raise RuntimeError("random sequential addition did not converge")
+    c6 = 4.0 * eps_ij * sig_ij**6
+    c12 = 4.0 * eps_ij * sig_ij**12
+    return System(
+        x=x.astype(np.float32),
+        box=np.full(3, edge, dtype=np.float32),
+        q=q,
+        type=types,
+        ntypes=ntypes,
+        nbfp=nbfp_from_c6c12(c6, c12),
+        excl_index=np.arange(n + 1, dtype=np.int32),
+        excl_list=np.arange(n, dtype=np.int32),
+        name=f"lj{n}",
+        sigma=sig_t.astype(np.float64),
+        epsilon=eps_t.astype(np.float64),
+    )

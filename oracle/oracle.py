@@ -1,0 +1,258 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` as the checker of the CUDA path; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libnbnxm_oracle.so")
+_lib = None
+
+COULOMB_EWALD = 0
+COULOMB_CUTOFF = 1
+COULOMB_RF = 2
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+            os.path.join(_HERE, "nbnxm_oracle.c")
+        ):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        vp = C.c_void_p
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int)
+        dp = C.POINTER(C.c_double)
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.c_int, fp, fp, fp, ip, C.c_int, fp, ip, ip, C.c_int,
+                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+        for name in ("orc_destroy", "orc_grid", "orc_search"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = None
+        L.orc_set_coordinates.argtypes = [vp, fp]
+        L.orc_set_x.argtypes = [vp, fp]
+        L.orc_prune.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.orc_force.argtypes = [vp, C.c_int]
+        L.orc_forces_original_order.argtypes = [vp, fp]
+        L.orc_virial.argtypes = [vp, fp, fp, dp]
+        L.orc_energies.argtypes = [vp, dp]
+        L.orc_fshift.argtypes = [vp, fp]
+        for name in ("orc_beta", "orc_table_scale", "orc_epsfac", "orc_rbb2"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = C.c_float
+        L.orc_table_size.argtypes = [vp]
+        L.orc_table_size.restype = C.c_int
+        L.orc_table.argtypes = [vp, fp, fp]
+        L.orc_grid_dims.argtypes = [vp, ip, fp]
+        L.orc_list_sizes.argtypes = [vp, ip]
+        for name in ("orc_cxy_ind", "orc_num_clusters", "orc_atom_indices", "orc_cells",
+                     "orc_types_grid", "orc_sci", "orc_cj4"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = ip
+        for name in ("orc_xq", "orc_bb", "orc_bbcz", "orc_fnb"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = fp
+        for name in ("orc_excl", "orc_imask_outer"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = C.POINTER(C.c_uint32)
+        L.orc_fp64_allpairs.argtypes = [C.c_int, fp, fp, fp, ip, C.c_int, fp, ip, ip, C.c_int,
+                                        C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, ip, C.c_int, dp, dp]
+        L.orc_one_4pi_eps0.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _f(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _copy(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).copy().astype(dtype, copy=False)
+
+
+class Oracle:
+    """One system in the oracle: grid, GPU-layout list, prune, force kernel."""
+
+    def __init__(self, system, coulomb=COULOMB_EWALD, rc=0.9, rlist=1.0, rlist_inner=None,
+                 ewald_rtol=1e-5, epsilon_rf=1.0, use_ewald_shift=False):
+        L = lib()
+        self.system = system
+        self._keep = []
+        x, xp = _f(system.x)
+        box, bp = _f(system.box)
+        q, qp = _f(system.q)
+        t, tp = _i(system.type)
+        nb, nbp = _f(system.nbfp)
+        ei, eip = _i(system.excl_index)
+        el, elp = _i(system.excl_list if len(system.excl_list) else np.zeros(1, np.int32))
+        self._keep += [x, box, q, t, nb, ei, el]
+        self.coulomb = coulomb
+        self.rc = rc
+        self.rlist = rlist
+        self.rlist_inner = rlist if rlist_inner is None else rlist_inner
+        self.use_ewald_shift = use_ewald_shift
+        self.c = L.orc_create(system.n, xp, bp, qp, tp, system.ntypes, nbp, eip, elp, coulomb,
+                              rc, rlist, self.rlist_inner, ewald_rtol, epsilon_rf,
+                              int(use_ewald_shift))
+
+    def __del__(self):
+        if getattr(self, "c", None):
+            lib().orc_destroy(self.c)
+            self.c = None
+
+    # -- pipeline --
+    def grid(self):
+        lib().orc_grid(self.c)
+
+    def search(self):
+        lib().orc_search(self.c)
+
+    def set_coordinates(self, x):
+        a, p = _f(x)
+        lib().orc_set_coordinates(self.c, p)
+
+    def set_x(self, x):
+        a, p = _f(x)
+        lib().orc_set_x(self.c, p)
+
+    def prune(self, fresh, part=0, nparts=1):
+        lib().orc_prune(self.c, int(fresh), part, nparts)
+
+    def force(self, energy=True):
+        lib().orc_force(self.c, int(energy))
+
+    def forces(self):
+        f = np.empty((self.system.n, 3), dtype=np.float32)
+        lib().orc_forces_original_order(self.c, f.ctypes.data_as(C.POINTER(C.c_float)))
+        return f
+
+    def energies(self):
+        e = np.zeros(2, dtype=np.float64)
+        lib().orc_energies(self.c, e.ctypes.data_as(C.POINTER(C.c_double)))
+        return e  # (Vlj, Vcoul)
+
+    def virial(self, x_inbox, f):
+        xa, xp = _f(x_inbox)
+        fa, fp_ = _f(f)
+        v = np.zeros(9, dtype=np.float64)
+        lib().orc_virial(self.c, xp, fp_, v.ctypes.data_as(C.POINTER(C.c_double)))
+        return v.reshape(3, 3)
+
+    def fshift(self):
+        f = np.zeros(135, dtype=np.float32)
+        lib().orc_fshift(self.c, f.ctypes.data_as(C.POINTER(C.c_float)))
+        return f.reshape(45, 3)
+
+    # -- setup values --
+    @property
+    def beta(self):
+        return lib().orc_beta(self.c)
+
+    @property
+    def epsfac(self):
+        return lib().orc_epsfac(self.c)
+
+    @property
+    def rbb2(self):
+        return lib().orc_rbb2(self.c)
+
+    def table(self):
+        n = lib().orc_table_size(self.c)
+        F = np.zeros(max(n, 1), np.float32)
+        V = np.zeros(max(n, 1), np.float32)
+        lib().orc_table(self.c, F.ctypes.data_as(C.POINTER(C.c_float)),
+                        V.ctypes.data_as(C.POINTER(C.c_float)))
+        return lib().orc_table_scale(self.c), F[:n], V[:n]
+
+    # -- grid / list --
+    def grid_arrays(self):
+        L = lib()
+        dims = np.zeros(6, np.int32)
+        cs = np.zeros(4, np.float32)
+        L.orc_grid_dims(self.c, dims.ctypes.data_as(C.POINTER(C.c_int)),
+                        cs.ctypes.data_as(C.POINTER(C.c_float)))
+        ncx, ncy, ncol, ncells, ncl, npad = (int(v) for v in dims)
+        return {
+            "ncx": ncx, "ncy": ncy, "ncol": ncol, "ncells": ncells, "nclusters_total": ncl,
+            "npad": npad, "cell_size": cs[:2].copy(), "inv_cell_size": cs[2:].copy(),
+            "cxy_ind": _copy(L.orc_cxy_ind(self.c), ncol + 1, np.int32),
+            "num_clusters": _copy(L.orc_num_clusters(self.c), ncells, np.int32),
+            "atom_indices": _copy(L.orc_atom_indices(self.c), npad, np.int32),
+            "cells": _copy(L.orc_cells(self.c), self.system.n, np.int32),
+            "xq": _copy(L.orc_xq(self.c), npad * 4, np.float32).reshape(-1, 4),
+            "types": _copy(L.orc_types_grid(self.c), npad, np.int32),
+            "bb": _copy(L.orc_bb(self.c), ncells * 8 * 6, np.float32).reshape(-1, 6),
+            "bbcz": _copy(L.orc_bbcz(self.c), ncells * 2, np.float32).reshape(-1, 2),
+        }
+
+    def pairlist(self):
+        L = lib()
+        s = np.zeros(3, np.int32)
+        L.orc_list_sizes(self.c, s.ctypes.data_as(C.POINTER(C.c_int)))
+        nsci, ncj4, nexcl = (int(v) for v in s)
+        return {
+            "sci": _copy(L.orc_sci(self.c), nsci * 4, np.int32).reshape(-1, 4),
+            "cj4": _copy(L.orc_cj4(self.c), ncj4 * 8, np.int32).reshape(-1, 8),
+            "excl": _copy(L.orc_excl(self.c), nexcl * 32, np.uint32).reshape(-1, 32),
+            "imask_outer": _copy(L.orc_imask_outer(self.c), ncj4 * 2, np.uint32).reshape(-1, 2),
+        }
+
+    def fnb(self):
+        npad = self.grid_arrays()["npad"]
+        return _copy(lib().orc_fnb(self.c), npad * 3, np.float32).reshape(-1, 3)
+
+
+def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
+                  use_ewald_shift=False, epsilon_rf=1.0):
+    """FP64 explicit-image forces (on ``subset``) and, for the full set, energies."""
+    L = lib()
+    n = system.n
+    epsfac = L.orc_one_4pi_eps0()
+    if coulomb == COULOMB_CUTOFF:
+        epsilon_rf = 1.0
+    if epsilon_rf == 0:
+        k_rf = 1.0 / (2 * rc**3)
+    else:
+        k_rf = (epsilon_rf - 1.0) / (2 * epsilon_rf + 1.0) / rc**3
+    c_rf = 1.0 / rc + k_rf * rc * rc
+    full = subset is None
+    sub = np.arange(n, dtype=np.int32) if full else np.ascontiguousarray(subset, dtype=np.int32)
+    x, xp = _f(system.x)
+    box, bp = _f(system.box)
+    q, qp = _f(system.q)
+    t, tp = _i(system.type)
+    nb, nbp = _f(system.nbfp)
+    ei, eip = _i(system.excl_index)
+    el, elp = _i(system.excl_list if len(system.excl_list) else np.zeros(1, np.int32))
+    s, sp = _i(sub)
+    f = np.zeros((len(sub), 3), np.float64)
+    e = np.zeros(2, np.float64)
+    L.orc_fp64_allpairs(n, xp, bp, qp, tp, system.ntypes, nbp, eip, elp, coulomb, rc,
+                        0.0 if beta is None else float(beta), epsfac, k_rf, c_rf,
+                        int(use_ewald_shift), sp, len(sub), f.ctypes.data_as(C.POINTER(C.c_double)),
+                        e.ctypes.data_as(C.POINTER(C.c_double)) if full else None)
+    return (f, e) if full else (f, None)

@@ -1,0 +1,113 @@
+"""The CPU oracle itself: pinned to the reference's golden vectors and to FP64.
+
+Mirrors api/nblib/tests/nbkernelsystem.cpp (ArgonForcesAreCorrect,
+SpcMethanolForcesAreCorrect, UpdateChangesForces) at the reference's own
+tolerance (api/nblib/tests/testhelpers.h:72-77: 200 single-precision ULP).
+"""
+import numpy as np
+import pytest
+
+from gmxapi_gb300 import systems
+from oracle import oracle as O
+from tests.helpers import canonical_pairs, nblib_golden_system, rel_rms, ulp_distance
+
+
+@pytest.mark.parametrize("key", ["argon", "spc_methanol"])
+def test_oracle_matches_nblib_golden(key):
+    s, ref = nblib_golden_system(key)
+    o = O.Oracle(s, coulomb=O.COULOMB_CUTOFF, rc=1.0, rlist=1.0)
+    o.grid()
+    o.search()
+    o.force(energy=False)
+    f = o.forces()
+    assert ulp_distance(f, ref).max() <= 200
+
+
+def test_oracle_repeatable_and_changes_with_update():
+    s, _ = nblib_golden_system("spc_methanol")
+    o = O.Oracle(s, coulomb=O.COULOMB_CUTOFF, rc=1.0, rlist=1.0)
+    o.grid()
+    o.search()
+    o.force(False)
+    f1 = o.forces()
+    o.force(False)
+    assert np.array_equal(f1, o.forces())
+    o.set_x(s.x + np.float32(0.001))
+    o.force(False)
+    assert not np.array_equal(f1, o.forces())
+
+
+def test_ewald_coefficient_and_table():
+    s = systems.water_small()
+    o = O.Oracle(s, rc=0.9, rlist=1.0)
+    # beta from erfc(beta*rc) = 1e-5 (ewald/ewald_utils.cpp:46-71)
+    assert abs(o.beta - 3.4705) < 1e-3
+    scale, F, V = o.table()
+    assert len(F) == int(0.9 * scale) + 2
+    # the F table approximates -d/dr erf(beta r)/r
+    from math import erf, exp, pi, sqrt
+    b = o.beta
+    for r in (0.1, 0.3, 0.6, 0.85):
+        exact = -(2 * b / sqrt(pi) * exp(-(b * r) ** 2) / r - erf(b * r) / r**2)
+        k = int(r * scale)
+        eps = r * scale - k
+        approx = (1 - eps) * F[k] + eps * F[k + 1]
+        assert abs(approx - exact) < 1e-5 * max(1.0, abs(exact))
+
+
+def test_oracle_vs_fp64_allpairs_water():
+    s = systems.water_small()
+    o = O.Oracle(s, rc=0.9, rlist=1.0)
+    o.grid()
+    o.search()
+    o.force(True)
+    f = o.forces()
+    f64, e64 = O.fp64_allpairs(s, rc=0.9, beta=o.beta)
+    assert rel_rms(f, f64) < 1e-5
+    e = o.energies()
+    assert abs(e[0] - e64[0]) / abs(e64[0]) < 1e-5
+    assert abs(e[1] - e64[1]) / abs(e64[1]) < 1e-5
+
+
+def test_pairlist_covers_every_pair_within_rlist():
+    """Every atom pair closer than rlist is in exactly one list entry."""
+    s = systems.spc_water(300, 2.08, seed=7)
+    o = O.Oracle(s, rc=0.9, rlist=1.0)
+    o.grid()
+    o.search()
+    g = o.grid_arrays()
+    pl = o.pairlist()
+    rows = canonical_pairs(pl["sci"], pl["cj4"], pl["excl"])
+    xq = g["xq"]
+    ai = g["atom_indices"]
+    box = s.box.astype(np.float64)
+    shifts = np.array([[(k - 2) * box[0], (l - 1) * box[1], (m - 1) * box[2]]
+                       for m in range(3) for l in range(3) for k in range(5)])
+    count = {}
+    for r in rows:
+        ci, cj, sh, mask = int(r["ci"]), int(r["cj"]), int(r["shift"]), int(r["mask"])
+        for ic in range(8):
+            a = ai[ci * 8 + ic]
+            for jc in range(8):
+                b = ai[cj * 8 + jc]
+                if a < 0 or b < 0:
+                    continue
+                d = xq[ci * 8 + ic, :3] + shifts[sh] - xq[cj * 8 + jc, :3]
+                if d @ d < 1.0:
+                    key = (min(a, b), max(a, b))
+                    if (mask >> (ic * 8 + jc)) & 1:
+                        count[key] = count.get(key, 0) + 1
+    # brute force: pairs within rlist (minimum image suffices: box > 2 rlist)
+    x = s.x.astype(np.float64) % box
+    n = s.n
+    mol = np.arange(n) // 3
+    for a in range(n):
+        d = x[a + 1:] - x[a]
+        d -= box * np.round(d / box)
+        r2 = (d * d).sum(1)
+        for k in np.nonzero(r2 < 0.99)[0]:
+            b = a + 1 + k
+            if mol[a] == mol[b]:
+                assert (a, b) not in count  # excluded pairs are masked out
+            else:
+                assert count.get((a, b), 0) == 1, (a, b)
