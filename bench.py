@@ -1,0 +1,326 @@
+"""Benchmark of the short-range nonbonded path on one GB300.
+
+Workload (one "step" = one force + energy + virial evaluation):
+  288,000-atom SPC water box (96,000 molecules, 14.21 nm), rc 0.9 nm,
+  rlist 1.0 nm, Ewald beta from rtol 1e-5, potential-shift LJ; a fresh
+  grid + pair list every 100 steps, rolling dynamic pruning every 10 steps
+  (rlist_inner 0.95 nm, 5 parts pruned on alternate steps); coordinates
+  perturbed by N(0, 0.002 nm) per coordinate and step; forces FP32,
+  energies and virial reduced in FP64.
+
+Metric: useful pair interactions per second, useful pairs per evaluation =
+N/2 * (rho * 4/3 pi rc^3 + 1) like gmx nonbonded-benchmark
+(src/gromacs/nbnxm/benchmark/bench_setup.cpp:272-276).
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "useful pair-interactions/s (288k-atom SPC water, F+E+virial, rc 0.9, rlist 1.0)"
+RC, RLIST, RLIST_INNER = 0.9, 1.0, 0.95
+NSTLIST, NSTPRUNE = 100, 10
+SIGMA_STEP = 0.002
+# Ewald-analytic + LJ flops per pair with energies (src/gromacs/gmxlib/nrnb.cpp:106)
+FLOPS_PER_PAIR_VF = 107
+
+
+def useful_pairs(n: int, box) -> float:
+    rho = n / float(np.prod(box))
+    return n * 0.5 * (rho * 4.0 / 3.0 * math.pi * RC**3 + 1.0)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [t.strip() for t in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline_port() -> dict:
+    """The oracle (plain-C restatement of the reference kernel) on the 3,000-atom box, 1 core."""
+    from gmxapi_gb300 import systems
+    from oracle import oracle as O
+
+    s = systems.water_small()
+    o = O.Oracle(s, rc=RC, rlist=RLIST)
+    o.grid()
+    o.search()
+    o.force(True)
+    reps = 0
+    t0 = time.perf_counter()
+    while True:
+        o.force(True)
+        reps += 1
+        if time.perf_counter() - t0 > 10.0 or reps >= 20:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": useful_pairs(s.n, s.box) / dt, "unit": "pairs/s", "cores": 1, "kind": "port",
+            "sample": f"{reps} F+E evaluations of the 3,000-atom SPC box (rc 0.9, rlist 1.0) by the "
+                      "plain-C oracle kernel, single thread"}
+
+
+def run_reference(args) -> None:
+    """--impl reference: the oracle port of the reference CPU kernel on this workload."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from gmxapi_gb300 import systems
+    from oracle import oracle as O
+
+    s = systems.water_large()
+    o = O.Oracle(s, rc=RC, rlist=RLIST, rlist_inner=RLIST_INNER)
+    o.grid()
+    o.search()
+    o.prune(fresh=True)
+    pl = o.pairlist()
+    nsci = len(pl["sci"])
+    cnt = np.array([bin(int(m)).count("1") for m in pl["cj4"][:, 4]]) + \
+        np.array([bin(int(m)).count("1") for m in pl["cj4"][:, 6]])
+    per_entry = np.array([cnt[a:b].sum() for a, b in pl["sci"][:, 2:4]], np.float64)
+    total_bits = per_entry.sum()
+    chunk = max(1, nsci // 200)
+    up = useful_pairs(s.n, s.box)
+    done_pairs, elapsed = 0.0, 0.0
+    rng = np.random.default_rng(0)
+    for it in range(args.warmup + args.steps):
+        e0 = int(rng.integers(0, max(1, nsci - chunk)))
+        t0 = time.perf_counter()
+        o.force_entries(e0, e0 + chunk, True)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            elapsed += dt
+            done_pairs += up * per_entry[e0:e0 + chunk].sum() / total_bits
+    value = done_pairs / elapsed
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": 1, "kind": "port",
+                         "sample": f"each step: {chunk} of {nsci} list entries of the 288k-atom box "
+                                   "through the plain-C oracle kernel (F+E), single thread"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config() -> dict:
+    return {"workload": "spc_water_288k", "atoms": 288000, "box_nm": 14.21, "rc_nm": RC, "rlist_nm": RLIST,
+            "rlist_inner_nm": RLIST_INNER, "nstlist": NSTLIST, "nstlist_prune": NSTPRUNE,
+            "perturb_sigma_nm": SIGMA_STEP, "coulomb": "ewald", "energy_virial": "fp64 every step",
+            "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"}
+
+
+def run_ours(args) -> None:
+    import torch
+
+    world, rank, local = dist_env()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from gmxapi_gb300 import nblib, systems
+
+    s = systems.water_large()
+    n = s.n
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=RLIST, rcoulomb=RC,
+                                 rlist_inner=RLIST_INNER, nstlist=NSTLIST, nstlist_prune=NSTPRUNE,
+                                 compute_virial_and_energy=True)
+    calc = nblib.ForceCalculator(s, opts, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    calc.set_stream(stream.cuda_stream)
+    total = args.warmup + args.steps
+    # coordinate frames: a Gaussian random walk, resident in HBM before timing
+    gen = torch.Generator(device=f"cuda:{dev}").manual_seed(1234 + rank)
+    frames = torch.empty((total, n * 3), dtype=torch.float32, device=f"cuda:{dev}")
+    frames[0] = torch.from_numpy(s.x.reshape(-1)).to(frames.device)
+    for t in range(1, total):
+        frames[t] = frames[t - 1] + SIGMA_STEP * torch.randn(n * 3, generator=gen, device=frames.device)
+    f = torch.empty(n * 3, dtype=torch.float32, device=frames.device)
+    ev = torch.zeros(11, dtype=torch.float64, device=frames.device)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=frames.device)  # 256 MB > L2
+
+    def step(t):
+        calc.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), ev.data_ptr(), ev[2:].data_ptr())
+
+    for t in range(args.warmup):
+        step(t)
+    torch.cuda.synchronize()
+    pairs0 = calc.pair_count()
+    calc.timings(reset=True)
+    calc.set_timing(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            step(args.warmup + k)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    force_ms, force_launches, launches = calc.timings(reset=True)
+    calc.set_timing(False)
+    pairs1 = calc.pair_count()
+    if world > 1:
+        t = torch.tensor([total_ms], device=frames.device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    up = useful_pairs(n, s.box)
+    value = world * up * args.steps / (total_ms * 1e-3)
+
+    # e2e: the same schedule through the C ABI with host arrays (pinned), H2D x and D2H f/E/virial per step
+    hx = frames.cpu().pin_memory()
+    hf = torch.empty(n * 3, dtype=torch.float32).pin_memory()
+    he = np.zeros(2)
+    hv = np.zeros(9)
+    import ctypes as C
+
+    from gmxapi_gb300 import _lib
+
+    L = _lib.load()
+    calc2 = nblib.ForceCalculator(s, opts, device=dev)
+    fp = C.POINTER(C.c_float)
+    dp = C.POINTER(C.c_double)
+
+    def hstep(t):
+        _lib.check(L.nbx_md_step(calc2.h, t, C.cast(hx[t].data_ptr(), fp), C.cast(hf.data_ptr(), fp),
+                                 he.ctypes.data_as(dp), hv.ctypes.data_as(dp)), calc2.h)
+
+    for t in range(args.warmup):
+        hstep(t)
+    torch.cuda.synchronize()
+    e2e_ms = 0.0
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hstep(args.warmup + k)
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_value = world * up * args.steps / (e2e_ms * 1e-3)
+    calc2.close()
+
+    if rank != 0:
+        return
+    from gmxapi_gb300.nblib import measure_fp32_peak
+
+    peak = measure_fp32_peak(dev)
+    pairs_avg = 0.5 * (pairs0 + pairs1)
+    flops = pairs_avg * FLOPS_PER_PAIR_VF
+    avg_force_ms = force_ms / max(1, force_launches)
+    achieved = flops / (avg_force_ms * 1e-3) / 1e12
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SPC water)",
+        "config": workload_config(),
+        "force_evals_per_s": world * args.steps / (total_ms * 1e-3),
+        "pairs_computed_per_eval": pairs_avg, "useful_pairs_per_eval": up,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "nbx::k_force<energy, ewald>",
+                     "note": f"{FLOPS_PER_PAIR_VF} flops per computed pair (nrnb.cpp:106) x "
+                             f"{pairs_avg:.4g} computed pairs / {avg_force_ms:.4f} ms average launch; "
+                             "peak = measured FFMA probe of this run"},
+        "cpu_baseline": cpu_baseline_port(),
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": n * 12,
+                "d2h_bytes_per_step": n * 12 + 11 * 8},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,124 @@
+"""ctypes binding of the C ABI in include/nbnxm_gb300.h.
+
+The engine is the in-tree shared library gmxapi_gb300/lib/libnbnxm_gb300.so,
+built by gmxapi_gb300/build.py (``python -c "import __graft_entry__ as g;
+g.build()"``).  There is no fallback: if the library is missing, loading
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libnbnxm_gb300.so")
+
+NBX_OK = 0
+STATUS_NAMES = {
+    0: "NBX_OK",
+    1: "NBX_ERR_INVALID_INPUT",
+    2: "NBX_ERR_OUT_OF_MEMORY",
+    3: "NBX_ERR_LIST_OVERFLOW",
+    4: "NBX_ERR_CUDA",
+    5: "NBX_ERR_TIMEOUT",
+    6: "NBX_ERR_NO_DEVICE",
+    7: "NBX_ERR_STATE",
+}
+
+#: every function include/nbnxm_gb300.h declares
+EXPORTED = [
+    "nbx_default_options", "nbx_create", "nbx_destroy", "nbx_last_error", "nbx_update_pairlist",
+    "nbx_compute", "nbx_set_stream", "nbx_get_stream", "nbx_search_device", "nbx_prune_device",
+    "nbx_compute_device", "nbx_md_step_device", "nbx_synchronize", "nbx_get_sizes", "nbx_get_grid",
+    "nbx_get_pairlist", "nbx_get_pair_counts", "nbx_measure_fp32_peak", "nbx_md_step",
+    "nbx_set_timing", "nbx_get_timings",
+]
+
+
+class nbx_system_desc(C.Structure):
+    _fields_ = [
+        ("num_atoms", C.c_int),
+        ("x", C.POINTER(C.c_float)),
+        ("q", C.POINTER(C.c_float)),
+        ("type", C.POINTER(C.c_int)),
+        ("num_types", C.c_int),
+        ("nbfp", C.POINTER(C.c_float)),
+        ("excl_index", C.POINTER(C.c_int)),
+        ("excl_list", C.POINTER(C.c_int)),
+        ("box", C.c_float * 3),
+    ]
+
+
+class nbx_options(C.Structure):
+    _fields_ = [
+        ("coulomb", C.c_int),
+        ("rcoulomb", C.c_float),
+        ("rlist", C.c_float),
+        ("rlist_inner", C.c_float),
+        ("ewald_rtol", C.c_float),
+        ("epsilon_rf", C.c_float),
+        ("use_ewald_shift", C.c_int),
+        ("nstlist", C.c_int),
+        ("nstlist_prune", C.c_int),
+        ("compute_energy", C.c_int),
+    ]
+
+
+class NbxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load the engine library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with gmxapi_gb300.build.build() "
+            "(nvcc, sm_103a); there is no CPU fallback"
+        )
+    L = C.CDLL(LIB_PATH)
+    vp, ip, fp, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_double)
+    u32p, llp = C.POINTER(C.c_uint32), C.POINTER(C.c_longlong)
+    L.nbx_default_options.argtypes = [C.POINTER(nbx_options)]
+    L.nbx_default_options.restype = None
+    L.nbx_create.argtypes = [C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int, C.POINTER(vp)]
+    L.nbx_destroy.argtypes = [vp]
+    L.nbx_last_error.argtypes = [vp]
+    L.nbx_last_error.restype = C.c_char_p
+    L.nbx_update_pairlist.argtypes = [vp, fp]
+    L.nbx_compute.argtypes = [vp, fp, fp, dp, dp]
+    L.nbx_set_stream.argtypes = [vp, vp]
+    L.nbx_get_stream.argtypes = [vp]
+    L.nbx_get_stream.restype = vp
+    L.nbx_search_device.argtypes = [vp, vp]
+    L.nbx_prune_device.argtypes = [vp, C.c_int]
+    L.nbx_compute_device.argtypes = [vp, vp, vp, vp, vp]
+    L.nbx_md_step_device.argtypes = [vp, C.c_longlong, vp, vp, vp, vp]
+    L.nbx_synchronize.argtypes = [vp]
+    L.nbx_get_sizes.argtypes = [vp, ip]
+    L.nbx_get_grid.argtypes = [vp, ip, ip, ip, ip, fp, fp, fp]
+    L.nbx_get_pairlist.argtypes = [vp, ip, ip, u32p, u32p]
+    L.nbx_get_pair_counts.argtypes = [vp, llp]
+    L.nbx_measure_fp32_peak.argtypes = [C.c_int, dp]
+    L.nbx_md_step.argtypes = [vp, C.c_longlong, fp, fp, dp, dp]
+    L.nbx_set_timing.argtypes = [vp, C.c_int]
+    L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
+    for name in EXPORTED:
+        f = getattr(L, name)
+        if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream"):
+            f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(code: int, handle=None):
+    if code != NBX_OK:
+        msg = load().nbx_last_error(handle)
+        raise NbxError(code, msg.decode() if msg else "")

@@ -1,0 +1,1039 @@
+// Host side of nbnxm_gb300: handle, device memory, set-up constants and the C ABI.
+//
+// Set-up mirrors nblib's GmxSetupDirector (api/nblib/gmxsetup.cpp:226-325):
+// interaction constants (Ewald beta by bisection, ewald/ewald_utils.cpp:46-71;
+// RF constants, mdlib/rf_util.cpp:54-66; potential shifts), the nbfp matrix
+// with one extra all-zero type (nbnxm/atomdata.cpp:440-620), the grid
+// dimensions (nbnxm/grid.cpp:103-262) and the shift vectors
+// (pbcutil/pbc.cpp:1187-1202).  Host arithmetic here is compiled with
+// -ffp-contract=off so these constants round exactly like the reference's.
+#include "../../include/nbnxm_gb300.h"
+#include "nbx_internal.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace nbx
+{
+cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s);
+cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s);
+} // namespace nbx
+
+using namespace nbx;
+
+struct nbx_handle
+{
+    int          device   = 0;
+    int          num_sms  = 152;
+    cudaStream_t stream   = nullptr;
+    bool         own_stream = false;
+    nbx_options  opts{};
+    int          n        = 0;
+    int          ntypes   = 0;
+    DeviceView   v{};
+    std::string  err;
+    bool         have_list = false;
+    long long    list_step = 0;   // step of the last search (nbx_md_step_device)
+    int          prune_part = 0;  // next rolling-prune part
+    int          nparts     = 1;
+    bool         use_prune  = false;
+    std::vector<void*> allocations;
+    // device buffers for the host-array interface
+    float*  d_x = nullptr;
+    float*  d_f = nullptr;
+    double* d_out = nullptr;  // energies[2] + virial[9]
+    unsigned long long* d_count = nullptr;
+    ListHeader* h_hdr = nullptr;  // pinned copy for reading sizes
+    // timing / launch accounting
+    bool        timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
+    double      force_ms = 0.0;
+    long long   force_launches = 0;
+    long long   launches = 0;
+};
+
+namespace
+{
+
+thread_local std::string g_create_error;
+
+double one_4pi_eps0()
+{
+    // src/gromacs/math/units.h:69-79
+    const double eps0 = (8.8541878128e-12 * 1e-9 * 1e3) / (1.602176634e-19 * 1.602176634e-19 * 6.02214076e23);
+    return 1.0 / (4.0 * 3.14159265358979323846 * eps0);
+}
+
+// ewald/ewald_utils.cpp:46-71 in single precision
+float calc_ewaldcoeff_q(float rc, float rtol)
+{
+    float beta = 5, low, high;
+    int   n, i = 0;
+    do
+    {
+        i++;
+        beta *= 2;
+    } while (erfcf(beta * rc) > rtol);
+    n    = i + 60;
+    low  = 0;
+    high = beta;
+    for (i = 0; i < n; i++)
+    {
+        beta = (low + high) / 2;
+        if (erfcf(beta * rc) > rtol)
+        {
+            low = beta;
+        }
+        else
+        {
+            high = beta;
+        }
+    }
+    return beta;
+}
+
+int set_error(nbx_handle* h, int code, const std::string& msg)
+{
+    if (h)
+    {
+        h->err = msg;
+    }
+    else
+    {
+        g_create_error = msg;
+    }
+    return code;
+}
+
+int cuda_check(nbx_handle* h, cudaError_t e, const char* where)
+{
+    if (e == cudaSuccess)
+    {
+        return NBX_OK;
+    }
+    if (e == cudaErrorMemoryAllocation)
+    {
+        return set_error(h, NBX_ERR_OUT_OF_MEMORY, std::string(where) + ": out of device memory");
+    }
+    return set_error(h, NBX_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template<typename T>
+cudaError_t dalloc(nbx_handle* h, T** p, size_t count)
+{
+    void*       q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess)
+    {
+        h->allocations.push_back(q);
+        *p = static_cast<T*>(q);
+    }
+    return e;
+}
+
+void dfree(nbx_handle* h, void* p)
+{
+    for (auto it = h->allocations.begin(); it != h->allocations.end(); ++it)
+    {
+        if (*it == p)
+        {
+            cudaFree(p);
+            h->allocations.erase(it);
+            return;
+        }
+    }
+}
+
+int status_to_error(nbx_handle* h, unsigned st)
+{
+    if (st & kStatusNaN)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "coordinates contain NaN");
+    }
+    if (st & kStatusWrapLimit)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "a coordinate is more than 127 box lengths outside the box");
+    }
+    if (st & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    {
+        return set_error(h, NBX_ERR_LIST_OVERFLOW, "pair list or grid capacity exceeded");
+    }
+    if (st & kStatusTimeout)
+    {
+        return set_error(h, NBX_ERR_TIMEOUT, "a device-side wait timed out");
+    }
+    return NBX_OK;
+}
+
+int read_header(nbx_handle* h)
+{
+    cudaError_t e = cudaMemcpyAsync(h->h_hdr, h->v.hdr, sizeof(ListHeader), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess)
+    {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    return cuda_check(h, e, "read list header");
+}
+
+// (Re)allocates the list arrays to hold num_sci / num_cj4 entries with headroom.
+int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
+{
+    DeviceView& v    = h->v;
+    const int   need_sci = num_sci + num_sci / 4 + 64;
+    const int   need_cj4 = num_cj4 + num_cj4 / 4 + 256;
+    if (v.sci && v.sci_cap >= num_sci && v.cj4_cap >= num_cj4)
+    {
+        return NBX_OK;
+    }
+    dfree(h, v.sci);
+    dfree(h, v.cj4);
+    dfree(h, v.excl);
+    dfree(h, v.imask_outer);
+    v.sci = nullptr;
+    v.cj4 = nullptr;
+    v.excl = nullptr;
+    v.imask_outer = nullptr;
+    v.sci_cap  = need_sci;
+    v.cj4_cap  = need_cj4;
+    v.excl_cap = 2 * need_cj4 + 1;  // at most one mask per cj4 half
+    cudaError_t e = dalloc(h, &v.sci, v.sci_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.cj4, v.cj4_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.excl, v.excl_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.imask_outer, 2 * (size_t)v.cj4_cap);
+    if (e != cudaSuccess)
+    {
+        return cuda_check(h, e, "list allocation");
+    }
+    // exclusion entry 0: all pairs interacting
+    e = cudaMemsetAsync(v.excl, 0xff, sizeof(Excl), h->stream);
+    ListHeader caps{};
+    caps.sci_capacity  = v.sci_cap;
+    caps.cj4_capacity  = v.cj4_cap;
+    caps.excl_capacity = v.excl_cap;
+    if (e == cudaSuccess)
+    {
+        e = cudaMemcpyAsync(&v.hdr->sci_capacity, &caps.sci_capacity, 3 * sizeof(int), cudaMemcpyHostToDevice,
+                            h->stream);
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaStreamSynchronize(h->stream);
+    }
+    return cuda_check(h, e, "list capacity");
+}
+
+// Grid + count, size the list, write, prune: the synchronous search.
+int search_sync(nbx_handle* h, float* d_x, int write_back)
+{
+    DeviceView& v = h->v;
+    cudaError_t e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
+    if (e == cudaSuccess) e = launch_grid(v, d_x, write_back, h->stream);
+    if (e == cudaSuccess) e = launch_search_count(v, h->stream);
+    h->launches += 6;
+    int rc = cuda_check(h, e, "grid/search count");
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    if ((rc = read_header(h)) != NBX_OK)
+    {
+        return rc;
+    }
+    unsigned st = h->h_hdr->status & ~(unsigned)kStatusListOverflow;
+    if ((rc = status_to_error(h, st)) != NBX_OK)
+    {
+        return rc;
+    }
+    if ((rc = ensure_list_capacity(h, h->h_hdr->num_sci, h->h_hdr->num_cj4)) != NBX_OK)
+    {
+        return rc;
+    }
+    // counts are unchanged; clear the overflow flag the count pass may have set
+    e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
+    if (e == cudaSuccess) e = launch_search_write(v, h->stream);
+    if (e == cudaSuccess && h->use_prune) e = launch_prune(v, 1, 0, 1, h->stream);
+    h->launches += 2 + (h->use_prune ? 1 : 0);
+    if ((rc = cuda_check(h, e, "search write")) != NBX_OK)
+    {
+        return rc;
+    }
+    if ((rc = read_header(h)) != NBX_OK)
+    {
+        return rc;
+    }
+    if ((rc = status_to_error(h, h->h_hdr->status)) != NBX_OK)
+    {
+        return rc;
+    }
+    h->have_list  = true;
+    h->prune_part = 0;
+    return NBX_OK;
+}
+
+cudaEvent_t take_event(nbx_handle* h)
+{
+    cudaEvent_t ev;
+    if (!h->ev_pool.empty())
+    {
+        ev = h->ev_pool.back();
+        h->ev_pool.pop_back();
+    }
+    else
+    {
+        cudaEventCreate(&ev);
+    }
+    return ev;
+}
+
+// Accumulates the finished force-kernel event pairs.
+void collect_timings(nbx_handle* h, bool wait)
+{
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> keep;
+    for (auto& p : h->ev_pending)
+    {
+        if (wait)
+        {
+            cudaEventSynchronize(p.second);
+        }
+        if (cudaEventQuery(p.second) == cudaSuccess)
+        {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, p.first, p.second);
+            h->force_ms += ms;
+            h->ev_pool.push_back(p.first);
+            h->ev_pool.push_back(p.second);
+        }
+        else
+        {
+            keep.push_back(p);
+        }
+    }
+    cudaGetLastError();
+    h->ev_pending.swap(keep);
+}
+
+int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, double* d_vir)
+{
+    DeviceView& v      = h->v;
+    const bool  energy = (d_e != nullptr) || (d_vir != nullptr);
+    cudaError_t e      = launch_convert_x(v, d_x, h->stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h->timing)
+    {
+        e0 = take_event(h);
+        e1 = take_event(h);
+        cudaEventRecord(e0, h->stream);
+    }
+    if (e == cudaSuccess) e = launch_force(v, d_e != nullptr, h->stream, h->num_sms);
+    if (h->timing)
+    {
+        cudaEventRecord(e1, h->stream);
+        h->ev_pending.emplace_back(e0, e1);
+        if (h->ev_pending.size() > 256)
+        {
+            collect_timings(h, false);
+        }
+    }
+    if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_x, d_vir != nullptr, h->stream);
+    if (e == cudaSuccess && energy) e = launch_finish_energy(v, d_e, d_vir, h->stream);
+    h->force_launches += 1;
+    h->launches += 3 + (energy ? 1 : 0);
+    return cuda_check(h, e, "compute");
+}
+
+bool valid_box(const float* box)
+{
+    for (int d = 0; d < 3; d++)
+    {
+        if (!(box[d] > 0.0f) || !std::isfinite(box[d]))
+        {
+            return false;
+        }
+    }
+    return true;
+}
+
+} // namespace
+
+extern "C" {
+
+void nbx_default_options(nbx_options* o)
+{
+    std::memset(o, 0, sizeof(*o));
+    o->coulomb         = NBX_COULOMB_EWALD;
+    o->rcoulomb        = 1.0f;
+    o->rlist           = 1.0f;
+    o->rlist_inner     = 0.0f;
+    o->ewald_rtol      = 1e-5f;
+    o->epsilon_rf      = 1.0f;
+    o->use_ewald_shift = 0;
+    o->nstlist         = 10;
+    o->nstlist_prune   = 0;
+    o->compute_energy  = 0;
+}
+
+const char* nbx_last_error(const nbx_handle* h)
+{
+    return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int device, nbx_handle** out)
+{
+    if (!sys || !out)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "null argument");
+    }
+    *out = nullptr;
+    nbx_options opts;
+    if (opts_in)
+    {
+        opts = *opts_in;
+    }
+    else
+    {
+        nbx_default_options(&opts);
+    }
+    const int n = sys->num_atoms;
+    if (n <= 0 || !sys->x || !sys->q || !sys->type || !sys->nbfp || !sys->excl_index || sys->num_types <= 0)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "empty system or missing arrays");
+    }
+    if (!valid_box(sys->box))
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "box edges must be positive and finite");
+    }
+    if (!(opts.rcoulomb > 0.0f) || !(opts.rlist >= opts.rcoulomb))
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "need 0 < rcoulomb <= rlist");
+    }
+    if (opts.coulomb < 0 || opts.coulomb > 2)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown Coulomb type");
+    }
+    if (sys->num_types + 1 > 64)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "at most 63 particle types");
+    }
+    for (int i = 0; i < 3 * n; i++)
+    {
+        if (!std::isfinite(sys->x[i]))
+        {
+            return set_error(nullptr, NBX_ERR_INVALID_INPUT, "input coordinates have at least one NaN");
+        }
+    }
+    for (int i = 0; i < n; i++)
+    {
+        if (sys->type[i] < 0 || sys->type[i] >= sys->num_types)
+        {
+            return set_error(nullptr, NBX_ERR_INVALID_INPUT, "particle type out of range");
+        }
+    }
+    if (sys->excl_index[0] != 0)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "exclusion offsets must start at 0");
+    }
+    for (int i = 0; i < n; i++)
+    {
+        if (sys->excl_index[i + 1] < sys->excl_index[i])
+        {
+            return set_error(nullptr, NBX_ERR_INVALID_INPUT, "exclusion offsets must be non-decreasing");
+        }
+        for (int k = sys->excl_index[i]; k < sys->excl_index[i + 1]; k++)
+        {
+            if (sys->excl_list[k] < 0 || sys->excl_list[k] >= n)
+            {
+                return set_error(nullptr, NBX_ERR_INVALID_INPUT, "excluded atom index out of range");
+            }
+        }
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    {
+        cudaGetLastError();
+        return set_error(nullptr, NBX_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "device index out of range");
+    }
+
+    nbx_handle* h = new nbx_handle();
+    h->device     = device;
+    h->opts       = opts;
+    h->n          = n;
+    h->ntypes     = sys->num_types;
+    cudaSetDevice(device);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    h->own_stream = true;
+    DeviceView& v = h->v;
+    v.n           = n;
+
+    // ---- interaction constants (gmxsetup.cpp:226-284) ----
+    const float rc = opts.rcoulomb;
+    v.coulomb      = opts.coulomb;
+    v.rc2          = rc * rc;
+    v.rlist        = opts.rlist;
+    v.rlist2       = opts.rlist * opts.rlist;
+    const float rin = (opts.rlist_inner > 0.0f) ? opts.rlist_inner : opts.rlist;
+    v.rlist_inner2 = rin * rin;
+    v.epsfac       = (float)one_4pi_eps0();
+    {
+        const float p3 = rc * rc * rc;
+        const float p6 = p3 * p3;
+        const float p12 = p6 * p6;
+        v.cpot6  = (float)(-1.0 / p6);
+        v.cpot12 = (float)(-1.0 / p12);
+    }
+    const float eps_rf = (opts.coulomb == NBX_COULOMB_CUTOFF) ? 1.0f : opts.epsilon_rf;
+    v.k_rf = (eps_rf == 0) ? 1 / (2 * rc * rc * rc) : (eps_rf - 1.0f) / (2 * eps_rf + 1.0f) / (rc * rc * rc);
+    v.c_rf = 1 / rc + v.k_rf * rc * rc;
+    double qsq = 0.0;
+    for (int i = 0; i < n; i++)
+    {
+        qsq += (double)sys->q[i] * (double)sys->q[i];
+    }
+    if (opts.coulomb == NBX_COULOMB_EWALD)
+    {
+        const float rtol = opts.ewald_rtol > 0.0f ? opts.ewald_rtol : 1e-5f;
+        v.beta           = calc_ewaldcoeff_q(rc, rtol);
+        v.sh_ewald       = opts.use_ewald_shift ? erfcf(v.beta * rc) / rc : 0.0f;
+        // Ewald self energy, kernel_gpu_ref.cpp:154-178
+        v.self_energy = -(double)v.epsfac * (double)v.beta * 0.56418958354775628695 * qsq;
+    }
+    else
+    {
+        v.beta        = 0.0f;
+        v.sh_ewald    = 0.0f;
+        v.self_energy = -(double)v.epsfac * 0.5 * (double)v.c_rf * qsq;
+    }
+    // ---- shift vectors (pbc.cpp:1187-1202), rectangular box ----
+    for (int s = 0, m = -1; m <= 1; m++)
+    {
+        for (int l = -1; l <= 1; l++)
+        {
+            for (int k = -2; k <= 2; k++, s++)
+            {
+                v.shiftvec[3 * s + 0] = k * sys->box[0];
+                v.shiftvec[3 * s + 1] = l * sys->box[1];
+                v.shiftvec[3 * s + 2] = m * sys->box[2];
+            }
+        }
+    }
+    // ---- grid dimensions (grid.cpp:103-262, GPU geometry; gmxcalculator.cpp:97) ----
+    GridDims& g = v.g;
+    for (int d = 0; d < 3; d++)
+    {
+        g.box[d] = sys->box[d];
+    }
+    const float det     = sys->box[0] * (sys->box[1] * sys->box[2]);
+    const float density = (float)n / det;
+    if (n > kSc)
+    {
+        const float tlen = cbrtf((float)kCl / density);
+        g.ncx            = std::max(1, (int)(sys->box[0] / (tlen * 2)));
+        g.ncy            = std::max(1, (int)(sys->box[1] / (tlen * 2)));
+    }
+    else
+    {
+        g.ncx = g.ncy = 1;
+    }
+    g.cs[0]          = sys->box[0] / g.ncx;
+    g.cs[1]          = sys->box[1] / g.ncy;
+    g.ics[0]         = 1 / g.cs[0];
+    g.ics[1]         = 1 / g.cs[1];
+    g.ncol           = g.ncx * g.ncy;
+    g.cells_capacity = n / kSc + g.ncol;
+    // ---- bounding-box-only distance (pairlist.cpp:2841-2878) ----
+    {
+        float  bbx = (float)(0.5 * (g.cs[0] + g.cs[0]));
+        float  bby = (float)(0.5 * (g.cs[1] + g.cs[1]));
+        bbx /= 2;
+        bby /= 2;
+        double r    = (double)opts.rlist - 0.5 * (double)sqrtf(bbx * bbx + bby * bby);
+        float  rbb  = (float)(r > 0.0 ? r : 0.0);
+        v.rbb2      = rbb * rbb;
+    }
+    // ---- nbfp with the dummy type (atomdata.cpp:498-530) ----
+    const int         nt1 = sys->num_types + 1;
+    v.ntypes1         = nt1;
+    std::vector<float2> nbfp((size_t)nt1 * nt1, make_float2(0.0f, 0.0f));
+    for (int i = 0; i < sys->num_types; i++)
+    {
+        for (int j = 0; j < sys->num_types; j++)
+        {
+            nbfp[i * nt1 + j] = make_float2(sys->nbfp[(i * sys->num_types + j) * 2],
+                                            sys->nbfp[(i * sys->num_types + j) * 2 + 1]);
+        }
+    }
+
+    // ---- device memory ----
+    const size_t npad = (size_t)g.cells_capacity * kSc;
+    const int    nexcl = sys->excl_index[n];
+    float*  q = nullptr;
+    int*    t = nullptr;
+    int*    ei = nullptr;
+    int*    el = nullptr;
+    float2* nb = nullptr;
+    if (e == cudaSuccess) e = dalloc(h, &q, n);
+    if (e == cudaSuccess) e = dalloc(h, &t, n);
+    if (e == cudaSuccess) e = dalloc(h, &ei, n + 1);
+    if (e == cudaSuccess) e = dalloc(h, &el, nexcl + 1);
+    if (e == cudaSuccess) e = dalloc(h, &nb, (size_t)nt1 * nt1);
+    if (e == cudaSuccess) e = dalloc(h, &v.xin, 3 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(h, &v.col, n);
+    if (e == cudaSuccess) e = dalloc(h, &v.image, n);
+    if (e == cudaSuccess) e = dalloc(h, &v.cxy_na, g.ncol + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.cxy_ind, g.ncol + 2);
+    if (e == cudaSuccess) e = dalloc(h, &v.cxy_fill, g.ncol + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.atom_indices, npad);
+    if (e == cudaSuccess) e = dalloc(h, &v.cells, n);
+    if (e == cudaSuccess) e = dalloc(h, &v.xq, npad);
+    if (e == cudaSuccess) e = dalloc(h, &v.tgrid, npad);
+    if (e == cudaSuccess) e = dalloc(h, &v.bb, (size_t)g.cells_capacity * kNcl * 2);
+    if (e == cudaSuccess) e = dalloc(h, &v.bbcz, g.cells_capacity);
+    if (e == cudaSuccess) e = dalloc(h, &v.nclusters, g.cells_capacity);
+    if (e == cudaSuccess) e = dalloc(h, &v.sci_count, g.cells_capacity + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.cj4_count, g.cells_capacity + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.sci_offset, g.cells_capacity + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.cj4_offset, g.cells_capacity + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.fnb, npad);
+    if (e == cudaSuccess) e = dalloc(h, &v.energy, 2);
+    if (e == cudaSuccess) e = dalloc(h, &v.fshift, kNShift * 3);
+    if (e == cudaSuccess) e = dalloc(h, &v.virial, 9);
+    if (e == cudaSuccess) e = dalloc(h, &v.hdr, 1);
+    if (e == cudaSuccess) e = dalloc(h, &h->d_x, 3 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(h, &h->d_f, 3 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(h, &h->d_out, 11);
+    if (e == cudaSuccess) e = dalloc(h, &h->d_count, 1);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_hdr, sizeof(ListHeader));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(q, sys->q, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t, sys->type, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ei, sys->excl_index, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && nexcl > 0) e = cudaMemcpyAsync(el, sys->excl_list, sizeof(int) * nexcl, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nb, nbfp.data(), sizeof(float2) * nbfp.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(v.hdr, 0, sizeof(ListHeader), h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_x, sys->x, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    v.q          = q;
+    v.type       = t;
+    v.excl_index = ei;
+    v.excl_list  = el;
+    v.nbfp       = nb;
+    int rc_ = cuda_check(h, e, "nbx_create");
+    if (rc_ == NBX_OK)
+    {
+        h->use_prune = opts.nstlist_prune > 0;
+        h->nparts    = h->use_prune ? std::max(1, opts.nstlist_prune / 2) : 1;
+        // SimulationState wraps the coordinates once (simulationstate.cpp:88), then the list is built
+        rc_ = search_sync(h, h->d_x, 0);
+    }
+    if (rc_ != NBX_OK)
+    {
+        g_create_error = h->err;
+        nbx_destroy(h);
+        return rc_;
+    }
+    *out = h;
+    return NBX_OK;
+}
+
+int nbx_destroy(nbx_handle* h)
+{
+    if (!h)
+    {
+        return NBX_OK;
+    }
+    cudaSetDevice(h->device);
+    if (h->stream)
+    {
+        cudaStreamSynchronize(h->stream);
+    }
+    for (void* p : h->allocations)
+    {
+        cudaFree(p);
+    }
+    if (h->h_hdr)
+    {
+        cudaFreeHost(h->h_hdr);
+    }
+    for (auto& p : h->ev_pending)
+    {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    for (auto ev : h->ev_pool)
+    {
+        cudaEventDestroy(ev);
+    }
+    if (h->own_stream && h->stream)
+    {
+        cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return NBX_OK;
+}
+
+int nbx_set_stream(nbx_handle* h, void* s)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    if (h->own_stream)
+    {
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream     = static_cast<cudaStream_t>(s);
+    h->own_stream = false;
+    return NBX_OK;
+}
+
+void* nbx_get_stream(nbx_handle* h)
+{
+    return h ? static_cast<void*>(h->stream) : nullptr;
+}
+
+int nbx_update_pairlist(nbx_handle* h, const float* x)
+{
+    if (!h || !x)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaMemcpyAsync(h->d_x, x, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream);
+    int         rc = cuda_check(h, e, "nbx_update_pairlist");
+    return rc != NBX_OK ? rc : search_sync(h, h->d_x, 0);
+}
+
+int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, double* virial)
+{
+    if (!h || !x || !f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->have_list)
+    {
+        return set_error(h, NBX_ERR_STATE, "no pair list");
+    }
+    cudaSetDevice(h->device);
+    const size_t bytes = sizeof(float) * 3 * h->n;
+    cudaError_t  e     = cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream);
+    int          rc    = cuda_check(h, e, "nbx_compute H2D");
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    rc = compute_async(h, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    e = cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
+    double hout[11];
+    if (e == cudaSuccess && (energies || virial))
+    {
+        e = cudaMemcpyAsync(hout, h->d_out, sizeof(hout), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->h_hdr, h->v.hdr, sizeof(ListHeader), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if ((rc = cuda_check(h, e, "nbx_compute D2H")) != NBX_OK)
+    {
+        return rc;
+    }
+    if (energies)
+    {
+        energies[0] = hout[0];
+        energies[1] = hout[1];
+    }
+    if (virial)
+    {
+        std::memcpy(virial, hout + 2, 9 * sizeof(double));
+    }
+    return status_to_error(h, h->h_hdr->status);
+}
+
+int nbx_search_device(nbx_handle* h, const float* d_x)
+{
+    if (!h || !d_x)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    return search_sync(h, const_cast<float*>(d_x), 0);
+}
+
+int nbx_prune_device(nbx_handle* h, int part)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->have_list)
+    {
+        return set_error(h, NBX_ERR_STATE, "no pair list");
+    }
+    cudaSetDevice(h->device);
+    cudaError_t e = (part < 0) ? launch_prune(h->v, 1, 0, 1, h->stream)
+                               : launch_prune(h->v, 0, part % h->nparts, h->nparts, h->stream);
+    h->launches += 1;
+    return cuda_check(h, e, "nbx_prune_device");
+}
+
+int nbx_compute_device(nbx_handle* h, const float* d_x, float* d_f, double* d_e, double* d_vir)
+{
+    if (!h || !d_x || !d_f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->have_list)
+    {
+        return set_error(h, NBX_ERR_STATE, "no pair list");
+    }
+    cudaSetDevice(h->device);
+    return compute_async(h, d_x, d_f, d_e, d_vir);
+}
+
+int nbx_md_step_device(nbx_handle* h, long long step, const float* d_x, float* d_f, double* d_e, double* d_vir)
+{
+    if (!h || !d_x || !d_f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    const int nstlist = std::max(1, h->opts.nstlist);
+    int       rc      = NBX_OK;
+    if (!h->have_list || step % nstlist == 0)
+    {
+        // the search grids the atoms put in the box (mdlib/sim_util.cpp:1316); their
+        // box shifts are kept for the coordinate conversion until the next search
+        rc = search_sync(h, const_cast<float*>(d_x), 0);
+        h->list_step = step;
+        if (rc != NBX_OK)
+        {
+            return rc;
+        }
+    }
+    else if (h->use_prune)
+    {
+        // isDynamicPruningStepGpu (pairlistsets.h:106-114): every second list age, rolling parts
+        const long long age = step - h->list_step;
+        if (age > 0 && age % 2 == 0)
+        {
+            cudaError_t e = launch_prune(h->v, 0, h->prune_part, h->nparts, h->stream);
+            h->prune_part = (h->prune_part + 1) % h->nparts;
+            h->launches += 1;
+            if ((rc = cuda_check(h, e, "rolling prune")) != NBX_OK)
+            {
+                return rc;
+            }
+        }
+    }
+    return compute_async(h, d_x, d_f, d_e, d_vir);
+}
+
+int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double* energies, double* virial)
+{
+    if (!h || !x || !f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    const size_t bytes = sizeof(float) * 3 * h->n;
+    cudaError_t  e     = cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream);
+    int          rc    = cuda_check(h, e, "nbx_md_step H2D");
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    rc = nbx_md_step_device(h, step, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    double hout[11];
+    e = cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && (energies || virial))
+    {
+        e = cudaMemcpyAsync(hout, h->d_out, sizeof(hout), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if ((rc = cuda_check(h, e, "nbx_md_step D2H")) != NBX_OK)
+    {
+        return rc;
+    }
+    if (energies)
+    {
+        energies[0] = hout[0];
+        energies[1] = hout[1];
+    }
+    if (virial)
+    {
+        std::memcpy(virial, hout + 2, 9 * sizeof(double));
+    }
+    return NBX_OK;
+}
+
+int nbx_set_timing(nbx_handle* h, int enable)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    h->timing = enable != 0;
+    return NBX_OK;
+}
+
+int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int reset)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    collect_timings(h, true);
+    if (force_ms)
+    {
+        *force_ms = h->force_ms;
+    }
+    if (counts)
+    {
+        counts[0] = h->force_launches;
+        counts[1] = h->launches;
+    }
+    if (reset)
+    {
+        h->force_ms       = 0.0;
+        h->force_launches = 0;
+        h->launches       = 0;
+    }
+    return NBX_OK;
+}
+
+int nbx_synchronize(nbx_handle* h)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    int rc = read_header(h);
+    return rc != NBX_OK ? rc : status_to_error(h, h->h_hdr->status);
+}
+
+int nbx_get_sizes(nbx_handle* h, int* sizes)
+{
+    if (!h || !sizes)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    int rc = read_header(h);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    sizes[0] = h->n;
+    sizes[1] = h->v.g.ncx;
+    sizes[2] = h->v.g.ncy;
+    sizes[3] = h->h_hdr->num_cells;
+    sizes[4] = h->h_hdr->num_sci;
+    sizes[5] = h->h_hdr->num_cj4;
+    sizes[6] = h->h_hdr->num_excl;
+    sizes[7] = h->h_hdr->num_cells * kSc;
+    return NBX_OK;
+}
+
+int nbx_get_grid(nbx_handle* h, int* atom_indices, int* cells, int* cxy_ind, int* num_clusters, float* bb,
+                 float* bbcz, float* xq)
+{
+    int sizes[8];
+    int rc = nbx_get_sizes(h, sizes);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    const int   nc = sizes[3];
+    cudaStream_t s = h->stream;
+    cudaError_t e  = cudaSuccess;
+    if (atom_indices) e = cudaMemcpyAsync(atom_indices, h->v.atom_indices, sizeof(int) * nc * kSc, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && cells) e = cudaMemcpyAsync(cells, h->v.cells, sizeof(int) * h->n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && cxy_ind) e = cudaMemcpyAsync(cxy_ind, h->v.cxy_ind, sizeof(int) * (h->v.g.ncol + 1), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && num_clusters) e = cudaMemcpyAsync(num_clusters, h->v.nclusters, sizeof(int) * nc, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && bbcz) e = cudaMemcpyAsync(bbcz, h->v.bbcz, sizeof(float2) * nc, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && xq) e = cudaMemcpyAsync(xq, h->v.xq, sizeof(float4) * nc * kSc, cudaMemcpyDeviceToHost, s);
+    std::vector<float4> tmp;
+    if (e == cudaSuccess && bb)
+    {
+        tmp.resize((size_t)nc * kNcl * 2);
+        e = cudaMemcpyAsync(tmp.data(), h->v.bb, sizeof(float4) * tmp.size(), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && bb)
+    {
+        for (size_t c = 0; c < (size_t)nc * kNcl; c++)
+        {
+            bb[6 * c + 0] = tmp[2 * c].x;
+            bb[6 * c + 1] = tmp[2 * c].y;
+            bb[6 * c + 2] = tmp[2 * c].z;
+            bb[6 * c + 3] = tmp[2 * c + 1].x;
+            bb[6 * c + 4] = tmp[2 * c + 1].y;
+            bb[6 * c + 5] = tmp[2 * c + 1].z;
+        }
+    }
+    return cuda_check(h, e, "nbx_get_grid");
+}
+
+int nbx_get_pairlist(nbx_handle* h, int* sci, int* cj4, uint32_t* excl, uint32_t* imask_outer)
+{
+    int sizes[8];
+    int rc = nbx_get_sizes(h, sizes);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    cudaStream_t s = h->stream;
+    cudaError_t  e = cudaSuccess;
+    if (sci) e = cudaMemcpyAsync(sci, h->v.sci, sizeof(Sci) * sizes[4], cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && cj4) e = cudaMemcpyAsync(cj4, h->v.cj4, sizeof(Cj4) * sizes[5], cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && excl) e = cudaMemcpyAsync(excl, h->v.excl, sizeof(Excl) * sizes[6], cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && imask_outer) e = cudaMemcpyAsync(imask_outer, h->v.imask_outer, sizeof(unsigned) * 2 * sizes[5], cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return cuda_check(h, e, "nbx_get_pairlist");
+}
+
+int nbx_get_pair_counts(nbx_handle* h, long long* pairs)
+{
+    if (!h || !pairs)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    unsigned long long c = 0;
+    cudaError_t        e = launch_pair_count(h->v, h->d_count, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&c, h->d_count, sizeof(c), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    pairs[0] = (long long)c;
+    pairs[1] = -1;
+    return cuda_check(h, e, "nbx_get_pair_counts");
+}
+
+int nbx_measure_fp32_peak(int device, double* tflops)
+{
+    if (!tflops)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(device);
+    cudaError_t e = measure_fp32_peak(tflops);
+    return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
+} // extern "C"

@@ -1,0 +1,510 @@
+// Cluster-pair LJ + Ewald real-space (or reaction-field) force / energy kernel.
+//
+// Physics of the reference's GPU-layout kernels
+// (src/gromacs/nbnxm/kernels_reference/kernel_gpu_ref.cpp:57-379 and
+// cuda/nbnxm_cuda_kernel.cuh:148-649): for every set bit of the pair-list
+// mask, the 8x8 atom pairs of an i-cluster / j-cluster within rc interact with
+//   LJ      6*C6, 12*C12 from nbfp, potential-shifted energies,
+//   Ewald   qq*erfc(beta r)/r (exclusions within rc: -qq*erf(beta r)/r),
+//   RF      qq*(1/r + k_rf r^2 - c_rf),
+// and the forces on j are the negated forces on i (half list).
+//
+// GB300 design (not the reference's 8x8-thread blocks):
+//  - persistent warps take list entries from an atomic work queue;
+//  - one warp owns one entry: lane = (j-atom of the half, 0..3) * 8 + i-atom;
+//    the 64 shifted i-atoms (x, y, z, q*epsfac, type row) live in registers,
+//    so i-data is loaded once per entry instead of once per pair;
+//  - the per-(i-cluster, j-cluster) mask test is warp-uniform, the per-pair
+//    cut-off / exclusion / self test is a multiply mask (no divergence);
+//  - erfc(beta r) uses the Abramowitz-Stegun 7.1.26 rational approximation
+//    (|error| <= 1.5e-7) times exp(-beta^2 r^2), which the force also needs;
+//  - j forces are reduced over the 8 i-lanes with shuffles and added with one
+//    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
+//    until the entry ends; shift forces and energies are reduced in FP64.
+#include "nbx_internal.cuh"
+
+namespace nbx
+{
+namespace
+{
+
+constexpr int kForceThreads   = 256;
+constexpr int kForceMinBlocks = 2;
+constexpr int kMaxTypes1      = 64;  // types + dummy held in shared memory
+
+// Abramowitz & Stegun 7.1.26: erfc(x) = t*(a1 + t*(a2 + t*(a3 + t*(a4 + t*a5)))) * exp(-x^2),
+// t = 1/(1 + p x), x >= 0.
+constexpr float kAsP  = 0.3275911f;
+constexpr float kAsA1 = 0.254829592f;
+constexpr float kAsA2 = -0.284496736f;
+constexpr float kAsA3 = 1.421413741f;
+constexpr float kAsA4 = -1.453152027f;
+constexpr float kAsA5 = 1.061405429f;
+
+__device__ __forceinline__ float fast_rcp(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float fast_ex2(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float z)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(0.0f)
+                 : "memory");
+}
+
+template<bool kEnergy, bool kEwald>
+__global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
+{
+    __shared__ float2 nbfp_s[kMaxTypes1 * kMaxTypes1];
+    const int         nt1 = v.ntypes1;
+    for (int k = threadIdx.x; k < nt1 * nt1; k += blockDim.x)
+    {
+        nbfp_s[k] = v.nbfp[k];
+    }
+    __syncthreads();
+    if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    {
+        return;
+    }
+    const unsigned full    = 0xffffffffu;
+    const int      lane    = threadIdx.x & 31;
+    const int      ii      = lane & 7;   // i-atom within the i-cluster
+    const int      jj      = lane >> 3;  // j-atom within the warp half
+    const int      numSci  = v.hdr->num_sci;
+    const float    rc2     = v.rc2;
+    const float    beta    = v.beta;
+    const float    beta2l2 = beta * beta * 1.4426950408889634f;  // beta^2 * log2(e)
+    const float    c2b     = 1.1283791670955126f * beta;           // 2 beta / sqrt(pi)
+    const float    k_rf2   = 2.0f * v.k_rf;
+
+    double e_lj_acc = 0.0, e_el_acc = 0.0;
+    for (;;)
+    {
+        int e = 0;
+        if (lane == 0)
+        {
+            e = atomicAdd(work_counter, 1);
+        }
+        e = __shfl_sync(full, e, 0);
+        if (e >= numSci)
+        {
+            break;
+        }
+        const Sci   s   = v.sci[e];
+        const float shx = v.shiftvec[3 * s.shift], shy = v.shiftvec[3 * s.shift + 1], shz = v.shiftvec[3 * s.shift + 2];
+        const bool  central = (s.shift == kCentral);
+        float       xi[kNcl], yi[kNcl], zi[kNcl], qi[kNcl];
+        int         ti[kNcl];
+        float       fix[kNcl], fiy[kNcl], fiz[kNcl];
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            const int    ai = (s.sci * kNcl + c) * kCl + ii;
+            const float4 x  = v.xq[ai];
+            xi[c]           = x.x + shx;
+            yi[c]           = x.y + shy;
+            zi[c]           = x.z + shz;
+            qi[c]           = x.w * v.epsfac;
+            ti[c]           = v.tgrid[ai] * nt1;
+            fix[c] = fiy[c] = fiz[c] = 0.0f;
+        }
+        float e_lj = 0.0f, e_el = 0.0f;
+        for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
+        {
+            const int4 cjs = *reinterpret_cast<const int4*>(&v.cj4[j4].cj[0]);
+            const int4 ime = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
+#pragma unroll
+            for (int h = 0; h < kSplit; h++)
+            {
+                const unsigned im = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
+                if (!im)
+                {
+                    continue;
+                }
+                const int      exi   = (h == 0) ? ime.y : ime.w;
+                const unsigned wexcl = v.excl[exi].pair[lane];
+#pragma unroll
+                for (int jm = 0; jm < kJg; jm++)
+                {
+                    if (!(im & (0xffu << (jm * kNcl))))
+                    {
+                        continue;
+                    }
+                    const int    cj = (jm == 0) ? cjs.x : (jm == 1) ? cjs.y : (jm == 2) ? cjs.z : cjs.w;
+                    const int    aj = cj * kCl + h * (kCl / kSplit) + jj;
+                    const float4 xj = v.xq[aj];
+                    const int    tj = v.tgrid[aj];
+                    float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < kNcl; c++)
+                    {
+                        const unsigned bit = 1u << (jm * kNcl + c);
+                        if (!(im & bit))
+                        {
+                            continue;
+                        }
+                        const float dx = xi[c] - xj.x;
+                        const float dy = yi[c] - xj.y;
+                        const float dz = zi[c] - xj.z;
+                        float       r2 = dx * dx + dy * dy + dz * dz;
+                        // the diagonal cluster pair counts j > i only (kernel_gpu_ref.cpp:242)
+                        const bool self_lower = central && (s.sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
+                        const float mask     = (r2 < rc2 && !self_lower) ? 1.0f : 0.0f;
+                        const float int_bit  = (wexcl & bit) ? 1.0f : 0.0f;
+                        r2                   = fmaxf(r2, kMinDist2);
+                        const float rinv     = rsqrtf(r2);
+                        const float rinv2    = rinv * rinv;
+                        const float2 lj      = nbfp_s[ti[c] + tj];
+                        const float rinv6    = int_bit * rinv2 * rinv2 * rinv2;
+                        const float vrep     = lj.y * rinv6 * rinv6;
+                        const float vdisp    = lj.x * rinv6;
+                        float       fscal    = (vrep - vdisp) * rinv2;
+                        const float qq       = qi[c] * xj.w;
+                        float       vc       = 0.0f;
+                        if (kEwald)
+                        {
+                            const float r     = r2 * rinv;
+                            const float br    = beta * r;
+                            const float t     = fast_rcp(1.0f + kAsP * br);
+                            const float poly  = t * (kAsA1 + t * (kAsA2 + t * (kAsA3 + t * (kAsA4 + t * kAsA5))));
+                            const float expm  = fast_ex2(-beta2l2 * r2);
+                            const float erfcv = poly * expm;
+                            // d/dr of erfc(br)/r, with the full 1/r removed for exclusions
+                            fscal += qq * ((erfcv * rinv + c2b * expm) * rinv2 - (1.0f - int_bit) * rinv * rinv2);
+                            if (kEnergy)
+                            {
+                                vc = qq * ((erfcv - (1.0f - int_bit)) * rinv - int_bit * v.sh_ewald);
+                            }
+                        }
+                        else
+                        {
+                            fscal += qq * (int_bit * rinv * rinv2 - k_rf2);
+                            if (kEnergy)
+                            {
+                                vc = qq * (int_bit * rinv + v.k_rf * r2 - v.c_rf);
+                            }
+                        }
+                        fscal *= mask;
+                        if (kEnergy)
+                        {
+                            e_el += mask * vc;
+                            e_lj += mask * ((vrep + int_bit * lj.y * v.cpot12) * (1.0f / 12.0f)
+                                            - (vdisp + int_bit * lj.x * v.cpot6) * (1.0f / 6.0f));
+                        }
+                        const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
+                        fix[c] += tx;
+                        fiy[c] += ty;
+                        fiz[c] += tz;
+                        fjx -= tx;
+                        fjy -= ty;
+                        fjz -= tz;
+                    }
+                    // reduce the j force over the 8 i-lanes
+#pragma unroll
+                    for (int o = 1; o < kCl; o <<= 1)
+                    {
+                        fjx += __shfl_xor_sync(full, fjx, o);
+                        fjy += __shfl_xor_sync(full, fjy, o);
+                        fjz += __shfl_xor_sync(full, fjz, o);
+                    }
+                    if (ii == 0)
+                    {
+                        red_add_v4(&v.fnb[aj], fjx, fjy, fjz);
+                    }
+                }
+            }
+            if (kEnergy)
+            {
+                e_lj_acc += (double)e_lj;
+                e_el_acc += (double)e_el;
+                e_lj = 0.0f;
+                e_el = 0.0f;
+            }
+        }
+        // i forces: reduce over the 4 j-lanes of each i-atom
+        float sfx = 0.0f, sfy = 0.0f, sfz = 0.0f;
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            float fx = fix[c], fy = fiy[c], fz = fiz[c];
+            fx += __shfl_xor_sync(full, fx, 8);
+            fy += __shfl_xor_sync(full, fy, 8);
+            fz += __shfl_xor_sync(full, fz, 8);
+            fx += __shfl_xor_sync(full, fx, 16);
+            fy += __shfl_xor_sync(full, fy, 16);
+            fz += __shfl_xor_sync(full, fz, 16);
+            if (jj == 0)
+            {
+                red_add_v4(&v.fnb[(s.sci * kNcl + c) * kCl + ii], fx, fy, fz);
+                sfx += fx;
+                sfy += fy;
+                sfz += fz;
+            }
+        }
+        if (!central)
+        {
+            // shift forces for the virial (the central shift vector is zero)
+#pragma unroll
+            for (int o = 1; o < kCl; o <<= 1)
+            {
+                sfx += __shfl_xor_sync(full, sfx, o);
+                sfy += __shfl_xor_sync(full, sfy, o);
+                sfz += __shfl_xor_sync(full, sfz, o);
+            }
+            if (lane == 0)
+            {
+                atomicAdd(&v.fshift[3 * s.shift + 0], (double)sfx);
+                atomicAdd(&v.fshift[3 * s.shift + 1], (double)sfy);
+                atomicAdd(&v.fshift[3 * s.shift + 2], (double)sfz);
+            }
+        }
+    }
+    if (kEnergy)
+    {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            e_lj_acc += __shfl_xor_sync(full, e_lj_acc, o);
+            e_el_acc += __shfl_xor_sync(full, e_el_acc, o);
+        }
+        if (lane == 0)
+        {
+            atomicAdd(&v.energy[0], e_lj_acc);
+            atomicAdd(&v.energy[1], e_el_acc);
+        }
+    }
+}
+
+// f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k in FP64.
+__global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double    w[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+    {
+        w[k] = 0.0;
+    }
+    if (a < v.n)
+    {
+        const int    k  = v.cells[a];
+        const float4 fa = v.fnb[k];
+        f[3 * a]        = fa.x;
+        f[3 * a + 1]    = fa.y;
+        f[3 * a + 2]    = fa.z;
+        if (do_virial)
+        {
+            const float4 xa = v.xq[k];
+            const double xv[3] = { xa.x, xa.y, xa.z };
+            const double fv[3] = { fa.x, fa.y, fa.z };
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+            {
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+                {
+                    w[p * 3 + q] = xv[p] * fv[q];
+                }
+            }
+        }
+    }
+    if (!do_virial)
+    {
+        return;
+    }
+    __shared__ double ws[9][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+    {
+        double t = w[k];
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            t += __shfl_xor_sync(0xffffffffu, t, o);
+        }
+        if (lane == 0)
+        {
+            ws[k][warp] = t;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 9)
+    {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++)
+        {
+            t += ws[threadIdx.x][k];
+        }
+        atomicAdd(&v.virial[threadIdx.x], t);
+    }
+}
+
+// energies += self term; virial = -1/2 (sum x (x) f + sum shift (x) fshift)
+// (mdlib/sim_util.cpp:157-176, calcvir.cpp:103-145).
+__global__ void k_finish(DeviceView v, double* d_energies, double* d_virial)
+{
+    const int t = threadIdx.x;
+    if (d_energies && t < 2)
+    {
+        d_energies[t] = v.energy[t] + (t == 1 ? v.self_energy : 0.0);
+    }
+    if (d_virial && t < 9)
+    {
+        const int p = t / 3, q = t % 3;
+        double    s = v.virial[t];
+        for (int sh = 0; sh < kNShift; sh++)
+        {
+            s += (double)v.shiftvec[3 * sh + p] * v.fshift[3 * sh + q];
+        }
+        d_virial[t] = -0.5 * s;
+    }
+}
+
+__global__ void k_pair_count(DeviceView v, unsigned long long* out)
+{
+    const int          j   = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long cnt = 0;
+    if (j < v.hdr->num_cj4)
+    {
+        cnt = 32ull * (__popc(v.cj4[j].imei[0].imask) + __popc(v.cj4[j].imei[1].imask));
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(out, cnt);
+    }
+}
+
+__global__ void k_fma_probe(float* out, int iters)
+{
+    float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+    float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; i++)
+    {
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+        {
+            a0 = fmaf(a0, m, c);
+            a1 = fmaf(a1, m, c);
+            a2 = fmaf(a2, m, c);
+            a3 = fmaf(a3, m, c);
+            a4 = fmaf(a4, m, c);
+            a5 = fmaf(a5, m, c);
+            a6 = fmaf(a6, m, c);
+            a7 = fmaf(a7, m, c);
+        }
+    }
+    const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.678f)
+    {
+        out[0] = s;
+    }
+}
+
+} // namespace
+
+cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms)
+{
+    if (v.ntypes1 > kMaxTypes1)
+    {
+        return cudaErrorInvalidValue;
+    }
+    int* counter = &v.hdr->work_counter;
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    cudaMemsetAsync(v.fnb, 0, sizeof(float4) * (size_t)v.g.cells_capacity * kSc, s);
+    cudaMemsetAsync(v.fshift, 0, sizeof(double) * kNShift * 3, s);
+    cudaMemsetAsync(v.energy, 0, sizeof(double) * 2, s);
+    const int blocks = num_sms * kForceMinBlocks;
+    const bool ewald = (v.coulomb == 0);
+    if (energy)
+    {
+        if (ewald)
+        {
+            k_force<true, true><<<blocks, kForceThreads, 0, s>>>(v, counter);
+        }
+        else
+        {
+            k_force<true, false><<<blocks, kForceThreads, 0, s>>>(v, counter);
+        }
+    }
+    else
+    {
+        if (ewald)
+        {
+            k_force<false, true><<<blocks, kForceThreads, 0, s>>>(v, counter);
+        }
+        else
+        {
+            k_force<false, false><<<blocks, kForceThreads, 0, s>>>(v, counter);
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* /*d_x*/, bool virial, cudaStream_t s)
+{
+    if (virial)
+    {
+        cudaMemsetAsync(v.virial, 0, sizeof(double) * 9, s);
+    }
+    const int tb = 256;
+    k_reduce_f<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, d_f, virial ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish_energy(const DeviceView& v, double* d_energies, double* d_virial, cudaStream_t s)
+{
+    k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cudaStream_t s)
+{
+    cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), s);
+    k_pair_count<<<(v.cj4_cap + 255) / 256, 256, 0, s>>>(v, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t measure_fp32_peak(double* tflops)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    float* out = nullptr;
+    if (cudaMalloc(&out, sizeof(float)) != cudaSuccess)
+    {
+        return cudaErrorMemoryAllocation;
+    }
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma_probe<<<blocks, threads>>>(out, 64);  // warm-up
+    cudaEventRecord(e0);
+    k_fma_probe<<<blocks, threads>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float       ms  = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    *tflops            = flops / (ms * 1e-3) / 1e12;
+    return err;
+}
+
+} // namespace nbx

@@ -1,0 +1,415 @@
+// Cell gridding on the GPU: the nbnxm GPU ("super-cluster") grid geometry.
+//
+// Follows src/gromacs/nbnxm/grid.cpp and gridset.cpp:
+//   calcColumnIndices (grid.cpp:1173-1268)  -> k_wrap_column
+//   setCellIndices    (grid.cpp:1287-1445)  -> k_column_scan, k_scatter
+//   sortColumnsGpuGeometry + sort_atoms + fillCell (grid.cpp:292-427, 860-986, 1051-1164)
+//                                           -> k_sort_fill
+// The reference's pigeonhole sort (sort_atoms) keeps every run of occupied
+// holes ordered on (coordinate, atom index) and the hole index is monotonic in
+// the coordinate, so its result is the atoms ordered on (coordinate, index),
+// reversed for a backwards sort.  Here that order comes from a bitonic sort
+// (columns, z) and from rank computation inside a warp (32-atom y slabs and
+// 16-atom x halves).  All coordinate arithmetic is plain IEEE single precision
+// (this file is compiled with --fmad=false) so the grid, and therefore the
+// pair list, is bit-identical to the reference's.
+#include "nbx_internal.cuh"
+
+#include <cfloat>
+
+namespace nbx
+{
+namespace
+{
+
+__device__ __forceinline__ void set_status(ListHeader* hdr, unsigned bits)
+{
+    atomicOr(&hdr->status, bits);
+}
+
+// put_atoms_in_box (pbcutil/pbc.cpp:1389-1450, rectangular branch), bounded
+// to 127 box lengths; *k returns the number of box lengths added.
+__device__ __forceinline__ float wrap_coord(float v, float L, ListHeader* hdr, int* k)
+{
+    *k = 0;
+    if (!(v == v))
+    {
+        set_status(hdr, kStatusNaN);
+        return 0.0f;
+    }
+    int it = 0;
+    while (v < 0.0f && it < 128)
+    {
+        v += L;
+        it++;
+        (*k)++;
+    }
+    while (v >= L && it < 128)
+    {
+        v -= L;
+        it++;
+        (*k)--;
+    }
+    if (it >= 128)
+    {
+        set_status(hdr, kStatusWrapLimit);
+        v  = 0.0f;
+        *k = 0;
+    }
+    return v;
+}
+
+__global__ void k_wrap_column(DeviceView v, float* x, int write_back)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n)
+    {
+        return;
+    }
+    float    c[3];
+    unsigned code = 0;
+    for (int d = 0; d < 3; d++)
+    {
+        int k;
+        c[d] = wrap_coord(x[3 * i + d], v.g.box[d], v.hdr, &k);
+        v.xin[3 * i + d] = c[d];
+        code |= ((unsigned)(k & 0xff)) << (8 * d);
+        if (write_back)
+        {
+            x[3 * i + d] = c[d];
+        }
+    }
+    v.image[i] = write_back ? 0 : (int)code;
+    // lower corner is 0, so (x - lower) == x exactly
+    int cx = (int)__fmul_rn(c[0], v.g.ics[0]);
+    int cy = (int)__fmul_rn(c[1], v.g.ics[1]);
+    cx     = min(cx, v.g.ncx - 1);
+    cy     = min(cy, v.g.ncy - 1);
+    const int cxy = cx * v.g.ncy + cy;
+    v.col[i]      = cxy;
+    atomicAdd(&v.cxy_na[cxy], 1);
+}
+
+// Cells per column and their prefix sum (grid.cpp:1300-1330), one block.
+__global__ void k_column_scan(DeviceView v)
+{
+    __shared__ int warp_sums[32];
+    const int      ncol     = v.g.ncol;
+    const int      nthreads = blockDim.x;
+    const int      per      = (ncol + nthreads - 1) / nthreads;
+    const int      c0       = threadIdx.x * per;
+    const int      c1       = min(ncol, c0 + per);
+    int            local    = 0;
+    for (int c = c0; c < c1; c++)
+    {
+        local += (v.cxy_na[c] + kSc - 1) / kSc;
+    }
+    // block exclusive scan of the per-thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int       incl = local;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+        {
+            incl += t;
+        }
+    }
+    if (lane == 31)
+    {
+        warp_sums[warp] = incl;
+    }
+    __syncthreads();
+    if (warp == 0)
+    {
+        int w = (lane < (nthreads >> 5)) ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o)
+            {
+                w += t;
+            }
+        }
+        warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    int run = incl - local + (warp > 0 ? warp_sums[warp - 1] : 0);
+    for (int c = c0; c < c1; c++)
+    {
+        v.cxy_ind[c] = run;
+        run += (v.cxy_na[c] + kSc - 1) / kSc;
+        v.cxy_fill[c] = 0;
+    }
+    if (threadIdx.x == nthreads - 1)
+    {
+        v.cxy_ind[ncol] = run;
+        if (run > v.g.cells_capacity)
+        {
+            set_status(v.hdr, kStatusGridOverflow);
+            v.hdr->num_cells = 0;
+        }
+        else
+        {
+            v.hdr->num_cells = run;
+        }
+    }
+}
+
+__global__ void k_scatter(DeviceView v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.n || v.hdr->num_cells == 0)
+    {
+        return;
+    }
+    const int c    = v.col[i];
+    const int slot = atomicAdd(&v.cxy_fill[c], 1);
+    v.atom_indices[v.cxy_ind[c] * kSc + slot] = i;
+}
+
+// Total order key on (coordinate, atom index), ascending; -0.0 equals +0.0.
+__device__ __forceinline__ unsigned long long sort_key(float f, int a)
+{
+    unsigned u = __float_as_uint(f);
+    if ((u << 1) == 0u)
+    {
+        u = 0u;
+    }
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((unsigned long long)u << 32) | (unsigned)a;
+}
+
+// Block-wide bitonic sort of keys[0..P), P a power of two.
+__device__ void bitonic_sort(unsigned long long* keys, int P)
+{
+    for (int k = 2; k <= P; k <<= 1)
+    {
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+            for (int t = threadIdx.x; t < P; t += blockDim.x)
+            {
+                const int p = t ^ j;
+                if (p > t)
+                {
+                    const unsigned long long a = keys[t], b = keys[p];
+                    const bool up = ((t & k) == 0);
+                    if ((a > b) == up)
+                    {
+                        keys[t] = b;
+                        keys[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Rank of this lane's (coordinate, atom) among the first `cnt` lanes of its
+// group of `gsize` lanes (ascending, or descending when `backwards`).
+__device__ __forceinline__ int group_rank(float c, int a, int cnt, int gsize, bool backwards)
+{
+    const int lane  = threadIdx.x & 31;
+    const int gbase = lane & ~(gsize - 1);
+    int       rank  = 0;
+    for (int m = 0; m < gsize; m++)
+    {
+        const float cm = __shfl_sync(0xffffffffu, c, gbase + m);
+        const int   am = __shfl_sync(0xffffffffu, a, gbase + m);
+        if (m < cnt && (gbase + m) != lane)
+        {
+            const bool before = backwards ? (cm > c || (cm == c && am > a))
+                                          : (cm < c || (cm == c && am < a));
+            rank += before ? 1 : 0;
+        }
+    }
+    return rank;
+}
+
+constexpr int kSortThreads   = 256;
+constexpr int kSmemSortItems = 4096;
+
+// One block per grid column: z sort, per-slab y and x sorts, fill (fillCell).
+__global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsigned long long* scratch)
+{
+    __shared__ unsigned long long skeys[kSmemSortItems];
+    __shared__ int                slab[kSortThreads / 32][32];
+    const int                     cxy = blockIdx.x;
+    if (v.hdr->num_cells == 0)
+    {
+        return;
+    }
+    const int n      = v.cxy_na[cxy];
+    const int cell0  = v.cxy_ind[cxy];
+    const int ncells = v.cxy_ind[cxy + 1] - cell0;
+    const int base   = cell0 * kSc;
+    if (ncells == 0)
+    {
+        return;
+    }
+    int P = 1;
+    while (P < n)
+    {
+        P <<= 1;
+    }
+    unsigned long long* keys = (P <= kSmemSortItems) ? skeys : scratch + 2 * (size_t)base;
+    for (int t = threadIdx.x; t < P; t += blockDim.x)
+    {
+        if (t < n)
+        {
+            const int a = v.atom_indices[base + t];
+            keys[t]     = sort_key(v.xin[3 * a + 2], a);
+        }
+        else
+        {
+            keys[t] = ~0ull;
+        }
+    }
+    __syncthreads();
+    bitonic_sort(keys, P);
+    for (int t = threadIdx.x; t < ncells * kSc; t += blockDim.x)
+    {
+        v.atom_indices[base + t] = (t < n) ? (int)(unsigned)(keys[t] & 0xffffffffu) : -1;
+    }
+    __syncthreads();
+
+    // Cell z bounds and cluster counts, from the z-sorted order (grid.cpp:1090-1108)
+    for (int cz = threadIdx.x; cz < ncells; cz += blockDim.x)
+    {
+        const int numAtoms = min(kSc, n - cz * kSc);
+        const int cell     = cell0 + cz;
+        v.nclusters[cell]  = min(kNcl, (numAtoms + kCl - 1) / kCl);
+        const int aLo      = v.atom_indices[base + cz * kSc];
+        const int aHi      = v.atom_indices[base + cz * kSc + numAtoms - 1];
+        v.bbcz[cell]       = make_float2(v.xin[3 * aLo + 2], v.xin[3 * aHi + 2]);
+    }
+    __syncthreads();
+
+    // 32-atom slabs: y sort (backwards on odd slabs), then x sort per 16-atom half
+    // (backwards on odd halves), then fill the four clusters.
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int sub_z = warp; sub_z < ncells * 2; sub_z += kSortThreads / 32)
+    {
+        const int off  = sub_z * 32;
+        const int nz   = n - off;  // may be <= 0
+        const bool real = lane < nz;
+        int   a        = real ? v.atom_indices[base + off + lane] : -1;
+        float yv       = real ? v.xin[3 * a + 1] : 0.0f;
+        const int ryr  = group_rank(yv, a, nz, 32, (sub_z & 1) != 0);
+        const int ry   = real ? ryr : lane;
+        __syncwarp();
+        slab[warp][ry] = a;
+        __syncwarp();
+        a              = slab[warp][lane];
+        const int half = lane >> 4;
+        const int ny   = min(16, n - (off + half * 16));
+        const bool realy = (lane & 15) < ny;
+        float xv       = realy ? v.xin[3 * a + 0] : 0.0f;
+        const int rxr  = group_rank(xv, a, ny, 16, half != 0);
+        const int rx   = realy ? rxr : (lane & 15);
+        __syncwarp();
+        slab[warp][half * 16 + rx] = a;
+        __syncwarp();
+        a               = slab[warp][lane];
+        const int slot  = base + off + lane;
+        const bool ra   = (off + lane) < n;
+        float4 xq;
+        if (ra)
+        {
+            xq = make_float4(v.xin[3 * a], v.xin[3 * a + 1], v.xin[3 * a + 2], v.q[a]);
+            v.cells[a]  = slot;
+            v.tgrid[slot] = v.type[a];
+        }
+        else
+        {
+            xq            = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+            v.tgrid[slot] = v.ntypes1 - 1;
+            a             = -1;
+        }
+        v.atom_indices[slot] = a;
+        v.xq[slot]           = xq;
+        // cluster bounding boxes over the real atoms (calc_bounding_box_xxxx,
+        // grid.cpp:582-607); a cluster of only fillers takes the filler position
+        float lo[3] = { ra ? xq.x : FLT_MAX, ra ? xq.y : FLT_MAX, ra ? xq.z : FLT_MAX };
+        float hi[3] = { ra ? xq.x : -FLT_MAX, ra ? xq.y : -FLT_MAX, ra ? xq.z : -FLT_MAX };
+        for (int o = 1; o < kCl; o <<= 1)
+        {
+            for (int d = 0; d < 3; d++)
+            {
+                lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+                hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+            }
+        }
+        if ((lane & (kCl - 1)) == 0)
+        {
+            const int cluster_in_col = (off + lane) / kCl;
+            const int cluster        = cell0 * kNcl + cluster_in_col;
+            const int nx             = n - (off + lane);
+            float4    blo, bhi;
+            if (nx <= 0)
+            {
+                blo = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+                bhi = blo;
+            }
+            else
+            {
+                blo = make_float4(lo[0], lo[1], lo[2], 0.0f);
+                bhi = make_float4(hi[0], hi[1], hi[2], 0.0f);
+            }
+            v.bb[2 * cluster]     = blo;
+            v.bb[2 * cluster + 1] = bhi;
+        }
+    }
+}
+
+// nbnxn_atomdata_copy_x_to_nbat_x (atomdata.cpp:1018-1073), plus the box
+// shift each atom received at the last search so that coordinates which left
+// the box since then stay consistent with the grid and the list.
+__global__ void k_convert_x(DeviceView v, const float* __restrict__ x)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const int a = v.atom_indices[k];
+    if (a >= 0)
+    {
+        const float4 old  = v.xq[k];
+        const int    code = v.image[a];
+        float        c[3];
+        for (int d = 0; d < 3; d++)
+        {
+            const int s = (int)(signed char)((code >> (8 * d)) & 0xff);
+            c[d]        = (s == 0) ? x[3 * a + d] : x[3 * a + d] + (float)s * v.g.box[d];
+        }
+        v.xq[k] = make_float4(c[0], c[1], c[2], old.w);
+    }
+}
+
+} // namespace
+
+// The fnb force buffer (cells_capacity*64 float4) doubles as the sort scratch
+// for columns too long for shared memory: a column starting at slot `base`
+// with n atoms needs next_pow2(n) < 2n keys at offset 2*base, which fits.
+cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s)
+{
+    cudaMemsetAsync(v.cxy_na, 0, sizeof(int) * (v.g.ncol + 1), s);
+    const int tb = 256;
+    k_wrap_column<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, d_x, write_back);
+    k_column_scan<<<1, 1024, 0, s>>>(v);
+    k_scatter<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v);
+    k_sort_fill<<<v.g.ncol, kSortThreads, 0, s>>>(v, reinterpret_cast<unsigned long long*>(v.fnb));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s)
+{
+    const int tb    = 256;
+    const int total = v.g.cells_capacity * kSc;
+    k_convert_x<<<(total + tb - 1) / tb, tb, 0, s>>>(v, d_x);
+    return cudaGetLastError();
+}
+
+} // namespace nbx

@@ -1,0 +1,148 @@
+// Internal declarations shared by the nbnxm_gb300 translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace nbx
+{
+
+// Cluster geometry of the GPU pair list (src/gromacs/nbnxm/pairlistparams.h:60-89,
+// pairlist.h:146-171): 8-atom clusters, 8 clusters (2x2x2) per 64-atom cell,
+// j-clusters in groups of 4, each 8x8 cluster pair split in two warp halves.
+constexpr int kCl       = 8;
+constexpr int kNcl      = 8;
+constexpr int kSc       = 64;
+constexpr int kJg       = 4;
+constexpr int kSplit    = 2;
+constexpr int kExclW    = 32;
+constexpr int kNShift   = 45;
+constexpr int kCentral  = 22;
+constexpr float kFarAway = -1000000.0f;         // atomdata.cpp:146
+constexpr float kMinDist2 = 3.82e-07f;          // pairlist.h:146
+
+// Device status word bits (nbx_status values are derived from these on the host).
+enum StatusBits : unsigned
+{
+    kStatusNaN            = 1u << 0,
+    kStatusListOverflow   = 1u << 1,
+    kStatusGridOverflow   = 1u << 2,
+    kStatusWrapLimit      = 1u << 3,
+    kStatusTimeout        = 1u << 4,
+    kStatusExclOverflow   = 1u << 5,
+};
+
+struct Sci
+{
+    int sci, shift, cj4_start, cj4_end;
+};
+
+struct Imei
+{
+    unsigned imask;
+    int      excl_ind;
+};
+
+struct Cj4
+{
+    int  cj[kJg];
+    Imei imei[kSplit];
+};
+
+struct Excl
+{
+    unsigned pair[kExclW];
+};
+
+// Sizes written by device kernels, read back only when needed.
+struct ListHeader
+{
+    int num_cells;       // cells in the current grid
+    int num_sci;         // entries in the list
+    int num_cj4;
+    int num_excl;        // exclusion masks in use (entry 0 = all interacting)
+    int sci_capacity;
+    int cj4_capacity;
+    int excl_capacity;
+    int num_clusters;    // non-empty clusters
+    unsigned status;     // StatusBits
+    int work_counter;    // persistent-kernel work queue head
+    int work_counter2;
+    int pad;
+};
+
+// Grid dimensions, fixed for a handle (box and atom count do not change).
+struct GridDims
+{
+    int   ncx, ncy, ncol;
+    float cs[2], ics[2];
+    float box[3];
+    int   cells_capacity;  // N/64 + ncol (grid.cpp:206-214)
+};
+
+// Everything the device kernels need, passed by value.
+struct DeviceView
+{
+    int        n;
+    GridDims   g;
+    // topology (original order)
+    const float* q;
+    const int*   type;
+    const int*   excl_index;
+    const int*   excl_list;
+    int          ntypes1;  // types + dummy
+    const float2* nbfp;    // ntypes1^2 {6C6, 12C12}
+    // grid
+    float*  xin;           // [3N] wrapped coordinates
+    int*    col;           // [N] column of each atom
+    int*    image;         // [N] box shifts applied by the wrap, 3 signed bytes (x, y, z)
+    int*    cxy_na;        // [ncol]
+    int*    cxy_ind;       // [ncol+1]
+    int*    cxy_fill;      // [ncol]
+    int*    atom_indices;  // [cap*64]
+    int*    cells;         // [N]
+    float4* xq;            // [cap*64]
+    int*    tgrid;         // [cap*64]
+    float4* bb;            // [cap*8*2] lower, upper
+    float2* bbcz;          // [cap]
+    int*    nclusters;     // [cap]
+    // list
+    Sci*      sci;
+    Cj4*      cj4;
+    Excl*     excl;
+    unsigned* imask_outer;  // [2*cj4_cap]
+    int       sci_cap, cj4_cap, excl_cap;
+    int*      sci_count;    // [cap] entries per cell (search count pass)
+    int*      cj4_count;    // [cap] cj4 per cell
+    int*      sci_offset;   // [cap+1]
+    int*      cj4_offset;   // [cap+1]
+    // outputs
+    float4*  fnb;           // [cap*64] grid-order forces
+    double*  energy;        // [2] {LJ, Coulomb}
+    double*  fshift;        // [45*3]
+    double*  virial;        // [9]
+    ListHeader* hdr;
+    // interaction constants
+    float rc2, rlist, rlist2, rbb2, rlist_inner2;
+    float beta, epsfac, k_rf, c_rf, sh_ewald, cpot6, cpot12;
+    int   coulomb;
+    float shiftvec[kNShift * 3];
+    double self_energy;     // Ewald / RF self term, constant for the system
+};
+
+// ---- launchers (one translation unit each) ----
+cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s);
+cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s);
+cudaError_t launch_search(const DeviceView& v, cudaStream_t s);
+cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s);
+cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms);
+cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* d_x, bool virial, cudaStream_t s);
+cudaError_t launch_finish_energy(const DeviceView& v, double* d_energies, double* d_virial, cudaStream_t s);
+cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cudaStream_t s);
+cudaError_t measure_fp32_peak(double* tflops);
+
+// Bounded spin limit for device-side waits (iterations); a wait that runs out
+// sets kStatusTimeout and returns instead of hanging.
+constexpr long long kSpinLimit = 1LL << 24;
+
+} // namespace nbx

@@ -1,0 +1,126 @@
+// Dynamic / rolling pair-list pruning on the GPU.
+//
+// Same masks as the reference's prune-only kernel
+// (src/gromacs/nbnxm/cuda/nbnxm_cuda_kernel_pruneonly.cuh:104-279):
+//  - fresh list: every set (j-cluster, i-cluster, warp-half) bit is re-tested;
+//    it stays in the outer mask if any of its 8x4 atom pairs is within
+//    rlistOuter, and is set in the inner mask (used by the force kernel) if
+//    any pair is within rlistInner;
+//  - rolling pass: only bits in (outer XOR inner) are re-tested and may be
+//    added to the inner mask.
+// One block per list entry, one warp per cj4 (lane = j-atom-in-half * 8 +
+// i-atom), the 64 shifted i-atoms staged in shared memory.  Compiled with
+// --fmad=false: r^2 rounds exactly like the CPU restatement.
+#include "nbx_internal.cuh"
+
+namespace nbx
+{
+namespace
+{
+
+constexpr int kPruneWarps = 4;
+
+__global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fresh, int part, int nparts)
+{
+    __shared__ float4 xib[kSc];
+    const int         numSci = v.hdr->num_sci;
+    if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow))
+    {
+        return;
+    }
+    const float outer2 = v.rlist2;
+    const float inner2 = v.rlist_inner2;
+    const int   lane   = threadIdx.x & 31;
+    const int   warp   = threadIdx.x >> 5;
+    const int   ii     = lane & 7;
+    const int   jj     = lane >> 3;
+    const unsigned full = 0xffffffffu;
+    // entries part, part + nparts, ... (all entries for a fresh list)
+    for (int e = part + blockIdx.x * nparts; e < numSci; e += gridDim.x * nparts)
+    {
+        const Sci   s  = v.sci[e];
+        const float sx = v.shiftvec[3 * s.shift], sy = v.shiftvec[3 * s.shift + 1], sz = v.shiftvec[3 * s.shift + 2];
+        __syncthreads();
+        for (int k = threadIdx.x; k < kSc; k += blockDim.x)
+        {
+            const float4 x = v.xq[s.sci * kSc + k];
+            xib[k]         = make_float4(x.x + sx, x.y + sy, x.z + sz, 0.0f);
+        }
+        __syncthreads();
+        for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
+        {
+            const Cj4 c4 = v.cj4[j4];
+            for (int w = 0; w < kSplit; w++)
+            {
+                unsigned full_m, check, nw;
+                if (fresh)
+                {
+                    full_m = c4.imei[w].imask;
+                    check  = full_m;
+                    nw     = 0u;
+                }
+                else
+                {
+                    full_m = v.imask_outer[2 * j4 + w];
+                    nw     = c4.imei[w].imask;
+                    check  = nw ^ full_m;
+                }
+                if (!check)
+                {
+                    continue;
+                }
+                for (int jm = 0; jm < kJg; jm++)
+                {
+                    if (!(check & (0xffu << (jm * kNcl))))
+                    {
+                        continue;
+                    }
+                    const float4 xj = v.xq[c4.cj[jm] * kCl + w * (kCl / kSplit) + jj];
+#pragma unroll
+                    for (int i = 0; i < kNcl; i++)
+                    {
+                        const unsigned bit = 1u << (jm * kNcl + i);
+                        if (check & bit)
+                        {
+                            const float4 xi = xib[i * kCl + ii];
+                            const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                            const float  r2 = dx * dx + dy * dy + dz * dz;
+                            if (fresh && !__any_sync(full, r2 < outer2))
+                            {
+                                full_m &= ~bit;
+                            }
+                            if (__any_sync(full, r2 < inner2))
+                            {
+                                nw |= bit;
+                            }
+                        }
+                    }
+                }
+                if (lane == 0)
+                {
+                    if (fresh)
+                    {
+                        v.imask_outer[2 * j4 + w] = full_m;
+                    }
+                    v.cj4[j4].imei[w].imask = nw;
+                }
+            }
+        }
+    }
+}
+
+} // namespace
+
+cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s)
+{
+    if (fresh)
+    {
+        part   = 0;
+        nparts = 1;
+    }
+    // enough blocks for ~8 per SM; entries beyond are picked up by the grid-stride loop
+    k_prune<<<152 * 8, 32 * kPruneWarps, 0, s>>>(v, fresh, part, nparts);
+    return cudaGetLastError();
+}
+
+} // namespace nbx

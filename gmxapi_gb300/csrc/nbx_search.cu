@@ -1,0 +1,685 @@
+// Cluster-pair search on the GPU into the nbnxm GPU list layout.
+//
+// Follows nbnxn_make_pairlist_part (src/gromacs/nbnxm/pairlist.cpp:3076-3582)
+// for one grid with full periodicity and a rectangular box, with
+// make_cluster_list_supersub (:1090-1244), get_cell_range (:286-309),
+// boundingbox_only_distance2 (:2841-2878), setSelfAndNewtonExclusionsGpu
+// (:880-904) and setExclusionsForIEntry for GPU lists (:1874-1972).
+//
+// One warp per i-cell (super-cluster).  The warp walks the shifts and the
+// candidate j-columns/cells in exactly the reference's order with the same
+// single-precision arithmetic (this file is compiled with --fmad=false), and
+// evaluates the 8x8 i/j cluster bounding-box distances of a j-cell in one
+// step (2 per lane).  A count pass sizes every cell's entries; after a prefix
+// sum, a write pass emits sci / cj4 entries at fixed offsets and then sets
+// the diagonal and topology exclusion masks.
+#include "nbx_internal.cuh"
+
+namespace nbx
+{
+namespace
+{
+
+constexpr int kWarpsPerBlock  = 4;
+constexpr int kMaxCj4PerEntry = 1024;  // per (i-cell, shift) entry; beyond it the list overflows
+
+__device__ __forceinline__ void set_status(ListHeader* hdr, unsigned bits)
+{
+    atomicOr(&hdr->status, bits);
+}
+
+__device__ __forceinline__ float sq(float x)
+{
+    return x * x;
+}
+
+__device__ __forceinline__ int xyz2is(int x, int y, int z)
+{
+    return 5 * (3 * (z + 1) + y + 1) + x + 2;
+}
+
+// get_cell_range (pairlist.cpp:286-309), lower corner 0.
+__device__ void get_cell_range(float b0, float b1, int numCells, float cellSize, float invCellSize, float d2,
+                               float rlist, int* cf, int* cl)
+{
+    const float listRangeBBToCell2 = rlist * rlist;
+    const float distanceInCells    = (b0 - 0.0f) * invCellSize;
+    int         f                  = max((int)distanceInCells, 0);
+    while (f > 0 && d2 + sq((b0 - 0.0f) - (float)(f - 1 + 1) * cellSize) < listRangeBBToCell2)
+    {
+        f--;
+    }
+    int l = min((int)((b1 - 0.0f) * invCellSize), numCells - 1);
+    while (l < numCells - 1 && d2 + sq((float)(l + 1) * cellSize - (b1 - 0.0f)) < listRangeBBToCell2)
+    {
+        l++;
+    }
+    *cf = f;
+    *cl = l;
+}
+
+// clusterBoundingBoxDistance2 (pairlist.cpp:351-372)
+__device__ __forceinline__ float bb_dist2(const float4 ilo, const float4 ihi, const float4 jlo, const float4 jhi)
+{
+    float dl  = ilo.x - jhi.x;
+    float dh  = jlo.x - ihi.x;
+    float dm  = fmaxf(dl, dh);
+    float dm0 = fmaxf(dm, 0.0f);
+    float d2  = dm0 * dm0;
+    dl        = ilo.y - jhi.y;
+    dh        = jlo.y - ihi.y;
+    dm        = fmaxf(dl, dh);
+    dm0       = fmaxf(dm, 0.0f);
+    d2        = d2 + dm0 * dm0;
+    dl        = ilo.z - jhi.z;
+    dh        = jlo.z - ihi.z;
+    dm        = fmaxf(dl, dh);
+    dm0       = fmaxf(dm, 0.0f);
+    d2        = d2 + dm0 * dm0;
+    return d2;
+}
+
+struct WarpSmem
+{
+    float4   bbi_lo[kNcl], bbi_hi[kNcl];  // shifted i-cluster bounding boxes
+    unsigned need[2 * kMaxCj4PerEntry / 32];  // per (cj4, half): exclusion mask needed
+    int      diag_pos[kNcl];               // list positions of the diagonal j-clusters
+    int      excl_base;
+};
+
+template<bool kWrite>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
+{
+    __shared__ WarpSmem wsm[kWarpsPerBlock];
+    const int           lane = threadIdx.x & 31;
+    const int           wib  = threadIdx.x >> 5;
+    WarpSmem&           sm   = wsm[wib];
+    const int           ci   = blockIdx.x * kWarpsPerBlock + wib;
+    const int           numCells = v.hdr->num_cells;
+    if (ci >= numCells)
+    {
+        return;
+    }
+    const unsigned full = 0xffffffffu;
+    // column of this cell (next_ci, pairlist.cpp:2808-2836)
+    int lo = 0, hi = v.g.ncol - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (v.cxy_ind[mid] <= ci)
+        {
+            lo = mid;
+        }
+        else
+        {
+            hi = mid - 1;
+        }
+    }
+    const int   ci_xy = lo;
+    const int   ci_x  = ci_xy / v.g.ncy;
+    const int   ci_y  = ci_xy - ci_x * v.g.ncy;
+    const float rlist = v.rlist, rlist2 = v.rlist2, rbb2 = v.rbb2;
+    const float listRangeBBToJCell2 = rlist * rlist;
+    const float* box  = v.g.box;
+    const float2 bbcz_i = v.bbcz[ci];
+    const int    ncl_i  = v.nclusters[ci];
+    int          shp_x  = (box[0] < rlist) ? 2 : 1;
+
+    int sci_out = 0, cj4_out = 0;
+    if (kWrite)
+    {
+        sci_out = v.sci_offset[ci];
+        cj4_out = v.cj4_offset[ci];
+        if (v.hdr->status & kStatusListOverflow)
+        {
+            return;
+        }
+    }
+    int num_entries = 0, num_cj4 = 0;
+
+    const float d2cx = 0.0f;
+    for (int tz = -1; tz <= 1; tz++)
+    {
+        const float shz = (float)tz * box[2];
+        const float bz0 = bbcz_i.x + shz;
+        const float bz1 = bbcz_i.y + shz;
+        float       d2z;
+        if (tz == 0)
+        {
+            d2z = 0.0f;
+        }
+        else if (tz < 0)
+        {
+            d2z = sq(bz1);
+        }
+        else
+        {
+            d2z = sq(bz0 - box[2]);
+        }
+        const float d2z_cx = d2z + d2cx;
+        if (d2z_cx >= rlist2)
+        {
+            continue;
+        }
+        float bz1_frac = bz1 / (float)(v.cxy_ind[ci_xy + 1] - v.cxy_ind[ci_xy]);
+        if (bz1_frac < 0.0f)
+        {
+            bz1_frac = 0.0f;
+        }
+        for (int ty = -1; ty <= 1; ty++)
+        {
+            const float shy = (float)ty * box[1] + (float)tz * 0.0f;
+            const float by0 = 0.0f + (float)ci_y * v.g.cs[1] + shy;
+            const float by1 = 0.0f + ((float)ci_y + 1.0f) * v.g.cs[1] + shy;
+            int         cyf, cyl;
+            get_cell_range(by0, by1, v.g.ncy, v.g.cs[1], v.g.ics[1], d2z_cx, rlist, &cyf, &cyl);
+            if (cyf > cyl)
+            {
+                continue;
+            }
+            float d2z_cy = d2z;
+            if (by1 < 0.0f)
+            {
+                d2z_cy = d2z_cy + sq(0.0f - by1);
+            }
+            else if (by0 > box[1])
+            {
+                d2z_cy = d2z_cy + sq(by0 - box[1]);
+            }
+            for (int tx = -shp_x; tx <= shp_x; tx++)
+            {
+                const int shift = xyz2is(tx, ty, tz);
+                if (shift > kCentral)
+                {
+                    continue;  // c_pbcShiftBackward (pairlist.cpp:94)
+                }
+                const bool  excludeSubDiagonal = (shift == kCentral);
+                const float shx = (float)tx * box[0] + (float)ty * 0.0f + (float)tz * 0.0f;
+                const float bx0 = 0.0f + (float)ci_x * v.g.cs[0] + shx;
+                const float bx1 = 0.0f + ((float)ci_x + 1.0f) * v.g.cs[0] + shx;
+                int         cxf, cxl;
+                get_cell_range(bx0, bx1, v.g.ncx, v.g.cs[0], v.g.ics[0], d2z_cy, rlist, &cxf, &cxl);
+                if (cxf > cxl)
+                {
+                    continue;
+                }
+                if (excludeSubDiagonal && cxf < ci_x)
+                {
+                    cxf = ci_x;
+                }
+                // shifted i-cluster bounding boxes (set_icell_bb, pairlist.cpp:2260-2303)
+                if (lane < kNcl)
+                {
+                    const float4 l = v.bb[2 * (ci * kNcl + lane)];
+                    const float4 h = v.bb[2 * (ci * kNcl + lane) + 1];
+                    sm.bbi_lo[lane] = make_float4(l.x + shx, l.y + shy, l.z + shz, 0.0f);
+                    sm.bbi_hi[lane] = make_float4(h.x + shx, h.y + shy, h.z + shz, 0.0f);
+                    sm.diag_pos[lane] = -1;
+                }
+                if (kWrite)
+                {
+                    for (int k = lane; k < 2 * kMaxCj4PerEntry / 32; k += 32)
+                    {
+                        sm.need[k] = 0u;
+                    }
+                }
+                __syncwarp();
+                int nj = 0;  // j-clusters in this entry
+                for (int cx = cxf; cx <= cxl; cx++)
+                {
+                    const float cx_real = (float)cx;
+                    float       d2zx    = d2z;
+                    if (0.0f + cx_real * v.g.cs[0] > bx1)
+                    {
+                        d2zx = d2zx + sq(0.0f + cx_real * v.g.cs[0] - bx1);
+                    }
+                    else if (0.0f + (cx_real + 1.0f) * v.g.cs[0] < bx0)
+                    {
+                        d2zx = d2zx + sq(0.0f + (cx_real + 1.0f) * v.g.cs[0] - bx0);
+                    }
+                    const int cyf_x = (cx == 0 && shift == kCentral && cyf < ci_y) ? ci_y : cyf;
+                    for (int cy = cyf_x; cy <= cyl; cy++)
+                    {
+                        const int   columnStart = v.cxy_ind[cx * v.g.ncy + cy];
+                        const int   columnEnd   = v.cxy_ind[cx * v.g.ncy + cy + 1];
+                        const float cy_real     = (float)cy;
+                        float       d2zxy       = d2zx;
+                        if (0.0f + cy_real * v.g.cs[1] > by1)
+                        {
+                            d2zxy = d2zxy + sq(0.0f + cy_real * v.g.cs[1] - by1);
+                        }
+                        else if (0.0f + (cy_real + 1.0f) * v.g.cs[1] < by0)
+                        {
+                            d2zxy = d2zxy + sq(0.0f + (cy_real + 1.0f) * v.g.cs[1] - by0);
+                        }
+                        if (!(columnStart < columnEnd && d2zxy < listRangeBBToJCell2))
+                        {
+                            continue;
+                        }
+                        int midCell = columnStart + (int)(bz1_frac * (float)(columnEnd - columnStart));
+                        if (midCell >= columnEnd)
+                        {
+                            midCell = columnEnd - 1;
+                        }
+                        const float d2xy = d2zxy - d2z;
+                        int         down = midCell;
+                        while (down >= columnStart)
+                        {
+                            const float u = v.bbcz[down].y;
+                            if (!(u >= bz0 || d2xy + sq(u - bz0) < rlist2))
+                            {
+                                break;
+                            }
+                            down--;
+                        }
+                        int firstCell = down + 1;
+                        int up        = midCell + 1;
+                        while (up < columnEnd)
+                        {
+                            const float l = v.bbcz[up].x;
+                            if (!(l <= bz1 || d2xy + sq(l - bz1) < rlist2))
+                            {
+                                break;
+                            }
+                            up++;
+                        }
+                        const int lastCell = up - 1;
+                        if (shift == kCentral && firstCell < ci)
+                        {
+                            firstCell = ci;
+                        }
+                        for (int scj = firstCell; scj <= lastCell; scj++)
+                        {
+                            // make_cluster_list_supersub for (ci, scj): lane = i-half*32? no:
+                            // lane l handles j-cluster jc = l & 7 against i-clusters l>>3 and (l>>3)+4
+                            const int  ncl_j = v.nclusters[scj];
+                            const int  jc    = lane & 7;
+                            const int  ia    = lane >> 3;
+                            const int  ib    = ia + 4;
+                            const bool diag  = excludeSubDiagonal && (scj == ci);
+                            const int  ci1   = diag ? jc + 1 : ncl_i;
+                            const bool va    = (jc < ncl_j) && (ia < ci1);
+                            const bool vb    = (jc < ncl_j) && (ib < ci1);
+                            float      d2a = 0.0f, d2b = 0.0f;
+                            if (jc < ncl_j)
+                            {
+                                const float4 jlo = v.bb[2 * (scj * kNcl + jc)];
+                                const float4 jhi = v.bb[2 * (scj * kNcl + jc) + 1];
+                                d2a = bb_dist2(sm.bbi_lo[ia], sm.bbi_hi[ia], jlo, jhi);
+                                d2b = bb_dist2(sm.bbi_lo[ib], sm.bbi_hi[ib], jlo, jhi);
+                            }
+                            const unsigned Ba = __ballot_sync(full, va && d2a < rlist2);
+                            const unsigned Bb = __ballot_sync(full, vb && d2b < rlist2);
+                            // 8-bit i-cluster mask of j-cluster jc (valid on every lane)
+                            unsigned im8 = 0;
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                            {
+                                im8 |= ((Ba >> (i * 8 + jc)) & 1u) << i;
+                                im8 |= ((Bb >> (i * 8 + jc)) & 1u) << (i + 4);
+                            }
+                            // a single cluster pair in range: check atom pairs (PRUNE_LIST_CPU_ONE)
+                            for (int j = 0; j < kNcl; j++)
+                            {
+                                const unsigned imj = __shfl_sync(full, im8, j);
+                                if (__popc(imj) != 1)
+                                {
+                                    continue;
+                                }
+                                const int   cl    = __ffs(imj) - 1;
+                                const int   srcl  = (cl & 3) * 8 + j;
+                                const float d2a_s = __shfl_sync(full, d2a, srcl);
+                                const float d2b_s = __shfl_sync(full, d2b, srcl);
+                                const float d2l   = (cl < 4) ? d2a_s : d2b_s;
+                                if (!(d2l >= rbb2))
+                                {
+                                    continue;
+                                }
+                                // clusterpair_in_range (pairlist.cpp:479-606): i atoms shifted
+                                const float4 xi  = v.xq[ci * kSc + cl * kCl + (lane & 7)];
+                                const float  ix  = xi.x + shx, iy = xi.y + shy, iz = xi.z + shz;
+                                const int    csj = scj * kNcl + j;
+                                bool         in  = false;
+#pragma unroll
+                                for (int h = 0; h < 2; h++)
+                                {
+                                    const float4 xj = v.xq[csj * kCl + (lane >> 3) + 4 * h];
+                                    const float  dx = ix - xj.x, dy = iy - xj.y, dz = iz - xj.z;
+                                    const float  r2 = dx * dx + dy * dy + dz * dz;
+                                    in              = in || (r2 < rlist2);
+                                }
+                                if (!__any_sync(full, in) && jc == j)
+                                {
+                                    im8 = 0u;
+                                }
+                            }
+                            const unsigned nz = __ballot_sync(full, lane < kNcl && im8 != 0u);
+                            if (kWrite && lane < kNcl && im8 != 0u)
+                            {
+                                const int pos = nj + __popc(nz & ((1u << lane) - 1u));
+                                if (pos < kMaxCj4PerEntry * kJg)
+                                {
+                                    const int j4  = cj4_out + pos / kJg;
+                                    const int off = pos % kJg;
+                                    v.cj4[j4].cj[off] = scj * kNcl + lane;
+                                    const unsigned bits = im8 << (off * kNcl);
+                                    atomicOr(&v.cj4[j4].imei[0].imask, bits);
+                                    atomicOr(&v.cj4[j4].imei[1].imask, bits);
+                                    if (diag)
+                                    {
+                                        sm.diag_pos[lane] = pos;
+                                        atomicOr(&sm.need[(2 * (pos / kJg)) / 32], 3u << ((2 * (pos / kJg)) % 32));
+                                    }
+                                }
+                            }
+                            nj += __popc(nz);
+                        }
+                    }
+                }
+                if (nj == 0)
+                {
+                    continue;  // closeIEntry drops empty entries
+                }
+                const int ncj4 = (nj + kJg - 1) / kJg;
+                if (ncj4 > kMaxCj4PerEntry)
+                {
+                    if (lane == 0)
+                    {
+                        set_status(v.hdr, kStatusListOverflow);
+                    }
+                    return;
+                }
+                if (kWrite)
+                {
+                    __syncwarp();
+                    __threadfence_block();
+                    if (lane == 0)
+                    {
+                        Sci e;
+                        e.sci       = ci;
+                        e.shift     = shift;
+                        e.cj4_start = cj4_out;
+                        e.cj4_end   = cj4_out + ncj4;
+                        v.sci[sci_out] = e;
+                    }
+                    // --- topology exclusions (setExclusionsForIEntry, GPU list) ---
+                    const int    cjFirst      = v.cj4[cj4_out].cj[0];
+                    const int    cjLast       = v.cj4[cj4_out + (nj - 1) / kJg].cj[(nj - 1) % kJg];
+                    const bool   diagRemoved  = excludeSubDiagonal;
+                    // pass A: flag (cj4, half) pairs that need an exclusion mask
+                    for (int rep = 0; rep < 2; rep++)
+                    {
+                        for (int i = lane; i < kSc; i += 32)
+                        {
+                            const int iIndex = ci * kSc + i;
+                            const int iAtom  = v.atom_indices[iIndex];
+                            if (iAtom < 0)
+                            {
+                                continue;
+                            }
+                            const int iCluster = i / kCl;
+                            for (int k = v.excl_index[iAtom]; k < v.excl_index[iAtom + 1]; k++)
+                            {
+                                const int jAtom = v.excl_list[k];
+                                if (jAtom == iAtom)
+                                {
+                                    continue;
+                                }
+                                const int jIndex = v.cells[jAtom];
+                                if (diagRemoved && jIndex <= ci * kSc + i)
+                                {
+                                    continue;
+                                }
+                                const int jCluster = jIndex / kCl;
+                                if (jCluster < cjFirst || jCluster > cjLast)
+                                {
+                                    continue;
+                                }
+                                // the j-list of an entry is sorted on cluster index
+                                int a = 0, b = nj - 1, index = -1;
+                                while (a <= b)
+                                {
+                                    const int m  = (a + b) >> 1;
+                                    const int cm = v.cj4[cj4_out + m / kJg].cj[m % kJg];
+                                    if (cm == jCluster)
+                                    {
+                                        index = m;
+                                        break;
+                                    }
+                                    if (cm < jCluster)
+                                    {
+                                        a = m + 1;
+                                    }
+                                    else
+                                    {
+                                        b = m - 1;
+                                    }
+                                }
+                                if (index < 0)
+                                {
+                                    continue;
+                                }
+                                const int      j4       = cj4_out + index / kJg;
+                                const unsigned pairMask = 1u << ((index % kJg) * kNcl + iCluster);
+                                if (!(v.cj4[j4].imei[0].imask & pairMask))
+                                {
+                                    continue;
+                                }
+                                const int innerI = i & (kCl - 1);
+                                const int innerJ = jIndex & (kCl - 1);
+                                const int jHalf  = innerJ / (kCl / kSplit);
+                                const int slot   = 2 * (index / kJg) + jHalf;
+                                if (rep == 0)
+                                {
+                                    atomicOr(&sm.need[slot / 32], 1u << (slot % 32));
+                                }
+                                else
+                                {
+                                    const int ei = v.cj4[j4].imei[jHalf].excl_ind;
+                                    atomicAnd(&v.excl[ei].pair[(innerJ & (kCl / kSplit - 1)) * kCl + innerI], ~pairMask);
+                                }
+                            }
+                        }
+                        if (rep == 0)
+                        {
+                            // pass B: allocate the flagged masks, all interacting
+                            __syncwarp();
+                            int nneed = 0;
+                            for (int k = 0; k < (2 * ncj4 + 31) / 32; k++)
+                            {
+                                nneed += __popc(sm.need[k]);
+                            }
+                            int basei = 0;
+                            if (lane == 0)
+                            {
+                                basei = atomicAdd(&v.hdr->num_excl, nneed);
+                            }
+                            basei = __shfl_sync(full, basei, 0);
+                            if (basei + nneed > v.hdr->excl_capacity)
+                            {
+                                if (lane == 0)
+                                {
+                                    set_status(v.hdr, kStatusExclOverflow);
+                                }
+                                return;
+                            }
+                            int run = basei;
+                            for (int k = 0; k < (2 * ncj4 + 31) / 32; k++)
+                            {
+                                unsigned w = sm.need[k];
+                                while (w)
+                                {
+                                    const int b    = __ffs(w) - 1;
+                                    w &= w - 1;
+                                    const int slot = k * 32 + b;
+                                    v.excl[run].pair[lane] = 0xffffffffu;
+                                    if (lane == 0)
+                                    {
+                                        v.cj4[cj4_out + slot / 2].imei[slot % 2].excl_ind = run;
+                                    }
+                                    run++;
+                                }
+                            }
+                            __syncwarp();
+                            __threadfence_block();
+                            // self and Newton exclusions of the diagonal cluster pairs
+                            // (setSelfAndNewtonExclusionsGpu): clear j <= i
+                            for (int dj = 0; dj < kNcl; dj++)
+                            {
+                                const int pos = sm.diag_pos[dj];
+                                if (pos < 0)
+                                {
+                                    continue;
+                                }
+                                const int j4  = cj4_out + pos / kJg;
+                                const int off = pos % kJg;
+                                // lane = (jIndexInPart, i): word jIndexInPart*8 + i
+                                const int jip = lane >> 3, ii = lane & 7;
+                                for (int part = 0; part < kSplit; part++)
+                                {
+                                    const int jOffset = part * (kCl / kSplit);
+                                    if (ii >= jOffset + jip)
+                                    {
+                                        const int ei = v.cj4[j4].imei[part].excl_ind;
+                                        atomicAnd(&v.excl[ei].pair[jip * kCl + ii], ~(1u << (off * kNcl + dj)));
+                                    }
+                                }
+                            }
+                            __syncwarp();
+                        }
+                    }
+                    __syncwarp();
+                }
+                num_entries++;
+                num_cj4 += ncj4;
+                sci_out++;
+                cj4_out += ncj4;
+                __syncwarp();
+            }
+        }
+    }
+    if (!kWrite && lane == 0)
+    {
+        v.sci_count[ci] = num_entries;
+        v.cj4_count[ci] = num_cj4;
+    }
+}
+
+// Exclusive prefix sums of the per-cell entry and cj4 counts, one block.
+__global__ void k_scan_counts(DeviceView v)
+{
+    __shared__ int ws[2][32];
+    const int      n        = v.hdr->num_cells;
+    const int      nthreads = blockDim.x;
+    const int      per      = (n + nthreads - 1) / nthreads;
+    const int      c0       = threadIdx.x * per;
+    const int      c1       = min(n, c0 + per);
+    int            ls = 0, lc = 0;
+    for (int c = c0; c < c1; c++)
+    {
+        ls += v.sci_count[c];
+        lc += v.cj4_count[c];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int       is = ls, ic = lc;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int ts = __shfl_up_sync(0xffffffffu, is, o);
+        const int tc = __shfl_up_sync(0xffffffffu, ic, o);
+        if (lane >= o)
+        {
+            is += ts;
+            ic += tc;
+        }
+    }
+    if (lane == 31)
+    {
+        ws[0][warp] = is;
+        ws[1][warp] = ic;
+    }
+    __syncthreads();
+    if (warp == 0)
+    {
+        int a = (lane < (nthreads >> 5)) ? ws[0][lane] : 0;
+        int b = (lane < (nthreads >> 5)) ? ws[1][lane] : 0;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int ta = __shfl_up_sync(0xffffffffu, a, o);
+            const int tb = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= o)
+            {
+                a += ta;
+                b += tb;
+            }
+        }
+        ws[0][lane] = a;
+        ws[1][lane] = b;
+    }
+    __syncthreads();
+    int rs = is - ls + (warp > 0 ? ws[0][warp - 1] : 0);
+    int rc = ic - lc + (warp > 0 ? ws[1][warp - 1] : 0);
+    for (int c = c0; c < c1; c++)
+    {
+        v.sci_offset[c] = rs;
+        v.cj4_offset[c] = rc;
+        rs += v.sci_count[c];
+        rc += v.cj4_count[c];
+    }
+    if (threadIdx.x == nthreads - 1)
+    {
+        v.sci_offset[n] = rs;
+        v.cj4_offset[n] = rc;
+        v.hdr->num_sci  = rs;
+        v.hdr->num_cj4  = rc;
+        v.hdr->num_excl = 1;
+        if (rs > v.hdr->sci_capacity || rc > v.hdr->cj4_capacity)
+        {
+            set_status(v.hdr, kStatusListOverflow);
+        }
+    }
+}
+
+// The fresh list's masks are also the outer masks until a prune refines them.
+__global__ void k_copy_outer(DeviceView v)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= v.hdr->num_cj4 || (v.hdr->status & kStatusListOverflow))
+    {
+        return;
+    }
+    v.imask_outer[2 * j]     = v.cj4[j].imei[0].imask;
+    v.imask_outer[2 * j + 1] = v.cj4[j].imei[1].imask;
+}
+
+} // namespace
+
+// count -> prefix sum | memset -> write (+ outer-mask copy).  All sizes stay
+// on the device; the host reads them between the two halves only when the
+// list capacity has to be checked.
+cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s)
+{
+    const int cap    = v.g.cells_capacity;
+    const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    k_search<false><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
+    k_scan_counts<<<1, 1024, 0, s>>>(v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s)
+{
+    const int cap    = v.g.cells_capacity;
+    const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    // cj4 entries are filled with atomicOr: start from zero (no bits, excl_ind 0)
+    cudaMemsetAsync(v.cj4, 0, sizeof(Cj4) * (size_t)v.cj4_cap, s);
+    k_search<true><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
+    k_copy_outer<<<(v.cj4_cap + 255) / 256, 256, 0, s>>>(v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search(const DeviceView& v, cudaStream_t s)
+{
+    cudaError_t e = launch_search_count(v, s);
+    return e == cudaSuccess ? launch_search_write(v, s) : e;
+}
+
+} // namespace nbx

@@ -1,0 +1,151 @@
+/*
+ * nbnxm_gb300 -- C ABI of the GB300 (sm_103a) short-range nonbonded engine.
+ *
+ * This is the drop-in boundary for the GROMACS nbnxm path that nblib's
+ * ForceCalculator drives:
+ *   cell gridding -> cluster-pair search (GPU 8x8x8 layout) -> rolling
+ *   prune -> cluster-pair LJ + Ewald real-space force / energy / virial.
+ * Plain pointers and sizes only; no C++ or torch types.  Every call returns
+ * an nbx_status; nbx_last_error() describes the last failure of a handle.
+ *
+ * Coordinate / force arrays are float[3*N] in the caller's atom order.
+ * Energies are double[2] = {LJ, Coulomb} in kJ/mol; the virial is
+ * double[9] (row-major 3x3, kJ/mol), both reduced in FP64 on the GPU.
+ */
+#ifndef NBNXM_GB300_H
+#define NBNXM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+    NBX_OK                = 0,
+    NBX_ERR_INVALID_INPUT = 1, /* bad sizes/options, NaN coordinates, non-positive box */
+    NBX_ERR_OUT_OF_MEMORY = 2,
+    NBX_ERR_LIST_OVERFLOW = 3, /* a list or grid capacity was exceeded (the call is retried internally once) */
+    NBX_ERR_CUDA          = 4, /* a CUDA runtime error; see nbx_last_error */
+    NBX_ERR_TIMEOUT       = 5, /* a bounded device-side wait gave up */
+    NBX_ERR_NO_DEVICE     = 6,
+    NBX_ERR_STATE         = 7  /* call order: e.g. compute before the first search */
+} nbx_status;
+
+/* Coulomb interaction, same values as nblib::CoulombType (api/nblib/kerneloptions.h:75-81) */
+typedef enum
+{
+    NBX_COULOMB_EWALD  = 0, /* nblib Pme: Ewald real space, beta from ewald_rtol */
+    NBX_COULOMB_CUTOFF = 1, /* nblib Cutoff: reaction field with eps_rf = 1 */
+    NBX_COULOMB_RF     = 2  /* nblib ReactionField with epsilon_rf */
+} nbx_coulomb;
+
+/* The system, as nblib's SimulationState + Topology hold it
+ * (api/nblib/simulationstate.h, api/nblib/topology.h:72-98). */
+typedef struct
+{
+    int          num_atoms;
+    const float* x;          /* [3N] initial coordinates; wrapped into the box like SimulationState */
+    const float* q;          /* [N] charges (e) */
+    const int*   type;       /* [N] particle type index in [0, num_types) */
+    int          num_types;
+    const float* nbfp;       /* [num_types^2 * 2] {6*C6, 12*C12} per type pair (api/nblib/gmxsetup.cpp:143-166) */
+    const int*   excl_index; /* [N+1] CSR offsets of the exclusion lists (gmx::ListOfLists) */
+    const int*   excl_list;  /* [excl_index[N]] excluded atoms (self entries allowed, ignored) */
+    float        box[3];     /* rectangular box edges (nm); triclinic boxes are rejected like nblib */
+} nbx_system_desc;
+
+/* Kernel options, nblib::NBKernelOptions plus the list parameters of
+ * PairlistParams (src/gromacs/nbnxm/pairlistparams.h:115-141). */
+typedef struct
+{
+    int   coulomb;          /* nbx_coulomb */
+    float rcoulomb;         /* interaction cut-off, also rvdw (nm) */
+    float rlist;            /* outer pair-list radius (nm), >= rcoulomb */
+    float rlist_inner;      /* inner radius after dynamic pruning (nm); <= 0: = rlist */
+    float ewald_rtol;       /* erfc(beta*rc) = ewald_rtol; 0 -> 1e-5 like nblib */
+    float epsilon_rf;       /* reaction-field dielectric for NBX_COULOMB_RF */
+    int   use_ewald_shift;  /* 1: shift the Ewald potential to 0 at rc (mdrun); 0: nblib (no shift) */
+    int   nstlist;          /* steps between searches for nbx_md_step_device (>= 1) */
+    int   nstlist_prune;    /* dynamic pruning interval (0 = off); rolling over nstlist_prune/2 parts */
+    int   compute_energy;   /* default energy/virial flag for nbx_compute */
+} nbx_options;
+
+typedef struct nbx_handle nbx_handle;
+
+/* Fills opts with nblib's defaults: Ewald, rc = rlist = 1.0, rtol 1e-5, no dynamic pruning. */
+void nbx_default_options(nbx_options* opts);
+
+/* Replaces nblib::ForceCalculator::ForceCalculator (api/nblib/forcecalculator.cpp:52-55 ->
+ * GmxSetupDirector::setupGmxForceCalculator, api/nblib/gmxsetup.cpp:306-325): copies the
+ * topology to the GPU, sets up the interaction constants, grids the atoms and builds the list. */
+int nbx_create(const nbx_system_desc* sys, const nbx_options* opts, int device, nbx_handle** out);
+int nbx_destroy(nbx_handle* h);
+/* Text of the last error on h (or of the last failed nbx_create when h is NULL). */
+const char* nbx_last_error(const nbx_handle* h);
+
+/* Replaces ForceCalculator::updatePairList (api/nblib/forcecalculator.cpp:62-67 ->
+ * GmxForceCalculator::setParticlesOnGrid, gmxcalculator.cpp:85-103) and, unlike the
+ * reference, also rebuilds the pair list and atom data (which the reference leaves stale).
+ * x: host [3N]. */
+int nbx_update_pairlist(nbx_handle* h, const float* x);
+
+/* Replaces ForceCalculator::compute (api/nblib/forcecalculator.cpp:57-60 ->
+ * GmxForceCalculator::compute, gmxcalculator.cpp:70-83): convertCoordinates ->
+ * nonbonded kernel -> atomdata_add_nbat_f_to_f.  Host arrays; forces are overwritten.
+ * energies (double[2]) and virial (double[9]) may be NULL. */
+int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, double* virial);
+
+/* ---- device-resident interface (pointers into device memory, asynchronous on the handle's stream) ---- */
+int nbx_set_stream(nbx_handle* h, void* cuda_stream);
+void* nbx_get_stream(nbx_handle* h);
+/* nbnxn_put_on_grid + constructPairlist (src/gromacs/nbnxm/nbnxm.cpp:58-74, pairlist.cpp:4247-4262),
+ * followed by the first prune when dynamic pruning is on (cuda/nbnxm_cuda.cu:510-517). */
+int nbx_search_device(nbx_handle* h, const float* d_x);
+/* Rolling prune of part `part` of nstlist_prune/2 parts, or a full prune of a fresh list for part < 0
+ * (nbnxm_cuda_kernel_pruneonly.cuh; dispatch prunekerneldispatch.cpp:99-113). */
+int nbx_prune_device(nbx_handle* h, int part);
+/* convertCoordinates + kernel + reduction, into device buffers.  d_energies double[2],
+ * d_virial double[9] may be NULL (then no energy/virial work is done). */
+int nbx_compute_device(nbx_handle* h, const float* d_x, float* d_f, double* d_energies, double* d_virial);
+/* One MD-style step with the reference's schedule: search when step % nstlist == 0, else a
+ * rolling prune on even list ages (pairlistsets.h:106-114), then compute. */
+int nbx_md_step_device(nbx_handle* h, long long step, const float* d_x, float* d_f, double* d_energies,
+                       double* d_virial);
+int nbx_synchronize(nbx_handle* h);
+/* nbx_md_step_device with host arrays (H2D of x and D2H of f / energies / virial inside the call). */
+int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double* energies, double* virial);
+
+/* ---- layout export, for parity checks against the nbnxm layout ---- */
+/* sizes[8] = {num_atoms, ncx, ncy, num_cells, num_sci, num_cj4, num_excl, padded_atoms} */
+int nbx_get_sizes(nbx_handle* h, int* sizes);
+/* Grid: atom_indices[padded] (grid slot -> atom or -1), cells[N] (atom -> slot),
+ * cxy_ind[ncx*ncy+1], num_clusters[num_cells], bb[num_cells*8*6] (lower xyz, upper xyz),
+ * bbcz[num_cells*2], xq[padded*4].  Any pointer may be NULL. */
+int nbx_get_grid(nbx_handle* h, int* atom_indices, int* cells, int* cxy_ind, int* num_clusters, float* bb,
+                 float* bbcz, float* xq);
+/* Pair list in the nbnxm GPU layout (pairlist.h:174-223): sci[4*num_sci] = {sci, shift, cj4_start,
+ * cj4_end}; cj4[8*num_cj4] = {cj[4], imask0, excl_ind0, imask1, excl_ind1}; excl[32*num_excl];
+ * imask_outer[2*num_cj4] (the rlist-pruned masks kept for rolling pruning).  Any pointer may be NULL. */
+int nbx_get_pairlist(nbx_handle* h, int* sci, int* cj4, uint32_t* excl, uint32_t* imask_outer);
+/* Per-pass counters of the last compute: pairs[0] = computed cluster pairs x 64 (all set imask bits),
+ * pairs[1] = pairs inside the cut-off. */
+int nbx_get_pair_counts(nbx_handle* h, long long* pairs);
+
+/* ---- measurement helpers ---- */
+/* enable != 0: record CUDA events around every force-kernel launch on the handle's stream. */
+int nbx_set_timing(nbx_handle* h, int enable);
+/* Since the last reset: force_ms = summed force-kernel event time, counts[0] = force-kernel launches,
+ * counts[1] = all kernels this handle launched.  reset != 0 clears the counters after reading. */
+int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int reset);
+/* Runs an FP32 FMA throughput probe on the device and returns the measured TFLOP/s
+ * (2 flops per FMA); used as the FP32 roofline denominator. */
+int nbx_measure_fp32_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBNXM_GB300_H */

@@ -67,6 +67,7 @@ struct orc_ctx
     int n;
     float box[3];
     float* x; /* in box, N*3 */
+    int*   image; /* N*3 box lengths added by the wrap */
     float* q;
     int* type;
     int ntypes;   /* real types */
@@ -255,6 +256,7 @@ orc_ctx* orc_create(int n, const float* x, const float* box, const float* q, con
         c->box[d] = box[d];
     }
     c->x    = (float*)xmalloc(sizeof(float) * 3 * (size_t)n);
+    c->image = (int*)calloc(3 * (size_t)n, sizeof(int));
     c->q    = (float*)xmalloc(sizeof(float) * (size_t)n);
     c->type = (int*)xmalloc(sizeof(int) * (size_t)n);
     memcpy(c->q, q, sizeof(float) * (size_t)n);
@@ -362,6 +364,7 @@ void orc_destroy(orc_ctx* c)
     }
     free_grid(c);
     free(c->x);
+    free(c->image);
     free(c->q);
     free(c->type);
     free(c->nbfp);
@@ -378,21 +381,26 @@ void orc_destroy(orc_ctx* c)
 
 void orc_set_coordinates(orc_ctx* c, const float* x)
 {
-    /* pbcutil/pbc.cpp:1389-1450 put_atoms_in_box, rectangular branch */
+    /* pbcutil/pbc.cpp:1389-1450 put_atoms_in_box, rectangular branch; the
+     * number of box lengths added is kept for orc_set_x */
     for (int i = 0; i < c->n; i++)
     {
         for (int d = 0; d < 3; d++)
         {
             float v = x[i * 3 + d];
+            int   k = 0;
             while (v < 0)
             {
                 v += c->box[d];
+                k++;
             }
             while (v >= c->box[d])
             {
                 v -= c->box[d];
+                k--;
             }
-            c->x[i * 3 + d] = v;
+            c->x[i * 3 + d]     = v;
+            c->image[i * 3 + d] = k;
         }
     }
 }
@@ -625,8 +633,9 @@ void orc_grid(orc_ctx* c)
 void orc_set_x(orc_ctx* c, const float* x)
 {
     /* atomdata.cpp:1018-1073 nbnxn_atomdata_copy_x_to_nbat_x: real atoms get
-     * their new coordinates, fillers keep FAR_AWAY */
-    orc_set_coordinates(c, x);
+     * the coordinates as given plus the box shift of their last wrap (so a
+     * continuous trajectory stays consistent with the grid), fillers keep
+     * FAR_AWAY */
     const int npad = c->ncells * SC;
     for (int k = 0; k < npad; k++)
     {
@@ -635,7 +644,8 @@ void orc_set_x(orc_ctx* c, const float* x)
         {
             for (int d = 0; d < 3; d++)
             {
-                c->xq[k * 4 + d] = c->x[a * 3 + d];
+                const int s      = c->image[a * 3 + d];
+                c->xq[k * 4 + d] = (s == 0) ? x[a * 3 + d] : x[a * 3 + d] + (float)s * c->box[d];
             }
         }
     }
@@ -1246,8 +1256,23 @@ void orc_prune(orc_ctx* c, int fresh, int part, int nparts)
 
 /* ------------------------------------------------------------ force kernel */
 
+static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy);
+
 /* kernels_reference/kernel_gpu_ref.cpp:57-379 nbnxn_kernel_gpu_ref */
 void orc_force(orc_ctx* c, int computeEnergy)
+{
+    force_range(c, 0, c->nsci, computeEnergy);
+}
+
+/* The same kernel over list entries [e0, e1) only (a bounded sample for timing). */
+void orc_force_entries(orc_ctx* c, int e0, int e1, int computeEnergy)
+{
+    e0 = e0 < 0 ? 0 : e0;
+    e1 = e1 > c->nsci ? c->nsci : e1;
+    force_range(c, e0, e1, computeEnergy);
+}
+
+static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
 {
     const int    npad   = c->ncells * SC;
     const int    bEwald = (c->coulomb == ORC_COULOMB_EWALD);
@@ -1260,7 +1285,7 @@ void orc_force(orc_ctx* c, int computeEnergy)
     memset(c->fnb, 0, sizeof(float) * (size_t)npad * 3);
     memset(c->fshift, 0, sizeof(c->fshift));
     double Vc = 0, Vvdw = 0;
-    for (int e = 0; e < c->nsci; e++)
+    for (int e = e_begin; e < e_end; e++)
     {
         const sci_t* nbln = &c->sci[e];
         const int    ish3 = 3 * nbln->shift;

@@ -56,6 +56,8 @@ void orc_set_x(orc_ctx* c, const float* x);
 void orc_prune(orc_ctx* c, int fresh, int part, int nparts);
 /* Force kernel: kernels_reference/kernel_gpu_ref.cpp nbnxn_kernel_gpu_ref. */
 void orc_force(orc_ctx* c, int compute_energy);
+/* The force kernel over list entries [e0, e1) only (bounded timing samples). */
+void orc_force_entries(orc_ctx* c, int e0, int e1, int compute_energy);
 
 /* Outputs */
 void orc_forces_original_order(const orc_ctx* c, float* f_out); /* N*3 */

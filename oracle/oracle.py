@@ -48,6 +48,7 @@ def lib():
         L.orc_set_x.argtypes = [vp, fp]
         L.orc_prune.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.orc_force.argtypes = [vp, C.c_int]
+        L.orc_force_entries.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.orc_forces_original_order.argtypes = [vp, fp]
         L.orc_virial.argtypes = [vp, fp, fp, dp]
         L.orc_energies.argtypes = [vp, dp]
@@ -144,6 +145,9 @@ class Oracle:
 
     def force(self, energy=True):
         lib().orc_force(self.c, int(energy))
+
+    def force_entries(self, e0, e1, energy=True):
+        lib().orc_force_entries(self.c, int(e0), int(e1), int(energy))
 
     def forces(self):
         f = np.empty((self.system.n, 3), dtype=np.float32)

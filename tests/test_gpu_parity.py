@@ -1,0 +1,191 @@
+"""CUDA path vs the CPU oracle, through the C ABI (needs a GB300).
+
+Bars (from the path's specification):
+  grid and pair list: bit-exact (lists compared as sorted sets of cluster
+  pairs with their 64-bit atom-pair masks);
+  forces: relative RMS <= 1e-5 against the oracle; energies relative <= 1e-6;
+  every case also reports its error against the FP64 all-pairs sum.
+"""
+import numpy as np
+import pytest
+
+from gmxapi_gb300 import nblib, systems
+from oracle import oracle as O
+from tests.helpers import canonical_pairs, nblib_golden_system, rel_rms
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+ENERGY_RTOL = 1e-6
+
+
+def _pair(s, coulomb=nblib.CoulombType.Pme, rc=0.9, rlist=1.0, rlist_inner=None, prune=0):
+    opts = nblib.NBKernelOptions(coulomb_type=coulomb, pairlist_cutoff=rlist, rcoulomb=rc,
+                                 rlist_inner=rlist_inner, nstlist_prune=prune,
+                                 compute_virial_and_energy=True)
+    calc = nblib.ForceCalculator(s, opts)
+    o = O.Oracle(s, coulomb=int(coulomb), rc=rc, rlist=rlist, rlist_inner=rlist_inner)
+    o.grid()
+    o.search()
+    return calc, o
+
+
+SYSTEMS = {
+    "water3000": lambda: systems.water_small(),
+    "water900": lambda: systems.spc_water(300, 2.08, seed=5),
+    "water_small_box": lambda: systems.spc_water(170, 1.72, seed=6),  # edge < 2 rlist: multiple images
+    "water_tiny": lambda: systems.spc_water(20, 0.84, seed=7),        # <= 64 atoms: one cell, shp_x = 2
+    "lj_liquid": lambda: systems.lj_liquid(n=1500, ntypes=8, seed=8),
+}
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_grid_bit_exact(name):
+    s = SYSTEMS[name]()
+    calc, o = _pair(s)
+    g = calc.grid()
+    r = o.grid_arrays()
+    assert g["ncx"] == r["ncx"] and g["ncy"] == r["ncy"] and g["ncells"] == r["ncells"]
+    np.testing.assert_array_equal(g["cxy_ind"], r["cxy_ind"])
+    np.testing.assert_array_equal(g["num_clusters"], r["num_clusters"])
+    np.testing.assert_array_equal(g["atom_indices"], r["atom_indices"])
+    np.testing.assert_array_equal(g["cells"], r["cells"])
+    np.testing.assert_array_equal(g["bbcz"], r["bbcz"])
+    np.testing.assert_array_equal(g["xq"], r["xq"])
+    # bounding boxes of the clusters in use
+    used = np.concatenate([np.arange(c * 8, c * 8 + k) for c, k in enumerate(r["num_clusters"])])
+    np.testing.assert_array_equal(g["bb"][used], r["bb"][used])
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_pairlist_bit_exact_as_sorted_sets(name):
+    s = SYSTEMS[name]()
+    calc, o = _pair(s)
+    pg = calc.pairlist()
+    po = o.pairlist()
+    a = canonical_pairs(pg["sci"], pg["cj4"], pg["excl"])
+    b = canonical_pairs(po["sci"], po["cj4"], po["excl"])
+    assert len(a) == len(b)
+    assert np.array_equal(a, b)
+    # same entries (sci, shift) and cj4 count
+    assert sorted(map(tuple, pg["sci"][:, :2])) == sorted(map(tuple, po["sci"][:, :2]))
+    assert len(pg["cj4"]) == len(po["cj4"])
+
+
+@pytest.mark.parametrize("name", ["water3000", "water_small_box"])
+def test_fresh_prune_masks_bit_exact(name):
+    s = SYSTEMS[name]()
+    calc, o = _pair(s, rlist_inner=0.95, prune=10)  # the engine prunes the fresh list at creation
+    o.prune(fresh=True)
+    pg = calc.pairlist()
+    po = o.pairlist()
+    assert np.array_equal(canonical_pairs(pg["sci"], pg["cj4"], pg["excl"]),
+                          canonical_pairs(po["sci"], po["cj4"], po["excl"]))
+    # outer masks, keyed by the canonical list position of each cj4
+    def outer_sets(p):
+        rows = []
+        for sc, sh, c0, c1 in p["sci"]:
+            for j4 in range(c0, c1):
+                rows.append((sc, sh, tuple(p["cj4"][j4][:4]), tuple(p["imask_outer"][j4])))
+        return sorted(rows)
+    assert outer_sets(pg) == outer_sets(po)
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+@pytest.mark.parametrize("coulomb", [nblib.CoulombType.Pme, nblib.CoulombType.ReactionField])
+def test_forces_energies_virial_vs_oracle(name, coulomb):
+    s = SYSTEMS[name]()
+    calc, o = _pair(s, coulomb=coulomb)
+    f = calc.compute(s.x)
+    e = calc.energies
+    vir = calc.virial
+    o.force(True)
+    fo = o.forces()
+    eo = o.energies()
+    assert rel_rms(f, fo) <= FORCE_RTOL
+    for k in range(2):
+        if abs(eo[k]) > 0:
+            assert abs(e[k] - eo[k]) <= ENERGY_RTOL * abs(eo[k]) + 1e-9, (k, e[k], eo[k])
+    g = calc.grid()
+    xin = g["xq"][g["cells"], :3]
+    vo = o.virial(xin, fo)
+    assert np.abs(vir - vo).max() <= 1e-5 * np.abs(vo).max()
+    # error against the FP64 explicit-image sum is reported and bounded
+    f64, e64 = O.fp64_allpairs(s, coulomb=int(coulomb), rc=0.9, beta=o.beta if coulomb == 0 else None)
+    err64 = rel_rms(f, f64)
+    print(f"{name} coulomb={int(coulomb)}: rel RMS vs oracle {rel_rms(f, fo):.2e}, vs FP64 {err64:.2e}")
+    assert err64 <= 1e-5
+
+
+@pytest.mark.parametrize("key", ["argon", "spc_methanol"])
+def test_nblib_golden_forces(key):
+    """The reference's own nblib golden vectors (Cutoff Coulomb, rc = rlist = 1.0)."""
+    s, ref = nblib_golden_system(key)
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Cutoff, pairlist_cutoff=1.0)
+    calc = nblib.ForceCalculator(s, opts)
+    f = calc.compute(s.x)
+    assert rel_rms(f, ref) <= FORCE_RTOL
+    assert np.abs(f - ref).max() <= 5e-5 * np.abs(ref).max()
+
+
+def test_rolling_prune_matches_oracle():
+    s = systems.water_small()
+    calc, o = _pair(s, rlist_inner=0.93, prune=10)
+    o.prune(fresh=True)
+    rng = np.random.default_rng(3)
+    x = s.x.copy()
+    for part in range(5):
+        x = systems.perturb(x, rng, 0.01)
+        calc.compute(x)  # converts x into the grid layout
+        calc.prune_device(part)
+        calc.synchronize()
+        o.set_x(x)
+        o.prune(fresh=False, part=part, nparts=5)
+    pg, po = calc.pairlist(), o.pairlist()
+    assert np.array_equal(canonical_pairs(pg["sci"], pg["cj4"], pg["excl"]),
+                          canonical_pairs(po["sci"], po["cj4"], po["excl"]))
+    f = calc.compute(x)
+    o.force(True)
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+
+
+def test_update_pairlist_after_motion():
+    s = systems.spc_water(300, 2.08, seed=12)
+    calc, o = _pair(s)
+    x = systems.perturb(s.x, np.random.default_rng(1), 0.05)
+    calc.update_pairlist(x)
+    o.set_coordinates(x)
+    o.grid()
+    o.search()
+    pg, po = calc.pairlist(), o.pairlist()
+    assert np.array_equal(canonical_pairs(pg["sci"], pg["cj4"], pg["excl"]),
+                          canonical_pairs(po["sci"], po["cj4"], po["excl"]))
+    f = calc.compute(x)
+    o.set_x(x)
+    o.force(False)
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+
+
+def test_invalid_input_raises():
+    s = systems.spc_water(30, 1.0, seed=1)
+    bad = systems.spc_water(30, 1.0, seed=1)
+    bad.x[3, 1] = np.nan
+    with pytest.raises(nblib.InputException):
+        nblib.ForceCalculator(bad)
+    calc = nblib.ForceCalculator(s)
+    with pytest.raises(nblib.InputException):
+        calc.compute(np.zeros((5, 3), np.float32))
+
+
+def test_repeat_compute_stable_and_changes_after_update():
+    """UpdateChangesForces (api/nblib/tests/nbkernelsystem.cpp:137-185).
+
+    The GPU sums forces with atomics, so repeats agree to rounding, not bitwise."""
+    s, _ = nblib_golden_system("spc_methanol")
+    calc = nblib.ForceCalculator(s, nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Cutoff))
+    f1 = calc.compute(s.x).copy()
+    f2 = calc.compute(s.x)
+    assert rel_rms(f2, f1) < 1e-6
+    x2 = systems.perturb(s.x, np.random.default_rng(0), 0.001)
+    f3 = calc.compute(x2)
+    assert np.all(f3 != f1)
