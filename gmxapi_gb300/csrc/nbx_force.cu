@@ -16,8 +16,16 @@
 //    so i-data is loaded once per entry instead of once per pair;
 //  - the per-(i-cluster, j-cluster) mask test is warp-uniform, the per-pair
 //    cut-off / exclusion / self test is a multiply mask (no divergence);
-//  - erfc(beta r) uses the Abramowitz-Stegun 7.1.26 rational approximation
-//    (|error| <= 1.5e-7) times exp(-beta^2 r^2), which the force also needs;
+//  - erfc(beta r) = t P(t) exp(-beta^2 r^2) with t = 1/(1 + p beta r) and a
+//    degree-7 polynomial P interpolated at set-up for this beta and rc
+//    (relative error ~1e-7 on [0, beta rc]); the exponential is shared with
+//    the force;
+//  - cj4 halves without an exclusion mask take a path with no exclusion or
+//    self-pair logic; energies are accumulated with compensated sums of
+//    q_i (q_j h(r)) (no single rounded q_i q_j per type pair, whose error
+//    would be systematic) and reduced in FP64; excluded pairs' Coulomb
+//    energies are evaluated in FP64 (rigid molecules repeat the same pair
+//    geometry, so their float rounding would not average out);
 //  - j forces are reduced over the 8 i-lanes with shuffles and added with one
 //    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
 //    until the entry ends; shift forces and energies are reduced in FP64.
@@ -31,15 +39,6 @@ namespace
 constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 64;  // types + dummy held in shared memory
-
-// Abramowitz & Stegun 7.1.26: erfc(x) = t*(a1 + t*(a2 + t*(a3 + t*(a4 + t*a5)))) * exp(-x^2),
-// t = 1/(1 + p x), x >= 0.
-constexpr float kAsP  = 0.3275911f;
-constexpr float kAsA1 = 0.254829592f;
-constexpr float kAsA2 = -0.284496736f;
-constexpr float kAsA3 = 1.421413741f;
-constexpr float kAsA4 = -1.453152027f;
-constexpr float kAsA5 = 1.061405429f;
 
 __device__ __forceinline__ float fast_rcp(float x)
 {
@@ -59,6 +58,185 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float
 {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(0.0f)
                  : "memory");
+}
+
+// Compensated (Kahan) accumulation: sum + c carries ~2x float precision.
+__device__ __forceinline__ void kahan_add(float& sum, float& c, float v)
+{
+    const float y = v - c;
+    const float t = sum + y;
+    c             = (t - sum) - y;
+    sum           = t;
+}
+
+// Per-warp state of one list entry.
+struct EntryState
+{
+    float xi[kNcl], yi[kNcl], zi[kNcl], qi[kNcl];
+    int   ti[kNcl];
+    float fix[kNcl], fiy[kNcl], fiz[kNcl];
+    float acc_el, cmp_el;              // sum q_i (q_j h_ij), compensated
+    float acc_lj, cmp_lj;
+    double excl_el;                    // excluded pairs' Coulomb energy (FP64), q_i q_j h
+};
+
+// Coulomb energy of an excluded pair within the cut-off, in FP64 (divided by
+// epsfac): -erf(beta r)/r for Ewald, k_rf r^2 - c_rf for reaction field.
+// Not inlined: it runs for a few lanes of the rare halves with exclusions.
+__device__ __noinline__ double excluded_pair_energy(float dx, float dy, float dz, float beta, float k_rf,
+                                                    float c_rf, int ewald)
+{
+    const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
+    if (ewald)
+    {
+        const double rd = sqrt(r2d);
+        return -erf((double)beta * rd) / rd;
+    }
+    return (double)k_rf * r2d - (double)c_rf;
+}
+
+// All pair interactions of one (cj4, warp half).  kExcl: this half has an
+// exclusion mask (diagonal cluster pair or topology exclusions).  The loop
+// over the 4 j-clusters stays rolled and only the loop over the 8 i-clusters
+// (register-resident i-data) is unrolled, which keeps the kernel inside the
+// instruction cache.
+template<bool kEnergy, bool kEwald, bool kExcl>
+__device__ __forceinline__ void process_half(const DeviceView& v, const float2* __restrict__ nbfp_s,
+                                             EntryState& st, const int cj_lane, unsigned im, unsigned wexcl,
+                                             int h, int sci, bool central, int ii, int jj, float rc2, float beta,
+                                             float beta2l2, float c2b, float k_rf2)
+{
+    const unsigned full = 0xffffffffu;
+#pragma unroll 1
+    for (int jm = 0; jm < kJg; jm++)
+    {
+        const unsigned imj = (im >> (jm * kNcl)) & 0xffu;
+        const int      cj  = __shfl_sync(full, cj_lane, jm);
+        if (!imj)
+        {
+            continue;
+        }
+        const int    aj  = cj * kCl + h * (kCl / kSplit) + jj;
+        const float4 xj  = v.xq[aj];
+        const int    tj  = v.tgrid[aj];
+        const float  qje = xj.w * v.epsfac;
+        const unsigned wj = wexcl >> (jm * kNcl);
+        float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            if (!(imj & (1u << c)))
+            {
+                continue;
+            }
+            const float dx = st.xi[c] - xj.x;
+            const float dy = st.yi[c] - xj.y;
+            const float dz = st.zi[c] - xj.z;
+            float       r2 = dx * dx + dy * dy + dz * dz;
+            float       mask, int_bit;
+            if (kExcl)
+            {
+                // the diagonal cluster pair counts j > i only (kernel_gpu_ref.cpp:242)
+                const bool self_lower = central && (sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
+                mask    = (r2 < rc2 && !self_lower) ? 1.0f : 0.0f;
+                int_bit = (wj & (1u << c)) ? 1.0f : 0.0f;
+            }
+            else
+            {
+                mask    = (r2 < rc2) ? 1.0f : 0.0f;
+                int_bit = 1.0f;
+            }
+            r2         = fmaxf(r2, kMinDist2);
+            float rinv = rsqrtf(r2);
+            if (kEnergy)
+            {
+                // one Newton step: rsqrt.approx -> ~correctly rounded, unbiased for the energy sums
+                rinv = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
+            }
+            const float  rinv2 = rinv * rinv;
+            const float2 lj    = nbfp_s[st.ti[c] + tj];
+            float        rinv6 = rinv2 * rinv2 * rinv2;
+            if (kExcl)
+            {
+                rinv6 *= int_bit;
+            }
+            const float vrep  = lj.y * rinv6 * rinv6;
+            const float vdisp = lj.x * rinv6;
+            float       fscal = (vrep - vdisp) * rinv2;
+            const float qq    = st.qi[c] * qje;
+            float       h_el  = 0.0f;  // q_i q_j h_el is the pair's Coulomb energy / epsfac
+            if (kEwald)
+            {
+                // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
+                const float br   = beta * r2 * rinv;
+                const float t    = fast_rcp(1.0f + v.erfc_p * br);
+                float       poly = v.erfc_c[kErfcTerms - 1];
+#pragma unroll
+                for (int k = kErfcTerms - 2; k >= 0; k--)
+                {
+                    poly = poly * t + v.erfc_c[k];
+                }
+                const float expm  = fast_ex2(-beta2l2 * r2);
+                const float erfcv = t * poly * expm;
+                // -(d/dr)(erfc(beta r)/r)/r; exclusions drop the full 1/r
+                float fc = (erfcv * rinv + c2b * expm) * rinv2;
+                if (kExcl)
+                {
+                    fc -= (1.0f - int_bit) * rinv * rinv2;
+                }
+                fscal += qq * fc;
+                if (kEnergy)
+                {
+                    h_el = erfcv * rinv - v.sh_ewald;
+                }
+            }
+            else
+            {
+                float fc = rinv * rinv2;
+                if (kExcl)
+                {
+                    fc *= int_bit;
+                }
+                fscal += qq * (fc - k_rf2);
+                if (kEnergy)
+                {
+                    h_el = (rinv - v.c_rf) + v.k_rf * r2;
+                }
+            }
+            fscal *= mask;
+            if (kEnergy)
+            {
+                const float w = kExcl ? mask * int_bit : mask;
+                kahan_add(st.acc_el, st.cmp_el, w * st.qi[c] * (xj.w * h_el));
+                kahan_add(st.acc_lj, st.cmp_lj,
+                          w * ((vrep + lj.y * v.cpot12) * (1.0f / 12.0f) - (vdisp + lj.x * v.cpot6) * (1.0f / 6.0f)));
+                if (kExcl && mask != 0.0f && int_bit == 0.0f)
+                {
+                    st.excl_el += (double)st.qi[c] * (double)xj.w
+                                  * excluded_pair_energy(dx, dy, dz, beta, v.k_rf, v.c_rf, kEwald ? 1 : 0);
+                }
+            }
+            const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
+            st.fix[c] += tx;
+            st.fiy[c] += ty;
+            st.fiz[c] += tz;
+            fjx -= tx;
+            fjy -= ty;
+            fjz -= tz;
+        }
+        // reduce the j force over the 8 i-lanes, one vector red per j-atom
+#pragma unroll
+        for (int o = 1; o < kCl; o <<= 1)
+        {
+            fjx += __shfl_xor_sync(full, fjx, o);
+            fjy += __shfl_xor_sync(full, fjy, o);
+            fjz += __shfl_xor_sync(full, fjz, o);
+        }
+        if (ii == 0)
+        {
+            red_add_v4(&v.fnb[aj], fjx, fjy, fjz);
+        }
+    }
 }
 
 template<bool kEnergy, bool kEwald>
@@ -102,132 +280,46 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         const Sci   s   = v.sci[e];
         const float shx = v.shiftvec[3 * s.shift], shy = v.shiftvec[3 * s.shift + 1], shz = v.shiftvec[3 * s.shift + 2];
         const bool  central = (s.shift == kCentral);
-        float       xi[kNcl], yi[kNcl], zi[kNcl], qi[kNcl];
-        int         ti[kNcl];
-        float       fix[kNcl], fiy[kNcl], fiz[kNcl];
+        EntryState  st;
 #pragma unroll
         for (int c = 0; c < kNcl; c++)
         {
             const int    ai = (s.sci * kNcl + c) * kCl + ii;
             const float4 x  = v.xq[ai];
-            xi[c]           = x.x + shx;
-            yi[c]           = x.y + shy;
-            zi[c]           = x.z + shz;
-            qi[c]           = x.w * v.epsfac;
-            ti[c]           = v.tgrid[ai] * nt1;
-            fix[c] = fiy[c] = fiz[c] = 0.0f;
+            st.xi[c]        = x.x + shx;
+            st.yi[c]        = x.y + shy;
+            st.zi[c]        = x.z + shz;
+            st.qi[c]        = x.w;
+            st.ti[c]        = v.tgrid[ai] * nt1;
+            st.fix[c] = st.fiy[c] = st.fiz[c] = 0.0f;
         }
-        float e_lj = 0.0f, e_el = 0.0f;
+        st.acc_el = st.cmp_el = 0.0f;
+        st.acc_lj = st.cmp_lj = 0.0f;
+        st.excl_el = 0.0;
         for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
         {
-            const int4 cjs = *reinterpret_cast<const int4*>(&v.cj4[j4].cj[0]);
-            const int4 ime = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
-#pragma unroll
+            const int4 ime     = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
+            const int  cj_lane = (lane < kJg) ? v.cj4[j4].cj[lane] : 0;
+#pragma unroll 1
             for (int h = 0; h < kSplit; h++)
             {
-                const unsigned im = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
+                const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
+                const int      exi = (h == 0) ? ime.y : ime.w;
                 if (!im)
                 {
                     continue;
                 }
-                const int      exi   = (h == 0) ? ime.y : ime.w;
-                const unsigned wexcl = v.excl[exi].pair[lane];
-#pragma unroll
-                for (int jm = 0; jm < kJg; jm++)
+                if (exi == 0)
                 {
-                    if (!(im & (0xffu << (jm * kNcl))))
-                    {
-                        continue;
-                    }
-                    const int    cj = (jm == 0) ? cjs.x : (jm == 1) ? cjs.y : (jm == 2) ? cjs.z : cjs.w;
-                    const int    aj = cj * kCl + h * (kCl / kSplit) + jj;
-                    const float4 xj = v.xq[aj];
-                    const int    tj = v.tgrid[aj];
-                    float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
-#pragma unroll
-                    for (int c = 0; c < kNcl; c++)
-                    {
-                        const unsigned bit = 1u << (jm * kNcl + c);
-                        if (!(im & bit))
-                        {
-                            continue;
-                        }
-                        const float dx = xi[c] - xj.x;
-                        const float dy = yi[c] - xj.y;
-                        const float dz = zi[c] - xj.z;
-                        float       r2 = dx * dx + dy * dy + dz * dz;
-                        // the diagonal cluster pair counts j > i only (kernel_gpu_ref.cpp:242)
-                        const bool self_lower = central && (s.sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
-                        const float mask     = (r2 < rc2 && !self_lower) ? 1.0f : 0.0f;
-                        const float int_bit  = (wexcl & bit) ? 1.0f : 0.0f;
-                        r2                   = fmaxf(r2, kMinDist2);
-                        const float rinv     = rsqrtf(r2);
-                        const float rinv2    = rinv * rinv;
-                        const float2 lj      = nbfp_s[ti[c] + tj];
-                        const float rinv6    = int_bit * rinv2 * rinv2 * rinv2;
-                        const float vrep     = lj.y * rinv6 * rinv6;
-                        const float vdisp    = lj.x * rinv6;
-                        float       fscal    = (vrep - vdisp) * rinv2;
-                        const float qq       = qi[c] * xj.w;
-                        float       vc       = 0.0f;
-                        if (kEwald)
-                        {
-                            const float r     = r2 * rinv;
-                            const float br    = beta * r;
-                            const float t     = fast_rcp(1.0f + kAsP * br);
-                            const float poly  = t * (kAsA1 + t * (kAsA2 + t * (kAsA3 + t * (kAsA4 + t * kAsA5))));
-                            const float expm  = fast_ex2(-beta2l2 * r2);
-                            const float erfcv = poly * expm;
-                            // d/dr of erfc(br)/r, with the full 1/r removed for exclusions
-                            fscal += qq * ((erfcv * rinv + c2b * expm) * rinv2 - (1.0f - int_bit) * rinv * rinv2);
-                            if (kEnergy)
-                            {
-                                vc = qq * ((erfcv - (1.0f - int_bit)) * rinv - int_bit * v.sh_ewald);
-                            }
-                        }
-                        else
-                        {
-                            fscal += qq * (int_bit * rinv * rinv2 - k_rf2);
-                            if (kEnergy)
-                            {
-                                vc = qq * (int_bit * rinv + v.k_rf * r2 - v.c_rf);
-                            }
-                        }
-                        fscal *= mask;
-                        if (kEnergy)
-                        {
-                            e_el += mask * vc;
-                            e_lj += mask * ((vrep + int_bit * lj.y * v.cpot12) * (1.0f / 12.0f)
-                                            - (vdisp + int_bit * lj.x * v.cpot6) * (1.0f / 6.0f));
-                        }
-                        const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
-                        fix[c] += tx;
-                        fiy[c] += ty;
-                        fiz[c] += tz;
-                        fjx -= tx;
-                        fjy -= ty;
-                        fjz -= tz;
-                    }
-                    // reduce the j force over the 8 i-lanes
-#pragma unroll
-                    for (int o = 1; o < kCl; o <<= 1)
-                    {
-                        fjx += __shfl_xor_sync(full, fjx, o);
-                        fjy += __shfl_xor_sync(full, fjy, o);
-                        fjz += __shfl_xor_sync(full, fjz, o);
-                    }
-                    if (ii == 0)
-                    {
-                        red_add_v4(&v.fnb[aj], fjx, fjy, fjz);
-                    }
+                    process_half<kEnergy, kEwald, false>(v, nbfp_s, st, cj_lane, im, 0u, h, s.sci, central, ii, jj,
+                                                         rc2, beta, beta2l2, c2b, k_rf2);
                 }
-            }
-            if (kEnergy)
-            {
-                e_lj_acc += (double)e_lj;
-                e_el_acc += (double)e_el;
-                e_lj = 0.0f;
-                e_el = 0.0f;
+                else
+                {
+                    const unsigned wexcl = v.excl[exi].pair[lane];
+                    process_half<kEnergy, kEwald, true>(v, nbfp_s, st, cj_lane, im, wexcl, h, s.sci, central, ii,
+                                                        jj, rc2, beta, beta2l2, c2b, k_rf2);
+                }
             }
         }
         // i forces: reduce over the 4 j-lanes of each i-atom
@@ -235,7 +327,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
 #pragma unroll
         for (int c = 0; c < kNcl; c++)
         {
-            float fx = fix[c], fy = fiy[c], fz = fiz[c];
+            float fx = st.fix[c], fy = st.fiy[c], fz = st.fiz[c];
             fx += __shfl_xor_sync(full, fx, 8);
             fy += __shfl_xor_sync(full, fy, 8);
             fz += __shfl_xor_sync(full, fz, 8);
@@ -249,6 +341,11 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
                 sfy += fy;
                 sfz += fz;
             }
+        }
+        if (kEnergy)
+        {
+            e_el_acc += (double)st.acc_el - (double)st.cmp_el + st.excl_el;
+            e_lj_acc += (double)st.acc_lj - (double)st.cmp_lj;
         }
         if (!central)
         {
@@ -279,7 +376,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         if (lane == 0)
         {
             atomicAdd(&v.energy[0], e_lj_acc);
-            atomicAdd(&v.energy[1], e_el_acc);
+            atomicAdd(&v.energy[1], e_el_acc * v.epsfac_d);
         }
     }
 }

@@ -20,6 +20,7 @@ constexpr int kNShift   = 45;
 constexpr int kCentral  = 22;
 constexpr float kFarAway = -1000000.0f;         // atomdata.cpp:146
 constexpr float kMinDist2 = 3.82e-07f;          // pairlist.h:146
+constexpr int kErfcTerms = 8;                    // degree-7 polynomial in t
 
 // Device status word bits (nbx_status values are derived from these on the host).
 enum StatusBits : unsigned
@@ -128,6 +129,10 @@ struct DeviceView
     int   coulomb;
     float shiftvec[kNShift * 3];
     double self_energy;     // Ewald / RF self term, constant for the system
+    double epsfac_d;        // 1/(4 pi eps0) in double for the energy sums
+    // erfc(x) = t * P(t) * exp(-x^2), t = 1/(1 + erfc_p x), fitted on [0, beta*rc] at set-up
+    float erfc_p;
+    float erfc_c[kErfcTerms];
 };
 
 // ---- launchers (one translation unit each) ----

@@ -8,8 +8,12 @@
  *    reference's OpenMP blocking and its GPU load-balancing split
  *    (pairlist.cpp split_sci_entry :2077-2165, sort_sci :3827) only permute
  *    or cut entries, so the list is the same as a sorted set of cluster pairs;
- *  - energies of individual pairs are computed in float exactly as
- *    kernel_gpu_ref.cpp does, but summed in double;
+ *  - energies: the per-pair formulas of kernel_gpu_ref.cpp evaluated in
+ *    double on the float pair geometry (float dx, dy, dz, charges and
+ *    parameters) and summed in double.  In float, the reference's own
+ *    per-pair rounding (e.g. the single rounded qq of every O-H pair of rigid
+ *    water) puts its Coulomb total 1e-6..4e-6 away from the exact sum, above
+ *    the 1e-6 energy bar the GPU kernel is held to;
  *  - the rolling prune covers entry indices part, part+nparts, ... up to the
  *    end of the list (the reference's (nsci-part)/nparts rounds down,
  *    cuda/nbnxm_cuda.cu:640, and can skip up to nparts-1 trailing entries).
@@ -1280,6 +1284,7 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
     const float  rvdw2  = c->rc * c->rc;
     const int    ntype  = c->numTypes;
     const float  facel  = c->epsfac;
+    const double epsfac_d = orc_one_4pi_eps0();
     const float* x      = c->xq;
     const int*   type   = c->tgrid;
     memset(c->fnb, 0, sizeof(float) * (size_t)npad * 3);
@@ -1301,17 +1306,17 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                 for (int ic = 0; ic < CL; ic++)
                 {
                     const int   ia = (sci * NCL + im) * CL + ic;
-                    const float iq = x[ia * 4 + 3];
-                    qsum += (double)(iq * iq);
+                    const double iq = x[ia * 4 + 3];
+                    qsum += iq * iq;
                 }
             }
             if (!bEwald)
             {
-                vctot += qsum * (-(double)facel * 0.5 * (double)c->c_rf);
+                vctot += qsum * (-epsfac_d * 0.5 * (double)c->c_rf);
             }
             else
             {
-                vctot += qsum * (-(double)facel * (double)c->beta * c_1_sqrtpi);
+                vctot += qsum * (-epsfac_d * (double)c->beta * c_1_sqrtpi);
             }
         }
         for (int cj4_ind = nbln->cj4_start; cj4_ind < nbln->cj4_end; cj4_ind++)
@@ -1336,6 +1341,7 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                         const float iy  = shY + x[ia * 4 + 1];
                         const float iz  = shZ + x[ia * 4 + 2];
                         const float iq  = facel * x[ia * 4 + 3];
+                        const float iq_raw = x[ia * 4 + 3];
                         const int   nti = ntype * 2 * type[ia];
                         float       fix = 0, fiy = 0, fiz = 0;
                         for (int jc = 0; jc < CL; jc++)
@@ -1363,15 +1369,11 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                             const float rinv   = 1.0f / sqrtf(rsq);
                             const float rinvsq = rinv * rinv;
                             const float qq     = iq * x[ja * 4 + 3];
-                            float       fscal, vcoul = 0;
+                            float       fscal;
                             if (!bEwald)
                             {
                                 const float krsq = c->k_rf * rsq;
                                 fscal            = qq * (int_bit * rinv - 2 * krsq) * rinvsq;
-                                if (computeEnergy)
-                                {
-                                    vcoul = qq * (int_bit * rinv + krsq - c->c_rf);
-                                }
                             }
                             else
                             {
@@ -1381,10 +1383,6 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                                 const float eps   = rt - (float)n0;
                                 const float fexcl = (1 - eps) * c->tabF[n0] + eps * c->tabF[n0 + 1];
                                 fscal             = qq * (int_bit * rinvsq - fexcl) * rinv;
-                                if (computeEnergy)
-                                {
-                                    vcoul = qq * ((int_bit - erff(c->beta * r)) * rinv - int_bit * c->sh_ewald);
-                                }
                             }
                             if (rsq < rvdw2)
                             {
@@ -1397,9 +1395,26 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                                 fscal += (Vvdw_rep - Vvdw_disp) * rinvsq;
                                 if (computeEnergy)
                                 {
-                                    vctot += vcoul;
-                                    Vvdwtot += (Vvdw_rep + int_bit * c12 * c->cpot_rep) / 12
-                                               - (Vvdw_disp + int_bit * c6 * c->cpot_disp) / 6;
+                                    /* the energy formulas of kernel_gpu_ref.cpp:286-291,327-336,
+                                     * evaluated in double on the float pair geometry */
+                                    const double r2d  = (double)dx * dx + (double)dy * dy + (double)dz * dz;
+                                    const double r2c  = r2d > (double)c_minDist2 ? r2d : (double)c_minDist2;
+                                    const double rd   = sqrt(r2c);
+                                    const double ib   = (double)int_bit;
+                                    const double qqd  = epsfac_d * (double)iq_raw * (double)x[ja * 4 + 3];
+                                    double       vc;
+                                    if (!bEwald)
+                                    {
+                                        vc = qqd * (ib / rd + (double)c->k_rf * r2c - (double)c->c_rf);
+                                    }
+                                    else
+                                    {
+                                        vc = qqd * ((ib - erf((double)c->beta * rd)) / rd - ib * (double)c->sh_ewald);
+                                    }
+                                    const double ir6 = ib / (r2c * r2c * r2c);
+                                    vctot += vc;
+                                    Vvdwtot += ((double)c12 * ir6 * ir6 + ib * (double)c12 * (double)c->cpot_rep) / 12
+                                               - ((double)c6 * ir6 + ib * (double)c6 * (double)c->cpot_disp) / 6;
                                 }
                             }
                             const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;

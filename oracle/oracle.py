@@ -238,11 +238,17 @@ def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
     epsfac = L.orc_one_4pi_eps0()
     if coulomb == COULOMB_CUTOFF:
         epsilon_rf = 1.0
-    if epsilon_rf == 0:
-        k_rf = 1.0 / (2 * rc**3)
+    # the interaction constants are single-precision values in the reference
+    # (gmxsetup.cpp:226-284, rf_util.cpp:54-66): use exactly those
+    f32 = np.float32
+    rcf = f32(rc)
+    eps = f32(epsilon_rf)
+    if eps == 0:
+        k_rf = f32(1) / (f32(2) * rcf * rcf * rcf)
     else:
-        k_rf = (epsilon_rf - 1.0) / (2 * epsilon_rf + 1.0) / rc**3
-    c_rf = 1.0 / rc + k_rf * rc * rc
+        k_rf = (eps - f32(1)) / (f32(2) * eps + f32(1)) / (rcf * rcf * rcf)
+    c_rf = f32(1) / rcf + k_rf * rcf * rcf
+    rc, k_rf, c_rf = float(rcf), float(k_rf), float(c_rf)
     full = subset is None
     sub = np.arange(n, dtype=np.int32) if full else np.ascontiguousarray(subset, dtype=np.int32)
     x, xp = _f(system.x)
