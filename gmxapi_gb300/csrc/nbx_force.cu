@@ -23,9 +23,9 @@
 //  - cj4 halves without an exclusion mask take a path with no exclusion or
 //    self-pair logic; energies are accumulated with compensated sums of
 //    q_i (q_j h(r)) (no single rounded q_i q_j per type pair, whose error
-//    would be systematic) and reduced in FP64; excluded pairs' Coulomb
-//    energies are evaluated in FP64 (rigid molecules repeat the same pair
-//    geometry, so their float rounding would not average out);
+//    would be systematic) and reduced in FP64; the Coulomb energies of
+//    excluded pairs come from k_excl_energy, in FP64 (rigid molecules repeat
+//    the same pair geometry, so their float rounding would not average out);
 //  - j forces are reduced over the 8 i-lanes with shuffles and added with one
 //    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
 //    until the entry ends; shift forces and energies are reduced in FP64.
@@ -77,23 +77,7 @@ struct EntryState
     float fix[kNcl], fiy[kNcl], fiz[kNcl];
     float acc_el, cmp_el;              // sum q_i (q_j h_ij), compensated
     float acc_lj, cmp_lj;
-    double excl_el;                    // excluded pairs' Coulomb energy (FP64), q_i q_j h
 };
-
-// Coulomb energy of an excluded pair within the cut-off, in FP64 (divided by
-// epsfac): -erf(beta r)/r for Ewald, k_rf r^2 - c_rf for reaction field.
-// Not inlined: it runs for a few lanes of the rare halves with exclusions.
-__device__ __noinline__ double excluded_pair_energy(float dx, float dy, float dz, float beta, float k_rf,
-                                                    float c_rf, int ewald)
-{
-    const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
-    if (ewald)
-    {
-        const double rd = sqrt(r2d);
-        return -erf((double)beta * rd) / rd;
-    }
-    return (double)k_rf * r2d - (double)c_rf;
-}
 
 // All pair interactions of one (cj4, warp half).  kExcl: this half has an
 // exclusion mask (diagonal cluster pair or topology exclusions).  The loop
@@ -210,11 +194,6 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
                 kahan_add(st.acc_el, st.cmp_el, w * st.qi[c] * (xj.w * h_el));
                 kahan_add(st.acc_lj, st.cmp_lj,
                           w * ((vrep + lj.y * v.cpot12) * (1.0f / 12.0f) - (vdisp + lj.x * v.cpot6) * (1.0f / 6.0f)));
-                if (kExcl && mask != 0.0f && int_bit == 0.0f)
-                {
-                    st.excl_el += (double)st.qi[c] * (double)xj.w
-                                  * excluded_pair_energy(dx, dy, dz, beta, v.k_rf, v.c_rf, kEwald ? 1 : 0);
-                }
             }
             const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
             st.fix[c] += tx;
@@ -295,7 +274,6 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         }
         st.acc_el = st.cmp_el = 0.0f;
         st.acc_lj = st.cmp_lj = 0.0f;
-        st.excl_el = 0.0;
         for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
         {
             const int4 ime     = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
@@ -344,7 +322,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         }
         if (kEnergy)
         {
-            e_el_acc += (double)st.acc_el - (double)st.cmp_el + st.excl_el;
+            e_el_acc += (double)st.acc_el - (double)st.cmp_el;
             e_lj_acc += (double)st.acc_lj - (double)st.cmp_lj;
         }
         if (!central)
@@ -378,6 +356,70 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
             atomicAdd(&v.energy[0], e_lj_acc);
             atomicAdd(&v.energy[1], e_el_acc * v.epsfac_d);
         }
+    }
+}
+
+// Coulomb energy of the excluded pairs within rc, in FP64, from the exclusion
+// lists: every excluded pair i < j and every periodic image of it with
+// r^2 < rc^2 in the pair kernel's float arithmetic, i.e. exactly the
+// excluded pairs the list-based kernel sees (the half list holds each image
+// pair once).  Ewald: -q_i q_j erf(beta r)/r; RF: q_i q_j (k_rf r^2 - c_rf)
+// (kernel_gpu_ref.cpp:259-291 with int_bit = 0).  Energies only.
+__global__ void k_excl_energy(DeviceView v)
+{
+    const int i   = blockIdx.x * blockDim.x + threadIdx.x;
+    double    acc = 0.0;
+    if (i < v.n)
+    {
+        const float4 xi  = v.xq[v.cells[i]];
+        const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
+        for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
+        {
+            const int j = v.excl_list[k];
+            if (j <= i)
+            {
+                continue;
+            }
+            const float4 xj = v.xq[v.cells[j]];
+            for (int tz = -1; tz <= 1; tz++)
+            {
+                for (int ty = -1; ty <= 1; ty++)
+                {
+                    for (int tx = -nx; tx <= nx; tx++)
+                    {
+                        const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
+                        const float dx = (xi.x + v.shiftvec[3 * s]) - xj.x;
+                        const float dy = (xi.y + v.shiftvec[3 * s + 1]) - xj.y;
+                        const float dz = (xi.z + v.shiftvec[3 * s + 2]) - xj.z;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (!(r2 < v.rc2))
+                        {
+                            continue;
+                        }
+                        const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
+                        double       h;
+                        if (v.coulomb == 0)
+                        {
+                            const double rd = sqrt(r2d);
+                            h               = -erf((double)v.beta * rd) / rd;
+                        }
+                        else
+                        {
+                            h = (double)v.k_rf * r2d - (double)v.c_rf;
+                        }
+                        acc += (double)xi.w * (double)xj.w * h;
+                    }
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    }
+    if ((threadIdx.x & 31) == 0 && acc != 0.0)
+    {
+        atomicAdd(&v.energy[1], acc * v.epsfac_d);
     }
 }
 
@@ -526,6 +568,10 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     cudaMemsetAsync(v.energy, 0, sizeof(double) * 2, s);
     const int blocks = num_sms * kForceMinBlocks;
     const bool ewald = (v.coulomb == 0);
+    if (energy)
+    {
+        k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
+    }
     if (energy)
     {
         if (ewald)
