@@ -31,7 +31,7 @@ EXPORTED = [
     "nbx_compute", "nbx_set_stream", "nbx_get_stream", "nbx_search_device", "nbx_prune_device",
     "nbx_compute_device", "nbx_md_step_device", "nbx_synchronize", "nbx_get_sizes", "nbx_get_grid",
     "nbx_get_pairlist", "nbx_get_pair_counts", "nbx_measure_fp32_peak", "nbx_md_step",
-    "nbx_set_timing", "nbx_get_timings",
+    "nbx_set_timing", "nbx_get_timings", "nbx_compute_noalloc",
 ]
 
 
@@ -61,6 +61,31 @@ class nbx_options(C.Structure):
         ("nstlist", C.c_int),
         ("nstlist_prune", C.c_int),
         ("compute_energy", C.c_int),
+    ]
+
+
+class nbx_noalloc_args(C.Structure):
+    _fields_ = [
+        ("num_atoms", C.c_int),
+        ("num_slots", C.c_int),
+        ("num_sci", C.c_int),
+        ("xq", C.c_void_p),
+        ("types", C.c_void_p),
+        ("num_types", C.c_int),
+        ("nbfp", C.c_void_p),
+        ("cells", C.c_void_p),
+        ("sci", C.c_void_p),
+        ("cj4", C.c_void_p),
+        ("excl", C.c_void_p),
+        ("excl_index", C.c_void_p),
+        ("excl_list", C.c_void_p),
+        ("box", C.c_float * 3),
+        ("coulomb", C.c_int),
+        ("rcoulomb", C.c_float),
+        ("rlist", C.c_float),
+        ("ewald_rtol", C.c_float),
+        ("epsilon_rf", C.c_float),
+        ("use_ewald_shift", C.c_int),
     ]
 
 
@@ -110,6 +135,7 @@ def load():
     L.nbx_md_step.argtypes = [vp, C.c_longlong, fp, fp, dp, dp]
     L.nbx_set_timing.argtypes = [vp, C.c_int]
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
+    L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream"):

@@ -57,10 +57,8 @@ struct nbx_handle
     long long   launches = 0;
 };
 
-namespace
+namespace nbx
 {
-
-thread_local std::string g_create_error;
 
 double one_4pi_eps0()
 {
@@ -160,6 +158,13 @@ void fit_erfc(double xmax, float* p_out, float* coef)
         coef[k] = (float)mt[k];
     }
 }
+
+} // namespace nbx
+
+namespace
+{
+
+thread_local std::string g_create_error;
 
 int set_error(nbx_handle* h, int code, const std::string& msg)
 {

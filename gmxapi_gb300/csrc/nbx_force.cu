@@ -29,7 +29,10 @@
 //  - j forces are reduced over the 8 i-lanes with shuffles and added with one
 //    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
 //    until the entry ends; shift forces and energies are reduced in FP64.
+#include "../../include/nbnxm_gb300.h"
 #include "nbx_internal.cuh"
+
+#include <mutex>
 
 namespace nbx
 {
@@ -372,6 +375,12 @@ __global__ void k_excl_energy(DeviceView v)
     if (i < v.n)
     {
         const float4 xi  = v.xq[v.cells[i]];
+        if (v.self_on_device)
+        {
+            // self term, kernel_gpu_ref.cpp:154-178 (acc is scaled by epsfac below)
+            acc += (double)xi.w * (double)xi.w
+                   * (v.coulomb == 0 ? -(double)v.beta * 0.56418958354775628695 : -0.5 * (double)v.c_rf);
+        }
         const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
         for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
         {
@@ -526,6 +535,14 @@ __global__ void k_pair_count(DeviceView v, unsigned long long* out)
     }
 }
 
+__global__ void k_noalloc_init(ListHeader* hdr, int num_sci, int num_cells)
+{
+    hdr->num_sci      = num_sci;
+    hdr->num_cells    = num_cells;
+    hdr->status       = 0u;
+    hdr->work_counter = 0;
+}
+
 __global__ void k_fma_probe(float* out, int iters)
 {
     float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
@@ -650,4 +667,192 @@ cudaError_t measure_fp32_peak(double* tflops)
     return err;
 }
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free force evaluation (nbx_compute_noalloc).
+//
+// The scratch this evaluation needs -- the grid-order force accumulator, the
+// FP64 energy / shift-force / virial sums and the work-queue header -- lives
+// in one file-scope device array, so the entry point calls no cudaMalloc,
+// cudaFree or allocating library routine.  That array is a host-side stand-in
+// in host code; its device address is fetched once per device with
+// cudaGetSymbolAddress (see noalloc_scratch_address).  Every call shares it.
+constexpr int    kNoAllocMaxSlots  = 65536;  // grid slots (padded atoms): 1 MiB of float4
+constexpr size_t kNoAllocFnbBytes  = sizeof(float4) * (size_t)kNoAllocMaxSlots;
+constexpr size_t kNoAllocSumsBytes = sizeof(double) * (2 + kNShift * 3 + 9);
+constexpr size_t kNoAllocBytes     = kNoAllocFnbBytes + 256 + kNoAllocSumsBytes + 256 + sizeof(ListHeader);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace
+{
+constexpr int kMaxDevices = 64;
+std::mutex    g_noalloc_mutex;
+void*         g_noalloc_addr[kMaxDevices] = { nullptr };
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device).
+cudaError_t noalloc_scratch_address(unsigned char** out)
+{
+    int         dev = 0;
+    cudaError_t e   = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+    {
+        return e;
+    }
+    if (dev < 0 || dev >= kMaxDevices)
+    {
+        return cudaErrorInvalidDevice;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev])
+    {
+        void* ptr = nullptr;
+        e         = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess)
+        {
+            return e;
+        }
+        g_noalloc_addr[dev] = ptr;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return cudaSuccess;
+}
+} // namespace
+
 } // namespace nbx
+
+extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double* d_energies, double* d_virial,
+                                   void* stream)
+{
+    using namespace nbx;
+    if (!a || !d_f || !a->xq || !a->types || !a->nbfp || !a->cells || !a->sci || !a->cj4 || !a->excl)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (a->num_atoms <= 0 || a->num_slots <= 0 || a->num_sci < 0 || a->num_types <= 0
+        || a->num_types + 1 > kMaxTypes1)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (a->num_slots > kNoAllocMaxSlots)
+    {
+        return NBX_ERR_LIST_OVERFLOW;  // the fixed scratch holds kNoAllocMaxSlots grid slots
+    }
+    const bool energy = (d_energies != nullptr) || (d_virial != nullptr);
+    if (energy && (!a->excl_index || !a->excl_list))
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!(a->rcoulomb > 0.0f) || !(a->rlist >= a->rcoulomb) || a->coulomb < 0 || a->coulomb > 2)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    unsigned char* base = nullptr;
+    if (noalloc_scratch_address(&base) != cudaSuccess)
+    {
+        return NBX_ERR_CUDA;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    DeviceView v{};
+    v.n          = a->num_atoms;
+    v.q          = nullptr;
+    v.type       = nullptr;
+    v.excl_index = a->excl_index;
+    v.excl_list  = a->excl_list;
+    v.ntypes1    = a->num_types + 1;
+    v.nbfp       = reinterpret_cast<const float2*>(a->nbfp);
+    v.xq         = const_cast<float4*>(reinterpret_cast<const float4*>(a->xq));
+    v.tgrid      = const_cast<int*>(a->types);
+    v.cells      = const_cast<int*>(a->cells);
+    v.sci        = const_cast<Sci*>(reinterpret_cast<const Sci*>(a->sci));
+    v.cj4        = const_cast<Cj4*>(reinterpret_cast<const Cj4*>(a->cj4));
+    v.excl       = const_cast<Excl*>(reinterpret_cast<const Excl*>(a->excl));
+    v.fnb        = reinterpret_cast<float4*>(base);
+    double* sums = reinterpret_cast<double*>(base + kNoAllocFnbBytes + 256);
+    v.energy     = sums;
+    v.fshift     = sums + 2;
+    v.virial     = sums + 2 + kNShift * 3;
+    v.hdr        = reinterpret_cast<ListHeader*>(base + kNoAllocFnbBytes + 256 + kNoAllocSumsBytes + 256);
+    for (int d = 0; d < 3; d++)
+    {
+        v.g.box[d] = a->box[d];
+    }
+    v.g.cells_capacity = a->num_slots / kSc;
+    // interaction constants, as in nbx_create (api/nblib/gmxsetup.cpp:226-284)
+    const float rc = a->rcoulomb;
+    v.coulomb      = a->coulomb;
+    v.rc2          = rc * rc;
+    v.rlist        = a->rlist;
+    v.rlist2       = a->rlist * a->rlist;
+    v.epsfac       = (float)one_4pi_eps0();
+    v.epsfac_d     = one_4pi_eps0();
+    {
+        const float p3 = rc * rc * rc, p6 = p3 * p3, p12 = p6 * p6;
+        v.cpot6        = (float)(-1.0 / p6);
+        v.cpot12       = (float)(-1.0 / p12);
+    }
+    const float eps_rf = (a->coulomb == NBX_COULOMB_CUTOFF) ? 1.0f : a->epsilon_rf;
+    v.k_rf = (eps_rf == 0) ? 1 / (2 * rc * rc * rc) : (eps_rf - 1.0f) / (2 * eps_rf + 1.0f) / (rc * rc * rc);
+    v.c_rf = 1 / rc + v.k_rf * rc * rc;
+    if (a->coulomb == NBX_COULOMB_EWALD)
+    {
+        v.beta     = calc_ewaldcoeff_q(rc, a->ewald_rtol > 0.0f ? a->ewald_rtol : 1e-5f);
+        v.sh_ewald = a->use_ewald_shift ? erfcf(v.beta * rc) / rc : 0.0f;
+        fit_erfc((double)v.beta * (double)rc, &v.erfc_p, v.erfc_c);
+    }
+    v.self_energy    = 0.0;
+    v.self_on_device = 1;
+    for (int sh = 0, m = -1; m <= 1; m++)
+    {
+        for (int l = -1; l <= 1; l++)
+        {
+            for (int k = -2; k <= 2; k++, sh++)
+            {
+                v.shiftvec[3 * sh + 0] = k * a->box[0];
+                v.shiftvec[3 * sh + 1] = l * a->box[1];
+                v.shiftvec[3 * sh + 2] = m * a->box[2];
+            }
+        }
+    }
+    // the array keeps the previous call's contents: clear what must start at zero
+    k_noalloc_init<<<1, 1, 0, s>>>(v.hdr, a->num_sci, a->num_slots / kSc);
+    cudaError_t e = cudaMemsetAsync(v.fnb, 0, sizeof(float4) * (size_t)a->num_slots, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sums, 0, kNoAllocSumsBytes, s);
+    int num_sms = 152, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+    {
+        const int blocks = num_sms * kForceMinBlocks;
+        int*      ctr    = &v.hdr->work_counter;
+        if (energy)
+        {
+            k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
+            if (v.coulomb == 0)
+            {
+                k_force<true, true><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+            }
+            else
+            {
+                k_force<true, false><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+            }
+        }
+        else if (v.coulomb == 0)
+        {
+            k_force<false, true><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+        }
+        else
+        {
+            k_force<false, false><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+        }
+        k_reduce_f<<<(v.n + 255) / 256, 256, 0, s>>>(v, d_f, d_virial ? 1 : 0);
+        if (energy)
+        {
+            k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);
+        }
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}

@@ -129,11 +129,17 @@ struct DeviceView
     int   coulomb;
     float shiftvec[kNShift * 3];
     double self_energy;     // Ewald / RF self term, constant for the system
+    int    self_on_device;  // 1: k_excl_energy adds the self term from the charges instead
     double epsfac_d;        // 1/(4 pi eps0) in double for the energy sums
     // erfc(x) = t * P(t) * exp(-x^2), t = 1/(1 + erfc_p x), fitted on [0, beta*rc] at set-up
     float erfc_p;
     float erfc_c[kErfcTerms];
 };
+
+// ---- host set-up helpers (nbx_api.cu) ----
+double one_4pi_eps0();
+float  calc_ewaldcoeff_q(float rc, float rtol);
+void   fit_erfc(double xmax, float* p_out, float* coef);
 
 // ---- launchers (one translation unit each) ----
 cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s);

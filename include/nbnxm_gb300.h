@@ -144,6 +144,47 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * (2 flops per FMA); used as the FP32 roofline denominator. */
 int nbx_measure_fp32_peak(int device, double* tflops);
 
+/* ---- allocation-free force evaluation ---- */
+/* Inputs of nbx_compute_noalloc: the atom data and pair list in the layouts that
+ * nbx_get_grid / nbx_get_pairlist export, all in device memory. */
+typedef struct
+{
+    int             num_atoms;  /* N */
+    int             num_slots;  /* grid slots (padded atoms) in xq / types; at most 65536 */
+    int             num_sci;    /* list entries */
+    const float*    xq;         /* [4*num_slots] x, y, z, q per grid slot (fillers: far away, q = 0) */
+    const int*      types;      /* [num_slots] type per slot; fillers carry num_types (the all-zero type) */
+    int             num_types;  /* real types; nbfp has (num_types+1)^2 pairs */
+    const float*    nbfp;       /* [(num_types+1)^2 * 2] {6*C6, 12*C12}, zero row/column for the filler type */
+    const int*      cells;      /* [N] grid slot of each atom */
+    const int*      sci;        /* [4*num_sci] */
+    const int*      cj4;        /* [8*num_cj4] */
+    const uint32_t* excl;       /* [32*num_excl] */
+    const int*      excl_index; /* [N+1], needed when energies or the virial are requested */
+    const int*      excl_list;
+    float           box[3];
+    int             coulomb;    /* nbx_coulomb */
+    float           rcoulomb, rlist, ewald_rtol, epsilon_rf;
+    int             use_ewald_shift;
+} nbx_noalloc_args;
+
+/* No counterpart in the reference: an extra entry point for callers that may not
+ * allocate device memory -- an engine that owns every device allocation through
+ * its own pool, or code that runs while allocation is forbidden.  It runs the
+ * same force / energy / virial kernels as nbx_compute_device on a pair list the
+ * caller already holds, and allocates nothing: its scratch (grid-order force
+ * accumulator, FP64 sums, work-queue header) is one file-scope device array
+ * sized for at most 65536 grid slots, which every GPU that loads the library
+ * keeps until exit.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current, so make the first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (different streams, or different threads) race and must
+ * be serialised by the caller.  Returns NBX_ERR_LIST_OVERFLOW when num_slots
+ * exceeds the maximum.  f: [3N] output in atom order; energies (double[2]) and
+ * virial (double[9]) may be NULL.  Asynchronous on cuda_stream. */
+int nbx_compute_noalloc(const nbx_noalloc_args* args, float* d_f, double* d_energies, double* d_virial,
+                        void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
