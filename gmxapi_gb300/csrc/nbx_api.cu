@@ -484,9 +484,9 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     {
         return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown Coulomb type");
     }
-    if (sys->num_types + 1 > 64)
+    if (sys->num_types + 1 > 48)
     {
-        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "at most 63 particle types");
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "at most 47 particle types");
     }
     for (int i = 0; i < 3 * n; i++)
     {

@@ -41,7 +41,7 @@ namespace
 
 constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
-constexpr int kMaxTypes1      = 64;  // types + dummy held in shared memory
+constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
 
 __device__ __forceinline__ float fast_rcp(float x)
 {
@@ -88,9 +88,9 @@ struct EntryState
 // (register-resident i-data) is unrolled, which keeps the kernel inside the
 // instruction cache.
 template<bool kEnergy, bool kEwald, bool kExcl>
-__device__ __forceinline__ void process_half(const DeviceView& v, const float2* __restrict__ nbfp_s,
+__device__ __forceinline__ void process_half(const DeviceView& v, const float4* __restrict__ nbfp_s,
                                              EntryState& st, const int cj_lane, unsigned im, unsigned wexcl,
-                                             int h, int sci, bool central, int ii, int jj, float rc2, float beta,
+                                             int h, int sci, bool central, int ii, int jj, float rc2, float pbeta,
                                              float beta2l2, float c2b, float k_rf2)
 {
     const unsigned full = 0xffffffffu;
@@ -133,6 +133,7 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
                 mask    = (r2 < rc2) ? 1.0f : 0.0f;
                 int_bit = 1.0f;
             }
+            const bool in_range = kExcl ? (mask != 0.0f) : (r2 < rc2);
             r2         = fmaxf(r2, kMinDist2);
             float rinv = rsqrtf(r2);
             if (kEnergy)
@@ -141,8 +142,17 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
                 rinv = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
             }
             const float  rinv2 = rinv * rinv;
-            const float2 lj    = nbfp_s[st.ti[c] + tj];
-            float        rinv6 = rinv2 * rinv2 * rinv2;
+            float4       lj;
+            if (kEnergy)
+            {
+                lj = nbfp_s[st.ti[c] + tj];
+            }
+            else
+            {
+                const float2 l2 = *reinterpret_cast<const float2*>(&nbfp_s[st.ti[c] + tj]);
+                lj              = make_float4(l2.x, l2.y, 0.0f, 0.0f);
+            }
+            float rinv6 = rinv2 * rinv2 * rinv2;
             if (kExcl)
             {
                 rinv6 *= int_bit;
@@ -155,26 +165,26 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
             if (kEwald)
             {
                 // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
-                const float br   = beta * r2 * rinv;
-                const float t    = fast_rcp(1.0f + v.erfc_p * br);
+                const float r    = r2 * rinv;
+                const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
                 float       poly = v.erfc_c[kErfcTerms - 1];
 #pragma unroll
                 for (int k = kErfcTerms - 2; k >= 0; k--)
                 {
-                    poly = poly * t + v.erfc_c[k];
+                    poly = fmaf(poly, t, v.erfc_c[k]);
                 }
-                const float expm  = fast_ex2(-beta2l2 * r2);
-                const float erfcv = t * poly * expm;
-                // -(d/dr)(erfc(beta r)/r)/r; exclusions drop the full 1/r
-                float fc = (erfcv * rinv + c2b * expm) * rinv2;
+                const float expm = fast_ex2(-beta2l2 * r2);
+                const float tp   = t * poly;  // erfc(beta r) = tp * expm
+                // -(d/dr)(erfc(beta r)/r)/r = expm (tp/r + 2 beta/sqrt(pi)) / r^2; exclusions drop 1/r^3
+                float fc = expm * fmaf(tp, rinv, c2b) * rinv2;
                 if (kExcl)
                 {
                     fc -= (1.0f - int_bit) * rinv * rinv2;
                 }
-                fscal += qq * fc;
+                fscal = fmaf(qq, fc, fscal);
                 if (kEnergy)
                 {
-                    h_el = erfcv * rinv - v.sh_ewald;
+                    h_el = fmaf(tp * expm, rinv, -v.sh_ewald);
                 }
             }
             else
@@ -184,27 +194,28 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
                 {
                     fc *= int_bit;
                 }
-                fscal += qq * (fc - k_rf2);
+                fscal = fmaf(qq, fc - k_rf2, fscal);
                 if (kEnergy)
                 {
                     h_el = (rinv - v.c_rf) + v.k_rf * r2;
                 }
             }
-            fscal *= mask;
+            fscal = in_range ? fscal : 0.0f;
             if (kEnergy)
             {
-                const float w = kExcl ? mask * int_bit : mask;
-                kahan_add(st.acc_el, st.cmp_el, w * st.qi[c] * (xj.w * h_el));
-                kahan_add(st.acc_lj, st.cmp_lj,
-                          w * ((vrep + lj.y * v.cpot12) * (1.0f / 12.0f) - (vdisp + lj.x * v.cpot6) * (1.0f / 6.0f)));
+                const bool counted = kExcl ? (in_range && int_bit != 0.0f) : in_range;
+                const float e_el   = counted ? st.qi[c] * (xj.w * h_el) : 0.0f;
+                // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair)
+                const float e_lj = counted ? fmaf(vrep, 1.0f / 12.0f, fmaf(vdisp, -1.0f / 6.0f, lj.z)) : 0.0f;
+                kahan_add(st.acc_el, st.cmp_el, e_el);
+                kahan_add(st.acc_lj, st.cmp_lj, e_lj);
             }
-            const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
-            st.fix[c] += tx;
-            st.fiy[c] += ty;
-            st.fiz[c] += tz;
-            fjx -= tx;
-            fjy -= ty;
-            fjz -= tz;
+            st.fix[c] = fmaf(fscal, dx, st.fix[c]);
+            st.fiy[c] = fmaf(fscal, dy, st.fiy[c]);
+            st.fiz[c] = fmaf(fscal, dz, st.fiz[c]);
+            fjx       = fmaf(-fscal, dx, fjx);
+            fjy       = fmaf(-fscal, dy, fjy);
+            fjz       = fmaf(-fscal, dz, fjz);
         }
         // reduce the j force over the 8 i-lanes, one vector red per j-atom
 #pragma unroll
@@ -224,11 +235,14 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const float2* 
 template<bool kEnergy, bool kEwald>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
 {
-    __shared__ float2 nbfp_s[kMaxTypes1 * kMaxTypes1];
-    const int         nt1 = v.ntypes1;
+    // {6*C6, 12*C12, LJ energy shift of the pair, 0} per type pair
+    extern __shared__ float4 nbfp_s[];
+    const int nt1 = v.ntypes1;
     for (int k = threadIdx.x; k < nt1 * nt1; k += blockDim.x)
     {
-        nbfp_s[k] = v.nbfp[k];
+        const float2 p = v.nbfp[k];
+        // (12C12 cpot12)/12 - (6C6 cpot6)/6 (kernel_gpu_ref.cpp:327-336)
+        nbfp_s[k] = make_float4(p.x, p.y, p.y * v.cpot12 * (1.0f / 12.0f) - p.x * v.cpot6 * (1.0f / 6.0f), 0.0f);
     }
     __syncthreads();
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
@@ -242,6 +256,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     const int      numSci  = v.hdr->num_sci;
     const float    rc2     = v.rc2;
     const float    beta    = v.beta;
+    const float    pbeta   = v.erfc_p * beta;
     const float    beta2l2 = beta * beta * 1.4426950408889634f;  // beta^2 * log2(e)
     const float    c2b     = 1.1283791670955126f * beta;           // 2 beta / sqrt(pi)
     const float    k_rf2   = 2.0f * v.k_rf;
@@ -293,13 +308,13 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
                 if (exi == 0)
                 {
                     process_half<kEnergy, kEwald, false>(v, nbfp_s, st, cj_lane, im, 0u, h, s.sci, central, ii, jj,
-                                                         rc2, beta, beta2l2, c2b, k_rf2);
+                                                         rc2, pbeta, beta2l2, c2b, k_rf2);
                 }
                 else
                 {
                     const unsigned wexcl = v.excl[exi].pair[lane];
                     process_half<kEnergy, kEwald, true>(v, nbfp_s, st, cj_lane, im, wexcl, h, s.sci, central, ii,
-                                                        jj, rc2, beta, beta2l2, c2b, k_rf2);
+                                                        jj, rc2, pbeta, beta2l2, c2b, k_rf2);
                 }
             }
         }
@@ -583,8 +598,9 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     cudaMemsetAsync(v.fnb, 0, sizeof(float4) * (size_t)v.g.cells_capacity * kSc, s);
     cudaMemsetAsync(v.fshift, 0, sizeof(double) * kNShift * 3, s);
     cudaMemsetAsync(v.energy, 0, sizeof(double) * 2, s);
-    const int blocks = num_sms * kForceMinBlocks;
-    const bool ewald = (v.coulomb == 0);
+    const int    blocks = num_sms * kForceMinBlocks;
+    const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1;
+    const bool   ewald  = (v.coulomb == 0);
     if (energy)
     {
         k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
@@ -593,22 +609,22 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     {
         if (ewald)
         {
-            k_force<true, true><<<blocks, kForceThreads, 0, s>>>(v, counter);
+            k_force<true, true><<<blocks, kForceThreads, smem, s>>>(v, counter);
         }
         else
         {
-            k_force<true, false><<<blocks, kForceThreads, 0, s>>>(v, counter);
+            k_force<true, false><<<blocks, kForceThreads, smem, s>>>(v, counter);
         }
     }
     else
     {
         if (ewald)
         {
-            k_force<false, true><<<blocks, kForceThreads, 0, s>>>(v, counter);
+            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(v, counter);
         }
         else
         {
-            k_force<false, false><<<blocks, kForceThreads, 0, s>>>(v, counter);
+            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, counter);
         }
     }
     return cudaGetLastError();
@@ -825,27 +841,28 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
     {
-        const int blocks = num_sms * kForceMinBlocks;
-        int*      ctr    = &v.hdr->work_counter;
+        const int    blocks = num_sms * kForceMinBlocks;
+        const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1;
+        int*         ctr    = &v.hdr->work_counter;
         if (energy)
         {
             k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
             if (v.coulomb == 0)
             {
-                k_force<true, true><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+                k_force<true, true><<<blocks, kForceThreads, smem, s>>>(v, ctr);
             }
             else
             {
-                k_force<true, false><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+                k_force<true, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
             }
         }
         else if (v.coulomb == 0)
         {
-            k_force<false, true><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
         else
         {
-            k_force<false, false><<<blocks, kForceThreads, 0, s>>>(v, ctr);
+            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
         k_reduce_f<<<(v.n + 255) / 256, 256, 0, s>>>(v, d_f, d_virial ? 1 : 0);
         if (energy)
