@@ -396,12 +396,11 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
     {
         e0 = take_event(h);
         e1 = take_event(h);
-        cudaEventRecord(e0, h->stream);
     }
-    if (e == cudaSuccess) e = launch_force(v, d_e != nullptr, h->stream, h->num_sms);
+    // the events bracket the force kernel alone
+    if (e == cudaSuccess) e = launch_force(v, energy, h->stream, h->num_sms, e0, e1);
     if (h->timing)
     {
-        cudaEventRecord(e1, h->stream);
         h->ev_pending.emplace_back(e0, e1);
         if (h->ev_pending.size() > 256)
         {
@@ -411,7 +410,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
     if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_x, d_vir != nullptr, h->stream);
     if (e == cudaSuccess && energy) e = launch_finish_energy(v, d_e, d_vir, h->stream);
     h->force_launches += 1;
-    h->launches += 3 + (energy ? 1 : 0);
+    h->launches += 3 + (energy ? 2 : 0);
     return cuda_check(h, e, "compute");
 }
 

@@ -383,6 +383,26 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
 // excluded pairs the list-based kernel sees (the half list holds each image
 // pair once).  Ewald: -q_i q_j erf(beta r)/r; RF: q_i q_j (k_rf r^2 - c_rf)
 // (kernel_gpu_ref.cpp:259-291 with int_bit = 0).  Energies only.
+// 1/(n! (2n+1)), n = 0..15
+__constant__ double kErfSeries[16] = {
+    1.0,
+    1.0 / 3.0,
+    1.0 / 10.0,
+    1.0 / 42.0,
+    1.0 / 216.0,
+    1.0 / 1320.0,
+    1.0 / 9360.0,
+    1.0 / 75600.0,
+    1.0 / 685440.0,
+    1.0 / 6894720.0,
+    1.0 / 76204800.0,
+    1.0 / 918086400.0,
+    1.0 / 11975040000.0,
+    1.0 / 168129561600.0,
+    1.0 / 2528170444800.0,
+    1.0 / 40537905408000.0,
+};
+
 __global__ void k_excl_energy(DeviceView v)
 {
     const int i   = blockIdx.x * blockDim.x + threadIdx.x;
@@ -424,8 +444,25 @@ __global__ void k_excl_energy(DeviceView v)
                         double       h;
                         if (v.coulomb == 0)
                         {
-                            const double rd = sqrt(r2d);
-                            h               = -erf((double)v.beta * rd) / rd;
+                            // erf(x)/x = 2/sqrt(pi) sum_n (-x^2)^n / (n! (2n+1)); 16 terms reach
+                            // double precision for x <= 1 (excluded pairs are short), no
+                            // square root or division needed
+                            const double b = (double)v.beta;
+                            const double w = b * b * r2d;
+                            if (w <= 1.0)
+                            {
+                                double sum = 0.0;
+                                for (int k = 15; k >= 0; k--)
+                                {
+                                    sum = fma(sum, -w, kErfSeries[k]);
+                                }
+                                h = -b * 1.1283791670955125739 * sum;
+                            }
+                            else
+                            {
+                                const double rd = sqrt(r2d);
+                                h               = -erf(b * rd) / rd;
+                            }
                         }
                         else
                         {
@@ -447,35 +484,44 @@ __global__ void k_excl_energy(DeviceView v)
     }
 }
 
-// f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k in FP64.
+// f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k: each
+// thread gathers kReduceAtoms atoms and sums their x (x) f in float, the
+// partial sums are reduced in FP64.
+constexpr int kReduceAtoms = 8;
+
 __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    double    w[9];
+    float w[9];
 #pragma unroll
     for (int k = 0; k < 9; k++)
     {
-        w[k] = 0.0;
+        w[k] = 0.0f;
     }
-    if (a < v.n)
+    const int a0 = (blockIdx.x * blockDim.x) * kReduceAtoms + threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < kReduceAtoms; r++)
     {
-        const int    k  = v.cells[a];
-        const float4 fa = v.fnb[k];
-        f[3 * a]        = fa.x;
-        f[3 * a + 1]    = fa.y;
-        f[3 * a + 2]    = fa.z;
-        if (do_virial)
+        const int a = a0 + r * blockDim.x;
+        if (a < v.n)
         {
-            const float4 xa = v.xq[k];
-            const double xv[3] = { xa.x, xa.y, xa.z };
-            const double fv[3] = { fa.x, fa.y, fa.z };
-#pragma unroll
-            for (int p = 0; p < 3; p++)
+            const int    k  = v.cells[a];
+            const float4 fa = v.fnb[k];
+            f[3 * a]        = fa.x;
+            f[3 * a + 1]    = fa.y;
+            f[3 * a + 2]    = fa.z;
+            if (do_virial)
             {
+                const float4 xa   = v.xq[k];
+                const float  xv[3] = { xa.x, xa.y, xa.z };
+                const float  fv[3] = { fa.x, fa.y, fa.z };
 #pragma unroll
-                for (int q = 0; q < 3; q++)
+                for (int p = 0; p < 3; p++)
                 {
-                    w[p * 3 + q] = xv[p] * fv[q];
+#pragma unroll
+                    for (int q = 0; q < 3; q++)
+                    {
+                        w[p * 3 + q] = fmaf(xv[p], fv[q], w[p * 3 + q]);
+                    }
                 }
             }
         }
@@ -489,7 +535,7 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
 #pragma unroll
     for (int k = 0; k < 9; k++)
     {
-        double t = w[k];
+        double t = (double)w[k];
         for (int o = 16; o > 0; o >>= 1)
         {
             t += __shfl_xor_sync(0xffffffffu, t, o);
@@ -587,7 +633,8 @@ __global__ void k_fma_probe(float* out, int iters)
 
 } // namespace
 
-cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms)
+cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, cudaEvent_t ev0,
+                         cudaEvent_t ev1)
 {
     if (v.ntypes1 > kMaxTypes1)
     {
@@ -604,6 +651,10 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     if (energy)
     {
         k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
+    }
+    if (ev0)
+    {
+        cudaEventRecord(ev0, s);
     }
     if (energy)
     {
@@ -627,6 +678,10 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
             k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, counter);
         }
     }
+    if (ev1)
+    {
+        cudaEventRecord(ev1, s);
+    }
     return cudaGetLastError();
 }
 
@@ -637,7 +692,7 @@ cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* /*d_x*
         cudaMemsetAsync(v.virial, 0, sizeof(double) * 9, s);
     }
     const int tb = 256;
-    k_reduce_f<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, d_f, virial ? 1 : 0);
+    k_reduce_f<<<(v.n + tb * kReduceAtoms - 1) / (tb * kReduceAtoms), tb, 0, s>>>(v, d_f, virial ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -864,7 +919,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         {
             k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
-        k_reduce_f<<<(v.n + 255) / 256, 256, 0, s>>>(v, d_f, d_virial ? 1 : 0);
+        k_reduce_f<<<(v.n + 256 * kReduceAtoms - 1) / (256 * kReduceAtoms), 256, 0, s>>>(v, d_f, d_virial ? 1 : 0);
         if (energy)
         {
             k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);

@@ -146,7 +146,8 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
 cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s);
 cudaError_t launch_search(const DeviceView& v, cudaStream_t s);
 cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s);
-cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms);
+cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, cudaEvent_t ev0 = nullptr,
+                         cudaEvent_t ev1 = nullptr);
 cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* d_x, bool virial, cudaStream_t s);
 cudaError_t launch_finish_energy(const DeviceView& v, double* d_energies, double* d_virial, cudaStream_t s);
 cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cudaStream_t s);
