@@ -36,6 +36,9 @@ NSTLIST, NSTPRUNE = 100, 10
 SIGMA_STEP = 0.002
 # Ewald-analytic + LJ flops per pair with energies (src/gromacs/gmxlib/nrnb.cpp:106)
 FLOPS_PER_PAIR_VF = 107
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_force launch on this workload, from an
+# ncu --set full capture (list + coordinates; forces stay in L2)
+FORCE_KERNEL_DRAM_BYTES = 21.54e6
 
 
 def useful_pairs(n: int, box) -> float:
@@ -295,11 +298,12 @@ def run_ours(args) -> None:
         "force_evals_per_s": world * args.steps / (total_ms * 1e-3),
         "pairs_computed_per_eval": pairs_avg, "useful_pairs_per_eval": up,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": FORCE_KERNEL_DRAM_BYTES,
                      "kernel": "nbx::k_force<energy, ewald>",
                      "note": f"{FLOPS_PER_PAIR_VF} flops per computed pair (nrnb.cpp:106) x "
                              f"{pairs_avg:.4g} computed pairs / {avg_force_ms:.4f} ms average launch; "
-                             "peak = measured FFMA probe of this run"},
+                             "peak = measured FFMA probe of this run (of measured); traffic = DRAM bytes "
+                             "per launch from ncu"},
         "cpu_baseline": cpu_baseline_port(),
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": n * 12,
                 "d2h_bytes_per_step": n * 12 + 11 * 8},
