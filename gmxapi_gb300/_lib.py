@@ -32,6 +32,10 @@ EXPORTED = [
     "nbx_compute_device", "nbx_md_step_device", "nbx_synchronize", "nbx_get_sizes", "nbx_get_grid",
     "nbx_get_pairlist", "nbx_get_pair_counts", "nbx_measure_fp32_peak", "nbx_md_step",
     "nbx_set_timing", "nbx_get_timings", "nbx_compute_noalloc",
+    "nbx_batch_create", "nbx_batch_destroy", "nbx_batch_last_error", "nbx_batch_atoms", "nbx_batch_set_stream",
+    "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
+    "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
+    "nbx_batch_set_prune",
 ]
 
 
@@ -136,9 +140,25 @@ def load():
     L.nbx_set_timing.argtypes = [vp, C.c_int]
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
+    L.nbx_batch_create.argtypes = [C.c_int, C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int,
+                                   C.POINTER(vp)]
+    L.nbx_batch_destroy.argtypes = [vp]
+    L.nbx_batch_last_error.argtypes = [vp]
+    L.nbx_batch_last_error.restype = C.c_char_p
+    L.nbx_batch_atoms.argtypes = [vp, llp, ip]
+    L.nbx_batch_set_stream.argtypes = [vp, vp]
+    L.nbx_batch_search_device.argtypes = [vp, vp]
+    L.nbx_batch_prune_device.argtypes = [vp, C.c_int]
+    L.nbx_batch_compute_device.argtypes = [vp, vp, vp, vp, vp]
+    L.nbx_batch_md_step_device.argtypes = [vp, C.c_longlong, vp, vp, vp, vp]
+    L.nbx_batch_sequential_md_step_device.argtypes = [vp, C.c_longlong, vp, vp, vp, vp]
+    L.nbx_batch_set_graph.argtypes = [vp, C.c_int]
+    L.nbx_batch_set_kernel_variant.argtypes = [vp, C.c_int]
+    L.nbx_batch_set_prune.argtypes = [vp, C.c_int, C.c_float]
     for name in EXPORTED:
         f = getattr(L, name)
-        if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream"):
+        if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",
+                                                "nbx_batch_last_error"):
             f.restype = C.c_int
     _lib = L
     return L

@@ -25,6 +25,7 @@ UNITS = {
     "nbx_search.cu": ["--fmad=false"],
     "nbx_prune.cu": ["--fmad=false"],
     "nbx_force.cu": [],
+    "nbx_batch.cu": [],
     "nbx_api.cu": [],
 }
 

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 namespace nbx
@@ -1104,6 +1105,467 @@ int nbx_measure_fp32_peak(int device, double* tflops)
     cudaSetDevice(device);
     cudaError_t e = measure_fp32_peak(tflops);
     return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
+
+} // extern "C"
+
+// ----------------------------------------------------------------- batches
+
+struct nbx_batch
+{
+    int                      device     = 0;
+    int                      num_sms    = 152;
+    cudaStream_t             stream     = nullptr;
+    bool                     own_stream = false;
+    std::vector<nbx_handle*> sys;
+    std::vector<int>         offsets;  // atom offsets, size nsys+1
+    nbx_options              opts{};
+    std::string              err;
+    DeviceView               cv{};     // interaction constants shared by all systems
+    BatchSys*                d_table  = nullptr;
+    BatchSys*                h_table  = nullptr;  // pinned
+    int*                     d_prefix = nullptr;
+    unsigned*                d_status = nullptr;
+    double*                  d_sums   = nullptr;
+    size_t                   sums_bytes = 0;
+    int*                     d_counter  = nullptr;
+    int                      max_slots  = 0;
+    int                      max_atoms  = 0;
+    bool                     have_list  = false;
+    long long                list_step  = 0;
+    int                      prune_part = 0;
+    int                      nparts     = 1;
+    bool                     use_prune  = false;
+    int                      variant    = 0;
+    bool                     use_graph  = true;
+    cudaGraphExec_t          graph      = nullptr;
+    const void*              graph_key[4] = { nullptr, nullptr, nullptr, nullptr };
+};
+
+namespace
+{
+thread_local std::string g_batch_error;
+
+int batch_error(nbx_batch* b, int code, const std::string& msg)
+{
+    if (b)
+    {
+        b->err = msg;
+    }
+    else
+    {
+        g_batch_error = msg;
+    }
+    return code;
+}
+
+void drop_graph(nbx_batch* b)
+{
+    if (b->graph)
+    {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    for (auto& k : b->graph_key)
+    {
+        k = nullptr;
+    }
+}
+
+// Rebuilds the device table of per-system pointers (they change when a list grows) and the
+// entry prefix sums; called after every search.
+int batch_refresh(nbx_batch* b)
+{
+    const int nsys = (int)b->sys.size();
+    for (int i = 0; i < nsys; i++)
+    {
+        const DeviceView& v = b->sys[i]->v;
+        BatchSys&         t = b->h_table[i];
+        t.xq                = v.xq;
+        t.tgrid             = v.tgrid;
+        t.fnb               = v.fnb;
+        t.sci               = v.sci;
+        t.cj4               = v.cj4;
+        t.excl              = v.excl;
+        t.imask_outer       = v.imask_outer;
+        t.cells             = v.cells;
+        t.atom_indices      = v.atom_indices;
+        t.image             = v.image;
+        t.hdr               = v.hdr;
+        t.excl_index        = v.excl_index;
+        t.excl_list         = v.excl_list;
+        t.n                 = v.n;
+        t.atom_base         = b->offsets[i];
+        t.self_energy       = v.self_energy;
+        for (int d = 0; d < 3; d++)
+        {
+            t.box[d] = v.g.box[d];
+        }
+        std::memcpy(t.shiftvec, v.shiftvec, sizeof(t.shiftvec));
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d_table, b->h_table, sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = launch_batch_prefix(b->d_table, nsys, b->d_prefix, b->d_status, b->stream);
+    unsigned st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, b->d_status, sizeof(st), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess)
+    {
+        return batch_error(b, NBX_ERR_CUDA, std::string("batch refresh: ") + cudaGetErrorString(e));
+    }
+    if (st & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    {
+        return batch_error(b, NBX_ERR_LIST_OVERFLOW, "a system's pair list or grid overflowed");
+    }
+    return NBX_OK;
+}
+
+int batch_search(nbx_batch* b, const float* d_x)
+{
+    for (size_t i = 0; i < b->sys.size(); i++)
+    {
+        int rc = search_sync(b->sys[i], const_cast<float*>(d_x) + 3 * (size_t)b->offsets[i], 0);
+        if (rc != NBX_OK)
+        {
+            return batch_error(b, rc, "system " + std::to_string(i) + ": " + b->sys[i]->err);
+        }
+    }
+    b->have_list  = true;
+    b->prune_part = 0;
+    return batch_refresh(b);
+}
+
+int batch_compute(nbx_batch* b, const float* d_x, float* d_f, double* d_e, double* d_vir)
+{
+    const int nsys = (int)b->sys.size();
+    auto      run  = [&](cudaStream_t s) {
+        return launch_batch_compute(b->cv, b->d_table, b->d_prefix, nsys, b->max_slots, b->max_atoms, d_x, d_f,
+                                    b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, b->variant, b->num_sms, s);
+    };
+    if (!b->use_graph)
+    {
+        cudaError_t e = run(b->stream);
+        return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const void* key[4] = { d_x, d_f, d_e, d_vir };
+    if (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0)
+    {
+        drop_graph(b);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess)
+        {
+            cudaError_t e2 = run(b->stream);
+            e              = cudaStreamEndCapture(b->stream, &g);
+            if (e2 != cudaSuccess)
+            {
+                e = e2;
+            }
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+        if (g)
+        {
+            cudaGraphDestroy(g);
+        }
+        if (e != cudaSuccess)
+        {
+            drop_graph(b);
+            return batch_error(b, NBX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        std::memcpy(b->graph_key, key, sizeof(key));
+    }
+    cudaError_t e = cudaGraphLaunch(b->graph, b->stream);
+    return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+} // namespace
+
+extern "C" {
+
+const char* nbx_batch_last_error(const nbx_batch* b)
+{
+    return b ? b->err.c_str() : g_batch_error.c_str();
+}
+
+int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_options* opts, int device,
+                     nbx_batch** out)
+{
+    if (num_systems <= 0 || !systems || !out)
+    {
+        return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "need at least one system");
+    }
+    *out = nullptr;
+    for (int i = 1; i < num_systems; i++)
+    {
+        const nbx_system_desc& a = systems[0];
+        const nbx_system_desc& c = systems[i];
+        if (c.num_types != a.num_types
+            || std::memcmp(c.nbfp, a.nbfp, sizeof(float) * 2 * (size_t)a.num_types * a.num_types) != 0)
+        {
+            return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "all systems of a batch share types and nbfp");
+        }
+    }
+    nbx_batch* b = new nbx_batch();
+    b->device    = device;
+    cudaSetDevice(device);
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    b->own_stream = true;
+    if (opts)
+    {
+        b->opts = *opts;
+    }
+    else
+    {
+        nbx_default_options(&b->opts);
+    }
+    b->offsets.push_back(0);
+    for (int i = 0; i < num_systems && e == cudaSuccess; i++)
+    {
+        nbx_handle* h  = nullptr;
+        int         rc = nbx_create(&systems[i], &b->opts, device, &h);
+        if (rc != NBX_OK)
+        {
+            std::string msg = "system " + std::to_string(i) + ": " + nbx_last_error(nullptr);
+            nbx_batch_destroy(b);
+            return batch_error(nullptr, rc, msg);
+        }
+        nbx_set_stream(h, b->stream);
+        b->sys.push_back(h);
+        b->offsets.push_back(b->offsets.back() + systems[i].num_atoms);
+        b->max_slots = std::max(b->max_slots, h->v.g.cells_capacity * kSc);
+        b->max_atoms = std::max(b->max_atoms, h->n);
+    }
+    b->cv        = b->sys[0]->v;
+    b->use_prune = b->opts.nstlist_prune > 0;
+    b->nparts    = b->use_prune ? std::max(1, b->opts.nstlist_prune / 2) : 1;
+    const size_t nsys = (size_t)num_systems;
+    b->sums_bytes     = sizeof(double) * (2 + kNShift * 3 + 9) * nsys + 64;
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(BatchSys) * nsys);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_table, sizeof(BatchSys) * nsys);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(int) * (nsys + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_sums, b->sums_bytes);
+    if (e != cudaSuccess)
+    {
+        nbx_batch_destroy(b);
+        return batch_error(nullptr, NBX_ERR_OUT_OF_MEMORY, "batch allocation");
+    }
+    // the work counter sits after the FP64 sums, inside the region cleared each step
+    b->d_counter = reinterpret_cast<int*>(reinterpret_cast<char*>(b->d_sums) + b->sums_bytes - 64);
+    int rc       = batch_refresh(b);
+    if (rc != NBX_OK)
+    {
+        std::string msg = b->err;
+        nbx_batch_destroy(b);
+        return batch_error(nullptr, rc, msg);
+    }
+    b->have_list = true;
+    *out         = b;
+    return NBX_OK;
+}
+
+int nbx_batch_destroy(nbx_batch* b)
+{
+    if (!b)
+    {
+        return NBX_OK;
+    }
+    cudaSetDevice(b->device);
+    if (b->stream)
+    {
+        cudaStreamSynchronize(b->stream);
+    }
+    drop_graph(b);
+    for (nbx_handle* h : b->sys)
+    {
+        nbx_destroy(h);
+    }
+    cudaFree(b->d_table);
+    cudaFreeHost(b->h_table);
+    cudaFree(b->d_prefix);
+    cudaFree(b->d_status);
+    cudaFree(b->d_sums);
+    if (b->own_stream && b->stream)
+    {
+        cudaStreamDestroy(b->stream);
+    }
+    delete b;
+    return NBX_OK;
+}
+
+int nbx_batch_atoms(nbx_batch* b, long long* total, int* offsets)
+{
+    if (!b)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (total)
+    {
+        *total = b->offsets.back();
+    }
+    if (offsets)
+    {
+        std::memcpy(offsets, b->offsets.data(), sizeof(int) * b->offsets.size());
+    }
+    return NBX_OK;
+}
+
+int nbx_batch_set_stream(nbx_batch* b, void* s)
+{
+    if (!b)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    if (b->own_stream)
+    {
+        cudaStreamDestroy(b->stream);
+    }
+    b->stream     = static_cast<cudaStream_t>(s);
+    b->own_stream = false;
+    for (nbx_handle* h : b->sys)
+    {
+        h->stream = b->stream;
+    }
+    return NBX_OK;
+}
+
+int nbx_batch_search_device(nbx_batch* b, const float* d_x)
+{
+    if (!b || !d_x)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    return batch_search(b, d_x);
+}
+
+int nbx_batch_prune_device(nbx_batch* b, int part)
+{
+    if (!b)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    const float outer2 = b->cv.rlist2, inner2 = b->cv.rlist_inner2;
+    cudaError_t e = (part < 0) ? launch_batch_prune(b->d_table, b->d_prefix, (int)b->sys.size(), outer2, inner2, 1, 0,
+                                                    1, b->stream)
+                               : launch_batch_prune(b->d_table, b->d_prefix, (int)b->sys.size(), outer2, inner2, 0,
+                                                    part % b->nparts, b->nparts, b->stream);
+    return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int nbx_batch_compute_device(nbx_batch* b, const float* d_x, float* d_f, double* d_e, double* d_vir)
+{
+    if (!b || !d_x || !d_f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    return batch_compute(b, d_x, d_f, d_e, d_vir);
+}
+
+int nbx_batch_md_step_device(nbx_batch* b, long long step, const float* d_x, float* d_f, double* d_e,
+                             double* d_vir)
+{
+    if (!b || !d_x || !d_f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    const int nstlist = std::max(1, b->opts.nstlist);
+    int       rc      = NBX_OK;
+    if (!b->have_list || step % nstlist == 0)
+    {
+        if ((rc = batch_search(b, d_x)) != NBX_OK)
+        {
+            return rc;
+        }
+        b->list_step = step;
+    }
+    else if (b->use_prune)
+    {
+        const long long age = step - b->list_step;
+        if (age > 0 && age % 2 == 0)
+        {
+            rc            = nbx_batch_prune_device(b, b->prune_part);
+            b->prune_part = (b->prune_part + 1) % b->nparts;
+            if (rc != NBX_OK)
+            {
+                return rc;
+            }
+        }
+    }
+    return batch_compute(b, d_x, d_f, d_e, d_vir);
+}
+
+int nbx_batch_sequential_md_step_device(nbx_batch* b, long long step, const float* d_x, float* d_f, double* d_e,
+                                        double* d_vir)
+{
+    if (!b || !d_x || !d_f)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    for (size_t i = 0; i < b->sys.size(); i++)
+    {
+        const size_t o  = 3 * (size_t)b->offsets[i];
+        int          rc = nbx_md_step_device(b->sys[i], step, d_x + o, d_f + o, d_e ? d_e + 2 * i : nullptr,
+                                             d_vir ? d_vir + 9 * i : nullptr);
+        if (rc != NBX_OK)
+        {
+            return batch_error(b, rc, "system " + std::to_string(i) + ": " + b->sys[i]->err);
+        }
+    }
+    return NBX_OK;
+}
+
+int nbx_batch_set_graph(nbx_batch* b, int enable)
+{
+    if (!b)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    b->use_graph = enable != 0;
+    drop_graph(b);
+    return NBX_OK;
+}
+
+int nbx_batch_set_kernel_variant(nbx_batch* b, int variant)
+{
+    if (!b || variant < 0 || variant > 3)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    b->variant = variant;
+    drop_graph(b);
+    return NBX_OK;
+}
+
+int nbx_batch_set_prune(nbx_batch* b, int nstlist_prune, float rlist_inner)
+{
+    if (!b || nstlist_prune < 0 || (nstlist_prune > 0 && !(rlist_inner >= b->opts.rcoulomb)))
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    b->opts.nstlist_prune = nstlist_prune;
+    b->opts.rlist_inner   = rlist_inner;
+    b->use_prune          = nstlist_prune > 0;
+    b->nparts             = b->use_prune ? std::max(1, nstlist_prune / 2) : 1;
+    const float rin       = (b->use_prune && rlist_inner > 0.0f) ? rlist_inner : b->opts.rlist;
+    b->cv.rlist_inner2    = rin * rin;
+    for (nbx_handle* h : b->sys)
+    {
+        h->opts.nstlist_prune = nstlist_prune;
+        h->opts.rlist_inner   = rlist_inner;
+        h->use_prune          = b->use_prune;
+        h->nparts             = b->nparts;
+        h->v.rlist_inner2     = rin * rin;
+    }
+    b->have_list = false;  // the next step searches and prunes with the new settings
+    return NBX_OK;
 }
 
 } // extern "C"

@@ -31,6 +31,7 @@
 //    until the entry ends; shift forces and energies are reduced in FP64.
 #include "../../include/nbnxm_gb300.h"
 #include "nbx_internal.cuh"
+#include "nbx_pair_core.cuh"
 
 #include <mutex>
 
@@ -42,195 +43,6 @@ namespace
 constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
-
-__device__ __forceinline__ float fast_rcp(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ float fast_ex2(float x)
-{
-    float r;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float z)
-{
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(0.0f)
-                 : "memory");
-}
-
-// Compensated (Kahan) accumulation: sum + c carries ~2x float precision.
-__device__ __forceinline__ void kahan_add(float& sum, float& c, float v)
-{
-    const float y = v - c;
-    const float t = sum + y;
-    c             = (t - sum) - y;
-    sum           = t;
-}
-
-// Per-warp state of one list entry.
-struct EntryState
-{
-    float xi[kNcl], yi[kNcl], zi[kNcl], qi[kNcl];
-    int   ti[kNcl];
-    float fix[kNcl], fiy[kNcl], fiz[kNcl];
-    float acc_el, cmp_el;              // sum q_i (q_j h_ij), compensated
-    float acc_lj, cmp_lj;
-};
-
-// All pair interactions of one (cj4, warp half).  kExcl: this half has an
-// exclusion mask (diagonal cluster pair or topology exclusions).  The loop
-// over the 4 j-clusters stays rolled and only the loop over the 8 i-clusters
-// (register-resident i-data) is unrolled, which keeps the kernel inside the
-// instruction cache.
-template<bool kEnergy, bool kEwald, bool kExcl>
-__device__ __forceinline__ void process_half(const DeviceView& v, const float4* __restrict__ nbfp_s,
-                                             EntryState& st, const int cj_lane, unsigned im, unsigned wexcl,
-                                             int h, int sci, bool central, int ii, int jj, float rc2, float pbeta,
-                                             float beta2l2, float c2b, float k_rf2)
-{
-    const unsigned full = 0xffffffffu;
-#pragma unroll 1
-    for (int jm = 0; jm < kJg; jm++)
-    {
-        const unsigned imj = (im >> (jm * kNcl)) & 0xffu;
-        const int      cj  = __shfl_sync(full, cj_lane, jm);
-        if (!imj)
-        {
-            continue;
-        }
-        const int    aj  = cj * kCl + h * (kCl / kSplit) + jj;
-        const float4 xj  = v.xq[aj];
-        const int    tj  = v.tgrid[aj];
-        const float  qje = xj.w * v.epsfac;
-        const unsigned wj = wexcl >> (jm * kNcl);
-        float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
-        {
-            if (!(imj & (1u << c)))
-            {
-                continue;
-            }
-            const float dx = st.xi[c] - xj.x;
-            const float dy = st.yi[c] - xj.y;
-            const float dz = st.zi[c] - xj.z;
-            float       r2 = dx * dx + dy * dy + dz * dz;
-            float       mask, int_bit;
-            if (kExcl)
-            {
-                // the diagonal cluster pair counts j > i only (kernel_gpu_ref.cpp:242)
-                const bool self_lower = central && (sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
-                mask    = (r2 < rc2 && !self_lower) ? 1.0f : 0.0f;
-                int_bit = (wj & (1u << c)) ? 1.0f : 0.0f;
-            }
-            else
-            {
-                mask    = (r2 < rc2) ? 1.0f : 0.0f;
-                int_bit = 1.0f;
-            }
-            const bool in_range = kExcl ? (mask != 0.0f) : (r2 < rc2);
-            r2         = fmaxf(r2, kMinDist2);
-            float rinv = rsqrtf(r2);
-            if (kEnergy)
-            {
-                // one Newton step: rsqrt.approx -> ~correctly rounded, unbiased for the energy sums
-                rinv = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
-            }
-            const float  rinv2 = rinv * rinv;
-            float4       lj;
-            if (kEnergy)
-            {
-                lj = nbfp_s[st.ti[c] + tj];
-            }
-            else
-            {
-                const float2 l2 = *reinterpret_cast<const float2*>(&nbfp_s[st.ti[c] + tj]);
-                lj              = make_float4(l2.x, l2.y, 0.0f, 0.0f);
-            }
-            float rinv6 = rinv2 * rinv2 * rinv2;
-            if (kExcl)
-            {
-                rinv6 *= int_bit;
-            }
-            const float vrep  = lj.y * rinv6 * rinv6;
-            const float vdisp = lj.x * rinv6;
-            float       fscal = (vrep - vdisp) * rinv2;
-            const float qq    = st.qi[c] * qje;
-            float       h_el  = 0.0f;  // q_i q_j h_el is the pair's Coulomb energy / epsfac
-            if (kEwald)
-            {
-                // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
-                const float r    = r2 * rinv;
-                const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
-                float       poly = v.erfc_c[kErfcTerms - 1];
-#pragma unroll
-                for (int k = kErfcTerms - 2; k >= 0; k--)
-                {
-                    poly = fmaf(poly, t, v.erfc_c[k]);
-                }
-                const float expm = fast_ex2(-beta2l2 * r2);
-                const float tp   = t * poly;  // erfc(beta r) = tp * expm
-                // -(d/dr)(erfc(beta r)/r)/r = expm (tp/r + 2 beta/sqrt(pi)) / r^2; exclusions drop 1/r^3
-                float fc = expm * fmaf(tp, rinv, c2b) * rinv2;
-                if (kExcl)
-                {
-                    fc -= (1.0f - int_bit) * rinv * rinv2;
-                }
-                fscal = fmaf(qq, fc, fscal);
-                if (kEnergy)
-                {
-                    h_el = fmaf(tp * expm, rinv, -v.sh_ewald);
-                }
-            }
-            else
-            {
-                float fc = rinv * rinv2;
-                if (kExcl)
-                {
-                    fc *= int_bit;
-                }
-                fscal = fmaf(qq, fc - k_rf2, fscal);
-                if (kEnergy)
-                {
-                    h_el = (rinv - v.c_rf) + v.k_rf * r2;
-                }
-            }
-            fscal = in_range ? fscal : 0.0f;
-            if (kEnergy)
-            {
-                const bool counted = kExcl ? (in_range && int_bit != 0.0f) : in_range;
-                const float e_el   = counted ? st.qi[c] * (xj.w * h_el) : 0.0f;
-                // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair)
-                const float e_lj = counted ? fmaf(vrep, 1.0f / 12.0f, fmaf(vdisp, -1.0f / 6.0f, lj.z)) : 0.0f;
-                kahan_add(st.acc_el, st.cmp_el, e_el);
-                kahan_add(st.acc_lj, st.cmp_lj, e_lj);
-            }
-            st.fix[c] = fmaf(fscal, dx, st.fix[c]);
-            st.fiy[c] = fmaf(fscal, dy, st.fiy[c]);
-            st.fiz[c] = fmaf(fscal, dz, st.fiz[c]);
-            fjx       = fmaf(-fscal, dx, fjx);
-            fjy       = fmaf(-fscal, dy, fjy);
-            fjz       = fmaf(-fscal, dz, fjz);
-        }
-        // reduce the j force over the 8 i-lanes, one vector red per j-atom
-#pragma unroll
-        for (int o = 1; o < kCl; o <<= 1)
-        {
-            fjx += __shfl_xor_sync(full, fjx, o);
-            fjy += __shfl_xor_sync(full, fjy, o);
-            fjz += __shfl_xor_sync(full, fjz, o);
-        }
-        if (ii == 0)
-        {
-            red_add_v4(&v.fnb[aj], fjx, fjy, fjz);
-        }
-    }
-}
 
 template<bool kEnergy, bool kEwald>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
@@ -274,92 +86,10 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         {
             break;
         }
-        const Sci   s   = v.sci[e];
-        const float shx = v.shiftvec[3 * s.shift], shy = v.shiftvec[3 * s.shift + 1], shz = v.shiftvec[3 * s.shift + 2];
-        const bool  central = (s.shift == kCentral);
-        EntryState  st;
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
-        {
-            const int    ai = (s.sci * kNcl + c) * kCl + ii;
-            const float4 x  = v.xq[ai];
-            st.xi[c]        = x.x + shx;
-            st.yi[c]        = x.y + shy;
-            st.zi[c]        = x.z + shz;
-            st.qi[c]        = x.w;
-            st.ti[c]        = v.tgrid[ai] * nt1;
-            st.fix[c] = st.fiy[c] = st.fiz[c] = 0.0f;
-        }
-        st.acc_el = st.cmp_el = 0.0f;
-        st.acc_lj = st.cmp_lj = 0.0f;
-        for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
-        {
-            const int4 ime     = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
-            const int  cj_lane = (lane < kJg) ? v.cj4[j4].cj[lane] : 0;
-#pragma unroll 1
-            for (int h = 0; h < kSplit; h++)
-            {
-                const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
-                const int      exi = (h == 0) ? ime.y : ime.w;
-                if (!im)
-                {
-                    continue;
-                }
-                if (exi == 0)
-                {
-                    process_half<kEnergy, kEwald, false>(v, nbfp_s, st, cj_lane, im, 0u, h, s.sci, central, ii, jj,
-                                                         rc2, pbeta, beta2l2, c2b, k_rf2);
-                }
-                else
-                {
-                    const unsigned wexcl = v.excl[exi].pair[lane];
-                    process_half<kEnergy, kEwald, true>(v, nbfp_s, st, cj_lane, im, wexcl, h, s.sci, central, ii,
-                                                        jj, rc2, pbeta, beta2l2, c2b, k_rf2);
-                }
-            }
-        }
-        // i forces: reduce over the 4 j-lanes of each i-atom
-        float sfx = 0.0f, sfy = 0.0f, sfz = 0.0f;
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
-        {
-            float fx = st.fix[c], fy = st.fiy[c], fz = st.fiz[c];
-            fx += __shfl_xor_sync(full, fx, 8);
-            fy += __shfl_xor_sync(full, fy, 8);
-            fz += __shfl_xor_sync(full, fz, 8);
-            fx += __shfl_xor_sync(full, fx, 16);
-            fy += __shfl_xor_sync(full, fy, 16);
-            fz += __shfl_xor_sync(full, fz, 16);
-            if (jj == 0)
-            {
-                red_add_v4(&v.fnb[(s.sci * kNcl + c) * kCl + ii], fx, fy, fz);
-                sfx += fx;
-                sfy += fy;
-                sfz += fz;
-            }
-        }
-        if (kEnergy)
-        {
-            e_el_acc += (double)st.acc_el - (double)st.cmp_el;
-            e_lj_acc += (double)st.acc_lj - (double)st.cmp_lj;
-        }
-        if (!central)
-        {
-            // shift forces for the virial (the central shift vector is zero)
-#pragma unroll
-            for (int o = 1; o < kCl; o <<= 1)
-            {
-                sfx += __shfl_xor_sync(full, sfx, o);
-                sfy += __shfl_xor_sync(full, sfy, o);
-                sfz += __shfl_xor_sync(full, sfz, o);
-            }
-            if (lane == 0)
-            {
-                atomicAdd(&v.fshift[3 * s.shift + 0], (double)sfx);
-                atomicAdd(&v.fshift[3 * s.shift + 1], (double)sfy);
-                atomicAdd(&v.fshift[3 * s.shift + 2], (double)sfz);
-            }
-        }
+        const Sci     s = v.sci[e];
+        const SysPtrs p = { v.xq, v.tgrid, v.fnb, v.cj4, v.excl, v.shiftvec, v.fshift };
+        process_entry<kEnergy, kEwald>(v, p, s, nbfp_s, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2, e_lj_acc,
+                                       e_el_acc);
     }
     if (kEnergy)
     {

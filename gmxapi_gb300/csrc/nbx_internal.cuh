@@ -136,6 +136,30 @@ struct DeviceView
     float erfc_c[kErfcTerms];
 };
 
+// One system of a batch, as the batched kernels see it (device table).
+struct BatchSys
+{
+    const float4*     xq;
+    const int*        tgrid;
+    float4*           fnb;
+    const Sci*        sci;
+    const Cj4*        cj4;
+    const Excl*       excl;
+    unsigned*         imask_outer;
+    const int*        cells;
+    const int*        atom_indices;
+    const int*        image;
+    const ListHeader* hdr;
+    const int*        excl_index;
+    const int*        excl_list;
+    int               n;          // atoms
+    int               atom_base;  // offset in the concatenated coordinate / force arrays
+    int               pad0, pad1;
+    double            self_energy;
+    float             box[3];
+    float             shiftvec[kNShift * 3];
+};
+
 // ---- host set-up helpers (nbx_api.cu) ----
 double one_4pi_eps0();
 float  calc_ewaldcoeff_q(float rc, float rtol);
@@ -152,6 +176,13 @@ cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* d_x, b
 cudaError_t launch_finish_energy(const DeviceView& v, double* d_energies, double* d_virial, cudaStream_t s);
 cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cudaStream_t s);
 cudaError_t measure_fp32_peak(double* tflops);
+cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
+                               int fresh, int part, int nparts, cudaStream_t s);
+cudaError_t launch_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsigned* status, cudaStream_t s);
+cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
+                                 int max_slots, int max_atoms, const float* d_x, float* d_f, double* sums,
+                                 size_t sums_bytes, int* counter, double* d_e, double* d_vir, int variant,
+                                 int num_sms, cudaStream_t s);
 
 // Bounded spin limit for device-side waits (iterations); a wait that runs out
 // sets kStatusTimeout and returns instead of hanging.

@@ -20,6 +20,85 @@ namespace
 
 constexpr int kPruneWarps = 4;
 
+// Prunes one list entry (block-cooperative): the shifted i-atoms go to shared
+// memory, each warp takes cj4 groups of the entry.
+__device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
+                            const float* shiftvec, float outer2, float inner2, int fresh, float4* xib)
+{
+    const int      lane = threadIdx.x & 31;
+    const int      warp = threadIdx.x >> 5;
+    const int      ii   = lane & 7;
+    const int      jj   = lane >> 3;
+    const unsigned full = 0xffffffffu;
+    const float sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
+    __syncthreads();
+    for (int k = threadIdx.x; k < kSc; k += blockDim.x)
+    {
+        const float4 x = xq[s.sci * kSc + k];
+        xib[k]         = make_float4(x.x + sx, x.y + sy, x.z + sz, 0.0f);
+    }
+    __syncthreads();
+    for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
+    {
+        const Cj4 c4 = cj4[j4];
+        for (int w = 0; w < kSplit; w++)
+        {
+            unsigned full_m, check, nw;
+            if (fresh)
+            {
+                full_m = c4.imei[w].imask;
+                check  = full_m;
+                nw     = 0u;
+            }
+            else
+            {
+                full_m = imask_outer[2 * j4 + w];
+                nw     = c4.imei[w].imask;
+                check  = nw ^ full_m;
+            }
+            if (!check)
+            {
+                continue;
+            }
+            for (int jm = 0; jm < kJg; jm++)
+            {
+                if (!(check & (0xffu << (jm * kNcl))))
+                {
+                    continue;
+                }
+                const float4 xj = xq[c4.cj[jm] * kCl + w * (kCl / kSplit) + jj];
+#pragma unroll
+                for (int i = 0; i < kNcl; i++)
+                {
+                    const unsigned bit = 1u << (jm * kNcl + i);
+                    if (check & bit)
+                    {
+                        const float4 xi = xib[i * kCl + ii];
+                        const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                        const float  r2 = dx * dx + dy * dy + dz * dz;
+                        if (fresh && !__any_sync(full, r2 < outer2))
+                        {
+                            full_m &= ~bit;
+                        }
+                        if (__any_sync(full, r2 < inner2))
+                        {
+                            nw |= bit;
+                        }
+                    }
+                }
+            }
+            if (lane == 0)
+            {
+                if (fresh)
+                {
+                    imask_outer[2 * j4 + w] = full_m;
+                }
+                const_cast<Cj4*>(cj4)[j4].imei[w].imask = nw;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fresh, int part, int nparts)
 {
     __shared__ float4 xib[kSc];
@@ -28,88 +107,56 @@ __global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fr
     {
         return;
     }
-    const float outer2 = v.rlist2;
-    const float inner2 = v.rlist_inner2;
-    const int   lane   = threadIdx.x & 31;
-    const int   warp   = threadIdx.x >> 5;
-    const int   ii     = lane & 7;
-    const int   jj     = lane >> 3;
-    const unsigned full = 0xffffffffu;
     // entries part, part + nparts, ... (all entries for a fresh list)
     for (int e = part + blockIdx.x * nparts; e < numSci; e += gridDim.x * nparts)
     {
-        const Sci   s  = v.sci[e];
-        const float sx = v.shiftvec[3 * s.shift], sy = v.shiftvec[3 * s.shift + 1], sz = v.shiftvec[3 * s.shift + 2];
-        __syncthreads();
-        for (int k = threadIdx.x; k < kSc; k += blockDim.x)
+        prune_entry(v.sci[e], v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2, v.rlist_inner2, fresh, xib);
+    }
+}
+
+// The same prune over a batch of systems: global entry index -> system by a
+// search of the entry prefix sums; entries whose index within their system is
+// part (mod nparts) are pruned.
+__global__ void __launch_bounds__(32 * kPruneWarps)
+        k_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2, int fresh,
+                      int part, int nparts)
+{
+    __shared__ float4 xib[kSc];
+    const int         total = entry_prefix[nsys];
+    for (int e = blockIdx.x; e < total; e += gridDim.x)
+    {
+        int lo = 0, hi = nsys - 1;
+        while (lo < hi)
         {
-            const float4 x = v.xq[s.sci * kSc + k];
-            xib[k]         = make_float4(x.x + sx, x.y + sy, x.z + sz, 0.0f);
-        }
-        __syncthreads();
-        for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
-        {
-            const Cj4 c4 = v.cj4[j4];
-            for (int w = 0; w < kSplit; w++)
+            const int mid = (lo + hi + 1) >> 1;
+            if (entry_prefix[mid] <= e)
             {
-                unsigned full_m, check, nw;
-                if (fresh)
-                {
-                    full_m = c4.imei[w].imask;
-                    check  = full_m;
-                    nw     = 0u;
-                }
-                else
-                {
-                    full_m = v.imask_outer[2 * j4 + w];
-                    nw     = c4.imei[w].imask;
-                    check  = nw ^ full_m;
-                }
-                if (!check)
-                {
-                    continue;
-                }
-                for (int jm = 0; jm < kJg; jm++)
-                {
-                    if (!(check & (0xffu << (jm * kNcl))))
-                    {
-                        continue;
-                    }
-                    const float4 xj = v.xq[c4.cj[jm] * kCl + w * (kCl / kSplit) + jj];
-#pragma unroll
-                    for (int i = 0; i < kNcl; i++)
-                    {
-                        const unsigned bit = 1u << (jm * kNcl + i);
-                        if (check & bit)
-                        {
-                            const float4 xi = xib[i * kCl + ii];
-                            const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-                            const float  r2 = dx * dx + dy * dy + dz * dz;
-                            if (fresh && !__any_sync(full, r2 < outer2))
-                            {
-                                full_m &= ~bit;
-                            }
-                            if (__any_sync(full, r2 < inner2))
-                            {
-                                nw |= bit;
-                            }
-                        }
-                    }
-                }
-                if (lane == 0)
-                {
-                    if (fresh)
-                    {
-                        v.imask_outer[2 * j4 + w] = full_m;
-                    }
-                    v.cj4[j4].imei[w].imask = nw;
-                }
+                lo = mid;
+            }
+            else
+            {
+                hi = mid - 1;
             }
         }
+        const int local = e - entry_prefix[lo];
+        if (!fresh && (local % nparts) != part)
+        {
+            continue;
+        }
+        const BatchSys& b = sys[lo];
+        prune_entry(b.sci[local], b.cj4, b.imask_outer, b.xq, b.shiftvec, outer2, inner2, fresh, xib);
     }
 }
 
 } // namespace
+
+cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
+                               int fresh, int part, int nparts, cudaStream_t s)
+{
+    k_batch_prune<<<152 * 8, 32 * kPruneWarps, 0, s>>>(sys, entry_prefix, nsys, outer2, inner2, fresh, part,
+                                                         fresh ? 1 : nparts);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s)
 {

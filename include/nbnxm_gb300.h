@@ -144,6 +144,38 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * (2 flops per FMA); used as the FP32 roofline denominator. */
 int nbx_measure_fp32_peak(int device, double* tflops);
 
+/* ---- batched ensembles ---- */
+/* Many independent systems (uneven sizes, shared types / nbfp / options) evaluated together:
+ * per-system grids and lists, one persistent force launch over all list entries, per-system
+ * FP64 energies and virials.  Coordinates and forces are one concatenated [3 * sum N] array in
+ * system order; energies are double[2 * num_systems], virials double[9 * num_systems]. */
+typedef struct nbx_batch nbx_batch;
+int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_options* opts, int device,
+                     nbx_batch** out);
+int nbx_batch_destroy(nbx_batch* b);
+const char* nbx_batch_last_error(const nbx_batch* b);
+/* offsets[num_systems+1]: atom offsets of the systems in the concatenated arrays (may be NULL) */
+int nbx_batch_atoms(nbx_batch* b, long long* total_atoms, int* offsets);
+int nbx_batch_set_stream(nbx_batch* b, void* cuda_stream);
+/* Search every system (grid + list + first prune), like nbx_search_device per system. */
+int nbx_batch_search_device(nbx_batch* b, const float* d_x);
+/* Rolling prune of part `part` over all systems in one launch (part < 0: full prune of fresh lists). */
+int nbx_batch_prune_device(nbx_batch* b, int part);
+/* One batched force / energy / virial evaluation (six launches, or one CUDA graph launch). */
+int nbx_batch_compute_device(nbx_batch* b, const float* d_x, float* d_f, double* d_energies, double* d_virial);
+/* Scheduled step (search every nstlist steps, batched rolling prune, batched compute). */
+int nbx_batch_md_step_device(nbx_batch* b, long long step, const float* d_x, float* d_f, double* d_energies,
+                             double* d_virial);
+/* The same step as num_systems sequential single-system nbx_md_step_device calls (comparison path). */
+int nbx_batch_sequential_md_step_device(nbx_batch* b, long long step, const float* d_x, float* d_f,
+                                        double* d_energies, double* d_virial);
+/* Tuning knobs: CUDA-graph capture of the batched compute (default on), force-kernel launch shape
+ * variant (0: 256x2, 1: 128x4, 2: 512x1, 3: 64x8 threads x blocks per SM) and the rolling-prune
+ * interval with its inner radius (takes effect at the next search). */
+int nbx_batch_set_graph(nbx_batch* b, int enable);
+int nbx_batch_set_kernel_variant(nbx_batch* b, int variant);
+int nbx_batch_set_prune(nbx_batch* b, int nstlist_prune, float rlist_inner);
+
 /* ---- allocation-free force evaluation ---- */
 /* Inputs of nbx_compute_noalloc: the atom data and pair list in the layouts that
  * nbx_get_grid / nbx_get_pairlist export, all in device memory. */
