@@ -1140,6 +1140,7 @@ struct nbx_batch
     int                      variant    = 0;
     bool                     use_graph  = true;
     cudaGraphExec_t          graph      = nullptr;
+    cudaStream_t             capture_stream = nullptr;  // private: capture is not allowed on legacy streams
     const void*              graph_key[4] = { nullptr, nullptr, nullptr, nullptr };
 };
 
@@ -1252,11 +1253,12 @@ int batch_compute(nbx_batch* b, const float* d_x, float* d_f, double* d_e, doubl
     {
         drop_graph(b);
         cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        // capture records without executing, so a private stream works for any caller stream
+        cudaError_t e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess)
         {
-            cudaError_t e2 = run(b->stream);
-            e              = cudaStreamEndCapture(b->stream, &g);
+            cudaError_t e2 = run(b->capture_stream);
+            e              = cudaStreamEndCapture(b->capture_stream, &g);
             if (e2 != cudaSuccess)
             {
                 e = e2;
@@ -1309,6 +1311,7 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
     b->own_stream = true;
     if (opts)
     {
@@ -1388,6 +1391,10 @@ int nbx_batch_destroy(nbx_batch* b)
     if (b->own_stream && b->stream)
     {
         cudaStreamDestroy(b->stream);
+    }
+    if (b->capture_stream)
+    {
+        cudaStreamDestroy(b->capture_stream);
     }
     delete b;
     return NBX_OK;

@@ -28,6 +28,8 @@ def test_batch_matches_single_systems(graph, variant):
     torch = pytest.importorskip("torch")
     ens = _ensemble()
     b = BatchForceCalculator(ens, _opts())
+    if variant == 2:
+        b.set_stream(0)  # the legacy default stream (graphs are captured on a private stream)
     b.set_graph(graph)
     b.set_kernel_variant(variant)
     dev = torch.device("cuda:0")
