@@ -227,6 +227,80 @@ def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
                                         "rolling prune as autotuned"}
 
 
+def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
+    """Force-matching gradient on the 24,000-atom random LJ + Coulomb liquid (8 types,
+    Lorentz-Berthelot): loss sum |F - F_target|^2 with F_target at parameters perturbed
+    by up to 5 %; one step = forward (F + E) + backward kernel (dL/dx, dL/dq, dL/dsigma,
+    dL/depsilon).  Reported: the forward alone, the full gradient step, and the
+    backward entry point alone, all on the current list (no search inside)."""
+    import torch
+
+    from gmxapi_gb300 import nblib, systems
+    from gmxapi_gb300.adjoint import DifferentiableNonbonded, lorentz_berthelot_nbfp
+
+    s = systems.lj_liquid(n=24000, ntypes=8, seed=4)
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=RLIST, rcoulomb=RC,
+                                 nstlist_prune=0)
+    eng = DifferentiableNonbonded(s, opts, device=dev)
+    d = torch.device("cuda", dev)
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(12)
+    x = torch.tensor(s.x, device=d, requires_grad=True)
+    q = torch.tensor(s.q, device=d, requires_grad=True)
+    sig = torch.tensor(s.sigma, dtype=torch.float64, device=d, requires_grad=True)
+    eps = torch.tensor(s.epsilon, dtype=torch.float64, device=d, requires_grad=True)
+    with torch.no_grad():
+        qt = q * torch.tensor(rng.uniform(0.95, 1.05, s.n), dtype=torch.float32, device=d)
+        nbt = lorentz_berthelot_nbfp(sig * torch.tensor(rng.uniform(0.95, 1.05, s.ntypes), device=d),
+                                     eps * torch.tensor(rng.uniform(0.95, 1.05, s.ntypes), device=d))
+        f_target, _ = eng(x, qt, nbt)
+
+    def forward():
+        with torch.no_grad():
+            eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+
+    def grad_step():
+        for t in (x, q, sig, eps):
+            t.grad = None
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        ((f - f_target) ** 2).sum().backward()
+
+    gf = torch.randn(s.n, 3, device=d)
+    ge = torch.tensor([0.5, 0.5], dtype=torch.float64, device=d)
+    gx = torch.empty(s.n, 3, device=d)
+    gq = torch.empty(s.n, device=d)
+    gp = torch.empty(s.ntypes, s.ntypes, 2, dtype=torch.float64, device=d)
+
+    def backward_only():
+        eng.calc.backward_device(x.data_ptr(), gf.data_ptr(), ge.data_ptr(), gx.data_ptr(), gq.data_ptr(),
+                                 gp.data_ptr())
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z) / steps
+
+    fwd_ms = timed(forward)
+    step_ms = timed(grad_step)
+    bwd_ms = timed(backward_only)
+    eng.close()
+    return {"workload": "random LJ+Coulomb liquid, 24000 atoms, 8 types, Lorentz-Berthelot, "
+                        "rejection at 0.5 sigma (seed 4)", "atoms": s.n, "steps": steps,
+            "forward_ms": fwd_ms, "gradient_step_ms": step_ms, "backward_entry_ms": bwd_ms,
+            "adjoint_cost_vs_forward": bwd_ms / fwd_ms,
+            "gradient_step_vs_forward": step_ms / fwd_ms,
+            "gradient_steps_per_s": 1e3 / step_ms,
+            "note": "forward = F+E (convert, force, reduce, energies); backward entry = convert, "
+                    "gradient prepare, adjoint kernel, finish, FP64 table gradients; inputs fit in L2"}
+
+
 def workload_config() -> dict:
     return {"workload": "spc_water_288k", "atoms": 288000, "box_nm": 14.21, "rc_nm": RC, "rlist_nm": RLIST,
             "rlist_inner_nm": RLIST_INNER, "nstlist": NSTLIST, "nstlist_prune": NSTPRUNE,
@@ -336,6 +410,7 @@ def run_ours(args) -> None:
     from gmxapi_gb300.nblib import measure_fp32_peak
 
     ensemble = measure_ensemble(dev) if not args.no_extras else None
+    adjoint = measure_adjoint(dev) if not args.no_extras else None
 
     peak = measure_fp32_peak(dev)
     pairs_avg = 0.5 * (pairs0 + pairs1)
@@ -365,6 +440,8 @@ def run_ours(args) -> None:
     }
     if ensemble is not None:
         line["batched_ensemble"] = ensemble
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     print(json.dumps(line))
 
 
@@ -374,7 +451,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched-ensemble and adjoint measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -35,7 +35,7 @@ EXPORTED = [
     "nbx_batch_create", "nbx_batch_destroy", "nbx_batch_last_error", "nbx_batch_atoms", "nbx_batch_set_stream",
     "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
-    "nbx_batch_set_prune",
+    "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
 ]
 
 
@@ -155,6 +155,8 @@ def load():
     L.nbx_batch_set_graph.argtypes = [vp, C.c_int]
     L.nbx_batch_set_kernel_variant.argtypes = [vp, C.c_int]
     L.nbx_batch_set_prune.argtypes = [vp, C.c_int, C.c_float]
+    L.nbx_backward_device.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.nbx_set_parameters_device.argtypes = [vp, vp, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",

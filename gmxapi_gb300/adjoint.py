@@ -1,0 +1,121 @@
+"""Differentiable short-range nonbonded forces for force matching.
+
+There is no counterpart in the reference, which only evaluates forces.  The
+forward pass is the cluster-pair force/energy kernel (nblib
+``ForceCalculator::compute``, api/nblib/gmxcalculator.cpp:88-101); the backward
+pass is a hand-written CUDA kernel that walks the same pair list, recomputes
+every pair term and returns, for upstream gradients G = dL/dF and
+gE = dL/d(E_lj, E_coul):
+
+* dL/dx  -- the Hessian-vector product with G plus the energy terms,
+* dL/dq  -- per atom,
+* dL/dnbfp -- per type pair, for the {6*C6, 12*C12} table (FP64 sums).
+
+Per-type sigma/epsilon gradients follow by the chain rule through the
+combination rule (``lorentz_berthelot_nbfp``), which autograd applies on the
+ntypes x ntypes table.  Everything stays on the GPU and runs on the current
+torch stream; there is no CPU path.
+"""
+from __future__ import annotations
+
+import torch
+from torch.autograd.function import once_differentiable
+
+from .nblib import CoulombType, ForceCalculator, NBKernelOptions
+
+
+def lorentz_berthelot_nbfp(sigma: torch.Tensor, epsilon: torch.Tensor) -> torch.Tensor:
+    """(ntypes, ntypes, 2) table {6*C6, 12*C12} from per-type sigma and epsilon.
+
+    sigma_ij = (sigma_i + sigma_j) / 2, epsilon_ij = sqrt(epsilon_i epsilon_j),
+    C6 = 4 eps s^6, C12 = 4 eps s^12 (the combination nblib applies in
+    api/nblib/particletype.cpp and gmxsetup.cpp:143-166).
+    """
+    sig = 0.5 * (sigma[:, None] + sigma[None, :])
+    eps = torch.sqrt(epsilon[:, None] * epsilon[None, :])
+    s6 = sig**6
+    c6 = 4.0 * eps * s6
+    c12 = c6 * s6
+    return torch.stack((6.0 * c6, 12.0 * c12), dim=-1)
+
+
+class _NonbondedFunction(torch.autograd.Function):
+    """(x, q, nbfp) -> (forces (N, 3) float32, energies [E_lj, E_coul] float64)."""
+
+    @staticmethod
+    def forward(ctx, x, q, nbfp, engine):
+        calc = engine.calc
+        calc.set_stream(torch.cuda.current_stream(x.device).cuda_stream)
+        # the kernels read float32 parameters; the table gradient comes back in the
+        # table's own dtype (FP64 sums when the table is float64)
+        nbfp32 = nbfp.to(torch.float32).contiguous()
+        calc.set_parameters_device(q.data_ptr(), nbfp32.data_ptr())
+        f = torch.empty_like(x)
+        e = torch.zeros(2, dtype=torch.float64, device=x.device)
+        calc.compute_device(x.data_ptr(), f.data_ptr(), e.data_ptr(), None)
+        ctx.engine = engine
+        ctx.save_for_backward(x, q, nbfp)
+        return f, e
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, g_f, g_e):
+        x, q, nbfp = ctx.saved_tensors
+        calc = ctx.engine.calc
+        dev = x.device
+        calc.set_stream(torch.cuda.current_stream(dev).cuda_stream)
+        # the handle may have seen other parameters since the forward pass
+        nbfp32 = nbfp.to(torch.float32).contiguous()
+        calc.set_parameters_device(q.data_ptr(), nbfp32.data_ptr())
+        g_f = torch.zeros_like(x) if g_f is None else g_f.to(torch.float32).contiguous()
+        g_e = None if g_e is None else g_e.to(torch.float64).contiguous()
+        need_x, need_q, need_p = ctx.needs_input_grad[:3]
+        gx = torch.empty_like(x) if need_x else None
+        gq = torch.empty_like(q) if need_q else None
+        gp = torch.empty(nbfp.shape, dtype=torch.float64, device=dev) if need_p else None
+        calc.backward_device(x.data_ptr(), g_f.data_ptr(), g_e.data_ptr() if g_e is not None else None,
+                             gx.data_ptr() if gx is not None else None, gq.data_ptr() if gq is not None else None,
+                             gp.data_ptr() if gp is not None else None)
+        return gx, gq, (gp.to(nbfp.dtype) if gp is not None else None), None
+
+
+class DifferentiableNonbonded:
+    """Pair-list force field on one GPU whose forces and energies are differentiable.
+
+    ``engine(x, q, nbfp)`` returns ``(forces, energies)`` for coordinates
+    ``x`` (N, 3) float32, charges ``q`` (N,) float32 and the type table
+    ``nbfp`` (ntypes, ntypes, 2) float32 or float64, all CUDA tensors.  ``nbfp`` is
+    symmetrised before use so its gradient does not depend on which atom of a
+    pair the list puts in the i-cluster.  The pair list is rebuilt from ``x``
+    on every call unless ``search=False`` (then the list of the last search
+    is used, as within an nstlist interval).
+    """
+
+    def __init__(self, system, options: NBKernelOptions | None = None, device: int = 0):
+        opts = options or NBKernelOptions(coulomb_type=CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
+                                          nstlist_prune=0)
+        opts.compute_virial_and_energy = True
+        self.system = system
+        self.ntypes = int(system.ntypes)
+        self.device = torch.device("cuda", device)
+        self.calc = ForceCalculator(system, opts, device)
+
+    def search(self, x: torch.Tensor):
+        self.calc.set_stream(torch.cuda.current_stream(x.device).cuda_stream)
+        self.calc.search_device(x.detach().contiguous().data_ptr())
+
+    def __call__(self, x: torch.Tensor, q: torch.Tensor, nbfp: torch.Tensor, search: bool = True):
+        if not (x.is_cuda and q.is_cuda and nbfp.is_cuda):
+            raise ValueError("x, q and nbfp must be CUDA tensors (there is no CPU path)")
+        nt = self.ntypes
+        if x.shape != (self.system.n, 3) or q.shape != (self.system.n,) or nbfp.shape != (nt, nt, 2):
+            raise ValueError("x must be (N, 3), q (N,) and nbfp (ntypes, ntypes, 2)")
+        x = x.to(torch.float32).contiguous()
+        q = q.to(torch.float32).contiguous()
+        nbfp = (0.5 * (nbfp + nbfp.transpose(0, 1))).contiguous()
+        if search:
+            self.search(x)
+        return _NonbondedFunction.apply(x, q, nbfp, self)
+
+    def close(self):
+        self.calc.close()

@@ -26,6 +26,7 @@ UNITS = {
     "nbx_prune.cu": ["--fmad=false"],
     "nbx_force.cu": [],
     "nbx_batch.cu": [],
+    "nbx_adjoint.cu": [],
     "nbx_api.cu": [],
 }
 

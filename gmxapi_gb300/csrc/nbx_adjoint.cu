@@ -1,0 +1,448 @@
+// Adjoint of the cluster-pair force / energy kernel.
+//
+// There is no counterpart in the reference (it only computes forces).  Given
+// upstream gradients G_i = dL/dF_i on the forces and gE = dL/dE on the LJ and
+// Coulomb energies, one pass over the same pair list recomputes every pair
+// term (nothing from the forward pass is stored) and accumulates
+//   dL/dx  (a Hessian-vector product with G, plus -gE times the forces),
+//   dL/dq  per atom,
+//   dL/d(6 C6), dL/d(12 C12) per type pair (FP64 sums).
+// For a pair with r = x_i - x_j (+ shift), s = r^2, force on i f = phi(s) r and
+// g = G_i - G_j:
+//   dL/dr = phi g + (2 phi'(s) (g.r) - gE_lj phi_lj - gE_c qq psi) r,
+// with phi = phi_lj + qq psi, phi_lj = (12C12 r^-12 - 6C6 r^-6) / r^2 and, for
+// Ewald, psi = erfc(br)/r^3 + (2b/sqrt(pi)) e^{-b^2 r^2}/r^2 (minus 1/r^3 for an
+// excluded pair), whose derivative is psi' = -(1.5 psi + (2b/sqrt(pi)) b^2
+// e^{-b^2 r^2}) / r^2 for normal and excluded pairs alike.
+//
+// Layout: as the forward kernel (persistent warps, one list entry per warp,
+// lane = j-atom-of-half * 8 + i-atom); the entry's shifted i-atoms and their
+// upstream gradients are staged in shared memory, the per-lane i accumulators
+// (dx, dy, dz, dq per i-cluster) stay in registers; j accumulators are reduced
+// over the 8 i-lanes and added with one vector red per j-atom.  Type-pair
+// gradients go to a warp-private shared table and are flushed to FP64 global
+// sums after every entry.
+#include "nbx_internal.cuh"
+#include "nbx_pair_core.cuh"
+
+namespace nbx
+{
+namespace
+{
+
+constexpr int kAdjThreads    = 256;
+constexpr int kAdjWarps      = kAdjThreads / 32;
+constexpr int kAdjMaxTypes1  = 16;
+
+struct AdjConsts
+{
+    float gE_lj, gE_c;  // upstream energy gradients
+};
+
+template<bool kEwald, bool kExcl>
+__device__ __forceinline__ void adj_half(const DeviceView& v, const float2* __restrict__ nbfp_s, float2* ttab,
+                                         const float4* __restrict__ xis, const float4* __restrict__ gis,
+                                         const float4* __restrict__ gnb, float4* dnb, const int cj_lane,
+                                         unsigned im, unsigned wexcl, int h, int sci, bool central, int ii, int jj,
+                                         float dxa[kNcl], float dya[kNcl], float dza[kNcl], float dqa[kNcl],
+                                         const AdjConsts& k, float pbeta, float beta2l2, float c2b, float b2c2b)
+{
+    const unsigned full = 0xffffffffu;
+    const int      nt1  = v.ntypes1;
+#pragma unroll 1
+    for (int jm = 0; jm < kJg; jm++)
+    {
+        const unsigned imj = (im >> (jm * kNcl)) & 0xffu;
+        const int      cj  = __shfl_sync(full, cj_lane, jm);
+        if (!imj)
+        {
+            continue;
+        }
+        const int      aj = cj * kCl + h * (kCl / kSplit) + jj;
+        const float4   xj = v.xq[aj];
+        const float4   gj = gnb[aj];
+        const int      tj = v.tgrid[aj];
+        const unsigned wj = wexcl >> (jm * kNcl);
+        float          djx = 0.0f, djy = 0.0f, djz = 0.0f, djq = 0.0f;
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            if (!(imj & (1u << c)))
+            {
+                continue;
+            }
+            const float4 xi = xis[c * kCl + ii];
+            const float4 gi = gis[c * kCl + ii];
+            const int    ti = __float_as_int(gi.w);
+            const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            float        r2 = dx * dx + dy * dy + dz * dz;
+            bool         in_range;
+            float        int_bit;
+            if (kExcl)
+            {
+                const bool self_lower = central && (sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
+                in_range              = (r2 < v.rc2) && !self_lower;
+                int_bit               = (wj & (1u << c)) ? 1.0f : 0.0f;
+            }
+            else
+            {
+                in_range = r2 < v.rc2;
+                int_bit  = 1.0f;
+            }
+            r2                  = fmaxf(r2, kMinDist2);
+            float       rinv    = rsqrtf(r2);
+            rinv                = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
+            const float rinv2   = rinv * rinv;
+            const float2 lj     = nbfp_s[ti * nt1 + tj];
+            float        rinv6  = rinv2 * rinv2 * rinv2;
+            if (kExcl)
+            {
+                rinv6 *= int_bit;
+            }
+            const float vrep    = lj.y * rinv6 * rinv6;
+            const float vdisp   = lj.x * rinv6;
+            const float phi_lj  = (vrep - vdisp) * rinv2;
+            const float dphi_lj = (4.0f * vdisp - 7.0f * vrep) * rinv2 * rinv2;
+            float       psi, dpsi, hq;  // Coulomb phi / qq, its s-derivative, energy / qq
+            if (kEwald)
+            {
+                const float r    = r2 * rinv;
+                const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
+                float       poly = v.erfc_c[kErfcTerms - 1];
+#pragma unroll
+                for (int m = kErfcTerms - 2; m >= 0; m--)
+                {
+                    poly = fmaf(poly, t, v.erfc_c[m]);
+                }
+                const float expm = fast_ex2(-beta2l2 * r2);
+                const float tp   = t * poly;
+                psi              = expm * fmaf(tp, rinv, c2b) * rinv2;
+                hq               = tp * expm * rinv - int_bit * v.sh_ewald;
+                if (kExcl)
+                {
+                    psi -= (1.0f - int_bit) * rinv * rinv2;
+                    hq -= (1.0f - int_bit) * rinv;
+                }
+                dpsi = -(1.5f * psi + b2c2b * expm) * rinv2;
+            }
+            else
+            {
+                const float r3 = rinv * rinv2;
+                psi            = int_bit * r3 - 2.0f * v.k_rf;
+                dpsi           = -1.5f * int_bit * r3 * rinv2;
+                hq             = int_bit * rinv + v.k_rf * r2 - v.c_rf;
+            }
+            const float qq   = v.epsfac * xi.w * xj.w;
+            const float phi  = fmaf(qq, psi, phi_lj);
+            const float dphi = fmaf(qq, dpsi, dphi_lj);
+            const float gx = gi.x - gj.x, gy = gi.y - gj.y, gz = gi.z - gj.z;
+            const float gr   = gx * dx + gy * dy + gz * dz;
+            const float coef = 2.0f * dphi * gr - fmaf(k.gE_c * qq, psi, k.gE_lj * phi_lj);
+            float       ux   = fmaf(phi, gx, coef * dx);
+            float       uy   = fmaf(phi, gy, coef * dy);
+            float       uz   = fmaf(phi, gz, coef * dz);
+            float       wq   = v.epsfac * fmaf(psi, gr, k.gE_c * hq);
+            ux               = in_range ? ux : 0.0f;
+            uy               = in_range ? uy : 0.0f;
+            uz               = in_range ? uz : 0.0f;
+            wq               = in_range ? wq : 0.0f;
+            dxa[c] += ux;
+            dya[c] += uy;
+            dza[c] += uz;
+            dqa[c] = fmaf(wq, xj.w, dqa[c]);
+            djx -= ux;
+            djy -= uy;
+            djz -= uz;
+            djq = fmaf(wq, xi.w, djq);
+            // dL/d(6C6), dL/d(12C12) of this type pair
+            if (in_range && int_bit != 0.0f)
+            {
+                const float dc12 = fmaf(gr * rinv6, rinv6 * rinv2, k.gE_lj * (rinv6 * rinv6 + v.cpot12) * (1.0f / 12.0f));
+                const float dc6  = -fmaf(gr * rinv6, rinv2, k.gE_lj * (rinv6 + v.cpot6) * (1.0f / 6.0f));
+                float2*     slot = &ttab[ti * nt1 + tj];
+                atomicAdd(&slot->x, dc6);
+                atomicAdd(&slot->y, dc12);
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < kCl; o <<= 1)
+        {
+            djx += __shfl_xor_sync(full, djx, o);
+            djy += __shfl_xor_sync(full, djy, o);
+            djz += __shfl_xor_sync(full, djz, o);
+            djq += __shfl_xor_sync(full, djq, o);
+        }
+        if (ii == 0)
+        {
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(&dnb[aj]), "f"(djx), "f"(djy),
+                         "f"(djz), "f"(djq)
+                         : "memory");
+        }
+    }
+}
+
+template<bool kEwald>
+__global__ void __launch_bounds__(kAdjThreads, 2)
+        k_backward(DeviceView v, const float4* __restrict__ gnb, float4* dnb, double* gnbfp, int* work_counter,
+                   const double* __restrict__ gE)
+{
+    AdjConsts k{ 0.0f, 0.0f };
+    if (gE)
+    {
+        k.gE_lj = (float)gE[0];
+        k.gE_c  = (float)gE[1];
+    }
+    __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ float4 xis_s[kAdjWarps][kSc];
+    __shared__ float4 gis_s[kAdjWarps][kSc];
+    const int         nt1  = v.ntypes1;
+    const int         warp = threadIdx.x >> 5;
+    const int         lane = threadIdx.x & 31;
+    for (int m = threadIdx.x; m < nt1 * nt1; m += blockDim.x)
+    {
+        nbfp_s[m] = v.nbfp[m];
+    }
+    for (int m = lane; m < nt1 * nt1; m += 32)
+    {
+        ttab_s[warp][m] = make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    {
+        return;
+    }
+    const unsigned full    = 0xffffffffu;
+    const int      ii      = lane & 7;
+    const int      jj      = lane >> 3;
+    const int      numSci  = v.hdr->num_sci;
+    const float    beta    = v.beta;
+    const float    pbeta   = v.erfc_p * beta;
+    const float    beta2l2 = beta * beta * 1.4426950408889634f;
+    const float    c2b     = 1.1283791670955126f * beta;
+    const float    b2c2b   = beta * beta * c2b;
+    float4*        xis     = xis_s[warp];
+    float4*        gis     = gis_s[warp];
+    float2*        ttab    = ttab_s[warp];
+    for (;;)
+    {
+        int e = 0;
+        if (lane == 0)
+        {
+            e = atomicAdd(work_counter, 1);
+        }
+        e = __shfl_sync(full, e, 0);
+        if (e >= numSci)
+        {
+            break;
+        }
+        const Sci   s  = v.sci[e];
+        const float sx = v.shiftvec[3 * s.shift], sy = v.shiftvec[3 * s.shift + 1], sz = v.shiftvec[3 * s.shift + 2];
+        const bool  central = (s.shift == kCentral);
+        for (int m = lane; m < kSc; m += 32)
+        {
+            const int    a = s.sci * kSc + m;
+            const float4 x = v.xq[a];
+            const float4 g = gnb[a];
+            xis[m]         = make_float4(x.x + sx, x.y + sy, x.z + sz, x.w);
+            gis[m]         = make_float4(g.x, g.y, g.z, __int_as_float(v.tgrid[a]));
+        }
+        __syncwarp();
+        float dxa[kNcl], dya[kNcl], dza[kNcl], dqa[kNcl];
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            dxa[c] = dya[c] = dza[c] = dqa[c] = 0.0f;
+        }
+        for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
+        {
+            const int4 ime     = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
+            const int  cj_lane = (lane < kJg) ? v.cj4[j4].cj[lane] : 0;
+#pragma unroll 1
+            for (int h = 0; h < kSplit; h++)
+            {
+                const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
+                const int      exi = (h == 0) ? ime.y : ime.w;
+                if (!im)
+                {
+                    continue;
+                }
+                if (exi == 0)
+                {
+                    adj_half<kEwald, false>(v, nbfp_s, ttab, xis, gis, gnb, dnb, cj_lane, im, 0u, h, s.sci, central,
+                                            ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                }
+                else
+                {
+                    const unsigned wexcl = v.excl[exi].pair[lane];
+                    adj_half<kEwald, true>(v, nbfp_s, ttab, xis, gis, gnb, dnb, cj_lane, im, wexcl, h, s.sci,
+                                           central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kNcl; c++)
+        {
+            float ax = dxa[c], ay = dya[c], az = dza[c], aq = dqa[c];
+            for (int o = 8; o < 32; o <<= 1)
+            {
+                ax += __shfl_xor_sync(full, ax, o);
+                ay += __shfl_xor_sync(full, ay, o);
+                az += __shfl_xor_sync(full, az, o);
+                aq += __shfl_xor_sync(full, aq, o);
+            }
+            if (jj == 0)
+            {
+                float4* dst = &dnb[(s.sci * kNcl + c) * kCl + ii];
+                asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(ax), "f"(ay), "f"(az),
+                             "f"(aq)
+                             : "memory");
+            }
+        }
+        // flush the type-pair gradients of this entry into the FP64 sums
+        __syncwarp();
+        for (int m = lane; m < nt1 * nt1; m += 32)
+        {
+            const float2 t = ttab[m];
+            if (t.x != 0.0f || t.y != 0.0f)
+            {
+                atomicAdd(&gnbfp[2 * m], (double)t.x);
+                atomicAdd(&gnbfp[2 * m + 1], (double)t.y);
+                ttab[m] = make_float2(0.0f, 0.0f);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Upstream force gradients to grid order; clears the output accumulators.
+__global__ void k_adj_prepare(DeviceView v, const float* __restrict__ gF, float4* gnb, float4* dnb)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const int a = v.atom_indices[k];
+    gnb[k]      = (a >= 0) ? make_float4(gF[3 * a], gF[3 * a + 1], gF[3 * a + 2], 0.0f) : make_float4(0, 0, 0, 0);
+    dnb[k]      = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// Atom-order outputs; dL/dq also gets the self-energy term.
+__global__ void k_adj_finish(DeviceView v, const float4* __restrict__ dnb, const double* __restrict__ gE, float* gx,
+                             float* gq)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= v.n)
+    {
+        return;
+    }
+    const int    k = v.cells[a];
+    const float4 d = dnb[k];
+    if (gx)
+    {
+        gx[3 * a]     = d.x;
+        gx[3 * a + 1] = d.y;
+        gx[3 * a + 2] = d.z;
+    }
+    if (gq)
+    {
+        const float q    = v.xq[k].w;
+        // d/dq of -epsfac beta/sqrt(pi) q^2 (Ewald) or -epsfac c_rf q^2 / 2 (RF)
+        const float self = (v.coulomb == 0) ? -2.0f * v.epsfac * v.beta * 0.5641895835477563f * q
+                                            : -v.epsfac * v.c_rf * q;
+        gq[a]            = gE ? d.w + (float)gE[1] * self : d.w;
+    }
+}
+
+} // namespace
+
+int adjoint_max_types1()
+{
+    return kAdjMaxTypes1;
+}
+
+cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double* d_gE, float4* gnb, float4* dnb,
+                            double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s)
+{
+    const int tb    = 256;
+    const int slots = v.g.cells_capacity * kSc;
+    k_adj_prepare<<<(slots + tb - 1) / tb, tb, 0, s>>>(v, d_gF, gnb, dnb);
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    cudaMemsetAsync(d_gnbfp, 0, sizeof(double) * 2 * v.ntypes1 * v.ntypes1, s);
+    if (v.coulomb == 0)
+    {
+        k_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+    }
+    else
+    {
+        k_backward<false><<<num_sms * 2, kAdjThreads, 0, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+    }
+    k_adj_finish<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, dnb, d_gE, d_gx, d_gq);
+    return cudaGetLastError();
+}
+
+// Charges and LJ parameters for force matching: q (atom order) into xq.w and the
+// nbfp table (with the all-zero filler type); the self energy follows the charges.
+__global__ void k_set_q(DeviceView v, const float* __restrict__ q)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const int a = v.atom_indices[k];
+    if (a >= 0)
+    {
+        v.xq[k].w = q[a];
+    }
+}
+
+__global__ void k_set_nbfp(float2* nbfp, const float* __restrict__ src, int nt)
+{
+    const int m   = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt1 = nt + 1;
+    if (m >= nt1 * nt1)
+    {
+        return;
+    }
+    const int i = m / nt1, j = m % nt1;
+    nbfp[m]     = (i < nt && j < nt) ? make_float2(src[2 * (i * nt + j)], src[2 * (i * nt + j) + 1])
+                                     : make_float2(0.0f, 0.0f);
+}
+
+__global__ void k_compact_gnbfp(const double* padded, double* out, int nt)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nt * nt)
+    {
+        return;
+    }
+    const int i = m / nt, j = m % nt;
+    out[2 * m]     = padded[2 * (i * (nt + 1) + j)];
+    out[2 * m + 1] = padded[2 * (i * (nt + 1) + j) + 1];
+}
+
+cudaError_t launch_compact_gnbfp(const double* padded, double* out, int nt, cudaStream_t s)
+{
+    k_compact_gnbfp<<<(nt * nt + 255) / 256, 256, 0, s>>>(padded, out, nt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s)
+{
+    const int tb = 256;
+    if (d_q)
+    {
+        cudaMemcpyAsync(const_cast<float*>(v.q), d_q, sizeof(float) * v.n, cudaMemcpyDeviceToDevice, s);
+        k_set_q<<<(v.g.cells_capacity * kSc + tb - 1) / tb, tb, 0, s>>>(v, d_q);
+    }
+    if (d_nbfp)
+    {
+        const int nt = v.ntypes1 - 1;
+        k_set_nbfp<<<(v.ntypes1 * v.ntypes1 + tb - 1) / tb, tb, 0, s>>>(const_cast<float2*>(v.nbfp), d_nbfp, nt);
+    }
+    return cudaGetLastError();
+}
+
+} // namespace nbx

@@ -49,6 +49,11 @@ struct nbx_handle
     double* d_out = nullptr;  // energies[2] + virial[9]
     unsigned long long* d_count = nullptr;
     ListHeader* h_hdr = nullptr;  // pinned copy for reading sizes
+    // adjoint scratch, allocated on the first backward call
+    float4* d_gnb   = nullptr;
+    float4* d_dnb   = nullptr;
+    double* d_gnbfp = nullptr;
+    int*    d_adj_counter = nullptr;
     // timing / launch accounting
     bool        timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -950,6 +955,68 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
         std::memcpy(virial, hout + 2, 9 * sizeof(double));
     }
     return NBX_OK;
+}
+
+int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, const double* d_gE, float* d_gx,
+                        float* d_gq, double* d_gnbfp)
+{
+    if (!h || !d_x || !d_gF)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->have_list)
+    {
+        return set_error(h, NBX_ERR_STATE, "no pair list");
+    }
+    if (h->v.ntypes1 > adjoint_max_types1())
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint supports at most 15 particle types");
+    }
+    cudaSetDevice(h->device);
+    DeviceView& v = h->v;
+    cudaError_t e = cudaSuccess;
+    if (!h->d_gnb)
+    {
+        const size_t slots = (size_t)v.g.cells_capacity * kSc;
+        e = dalloc(h, &h->d_gnb, slots);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_dnb, slots);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_gnbfp, 2 * (size_t)v.ntypes1 * v.ntypes1);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_adj_counter, 1);
+        if (e != cudaSuccess)
+        {
+            return cuda_check(h, e, "adjoint allocation");
+        }
+    }
+    e = launch_convert_x(v, d_x, h->stream);
+    if (e == cudaSuccess)
+    {
+        e = launch_backward(v, d_gF, d_gE, h->d_gnb, h->d_dnb, h->d_gnbfp, h->d_adj_counter, d_gx, d_gq, h->num_sms,
+                            h->stream);
+    }
+    if (e == cudaSuccess && d_gnbfp)
+    {
+        e = launch_compact_gnbfp(h->d_gnbfp, d_gnbfp, v.ntypes1 - 1, h->stream);
+    }
+    h->launches += 4 + (d_gnbfp ? 1 : 0);
+    return cuda_check(h, e, "nbx_backward_device");
+}
+
+int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nbfp)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    if (d_q)
+    {
+        // the self energy now comes from the charges on the device
+        h->v.self_on_device = 1;
+        h->v.self_energy    = 0.0;
+    }
+    cudaError_t e = launch_set_parameters(h->v, d_q, d_nbfp, h->stream);
+    h->launches += (d_q ? 1 : 0) + (d_nbfp ? 1 : 0);
+    return cuda_check(h, e, "nbx_set_parameters_device");
 }
 
 int nbx_set_timing(nbx_handle* h, int enable)

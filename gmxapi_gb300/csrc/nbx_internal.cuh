@@ -178,6 +178,11 @@ cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cu
 cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
                                int fresh, int part, int nparts, cudaStream_t s);
+int         adjoint_max_types1();
+cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double* d_gE, float4* gnb, float4* dnb,
+                            double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s);
+cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);
+cudaError_t launch_compact_gnbfp(const double* padded, double* out, int nt, cudaStream_t s);
 cudaError_t launch_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsigned* status, cudaStream_t s);
 cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
                                  int max_slots, int max_atoms, const float* d_x, float* d_f, double* sums,

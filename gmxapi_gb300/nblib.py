@@ -182,6 +182,19 @@ class ForceCalculator:
             self.virial = vir.reshape(3, 3)
         return out
 
+    def set_parameters_device(self, q_ptr: int | None, nbfp_ptr: int | None):
+        """New charges ([N] float32) and/or nbfp ([ntypes^2 * 2] float32) from device memory."""
+        check(_lib.load().nbx_set_parameters_device(self.h, C.c_void_p(q_ptr) if q_ptr else None,
+                                                    C.c_void_p(nbfp_ptr) if nbfp_ptr else None), self.h)
+
+    def backward_device(self, x_ptr: int, gf_ptr: int, ge_ptr: int | None, gx_ptr: int | None,
+                        gq_ptr: int | None, gnbfp_ptr: int | None):
+        """Adjoint pass over the current list (all arguments are device pointers)."""
+        vp = C.c_void_p
+        check(_lib.load().nbx_backward_device(self.h, vp(x_ptr), vp(gf_ptr), vp(ge_ptr) if ge_ptr else None,
+                                              vp(gx_ptr) if gx_ptr else None, vp(gq_ptr) if gq_ptr else None,
+                                              vp(gnbfp_ptr) if gnbfp_ptr else None), self.h)
+
     def set_timing(self, enable: bool):
         check(_lib.load().nbx_set_timing(self.h, int(bool(enable))), self.h)
 

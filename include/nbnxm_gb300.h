@@ -144,6 +144,20 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * (2 flops per FMA); used as the FP32 roofline denominator. */
 int nbx_measure_fp32_peak(int device, double* tflops);
 
+/* ---- adjoint (differentiable forces) ---- */
+/* No counterpart in the reference.  Given upstream gradients d_gF = dL/dF ([3N] float, atom
+ * order) and d_gE = dL/dE for {LJ, Coulomb} energies ([2] double, NULL = zero), all in device
+ * memory, recomputes every pair term of the current list at the coordinates d_x and writes
+ * dL/dx ([3N] float: the Hessian-vector product with d_gF plus the energy terms), dL/dq ([N]
+ * float) and dL/d(nbfp) ([num_types^2 * 2] double: gradients of the {6*C6, 12*C12} entries as the
+ * list uses them, FP64 sums; entry (a, b) gets the pairs whose i-cluster atom has type a).
+ * Any output may be NULL.  At most 15 particle types.  Runs on the handle's stream. */
+int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, const double* d_gE, float* d_gx,
+                        float* d_gq, double* d_gnbfp);
+/* Replaces the charges ([N], atom order) and/or the nbfp matrix ([num_types^2 * 2]), both in device
+ * memory (either may be NULL); the list is kept.  The self energy then follows the new charges. */
+int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nbfp);
+
 /* ---- batched ensembles ---- */
 /* Many independent systems (uneven sizes, shared types / nbfp / options) evaluated together:
  * per-system grids and lists, one persistent force launch over all list entries, per-system
