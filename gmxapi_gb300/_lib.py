@@ -14,6 +14,13 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libnbnxm_gb300.so")
 
 NBX_OK = 0
+NBX_ERR_INVALID_INPUT = 1
+NBX_ERR_OUT_OF_MEMORY = 2
+NBX_ERR_LIST_OVERFLOW = 3
+NBX_ERR_CUDA = 4
+NBX_ERR_TIMEOUT = 5
+NBX_ERR_NO_DEVICE = 6
+NBX_ERR_STATE = 7
 STATUS_NAMES = {
     0: "NBX_OK",
     1: "NBX_ERR_INVALID_INPUT",
