@@ -271,6 +271,12 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
     gq = torch.empty(s.n, device=d)
     gp = torch.empty(s.ntypes, s.ntypes, 2, dtype=torch.float64, device=d)
 
+    fe = torch.empty(2, dtype=torch.float64, device=d)
+    fo = torch.empty(s.n, 3, device=d)
+
+    def forward_only():
+        eng.calc.compute_device(x.data_ptr(), fo.data_ptr(), fe.data_ptr(), None)
+
     def backward_only():
         eng.calc.backward_device(x.data_ptr(), gf.data_ptr(), ge.data_ptr(), gx.data_ptr(), gq.data_ptr(),
                                  gp.data_ptr())
@@ -289,16 +295,84 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
 
     fwd_ms = timed(forward)
     step_ms = timed(grad_step)
+    fwd_entry_ms = timed(forward_only)
     bwd_ms = timed(backward_only)
     eng.close()
     return {"workload": "random LJ+Coulomb liquid, 24000 atoms, 8 types, Lorentz-Berthelot, "
                         "rejection at 0.5 sigma (seed 4)", "atoms": s.n, "steps": steps,
-            "forward_ms": fwd_ms, "gradient_step_ms": step_ms, "backward_entry_ms": bwd_ms,
-            "adjoint_cost_vs_forward": bwd_ms / fwd_ms,
+            "forward_ms": fwd_ms, "gradient_step_ms": step_ms, "forward_entry_ms": fwd_entry_ms,
+            "backward_entry_ms": bwd_ms, "adjoint_cost_vs_forward": bwd_ms / fwd_entry_ms,
             "gradient_step_vs_forward": step_ms / fwd_ms,
             "gradient_steps_per_s": 1e3 / step_ms,
-            "note": "forward = F+E (convert, force, reduce, energies); backward entry = convert, "
-                    "gradient prepare, adjoint kernel, finish, FP64 table gradients; inputs fit in L2"}
+            "note": "forward = the autograd forward (parameter upload, F+E); forward entry = C-ABI F+E "
+                    "(convert, force, reduce, energies); backward entry = C-ABI adjoint (convert, gradient "
+                    "prepare, adjoint kernel, finish, FP64 table gradients); gradient step = autograd "
+                    "forward + loss + backward; inputs fit in L2"}
+
+
+def hbm_peak_gbs() -> float:
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0  # fallback: one earlier GB300 copy measurement
+
+
+def measure_memory_kernels(calc, frames, flush, stream, reps: int = 8) -> dict:
+    """Gridding, search and prune passes of the 288k-atom workload, each after an L2
+    flush, timed by the engine's phase events; bytes are the algorithmic bytes per pass:
+    grid 39 B/atom (x 12, xq 16, atom index 4, cell 4, bounding boxes 3); search (lower
+    bound) = bounding boxes read once (24 B/cluster) + list written (16 B/entry, 32 B/cj4,
+    128 B/exclusion mask); prune = 48 B per cj4 examined (cj4 32, outer mask 8, inner mask 8;
+    +8 for the outer mask on a fresh list) + 16 B per i-atom and per j-atom read once."""
+    import torch
+
+    peak = hbm_peak_gbs()
+    sz = calc.sizes()
+    calc.phase_timings(reset=True)
+    calc.set_timing(True)
+    for k in range(reps):
+        flush.zero_()
+        calc.search_device(frames[k].data_ptr())
+    torch.cuda.synchronize()
+    t = calc.phase_timings(reset=True)
+    sz = calc.sizes()
+    nparts = max(1, NSTPRUNE // 2)
+    for k in range(reps):
+        flush.zero_()
+        calc.prune_device(k % nparts)
+    torch.cuda.synchronize()
+    tr = calc.phase_timings(reset=True)
+    for k in range(reps):
+        flush.zero_()
+        calc.prune_device(-1)
+    torch.cuda.synchronize()
+    tf = calc.phase_timings(reset=True)
+    calc.set_timing(False)
+    n, npad, ncj4, nsci, nexcl = sz["num_atoms"], sz["npad"], sz["num_cj4"], sz["num_sci"], sz["num_excl"]
+    nclusters = npad // 8
+
+    def entry(ms_count, nbytes, what):
+        ms, cnt = ms_count
+        avg = ms / max(1, cnt)
+        gbs = nbytes / (avg * 1e-3) / 1e9 if avg > 0 else None
+        return {"ms": avg, "bytes": nbytes, "GB/s": gbs, "frac": gbs / peak if gbs else None,
+                "peak": peak, "bytes_rule": what}
+
+    grid_b = 39 * n
+    search_b = 24 * nclusters + 16 * nsci + 32 * ncj4 + 128 * nexcl
+    prune_fresh_b = 56 * ncj4 + 16 * npad + 16 * npad
+    prune_roll_b = (48 * ncj4 + 16 * npad) / nparts + 16 * npad
+    return {
+        "grid": entry(t["grid"], grid_b, "39 B/atom"),
+        "search_count": entry(t["search_count"], search_b, "lower bound: bb once + list size"),
+        "search_write": entry(t["search_write"], search_b, "lower bound: bb once + list written"),
+        "prune_fresh": entry(tf["prune"], prune_fresh_b, "56 B/cj4 + 16 B/i-atom + 16 B/j-atom"),
+        "prune_rolling": entry(tr["prune"], prune_roll_b,
+                               f"(48 B/cj4 + 16 B/i-atom) / {nparts} parts + 16 B/j-atom"),
+        "list": {"atoms": n, "npad": npad, "num_sci": nsci, "num_cj4": ncj4, "num_excl": nexcl},
+        "note": "each pass after a 256 MB L2 flush; peak = MEASURED_PEAKS.json hbm_gbs (of measured)",
+    }
 
 
 def workload_config() -> dict:
@@ -404,6 +478,7 @@ def run_ours(args) -> None:
         e2e_ms += (time.perf_counter() - t0) * 1e3
     e2e_value = world * up * args.steps / (e2e_ms * 1e-3)
     calc2.close()
+    memory_kernels = measure_memory_kernels(calc, frames, flush, stream) if rank == 0 else None
 
     if rank != 0:
         return
@@ -438,6 +513,7 @@ def run_ours(args) -> None:
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    line["memory_kernels"] = memory_kernels
     if ensemble is not None:
         line["batched_ensemble"] = ensemble
     if adjoint is not None:

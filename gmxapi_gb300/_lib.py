@@ -43,6 +43,7 @@ EXPORTED = [
     "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
     "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
+    "nbx_get_phase_timings",
 ]
 
 
@@ -146,6 +147,7 @@ def load():
     L.nbx_md_step.argtypes = [vp, C.c_longlong, fp, fp, dp, dp]
     L.nbx_set_timing.argtypes = [vp, C.c_int]
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
+    L.nbx_get_phase_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
     L.nbx_batch_create.argtypes = [C.c_int, C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int,
                                    C.POINTER(vp)]

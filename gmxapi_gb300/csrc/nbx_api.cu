@@ -57,8 +57,15 @@ struct nbx_handle
     // timing / launch accounting
     bool        timing = false;
     std::vector<cudaEvent_t> ev_pool;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
-    double      force_ms = 0.0;
+    struct PendingEvents
+    {
+        cudaEvent_t a, b;
+        int         phase;
+    };
+    std::vector<PendingEvents> ev_pending;
+    // summed event times and counts per phase (nbx_phase: force, grid, search count, search write, prune)
+    double      phase_ms[5]    = { 0, 0, 0, 0, 0 };
+    long long   phase_count[5] = { 0, 0, 0, 0, 0 };
     long long   force_launches = 0;
     long long   launches = 0;
 };
@@ -302,13 +309,61 @@ int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
     return cuda_check(h, e, "list capacity");
 }
 
+cudaEvent_t take_event(nbx_handle* h)
+{
+    cudaEvent_t ev;
+    if (!h->ev_pool.empty())
+    {
+        ev = h->ev_pool.back();
+        h->ev_pool.pop_back();
+    }
+    else
+    {
+        cudaEventCreate(&ev);
+    }
+    return ev;
+}
+
+// Events around a group of launches on the handle's stream when timing is on.
+struct PhaseTimer
+{
+    nbx_handle* h;
+    int         phase;
+    cudaEvent_t a = nullptr, b = nullptr;
+    PhaseTimer(nbx_handle* hh, int ph) : h(hh), phase(ph)
+    {
+        if (h->timing)
+        {
+            a = take_event(h);
+            b = take_event(h);
+            cudaEventRecord(a, h->stream);
+        }
+    }
+    void stop()
+    {
+        if (a)
+        {
+            cudaEventRecord(b, h->stream);
+            h->ev_pending.push_back({ a, b, phase });
+            a = nullptr;
+        }
+    }
+    ~PhaseTimer() { stop(); }
+};
+
 // Grid + count, size the list, write, prune: the synchronous search.
 int search_sync(nbx_handle* h, float* d_x, int write_back)
 {
     DeviceView& v = h->v;
     cudaError_t e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
-    if (e == cudaSuccess) e = launch_grid(v, d_x, write_back, h->stream);
-    if (e == cudaSuccess) e = launch_search_count(v, h->stream);
+    {
+        PhaseTimer t(h, 1);
+        if (e == cudaSuccess) e = launch_grid(v, d_x, write_back, h->stream);
+    }
+    {
+        PhaseTimer t(h, 2);
+        if (e == cudaSuccess) e = launch_search_count(v, h->stream);
+    }
     h->launches += 6;
     int rc = cuda_check(h, e, "grid/search count");
     if (rc != NBX_OK)
@@ -330,8 +385,15 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
     }
     // counts are unchanged; clear the overflow flag the count pass may have set
     e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
-    if (e == cudaSuccess) e = launch_search_write(v, h->stream);
-    if (e == cudaSuccess && h->use_prune) e = launch_prune(v, 1, 0, 1, h->stream);
+    {
+        PhaseTimer t(h, 3);
+        if (e == cudaSuccess) e = launch_search_write(v, h->stream);
+    }
+    if (e == cudaSuccess && h->use_prune)
+    {
+        PhaseTimer t(h, 4);
+        e = launch_prune(v, 1, 0, 1, h->stream);
+    }
     h->launches += 2 + (h->use_prune ? 1 : 0);
     if ((rc = cuda_check(h, e, "search write")) != NBX_OK)
     {
@@ -350,38 +412,24 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
     return NBX_OK;
 }
 
-cudaEvent_t take_event(nbx_handle* h)
-{
-    cudaEvent_t ev;
-    if (!h->ev_pool.empty())
-    {
-        ev = h->ev_pool.back();
-        h->ev_pool.pop_back();
-    }
-    else
-    {
-        cudaEventCreate(&ev);
-    }
-    return ev;
-}
-
-// Accumulates the finished force-kernel event pairs.
+// Accumulates the finished event pairs into their phases.
 void collect_timings(nbx_handle* h, bool wait)
 {
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> keep;
+    std::vector<nbx_handle::PendingEvents> keep;
     for (auto& p : h->ev_pending)
     {
         if (wait)
         {
-            cudaEventSynchronize(p.second);
+            cudaEventSynchronize(p.b);
         }
-        if (cudaEventQuery(p.second) == cudaSuccess)
+        if (cudaEventQuery(p.b) == cudaSuccess)
         {
             float ms = 0.0f;
-            cudaEventElapsedTime(&ms, p.first, p.second);
-            h->force_ms += ms;
-            h->ev_pool.push_back(p.first);
-            h->ev_pool.push_back(p.second);
+            cudaEventElapsedTime(&ms, p.a, p.b);
+            h->phase_ms[p.phase] += ms;
+            h->phase_count[p.phase] += 1;
+            h->ev_pool.push_back(p.a);
+            h->ev_pool.push_back(p.b);
         }
         else
         {
@@ -407,7 +455,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
     if (e == cudaSuccess) e = launch_force(v, energy, h->stream, h->num_sms, e0, e1);
     if (h->timing)
     {
-        h->ev_pending.emplace_back(e0, e1);
+        h->ev_pending.push_back({ e0, e1, 0 });
         if (h->ev_pending.size() > 256)
         {
             collect_timings(h, false);
@@ -740,8 +788,8 @@ int nbx_destroy(nbx_handle* h)
     }
     for (auto& p : h->ev_pending)
     {
-        cudaEventDestroy(p.first);
-        cudaEventDestroy(p.second);
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
     }
     for (auto ev : h->ev_pool)
     {
@@ -857,8 +905,10 @@ int nbx_prune_device(nbx_handle* h, int part)
         return set_error(h, NBX_ERR_STATE, "no pair list");
     }
     cudaSetDevice(h->device);
+    PhaseTimer  t(h, 4);
     cudaError_t e = (part < 0) ? launch_prune(h->v, 1, 0, 1, h->stream)
                                : launch_prune(h->v, 0, part % h->nparts, h->nparts, h->stream);
+    t.stop();
     h->launches += 1;
     return cuda_check(h, e, "nbx_prune_device");
 }
@@ -903,7 +953,9 @@ int nbx_md_step_device(nbx_handle* h, long long step, const float* d_x, float* d
         const long long age = step - h->list_step;
         if (age > 0 && age % 2 == 0)
         {
+            PhaseTimer  t(h, 4);
             cudaError_t e = launch_prune(h->v, 0, h->prune_part, h->nparts, h->stream);
+            t.stop();
             h->prune_part = (h->prune_part + 1) % h->nparts;
             h->launches += 1;
             if ((rc = cuda_check(h, e, "rolling prune")) != NBX_OK)
@@ -1039,7 +1091,7 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
     collect_timings(h, true);
     if (force_ms)
     {
-        *force_ms = h->force_ms;
+        *force_ms = h->phase_ms[0];
     }
     if (counts)
     {
@@ -1048,9 +1100,40 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
     }
     if (reset)
     {
-        h->force_ms       = 0.0;
+        for (int k = 0; k < 5; k++)
+        {
+            h->phase_ms[k]    = 0.0;
+            h->phase_count[k] = 0;
+        }
         h->force_launches = 0;
         h->launches       = 0;
+    }
+    return NBX_OK;
+}
+
+int nbx_get_phase_timings(nbx_handle* h, double* ms, long long* counts, int reset)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(h->device);
+    collect_timings(h, true);
+    for (int k = 0; k < 5; k++)
+    {
+        if (ms)
+        {
+            ms[k] = h->phase_ms[k];
+        }
+        if (counts)
+        {
+            counts[k] = h->phase_count[k];
+        }
+        if (reset)
+        {
+            h->phase_ms[k]    = 0.0;
+            h->phase_count[k] = 0;
+        }
     }
     return NBX_OK;
 }

@@ -205,6 +205,15 @@ class ForceCalculator:
         check(_lib.load().nbx_get_timings(self.h, C.byref(ms), cnt, int(reset)), self.h)
         return float(ms.value), int(cnt[0]), int(cnt[1])
 
+    PHASES = ("force", "grid", "search_count", "search_write", "prune")
+
+    def phase_timings(self, reset: bool = False) -> dict:
+        """{phase: (summed ms, event pairs)} for force, grid, search passes and prune."""
+        ms = (C.c_double * 5)()
+        cnt = (C.c_longlong * 5)()
+        check(_lib.load().nbx_get_phase_timings(self.h, ms, cnt, int(reset)), self.h)
+        return {p: (float(ms[k]), int(cnt[k])) for k, p in enumerate(self.PHASES)}
+
     def set_stream(self, stream_ptr: int):
         check(_lib.load().nbx_set_stream(self.h, C.c_void_p(stream_ptr)), self.h)
 

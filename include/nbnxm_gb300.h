@@ -140,6 +140,11 @@ int nbx_set_timing(nbx_handle* h, int enable);
 /* Since the last reset: force_ms = summed force-kernel event time, counts[0] = force-kernel launches,
  * counts[1] = all kernels this handle launched.  reset != 0 clears the counters after reading. */
 int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int reset);
+/* Summed device time (ms, CUDA events on the handle's stream, recorded while timing is on) and
+ * event-pair counts per phase: [0] force kernel, [1] gridding (wrap, column scan, scatter, sort),
+ * [2] search count pass, [3] search write pass, [4] prune (fresh or rolling).  ms and counts
+ * are double[5] / long long[5] (either may be NULL); reset = 1 clears them. */
+int nbx_get_phase_timings(nbx_handle* h, double* ms, long long* counts, int reset);
 /* Runs an FP32 FMA throughput probe on the device and returns the measured TFLOP/s
  * (2 flops per FMA); used as the FP32 roofline denominator. */
 int nbx_measure_fp32_peak(int device, double* tflops);
