@@ -106,7 +106,8 @@ def test_adapter_reproduces_nblib_golden_forces(driver, tmp_path, key):
     assert r["outcome"] == 0, r["msg"]
     assert rel_rms(r["f"], ref) <= 1e-5
     assert np.abs(r["f"] - ref).max() <= 5e-5 * np.abs(ref).max()
-    np.testing.assert_array_equal(r["f"], r["f2"])
+    # the force kernel adds j-forces with atomics: repeat evaluations agree to rounding
+    assert rel_rms(r["f2"], r["f"]) <= 1e-6
     assert r["size_check"] == 1
 
 
@@ -124,5 +125,5 @@ def test_adapter_matches_oracle_on_water(driver, tmp_path):
     assert r["outcome"] == 0, r["msg"]
     assert rel_rms(r["f"], o.forces()) <= 1e-5
     np.testing.assert_allclose(r["e"], o.energies(), rtol=1e-6)
-    np.testing.assert_array_equal(r["f"], r["f2"])
+    assert rel_rms(r["f2"], r["f"]) <= 1e-6
     assert r["size_check"] == 1
