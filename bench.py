@@ -333,7 +333,7 @@ def measure_memory_kernels(calc, frames, flush, stream, reps: int = 8) -> dict:
     calc.set_timing(True)
     for k in range(reps):
         flush.zero_()
-        calc.search_device(frames[k].data_ptr())
+        calc.search_device(frames[k % frames.shape[0]].data_ptr())
     torch.cuda.synchronize()
     t = calc.phase_timings(reset=True)
     sz = calc.sizes()

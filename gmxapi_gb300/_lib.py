@@ -43,7 +43,7 @@ EXPORTED = [
     "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
     "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
-    "nbx_get_phase_timings",
+    "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
 ]
 
 
@@ -148,6 +148,8 @@ def load():
     L.nbx_set_timing.argtypes = [vp, C.c_int]
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_get_phase_timings.argtypes = [vp, dp, llp, C.c_int]
+    L.nbx_set_list_balance.argtypes = [vp, C.c_int]
+    L.nbx_get_list_balance.argtypes = [vp, ip]
     L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
     L.nbx_batch_create.argtypes = [C.c_int, C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int,
                                    C.POINTER(vp)]

@@ -22,6 +22,7 @@ namespace nbx
 {
 cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s);
 cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s);
+cudaError_t launch_balance(const DeviceView& v, int min_ci_balanced, cudaStream_t s);
 } // namespace nbx
 
 using namespace nbx;
@@ -42,6 +43,7 @@ struct nbx_handle
     int          prune_part = 0;  // next rolling-prune part
     int          nparts     = 1;
     bool         use_prune  = false;
+    int          min_ci_balanced = 0;  // list balancing threshold (44 x SMs like the reference)
     std::vector<void*> allocations;
     // device buffers for the host-array interface
     float*  d_x = nullptr;
@@ -266,17 +268,22 @@ int read_header(nbx_handle* h)
 int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
 {
     DeviceView& v    = h->v;
-    const int   need_sci = num_sci + num_sci / 4 + 64;
     const int   need_cj4 = num_cj4 + num_cj4 / 4 + 256;
-    if (v.sci && v.sci_cap >= num_sci && v.cj4_cap >= num_cj4)
+    // balancing splits entries into at most one piece per cj4 group
+    const int   need_sci = num_sci + num_sci / 4 + 64 + need_cj4;
+    if (v.sci && v.sci_cap >= num_sci + num_cj4 && v.cj4_cap >= num_cj4)
     {
         return NBX_OK;
     }
     dfree(h, v.sci);
+    dfree(h, v.sci_tmp);
+    dfree(h, v.sci_pieces);
     dfree(h, v.cj4);
     dfree(h, v.excl);
     dfree(h, v.imask_outer);
     v.sci = nullptr;
+    v.sci_tmp = nullptr;
+    v.sci_pieces = nullptr;
     v.cj4 = nullptr;
     v.excl = nullptr;
     v.imask_outer = nullptr;
@@ -284,6 +291,8 @@ int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
     v.cj4_cap  = need_cj4;
     v.excl_cap = 2 * need_cj4 + 1;  // at most one mask per cj4 half
     cudaError_t e = dalloc(h, &v.sci, v.sci_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.sci_tmp, v.sci_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.sci_pieces, (size_t)v.sci_cap + 1);
     if (e == cudaSuccess) e = dalloc(h, &v.cj4, v.cj4_cap);
     if (e == cudaSuccess) e = dalloc(h, &v.excl, v.excl_cap);
     if (e == cudaSuccess) e = dalloc(h, &v.imask_outer, 2 * (size_t)v.cj4_cap);
@@ -388,13 +397,15 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
     {
         PhaseTimer t(h, 3);
         if (e == cudaSuccess) e = launch_search_write(v, h->stream);
+        // split long entries and order them large-first (the GPU list's load balancing)
+        if (e == cudaSuccess) e = launch_balance(v, h->min_ci_balanced, h->stream);
     }
     if (e == cudaSuccess && h->use_prune)
     {
         PhaseTimer t(h, 4);
         e = launch_prune(v, 1, 0, 1, h->stream);
     }
-    h->launches += 2 + (h->use_prune ? 1 : 0);
+    h->launches += 6 + (h->use_prune ? 1 : 0);
     if ((rc = cuda_check(h, e, "search write")) != NBX_OK)
     {
         return rc;
@@ -591,6 +602,8 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     h->ntypes     = sys->num_types;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+    // gpu_min_ci_balanced (cuda/nbnxm_cuda_data_mgmt.cu:93,545-548): 44 entries per SM
+    h->min_ci_balanced = 44 * h->num_sms;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     h->own_stream = true;
     DeviceView& v = h->v;
@@ -1069,6 +1082,39 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
     cudaError_t e = launch_set_parameters(h->v, d_q, d_nbfp, h->stream);
     h->launches += (d_q ? 1 : 0) + (d_nbfp ? 1 : 0);
     return cuda_check(h, e, "nbx_set_parameters_device");
+}
+
+int nbx_set_list_balance(nbx_handle* h, int entries_per_sm)
+{
+    if (!h || entries_per_sm < 0)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    h->min_ci_balanced = entries_per_sm * h->num_sms;
+    return NBX_OK;
+}
+
+int nbx_get_list_balance(nbx_handle* h, int* out)
+{
+    if (!h || !out)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->have_list)
+    {
+        return set_error(h, NBX_ERR_STATE, "no pair list");
+    }
+    cudaSetDevice(h->device);
+    int rc = read_header(h);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    out[0] = h->min_ci_balanced;
+    out[1] = h->h_hdr->nsp_max;
+    out[2] = h->h_hdr->num_sci_unsplit;
+    out[3] = h->h_hdr->num_sci;
+    return NBX_OK;
 }
 
 int nbx_set_timing(nbx_handle* h, int enable)

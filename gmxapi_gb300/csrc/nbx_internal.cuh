@@ -69,7 +69,10 @@ struct ListHeader
     unsigned status;     // StatusBits
     int work_counter;    // persistent-kernel work queue head
     int work_counter2;
-    int pad;
+    int num_subpairs;    // cluster pairs of the searched list (bits of imei[0].imask)
+    int nsp_max;         // split target of the last balancing (0: no split)
+    int num_sci_unsplit; // entries before splitting
+    int num_sci_split;   // entries after splitting (scan result)
 };
 
 // Grid dimensions, fixed for a handle (box and atom count do not change).
@@ -109,6 +112,8 @@ struct DeviceView
     int*    nclusters;     // [cap]
     // list
     Sci*      sci;
+    Sci*      sci_tmp;      // [sci_cap] split entries before the size sort
+    int*      sci_pieces;   // [sci_cap + 1] pieces per searched entry, then their offsets
     Cj4*      cj4;
     Excl*     excl;
     unsigned* imask_outer;  // [2*cj4_cap]

@@ -642,13 +642,26 @@ __global__ void k_scan_counts(DeviceView v)
 // The fresh list's masks are also the outer masks until a prune refines them.
 __global__ void k_copy_outer(DeviceView v)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= v.hdr->num_cj4 || (v.hdr->status & kStatusListOverflow))
+    const int  j  = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = j < v.hdr->num_cj4 && !(v.hdr->status & kStatusListOverflow);
+    int        n  = 0;
+    if (ok)
     {
-        return;
+        const unsigned m0        = v.cj4[j].imei[0].imask;
+        v.imask_outer[2 * j]     = m0;
+        v.imask_outer[2 * j + 1] = v.cj4[j].imei[1].imask;
+        n                        = __popc(m0);
     }
-    v.imask_outer[2 * j]     = v.cj4[j].imei[0].imask;
-    v.imask_outer[2 * j + 1] = v.cj4[j].imei[1].imask;
+    // cluster pairs of the list, the count that list balancing splits by
+    // (whole warps reach this point: the grid is a multiple of 32 threads)
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        n += __shfl_xor_sync(0xffffffffu, n, o);
+    }
+    if ((threadIdx.x & 31) == 0 && n > 0)
+    {
+        atomicAdd(&v.hdr->num_subpairs, n);
+    }
 }
 
 } // namespace
@@ -671,6 +684,7 @@ cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s)
     const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
     // cj4 entries are filled with atomicOr: start from zero (no bits, excl_ind 0)
     cudaMemsetAsync(v.cj4, 0, sizeof(Cj4) * (size_t)v.cj4_cap, s);
+    cudaMemsetAsync(&v.hdr->num_subpairs, 0, sizeof(int), s);
     k_search<true><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
     k_copy_outer<<<(v.cj4_cap + 255) / 256, 256, 0, s>>>(v);
     return cudaGetLastError();

@@ -205,6 +205,16 @@ class ForceCalculator:
         check(_lib.load().nbx_get_timings(self.h, C.byref(ms), cnt, int(reset)), self.h)
         return float(ms.value), int(cnt[0]), int(cnt[1])
 
+    def set_list_balance(self, entries_per_sm: int):
+        """Entries per SM below which long list entries are split (0: never); next search."""
+        check(_lib.load().nbx_set_list_balance(self.h, int(entries_per_sm)), self.h)
+
+    def list_balance(self) -> dict:
+        o = np.zeros(4, np.int32)
+        check(_lib.load().nbx_get_list_balance(self.h, _iptr(o)), self.h)
+        return {"min_ci_balanced": int(o[0]), "nsp_max": int(o[1]), "entries_unsplit": int(o[2]),
+                "entries": int(o[3])}
+
     PHASES = ("force", "grid", "search_count", "search_write", "prune")
 
     def phase_timings(self, reset: bool = False) -> dict:

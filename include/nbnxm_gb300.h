@@ -145,6 +145,13 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * [2] search count pass, [3] search write pass, [4] prune (fresh or rolling).  ms and counts
  * are double[5] / long long[5] (either may be NULL); reset = 1 clears them. */
 int nbx_get_phase_timings(nbx_handle* h, double* ms, long long* counts, int reset);
+/* GPU list balancing (pairlist.cpp split_sci_entry / sort_sci): entries are split when the grid
+ * has fewer than entries_per_sm x SMs cells (default 44, the reference's factor; 0 = never
+ * split; entries are always sorted large-first).  Takes effect at the next search. */
+int nbx_set_list_balance(nbx_handle* h, int entries_per_sm);
+/* out[4] = {min_ci_balanced, split target in cluster pairs (0: none), entries before
+ * splitting, entries after} of the current list. */
+int nbx_get_list_balance(nbx_handle* h, int* out);
 /* Runs an FP32 FMA throughput probe on the device and returns the measured TFLOP/s
  * (2 flops per FMA); used as the FP32 roofline denominator. */
 int nbx_measure_fp32_peak(int device, double* tflops);

@@ -1155,6 +1155,129 @@ void orc_search(orc_ctx* c)
     }
 }
 
+/* ------------------------------------------------------------ balancing */
+
+static int popcount32(uint32_t v)
+{
+    int n = 0;
+    while (v)
+    {
+        v &= v - 1;
+        n++;
+    }
+    return n;
+}
+
+/* Target cluster pairs per entry: get_nsubpair_target (pairlist.cpp:2485-2585), with the
+ * exact number of cluster pairs of the list (bits of imei[0].imask) in place of the
+ * geometric estimate; 0 = no splitting.  Integer rounding of nsp / min_ci_balanced. */
+static int balance_target(const orc_ctx* c, int min_ci_balanced)
+{
+    if (min_ci_balanced <= 0 || c->ncells >= min_ci_balanced || c->ncells == 0)
+    {
+        return 0;
+    }
+    long long nsp = 0;
+    for (int j = 0; j < c->ncj4; j++)
+    {
+        nsp += popcount32(c->cj4[j].imei[0].imask);
+    }
+    const long long t = (2 * nsp + min_ci_balanced) / (2 * (long long)min_ci_balanced);
+    return t > 36 ? (int)t : 36;
+}
+
+/* split_sci_entry (pairlist.cpp:2077-2165) without progressive balancing: pieces of close to
+ * nsp_max cluster pairs, the last two evened out.  Appends the pieces of e to out. */
+static int split_entry(const orc_ctx* c, sci_t e, int nsp_max, sci_t* out)
+{
+    const int j4len = e.cj4_end - e.cj4_start;
+    int       n     = 0;
+    out[n++]        = e;
+    if (!(nsp_max > 0 && j4len > 1 && j4len * NCL * JG > nsp_max))
+    {
+        return n;
+    }
+    int nsp = 0, nsp_sci = 0, nsp_cj4_e = 0, nsp_cj4 = 0;
+    for (int j = e.cj4_start; j < e.cj4_end; j++)
+    {
+        const int nsp_cj4_p = nsp_cj4;
+        nsp_cj4             = popcount32(c->cj4[j].imei[0].imask);
+        if (nsp > 0 && nsp_max - nsp < nsp + nsp_cj4 - nsp_max)
+        {
+            out[n - 1].cj4_end = j;
+            sci_t next         = e;
+            next.cj4_start     = j;
+            out[n++]           = next;
+            nsp_sci            = nsp;
+            nsp_cj4_e          = nsp_cj4_p;
+            nsp                = 0;
+        }
+        nsp += nsp_cj4;
+    }
+    out[n - 1].cj4_end = e.cj4_end;
+    if (n >= 2 && nsp_sci - nsp_cj4_e >= nsp + nsp_cj4_e)
+    {
+        out[n - 2].cj4_end--;
+        out[n - 1].cj4_start--;
+    }
+    return n;
+}
+
+/* sort_sci (pairlist.cpp:3827-3873): stable counting sort on the number of cj4 groups,
+ * large first, sizes above twice the average (capped at 255) sharing one class. */
+static void sort_entries(orc_ctx* c)
+{
+    if (c->ncj4 <= c->nsci)
+    {
+        return;
+    }
+    int m = (int)((2LL * c->ncj4) / c->nsci);
+    m     = m > 255 ? 255 : m;
+    int*   count  = (int*)calloc((size_t)m + 2, sizeof(int));
+    sci_t* sorted = (sci_t*)xmalloc(sizeof(sci_t) * (size_t)c->nsci);
+    for (int e = 0; e < c->nsci; e++)
+    {
+        const int len = c->sci[e].cj4_end - c->sci[e].cj4_start;
+        count[len < m ? len : m]++;
+    }
+    /* offsets: class m first */
+    int off = 0;
+    for (int i = m; i >= 0; i--)
+    {
+        const int k = count[i];
+        count[i]    = off;
+        off += k;
+    }
+    for (int e = 0; e < c->nsci; e++)
+    {
+        const int len      = c->sci[e].cj4_end - c->sci[e].cj4_start;
+        sorted[count[len < m ? len : m]++] = c->sci[e];
+    }
+    memcpy(c->sci, sorted, sizeof(sci_t) * (size_t)c->nsci);
+    free(sorted);
+    free(count);
+}
+
+int orc_balance(orc_ctx* c, int min_ci_balanced)
+{
+    const int nsp_max = balance_target(c, min_ci_balanced);
+    if (nsp_max > 0)
+    {
+        sci_t* out = (sci_t*)xmalloc(sizeof(sci_t) * ((size_t)c->ncj4 + (size_t)c->nsci + 1));
+        int    n   = 0;
+        for (int e = 0; e < c->nsci; e++)
+        {
+            n += split_entry(c, c->sci[e], nsp_max, out + n);
+        }
+        free(c->sci);
+        c->sci     = out;
+        c->nsci    = n;
+        c->cap_sci = c->ncj4 + c->nsci + 1;
+    }
+    sort_entries(c);
+    return nsp_max;
+}
+
 /* ------------------------------------------------------------------ prune */
 
 static float pair_r2(const float* xi, const float* xj)

@@ -47,6 +47,11 @@ void orc_set_coordinates(orc_ctx* c, const float* x);
 void orc_grid(orc_ctx* c);
 /* Pair search into the GPU layout: pairlist.cpp nbnxn_make_pairlist_part. */
 void orc_search(orc_ctx* c);
+/* GPU list balancing after a search: split_sci_entry (pairlist.cpp:2077-2165) with the
+ * target of get_nsubpair_target (pairlist.cpp:2485-2585; exact pair count), then
+ * sort_sci (pairlist.cpp:3827-3873).  min_ci_balanced = 44 x SM count in the reference
+ * (cuda/nbnxm_cuda_data_mgmt.cu:93,545-548).  Returns the split target (0: none). */
+int orc_balance(orc_ctx* c, int min_ci_balanced);
 /* Copy coordinates (original order) into grid order without re-gridding:
  * atomdata.cpp nbnxn_atomdata_copy_x_to_nbat_x. */
 void orc_set_x(orc_ctx* c, const float* x);

@@ -47,6 +47,8 @@ def lib():
         L.orc_set_coordinates.argtypes = [vp, fp]
         L.orc_set_x.argtypes = [vp, fp]
         L.orc_prune.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.orc_balance.argtypes = [vp, C.c_int]
+        L.orc_balance.restype = C.c_int
         L.orc_force.argtypes = [vp, C.c_int]
         L.orc_force_entries.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.orc_forces_original_order.argtypes = [vp, fp]
@@ -131,6 +133,10 @@ class Oracle:
 
     def search(self):
         lib().orc_search(self.c)
+
+    def balance(self, min_ci_balanced):
+        """Split long entries and sort entries by size, as the GPU list does."""
+        return int(lib().orc_balance(self.c, int(min_ci_balanced)))
 
     def set_coordinates(self, x):
         a, p = _f(x)

@@ -31,6 +31,8 @@ def _pair(s, coulomb=nblib.CoulombType.Pme, rc=0.9, rlist=1.0, rlist_inner=None,
     o = O.Oracle(s, coulomb=int(coulomb), rc=rc, rlist=rlist, rlist_inner=rlist_inner)
     o.grid()
     o.search()
+    # the same split + size sort the engine applies to its list
+    o.balance(calc.list_balance()["min_ci_balanced"])
     return calc, o
 
 
@@ -74,6 +76,40 @@ def test_pairlist_bit_exact_as_sorted_sets(name):
     # same entries (sci, shift) and cj4 count
     assert sorted(map(tuple, pg["sci"][:, :2])) == sorted(map(tuple, po["sci"][:, :2]))
     assert len(pg["cj4"]) == len(po["cj4"])
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_balanced_list_entries_match_oracle_in_order(name):
+    """Split + large-first sort (split_sci_entry / sort_sci): the same entries in the same order."""
+    s = SYSTEMS[name]()
+    calc, o = _pair(s)
+    bal = calc.list_balance()
+    pg, po = calc.pairlist(), o.pairlist()
+    np.testing.assert_array_equal(pg["sci"], po["sci"])
+    sizes = pg["sci"][:, 3] - pg["sci"][:, 2]
+    assert bal["entries"] == len(pg["sci"]) >= bal["entries_unsplit"]
+    if bal["nsp_max"] > 0 and len(pg["cj4"]) > 0:
+        # pieces are close to the target: no piece above twice its pair budget
+        m0 = np.array([bin(int(v)).count("1") for v in pg["cj4"][:, 4].astype(np.uint32)])
+        pairs = np.array([m0[a:b].sum() for a, b in pg["sci"][:, 2:4]])
+        assert (pairs[sizes > 1] <= 2 * bal["nsp_max"] + 32).all()
+    # large first, up to the size-class cap of twice the average
+    cap = min(255, (2 * len(pg["cj4"])) // max(1, len(sizes)))
+    cls = np.minimum(sizes, cap)
+    assert (np.diff(cls) <= 0).all()
+
+
+def test_balancing_leaves_forces_unchanged():
+    s = systems.water_small()
+    calc, _o = _pair(s)
+    f1 = calc.compute(s.x).copy()
+    e1 = calc.energies.copy()
+    calc.set_list_balance(0)
+    calc.update_pairlist(s.x)
+    assert calc.list_balance()["nsp_max"] == 0
+    f2 = calc.compute(s.x)
+    assert rel_rms(f2, f1) < 1e-6
+    np.testing.assert_allclose(calc.energies, e1, rtol=1e-7)
 
 
 @pytest.mark.parametrize("name", ["water3000", "water_small_box"])
@@ -165,7 +201,9 @@ def test_update_pairlist_after_motion():
     o.set_coordinates(x)
     o.grid()
     o.search()
+    o.balance(calc.list_balance()["min_ci_balanced"])
     pg, po = calc.pairlist(), o.pairlist()
+    np.testing.assert_array_equal(pg["sci"], po["sci"])
     assert np.array_equal(canonical_pairs(pg["sci"], pg["cj4"], pg["excl"]),
                           canonical_pairs(po["sci"], po["cj4"], po["excl"]))
     f = calc.compute(x)

@@ -111,3 +111,33 @@ def test_pairlist_covers_every_pair_within_rlist():
                 assert (a, b) not in count  # excluded pairs are masked out
             else:
                 assert count.get((a, b), 0) == 1, (a, b)
+
+
+def test_balancing_splits_and_sorts_without_changing_pairs():
+    """split_sci_entry + sort_sci in the oracle: a partition of each entry's cj4
+    groups into pieces, entries ordered large-first, the same cluster pairs."""
+    s = systems.water_small()
+    o = O.Oracle(s, rc=0.9, rlist=1.0)
+    o.grid()
+    o.search()
+    p0 = o.pairlist()
+    before = canonical_pairs(p0["sci"], p0["cj4"], p0["excl"])
+    nsp_max = o.balance(44 * 152)
+    p1 = o.pairlist()
+    assert nsp_max >= 36
+    assert len(p1["sci"]) > len(p0["sci"])
+    assert np.array_equal(canonical_pairs(p1["sci"], p1["cj4"], p1["excl"]), before)
+    # every cj4 group in exactly one entry
+    covered = np.zeros(len(p1["cj4"]), int)
+    for _sc, _sh, a, b in p1["sci"]:
+        covered[a:b] += 1
+    assert (covered == 1).all()
+    sizes = p1["sci"][:, 3] - p1["sci"][:, 2]
+    cap = min(255, 2 * len(p1["cj4"]) // len(sizes))
+    assert (np.diff(np.minimum(sizes, cap)) <= 0).all()
+    # a large grid (>= min_ci_balanced cells) is only sorted
+    o2 = O.Oracle(s, rc=0.9, rlist=1.0)
+    o2.grid()
+    o2.search()
+    assert o2.balance(1) == 0
+    assert len(o2.pairlist()["sci"]) == len(p0["sci"])
