@@ -91,6 +91,9 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
         const float  qje = xj.w * v.epsfac;
         const unsigned wj = wexcl >> (jm * kNcl);
         float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
+        // energies of this j-atom's (up to 8) pairs: plain float partial sums, folded
+        // into the compensated per-lane totals once per j-cluster
+        float        ej_el = 0.0f, ej_lj = 0.0f;
 #pragma unroll
         for (int c = 0; c < kNcl; c++)
         {
@@ -186,11 +189,11 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             if (kEnergy)
             {
                 const bool counted = kExcl ? (in_range && int_bit != 0.0f) : in_range;
-                const float e_el   = counted ? st.qi[c] * (xj.w * h_el) : 0.0f;
+                // q_i h_ij here; q_j multiplies the j-cluster's sum
+                ej_el = fmaf(st.qi[c], counted ? h_el : 0.0f, ej_el);
                 // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair)
-                const float e_lj = counted ? fmaf(vrep, 1.0f / 12.0f, fmaf(vdisp, -1.0f / 6.0f, lj.z)) : 0.0f;
-                kahan_add(st.acc_el, st.cmp_el, e_el);
-                kahan_add(st.acc_lj, st.cmp_lj, e_lj);
+                const float e_lj = fmaf(vrep, 1.0f / 12.0f, fmaf(vdisp, -1.0f / 6.0f, lj.z));
+                ej_lj += counted ? e_lj : 0.0f;
             }
             st.fix[c] = fmaf(fscal, dx, st.fix[c]);
             st.fiy[c] = fmaf(fscal, dy, st.fiy[c]);
@@ -198,6 +201,11 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             fjx       = fmaf(-fscal, dx, fjx);
             fjy       = fmaf(-fscal, dy, fjy);
             fjz       = fmaf(-fscal, dz, fjz);
+        }
+        if (kEnergy)
+        {
+            kahan_add(st.acc_el, st.cmp_el, xj.w * ej_el);
+            kahan_add(st.acc_lj, st.cmp_lj, ej_lj);
         }
         // reduce the j force over the 8 i-lanes, one vector red per j-atom
 #pragma unroll
