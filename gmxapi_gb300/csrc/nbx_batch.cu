@@ -205,6 +205,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const float    beta2l2 = beta * beta * 1.4426950408889634f;
     const float    c2b     = 1.1283791670955126f * beta;
     const float    k_rf2   = 2.0f * cv.k_rf;
+    // per-warp stage of one cj4 group's j-atoms, after the type table
+    float4* jx = nbfp_s + nt1 * nt1 + (threadIdx.x >> 5) * 32;
+    int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;
     for (;;)
     {
         int e = 0;
@@ -222,8 +225,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const Sci       s    = b.sci[e - prefix[sidx]];
         const SysPtrs   p    = { b.xq, b.tgrid, b.fnb, b.cj4, b.excl, b.shiftvec, fshift + (size_t)kNShift * 3 * sidx };
         double          elj = 0.0, eel = 0.0;
-        process_entry<kEnergy, kEwald>(cv, p, s, nbfp_s, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2, elj,
-                                       eel);
+        process_entry<kEnergy, kEwald>(cv, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2,
+                                       elj, eel);
         if (kEnergy)
         {
 #pragma unroll
@@ -348,7 +351,7 @@ template<bool kE, bool kW, int kT, int kM>
 void launch_batch_force_t(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys, int* ctr,
                           double* en, double* fs, int num_sms, cudaStream_t s)
 {
-    const size_t smem = sizeof(float4) * (size_t)cv.ntypes1 * cv.ntypes1;
+    const size_t smem = sizeof(float4) * (size_t)cv.ntypes1 * cv.ntypes1 + (size_t)(kT / 32) * 32 * (16 + 4);
     k_batch_force<kE, kW, kT, kM><<<num_sms * kM, kT, smem, s>>>(cv, sys, prefix, nsys, ctr, en, fs);
 }
 

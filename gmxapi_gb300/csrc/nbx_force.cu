@@ -43,6 +43,7 @@ namespace
 constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
+constexpr int kStageBytes     = 32 * (16 + 4);  // per warp: 32 staged j-atoms (xq, type)
 
 template<bool kEnergy, bool kEwald>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
@@ -66,6 +67,9 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     const int      ii      = lane & 7;   // i-atom within the i-cluster
     const int      jj      = lane >> 3;  // j-atom within the warp half
     const int      numSci  = v.hdr->num_sci;
+    // per-warp stage of one cj4 group's j-atoms, after the type table
+    float4* jx = nbfp_s + nt1 * nt1 + (threadIdx.x >> 5) * 32;
+    int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;
     const float    rc2     = v.rc2;
     const float    beta    = v.beta;
     const float    pbeta   = v.erfc_p * beta;
@@ -88,8 +92,8 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         }
         const Sci     s = v.sci[e];
         const SysPtrs p = { v.xq, v.tgrid, v.fnb, v.cj4, v.excl, v.shiftvec, v.fshift };
-        process_entry<kEnergy, kEwald>(v, p, s, nbfp_s, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2, e_lj_acc,
-                                       e_el_acc);
+        process_entry<kEnergy, kEwald>(v, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2,
+                                       e_lj_acc, e_el_acc);
     }
     if (kEnergy)
     {
@@ -376,7 +380,7 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     cudaMemsetAsync(v.fshift, 0, sizeof(double) * kNShift * 3, s);
     cudaMemsetAsync(v.energy, 0, sizeof(double) * 2, s);
     const int    blocks = num_sms * kForceMinBlocks;
-    const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1;
+    const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1 + kStageBytes * (kForceThreads / 32);
     const bool   ewald  = (v.coulomb == 0);
     if (energy)
     {
@@ -627,7 +631,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     if (e == cudaSuccess)
     {
         const int    blocks = num_sms * kForceMinBlocks;
-        const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1;
+        const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1 + kStageBytes * (kForceThreads / 32);
         int*         ctr    = &v.hdr->work_counter;
         if (energy)
         {

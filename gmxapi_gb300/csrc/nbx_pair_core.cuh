@@ -71,6 +71,7 @@ struct EntryState
 // instruction cache.
 template<bool kEnergy, bool kEwald, bool kExcl>
 __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs& p, const float4* __restrict__ nbfp_s,
+                                             const float4* __restrict__ jx, const int* __restrict__ jt,
                                              EntryState& st, const int cj_lane, unsigned im, unsigned wexcl,
                                              int h, int sci, bool central, int ii, int jj, float rc2, float pbeta,
                                              float beta2l2, float c2b, float k_rf2)
@@ -86,8 +87,9 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             continue;
         }
         const int    aj  = cj * kCl + h * (kCl / kSplit) + jj;
-        const float4 xj  = p.xq[aj];
-        const int    tj  = p.tgrid[aj];
+        // the cj4 group's 32 j-atoms are staged in shared memory (slot jm * 8 + atom)
+        const float4 xj  = jx[jm * kCl + h * (kCl / kSplit) + jj];
+        const int    tj  = jt[jm * kCl + h * (kCl / kSplit) + jj];
         const float  qje = xj.w * v.epsfac;
         const unsigned wj = wexcl >> (jm * kNcl);
         float        fjx = 0.0f, fjy = 0.0f, fjz = 0.0f;
@@ -227,9 +229,9 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
 // to e_lj_acc / e_el_acc (per lane, FP64).
 template<bool kEnergy, bool kEwald>
 __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs& p, const Sci& s,
-                                              const float4* __restrict__ nbfp_s, int nt1, int lane, int ii, int jj,
-                                              float rc2, float pbeta, float beta2l2, float c2b, float k_rf2,
-                                              double& e_lj_acc, double& e_el_acc)
+                                              const float4* __restrict__ nbfp_s, float4* jx, int* jt, int nt1,
+                                              int lane, int ii, int jj, float rc2, float pbeta, float beta2l2,
+                                              float c2b, float k_rf2, double& e_lj_acc, double& e_el_acc)
 {
     const unsigned full = 0xffffffffu;
     const float shx = p.shiftvec[3 * s.shift], shy = p.shiftvec[3 * s.shift + 1], shz = p.shiftvec[3 * s.shift + 2];
@@ -249,13 +251,46 @@ __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs
     }
     st.acc_el = st.cmp_el = 0.0f;
     st.acc_lj = st.cmp_lj = 0.0f;
+    // Software pipeline over the cj4 groups: the record (masks, j-clusters) of group
+    // k+1 is loaded when group k starts, its 32 j-atoms (xq, type; one per lane) after
+    // group k's first half, and they go to the warp's shared-memory stage when k+1
+    // starts, so neither load is waited for.
+    const unsigned full_m = 0xffffffffu;
+    int4           rec_ime{};
+    int            rec_cj = 0;
+    float4         xr{};
+    int            tr = 0;
+    if (s.cj4_start < s.cj4_end)
+    {
+        rec_ime   = *reinterpret_cast<const int4*>(&p.cj4[s.cj4_start].imei[0]);
+        rec_cj    = (lane < kJg) ? p.cj4[s.cj4_start].cj[lane] : 0;
+        const int a = __shfl_sync(full_m, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
+        xr        = p.xq[a];
+        tr        = p.tgrid[a];
+    }
     for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
     {
-        const int4 ime     = *reinterpret_cast<const int4*>(&p.cj4[j4].imei[0]);
-        const int  cj_lane = (lane < kJg) ? p.cj4[j4].cj[lane] : 0;
+        const int4 ime     = rec_ime;
+        const int  cj_lane = rec_cj;
+        __syncwarp();
+        jx[lane] = xr;
+        jt[lane] = tr;
+        __syncwarp();
+        const bool more = j4 + 1 < s.cj4_end;
+        if (more)
+        {
+            rec_ime = *reinterpret_cast<const int4*>(&p.cj4[j4 + 1].imei[0]);
+            rec_cj  = (lane < kJg) ? p.cj4[j4 + 1].cj[lane] : 0;
+        }
 #pragma unroll 1
         for (int h = 0; h < kSplit; h++)
         {
+            if (h == 1 && more)
+            {
+                const int a = __shfl_sync(full_m, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
+                xr          = p.xq[a];
+                tr          = p.tgrid[a];
+            }
             const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
             const int      exi = (h == 0) ? ime.y : ime.w;
             if (!im)
@@ -264,14 +299,14 @@ __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs
             }
             if (exi == 0)
             {
-                process_half<kEnergy, kEwald, false>(v, p, nbfp_s, st, cj_lane, im, 0u, h, s.sci, central, ii, jj,
-                                                     rc2, pbeta, beta2l2, c2b, k_rf2);
+                process_half<kEnergy, kEwald, false>(v, p, nbfp_s, jx, jt, st, cj_lane, im, 0u, h, s.sci, central,
+                                                     ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2);
             }
             else
             {
                 const unsigned wexcl = p.excl[exi].pair[lane];
-                process_half<kEnergy, kEwald, true>(v, p, nbfp_s, st, cj_lane, im, wexcl, h, s.sci, central, ii,
-                                                    jj, rc2, pbeta, beta2l2, c2b, k_rf2);
+                process_half<kEnergy, kEwald, true>(v, p, nbfp_s, jx, jt, st, cj_lane, im, wexcl, h, s.sci,
+                                                    central, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2);
             }
         }
     }
