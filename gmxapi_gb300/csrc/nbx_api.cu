@@ -649,6 +649,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
         v.sh_ewald    = 0.0f;
         v.self_energy = -v.epsfac_d * 0.5 * (double)v.c_rf * qsq;
     }
+    set_pair_constants(v);
     // ---- shift vectors (pbc.cpp:1187-1202), rectangular box ----
     for (int s = 0, m = -1; m <= 1; m++)
     {

@@ -201,10 +201,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int      total   = prefix[nsys];
     const float    rc2     = cv.rc2;
     const float    beta    = cv.beta;
-    const float    pbeta   = cv.erfc_p * beta;
-    const float    beta2l2 = beta * beta * 1.4426950408889634f;
-    const float    c2b     = 1.1283791670955126f * beta;
-    const float    k_rf2   = 2.0f * cv.k_rf;
+    const float    pbeta   = cv.pbeta;
+    const float    beta2l2 = cv.beta2l2;  // beta^2 * log2(e)
+    const float    c2b     = cv.c2b;      // 2 beta / sqrt(pi)
+    const float    k_rf2   = cv.k_rf2;
     // per-warp stage of one cj4 group's j-atoms, after the type table
     float4* jx = nbfp_s + nt1 * nt1 + (threadIdx.x >> 5) * 32;
     int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;

@@ -72,10 +72,10 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;
     const float    rc2     = v.rc2;
     const float    beta    = v.beta;
-    const float    pbeta   = v.erfc_p * beta;
-    const float    beta2l2 = beta * beta * 1.4426950408889634f;  // beta^2 * log2(e)
-    const float    c2b     = 1.1283791670955126f * beta;           // 2 beta / sqrt(pi)
-    const float    k_rf2   = 2.0f * v.k_rf;
+    const float    pbeta   = v.pbeta;
+    const float    beta2l2 = v.beta2l2;  // beta^2 * log2(e)
+    const float    c2b     = v.c2b;      // 2 beta / sqrt(pi)
+    const float    k_rf2   = v.k_rf2;
 
     double e_lj_acc = 0.0, e_el_acc = 0.0;
     for (;;)
@@ -607,6 +607,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         v.sh_ewald = a->use_ewald_shift ? erfcf(v.beta * rc) / rc : 0.0f;
         fit_erfc((double)v.beta * (double)rc, &v.erfc_p, v.erfc_c);
     }
+    set_pair_constants(v);
     v.self_energy    = 0.0;
     v.self_on_device = 1;
     for (int sh = 0, m = -1; m <= 1; m++)

@@ -139,9 +139,24 @@ struct DeviceView
     // erfc(x) = t * P(t) * exp(-x^2), t = 1/(1 + erfc_p x), fitted on [0, beta*rc] at set-up
     float erfc_p;
     float erfc_c[kErfcTerms];
+    // derived per-pair constants (set_pair_constants), read straight from the
+    // kernel parameters inside the pair loop
+    float pbeta;    // erfc_p * beta
+    float beta2l2;  // beta^2 log2(e)
+    float c2b;      // 2 beta / sqrt(pi)
+    float k_rf2;    // 2 k_rf
 };
 
 // One system of a batch, as the batched kernels see it (device table).
+// Fills the derived pair constants of a view whose beta / erfc fit / k_rf are set.
+inline void set_pair_constants(DeviceView& v)
+{
+    v.pbeta   = v.erfc_p * v.beta;
+    v.beta2l2 = v.beta * v.beta * 1.4426950408889634f;
+    v.c2b     = 1.1283791670955126f * v.beta;
+    v.k_rf2   = 2.0f * v.k_rf;
+}
+
 struct BatchSys
 {
     const float4*     xq;

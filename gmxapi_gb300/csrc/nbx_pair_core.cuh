@@ -144,11 +144,13 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             {
                 rinv6 *= int_bit;
             }
-            const float vrep  = lj.y * rinv6 * rinv6;
+            // everything below is F r^2 until the one multiply by rinv2
+            const float c12r6 = lj.y * rinv6;
             const float vdisp = lj.x * rinv6;
-            float       fscal = (vrep - vdisp) * rinv2;
+            const float flj   = fmaf(c12r6, rinv6, -vdisp);  // vrep - vdisp, vrep = 12 C12 / r^12
             const float qq    = st.qi[c] * qje;
-            float       h_el  = 0.0f;  // q_i q_j h_el is the pair's Coulomb energy / epsfac
+            float       fcr2;                                 // Coulomb F r^2 / (q_i q_j)
+            float       h_el = 0.0f;  // q_i q_j h_el is the pair's Coulomb energy / epsfac
             if (kEwald)
             {
                 // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
@@ -161,40 +163,35 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
                     poly = fmaf(poly, t, v.erfc_c[k]);
                 }
                 const float expm = fast_ex2(-beta2l2 * r2);
-                const float tp   = t * poly;  // erfc(beta r) = tp * expm
-                // -(d/dr)(erfc(beta r)/r)/r = expm (tp/r + 2 beta/sqrt(pi)) / r^2; exclusions drop 1/r^3
-                float fc = expm * fmaf(tp, rinv, c2b) * rinv2;
+                const float tpr  = t * poly * rinv;  // erfc(beta r) / r = tpr * expm
+                // -(d/dr)(erfc(beta r)/r) r = expm (erfc/r-part + 2 beta/sqrt(pi)); exclusions drop 1/r
+                fcr2 = expm * (tpr + c2b);
                 if (kExcl)
                 {
-                    fc -= (1.0f - int_bit) * rinv * rinv2;
+                    fcr2 -= (1.0f - int_bit) * rinv;
                 }
-                fscal = fmaf(qq, fc, fscal);
                 if (kEnergy)
                 {
-                    h_el = fmaf(tp * expm, rinv, -v.sh_ewald);
+                    h_el = fmaf(tpr, expm, -v.sh_ewald);
                 }
             }
             else
             {
-                float fc = rinv * rinv2;
-                if (kExcl)
-                {
-                    fc *= int_bit;
-                }
-                fscal = fmaf(qq, fc - k_rf2, fscal);
+                fcr2 = kExcl ? fmaf(-k_rf2, r2, rinv * int_bit) : fmaf(-k_rf2, r2, rinv);
                 if (kEnergy)
                 {
                     h_el = (rinv - v.c_rf) + v.k_rf * r2;
                 }
             }
-            fscal = in_range ? fscal : 0.0f;
+            float fscal = fmaf(qq, fcr2, flj) * rinv2;
+            fscal       = in_range ? fscal : 0.0f;
             if (kEnergy)
             {
                 const bool counted = kExcl ? (in_range && int_bit != 0.0f) : in_range;
                 // q_i h_ij here; q_j multiplies the j-cluster's sum
                 ej_el = fmaf(st.qi[c], counted ? h_el : 0.0f, ej_el);
-                // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair)
-                const float e_lj = fmaf(vrep, 1.0f / 12.0f, fmaf(vdisp, -1.0f / 6.0f, lj.z));
+                // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair) = (flj - vdisp)/12 + shift
+                const float e_lj = fmaf(flj - vdisp, 1.0f / 12.0f, lj.z);
                 ej_lj += counted ? e_lj : 0.0f;
             }
             st.fix[c] = fmaf(fscal, dx, st.fix[c]);
