@@ -21,6 +21,7 @@
 #include "nbnxm_oracle.h"
 
 #include <float.h>
+#include <pthread.h>
 #include <limits.h>
 #include <math.h>
 #include <stdlib.h>
@@ -1399,7 +1400,10 @@ void orc_force_entries(orc_ctx* c, int e0, int e1, int computeEnergy)
     force_range(c, e0, e1, computeEnergy);
 }
 
-static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
+/* Kernel body over entries [e_begin, e_end) into the given force / shift-force buffers
+ * (cleared here) and energies; the single-threaded entry points pass the context's own. */
+static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int computeEnergy, float* fnb, float* fsh,
+                             double* vc_out, double* vlj_out)
 {
     const int    npad   = c->ncells * SC;
     const int    bEwald = (c->coulomb == ORC_COULOMB_EWALD);
@@ -1410,8 +1414,8 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
     const double epsfac_d = orc_one_4pi_eps0();
     const float* x      = c->xq;
     const int*   type   = c->tgrid;
-    memset(c->fnb, 0, sizeof(float) * (size_t)npad * 3);
-    memset(c->fshift, 0, sizeof(c->fshift));
+    memset(fnb, 0, sizeof(float) * (size_t)npad * 3);
+    memset(fsh, 0, sizeof(float) * NSHIFT * 3);
     double Vc = 0, Vvdw = 0;
     for (int e = e_begin; e < e_end; e++)
     {
@@ -1544,16 +1548,16 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
                             fix = fix + tx;
                             fiy = fiy + ty;
                             fiz = fiz + tz;
-                            c->fnb[ja * 3 + 0] -= tx;
-                            c->fnb[ja * 3 + 1] -= ty;
-                            c->fnb[ja * 3 + 2] -= tz;
+                            fnb[ja * 3 + 0] -= tx;
+                            fnb[ja * 3 + 1] -= ty;
+                            fnb[ja * 3 + 2] -= tz;
                         }
-                        c->fnb[ia * 3 + 0] += fix;
-                        c->fnb[ia * 3 + 1] += fiy;
-                        c->fnb[ia * 3 + 2] += fiz;
-                        c->fshift[ish3 + 0] += fix;
-                        c->fshift[ish3 + 1] += fiy;
-                        c->fshift[ish3 + 2] += fiz;
+                        fnb[ia * 3 + 0] += fix;
+                        fnb[ia * 3 + 1] += fiy;
+                        fnb[ia * 3 + 2] += fiz;
+                        fsh[ish3 + 0] += fix;
+                        fsh[ish3 + 1] += fiy;
+                        fsh[ish3 + 2] += fiz;
                     }
                 }
             }
@@ -1561,8 +1565,95 @@ static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
         Vc += vctot;
         Vvdw += Vvdwtot;
     }
-    c->vc  = computeEnergy ? Vc : 0;
-    c->vlj = computeEnergy ? Vvdw : 0;
+    *vc_out  = computeEnergy ? Vc : 0;
+    *vlj_out = computeEnergy ? Vvdw : 0;
+}
+
+static void force_range(orc_ctx* c, int e_begin, int e_end, int computeEnergy)
+{
+    force_range_into(c, e_begin, e_end, computeEnergy, c->fnb, c->fshift, &c->vc, &c->vlj);
+}
+
+/* The same kernel split over nthreads POSIX threads (contiguous entry ranges, private
+ * force buffers summed afterwards): the reference's OpenMP-parallel CPU kernel layout
+ * (nbnxm/kerneldispatch.cpp, one output buffer per thread reduced in
+ * atomdata.cpp:1181-1228).  Used as the multi-core CPU timing baseline. */
+typedef struct
+{
+    const orc_ctx* c;
+    int            e0, e1, energy;
+    float*         fnb;
+    float          fsh[NSHIFT * 3];
+    double         vc, vlj;
+} mt_task;
+
+static void* mt_run(void* arg)
+{
+    mt_task* t = (mt_task*)arg;
+    force_range_into(t->c, t->e0, t->e1, t->energy, t->fnb, t->fsh, &t->vc, &t->vlj);
+    return NULL;
+}
+
+int orc_force_entries_mt(orc_ctx* c, int e0, int e1, int computeEnergy, int nthreads)
+{
+    e0 = e0 < 0 ? 0 : e0;
+    e1 = e1 > c->nsci ? c->nsci : e1;
+    if (nthreads < 1)
+    {
+        nthreads = 1;
+    }
+    const size_t npad3 = (size_t)c->ncells * SC * 3;
+    mt_task*     tasks = (mt_task*)calloc((size_t)nthreads, sizeof(mt_task));
+    pthread_t*   tid   = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    int          ok    = tasks && tid;
+    for (int t = 0; ok && t < nthreads; t++)
+    {
+        tasks[t].c      = c;
+        tasks[t].e0     = e0 + (int)(((long long)(e1 - e0) * t) / nthreads);
+        tasks[t].e1     = e0 + (int)(((long long)(e1 - e0) * (t + 1)) / nthreads);
+        tasks[t].energy = computeEnergy;
+        tasks[t].fnb    = (float*)malloc(sizeof(float) * npad3 + 4);
+        ok              = tasks[t].fnb != NULL;
+    }
+    int started = 0;
+    for (int t = 0; ok && t < nthreads; t++, started++)
+    {
+        if (pthread_create(&tid[t], NULL, mt_run, &tasks[t]) != 0)
+        {
+            ok = 0;
+            break;
+        }
+    }
+    for (int t = 0; t < started; t++)
+    {
+        pthread_join(tid[t], NULL);
+    }
+    if (ok)
+    {
+        memset(c->fnb, 0, sizeof(float) * npad3);
+        memset(c->fshift, 0, sizeof(c->fshift));
+        c->vc = c->vlj = 0;
+        for (int t = 0; t < nthreads; t++)
+        {
+            for (size_t k = 0; k < npad3; k++)
+            {
+                c->fnb[k] += tasks[t].fnb[k];
+            }
+            for (int k = 0; k < NSHIFT * 3; k++)
+            {
+                c->fshift[k] += tasks[t].fsh[k];
+            }
+            c->vc += tasks[t].vc;
+            c->vlj += tasks[t].vlj;
+        }
+    }
+    for (int t = 0; tasks && t < nthreads; t++)
+    {
+        free(tasks[t].fnb);
+    }
+    free(tasks);
+    free(tid);
+    return ok ? 0 : -1;
 }
 
 /* atomdata.cpp:1181-1228 nbnxn_atomdata_add_nbat_f_to_f_part: f[a] = fnb[cell[a]] */

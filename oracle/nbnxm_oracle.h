@@ -64,6 +64,9 @@ void orc_force(orc_ctx* c, int compute_energy);
 /* The force kernel over list entries [e0, e1) only (bounded timing samples). */
 void orc_force_entries(orc_ctx* c, int e0, int e1, int compute_energy);
 
+/* The same over nthreads threads (private force buffers, summed); 0 on success. */
+int orc_force_entries_mt(orc_ctx* c, int e0, int e1, int compute_energy, int nthreads);
+
 /* Outputs */
 void orc_forces_original_order(const orc_ctx* c, float* f_out); /* N*3 */
 void orc_virial(const orc_ctx* c, const float* x, const float* f, double* vir9);

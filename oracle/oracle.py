@@ -51,6 +51,8 @@ def lib():
         L.orc_balance.restype = C.c_int
         L.orc_force.argtypes = [vp, C.c_int]
         L.orc_force_entries.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.orc_force_entries_mt.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_force_entries_mt.restype = C.c_int
         L.orc_forces_original_order.argtypes = [vp, fp]
         L.orc_virial.argtypes = [vp, fp, fp, dp]
         L.orc_energies.argtypes = [vp, dp]
@@ -154,6 +156,11 @@ class Oracle:
 
     def force_entries(self, e0, e1, energy=True):
         lib().orc_force_entries(self.c, int(e0), int(e1), int(energy))
+
+    def force_entries_mt(self, e0, e1, energy=True, threads=1):
+        """force_entries over `threads` POSIX threads (multi-core timing baseline)."""
+        if lib().orc_force_entries_mt(self.c, int(e0), int(e1), int(energy), int(threads)) != 0:
+            raise RuntimeError("threaded oracle kernel failed")
 
     def forces(self):
         f = np.empty((self.system.n, 3), dtype=np.float32)
