@@ -725,10 +725,10 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (e == cudaSuccess) e = dalloc(h, &nb, (size_t)nt1 * nt1);
     if (e == cudaSuccess) e = dalloc(h, &v.xin, 3 * (size_t)n);
     if (e == cudaSuccess) e = dalloc(h, &v.col, n);
+    if (e == cudaSuccess) e = dalloc(h, &v.slot, n);
     if (e == cudaSuccess) e = dalloc(h, &v.image, n);
     if (e == cudaSuccess) e = dalloc(h, &v.cxy_na, g.ncol + 1);
     if (e == cudaSuccess) e = dalloc(h, &v.cxy_ind, g.ncol + 2);
-    if (e == cudaSuccess) e = dalloc(h, &v.cxy_fill, g.ncol + 1);
     if (e == cudaSuccess) e = dalloc(h, &v.atom_indices, npad);
     if (e == cudaSuccess) e = dalloc(h, &v.cells, n);
     if (e == cudaSuccess) e = dalloc(h, &v.xq, npad);

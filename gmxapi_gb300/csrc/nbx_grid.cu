@@ -59,35 +59,89 @@ __device__ __forceinline__ float wrap_coord(float v, float L, ListHeader* hdr, i
     return v;
 }
 
-__global__ void k_wrap_column(DeviceView v, float* x, int write_back)
+constexpr int kGridThreads   = 1024;
+constexpr int kAtomsPerThread = 4;
+constexpr int kMaxSmemCols    = 8192;  // column counters kept in shared memory up to this many columns
+
+// Wrap into the box, column index, and each atom's slot within its column.
+// Column counts are gathered per block in shared memory; each block then
+// reserves one contiguous range per column it touches with a single global
+// atomic, so a column sees one global atomic per block instead of one per atom.
+__global__ void __launch_bounds__(kGridThreads) k_wrap_column(DeviceView v, float* x, int write_back)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.n)
+    extern __shared__ int s_cnt[];  // [ncol]: counts, then the block's base slot per column
+    const int  ncol     = v.g.ncol;
+    const bool use_smem = ncol <= kMaxSmemCols;
+    if (use_smem)
+    {
+        for (int c = threadIdx.x; c < ncol; c += blockDim.x)
+        {
+            s_cnt[c] = 0;
+        }
+        __syncthreads();
+    }
+    int col[kAtomsPerThread], rank[kAtomsPerThread];
+#pragma unroll
+    for (int k = 0; k < kAtomsPerThread; k++)
+    {
+        const int i = (blockIdx.x * kAtomsPerThread + k) * blockDim.x + threadIdx.x;
+        col[k]      = -1;
+        if (i >= v.n)
+        {
+            continue;
+        }
+        float    c[3];
+        unsigned code = 0;
+        for (int d = 0; d < 3; d++)
+        {
+            int kk;
+            c[d]             = wrap_coord(x[3 * i + d], v.g.box[d], v.hdr, &kk);
+            v.xin[3 * i + d] = c[d];
+            code |= ((unsigned)(kk & 0xff)) << (8 * d);
+            if (write_back)
+            {
+                x[3 * i + d] = c[d];
+            }
+        }
+        v.image[i] = write_back ? 0 : (int)code;
+        // lower corner is 0, so (x - lower) == x exactly
+        int cx    = (int)__fmul_rn(c[0], v.g.ics[0]);
+        int cy    = (int)__fmul_rn(c[1], v.g.ics[1]);
+        cx        = min(cx, v.g.ncx - 1);
+        cy        = min(cy, v.g.ncy - 1);
+        col[k]    = cx * v.g.ncy + cy;
+        v.col[i]  = col[k];
+        if (use_smem)
+        {
+            rank[k] = atomicAdd(&s_cnt[col[k]], 1);
+        }
+        else
+        {
+            v.slot[i] = atomicAdd(&v.cxy_na[col[k]], 1);
+        }
+    }
+    if (!use_smem)
     {
         return;
     }
-    float    c[3];
-    unsigned code = 0;
-    for (int d = 0; d < 3; d++)
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x)
     {
-        int k;
-        c[d] = wrap_coord(x[3 * i + d], v.g.box[d], v.hdr, &k);
-        v.xin[3 * i + d] = c[d];
-        code |= ((unsigned)(k & 0xff)) << (8 * d);
-        if (write_back)
+        const int cnt = s_cnt[c];
+        if (cnt > 0)
         {
-            x[3 * i + d] = c[d];
+            s_cnt[c] = atomicAdd(&v.cxy_na[c], cnt);
         }
     }
-    v.image[i] = write_back ? 0 : (int)code;
-    // lower corner is 0, so (x - lower) == x exactly
-    int cx = (int)__fmul_rn(c[0], v.g.ics[0]);
-    int cy = (int)__fmul_rn(c[1], v.g.ics[1]);
-    cx     = min(cx, v.g.ncx - 1);
-    cy     = min(cy, v.g.ncy - 1);
-    const int cxy = cx * v.g.ncy + cy;
-    v.col[i]      = cxy;
-    atomicAdd(&v.cxy_na[cxy], 1);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kAtomsPerThread; k++)
+    {
+        if (col[k] >= 0)
+        {
+            v.slot[(blockIdx.x * kAtomsPerThread + k) * blockDim.x + threadIdx.x] = s_cnt[col[k]] + rank[k];
+        }
+    }
 }
 
 // Cells per column and their prefix sum (grid.cpp:1300-1330), one block.
@@ -139,7 +193,6 @@ __global__ void k_column_scan(DeviceView v)
     {
         v.cxy_ind[c] = run;
         run += (v.cxy_na[c] + kSc - 1) / kSc;
-        v.cxy_fill[c] = 0;
     }
     if (threadIdx.x == nthreads - 1)
     {
@@ -163,9 +216,7 @@ __global__ void k_scatter(DeviceView v)
     {
         return;
     }
-    const int c    = v.col[i];
-    const int slot = atomicAdd(&v.cxy_fill[c], 1);
-    v.atom_indices[v.cxy_ind[c] * kSc + slot] = i;
+    v.atom_indices[v.cxy_ind[v.col[i]] * kSc + v.slot[i]] = i;
 }
 
 // Total order key on (coordinate, atom index), ascending; -0.0 equals +0.0.
@@ -397,7 +448,9 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
 {
     cudaMemsetAsync(v.cxy_na, 0, sizeof(int) * (v.g.ncol + 1), s);
     const int tb = 256;
-    k_wrap_column<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, d_x, write_back);
+    const int per_block = kGridThreads * kAtomsPerThread;
+    const size_t smem   = v.g.ncol <= kMaxSmemCols ? sizeof(int) * (size_t)v.g.ncol : 0;
+    k_wrap_column<<<(v.n + per_block - 1) / per_block, kGridThreads, smem, s>>>(v, d_x, write_back);
     k_column_scan<<<1, 1024, 0, s>>>(v);
     k_scatter<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v);
     k_sort_fill<<<v.g.ncol, kSortThreads, 0, s>>>(v, reinterpret_cast<unsigned long long*>(v.fnb));

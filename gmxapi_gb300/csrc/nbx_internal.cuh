@@ -99,10 +99,10 @@ struct DeviceView
     // grid
     float*  xin;           // [3N] wrapped coordinates
     int*    col;           // [N] column of each atom
+    int*    slot;          // [N] position of each atom within its column (before the column sort)
     int*    image;         // [N] box shifts applied by the wrap, 3 signed bytes (x, y, z)
     int*    cxy_na;        // [ncol]
     int*    cxy_ind;       // [ncol+1]
-    int*    cxy_fill;      // [ncol]
     int*    atom_indices;  // [cap*64]
     int*    cells;         // [N]
     float4* xq;            // [cap*64]
