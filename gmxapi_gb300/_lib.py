@@ -44,6 +44,7 @@ EXPORTED = [
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
     "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
     "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
+    "nbx_batch_set_parameters_device", "nbx_batch_backward_device", "nbx_batch_force_match_device",
 ]
 
 
@@ -149,6 +150,9 @@ def load():
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_get_phase_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_set_list_balance.argtypes = [vp, C.c_int]
+    L.nbx_batch_set_parameters_device.argtypes = [vp, vp, vp]
+    L.nbx_batch_backward_device.argtypes = [vp] * 7
+    L.nbx_batch_force_match_device.argtypes = [vp] * 10
     L.nbx_get_list_balance.argtypes = [vp, ip]
     L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
     L.nbx_batch_create.argtypes = [C.c_int, C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int,

@@ -119,3 +119,76 @@ class DifferentiableNonbonded:
 
     def close(self):
         self.calc.close()
+
+
+class _BatchMatchLoss(torch.autograd.Function):
+    """(q, nbfp) -> force-matching loss of a batch; one graph launch computes the loss and
+    both gradients, which backward returns scaled by the upstream gradient."""
+
+    @staticmethod
+    def forward(ctx, q, nbfp, matcher):
+        loss = matcher._run(q, nbfp)
+        ctx.matcher = matcher
+        ctx.nbfp_dtype = nbfp.dtype
+        return loss
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, g):
+        m = ctx.matcher
+        return g.to(torch.float32) * m._gq, (g * m._gnbfp).to(ctx.nbfp_dtype), None
+
+
+class BatchForceMatcher:
+    """Force matching over a batch of systems with shared type parameters.
+
+    ``matcher(q, nbfp)`` returns the loss sum over systems and atoms of
+    |F - F_target|^2 (FP64) as a differentiable scalar: q holds all systems'
+    charges (concatenated atom order, float32) and nbfp the shared
+    (ntypes, ntypes, 2) table.  Each call is one CUDA-graph launch on the GPU
+    (parameters -> forces, energies, virials -> loss -> adjoint); the pair
+    lists are built once from the fixed coordinates.
+    """
+
+    def __init__(self, systems, f_target: torch.Tensor, options: NBKernelOptions | None = None, device: int = 0):
+        from .batch import BatchForceCalculator
+
+        opts = options or NBKernelOptions(coulomb_type=CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
+                                          nstlist_prune=0)
+        opts.compute_virial_and_energy = True
+        self.dev = torch.device("cuda", device)
+        self.batch = BatchForceCalculator(systems, opts, device)
+        self.nsys = len(systems)
+        self.ntypes = int(systems[0].ntypes)
+        self.x = torch.cat([torch.as_tensor(s.x, dtype=torch.float32).reshape(-1) for s in systems]).to(self.dev)
+        n = self.x.numel() // 3
+        self.f_target = f_target.to(self.dev, torch.float32).reshape(-1).contiguous()
+        if self.f_target.numel() != 3 * n:
+            raise ValueError("f_target must hold 3 values per atom of the batch")
+        self.batch.set_stream(torch.cuda.current_stream(self.dev).cuda_stream)
+        self.batch.search_device(self.x.data_ptr())
+        self._loss = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        self._gq = torch.empty(n, dtype=torch.float32, device=self.dev)
+        self._gnbfp = torch.empty(self.ntypes, self.ntypes, 2, dtype=torch.float64, device=self.dev)
+        self.energies = torch.zeros(2 * self.nsys, dtype=torch.float64, device=self.dev)
+        self.virials = torch.zeros(9 * self.nsys, dtype=torch.float64, device=self.dev)
+        self._q = torch.empty(n, dtype=torch.float32, device=self.dev)
+        self._nbfp = torch.empty(self.ntypes * self.ntypes * 2, dtype=torch.float32, device=self.dev)
+
+    def _run(self, q, nbfp):
+        # fixed buffers keep the captured graph's pointers valid between calls
+        self._q.copy_(q.detach().reshape(-1))
+        self._nbfp.copy_((0.5 * (nbfp + nbfp.transpose(0, 1))).detach().reshape(-1))
+        self.batch.set_stream(torch.cuda.current_stream(self.dev).cuda_stream)
+        self.batch.force_match_device(self.x.data_ptr(), self._q.data_ptr(), self._nbfp.data_ptr(),
+                                      self.f_target.data_ptr(), self._loss.data_ptr(), self._gq.data_ptr(),
+                                      self._gnbfp.data_ptr(), self.energies.data_ptr(), self.virials.data_ptr())
+        # the table gradient of the symmetrised table, back onto the input table
+        self._gnbfp.copy_(0.5 * (self._gnbfp + self._gnbfp.transpose(0, 1)))
+        return self._loss[0].clone()
+
+    def __call__(self, q: torch.Tensor, nbfp: torch.Tensor):
+        return _BatchMatchLoss.apply(q, nbfp, self)
+
+    def close(self):
+        self.batch.close()

@@ -88,6 +88,24 @@ class BatchForceCalculator:
             self.h, int(step), C.c_void_p(x_ptr), C.c_void_p(f_ptr), C.c_void_p(e_ptr) if e_ptr else None,
             C.c_void_p(vir_ptr) if vir_ptr else None))
 
+    # ---- adjoint / force matching (raw device pointers) ----
+    def set_parameters_device(self, q_ptr: int | None, nbfp_ptr: int | None):
+        self._check(_lib.load().nbx_batch_set_parameters_device(
+            self.h, C.c_void_p(q_ptr) if q_ptr else None, C.c_void_p(nbfp_ptr) if nbfp_ptr else None))
+
+    def backward_device(self, x_ptr, gf_ptr, ge_ptr=None, gx_ptr=None, gq_ptr=None, gnbfp_ptr=None):
+        vp = C.c_void_p
+        self._check(_lib.load().nbx_batch_backward_device(
+            self.h, vp(x_ptr), vp(gf_ptr), vp(ge_ptr) if ge_ptr else None, vp(gx_ptr) if gx_ptr else None,
+            vp(gq_ptr) if gq_ptr else None, vp(gnbfp_ptr) if gnbfp_ptr else None))
+
+    def force_match_device(self, x_ptr, q_ptr, nbfp_ptr, ftarget_ptr, loss_ptr, gq_ptr, gnbfp_ptr, e_ptr=None,
+                           vir_ptr=None):
+        vp = C.c_void_p
+        self._check(_lib.load().nbx_batch_force_match_device(
+            self.h, vp(x_ptr), vp(q_ptr), vp(nbfp_ptr), vp(ftarget_ptr), vp(loss_ptr), vp(gq_ptr), vp(gnbfp_ptr),
+            vp(e_ptr) if e_ptr else None, vp(vir_ptr) if vir_ptr else None))
+
     def set_graph(self, enable: bool):
         self._check(_lib.load().nbx_batch_set_graph(self.h, int(bool(enable))))
 

@@ -39,9 +39,22 @@ struct AdjConsts
     float gE_lj, gE_c;  // upstream energy gradients
 };
 
+// The per-system arrays one list entry of the adjoint touches.
+struct AdjPtrs
+{
+    const float4* xq;
+    const int*    tgrid;
+    const Cj4*    cj4;
+    const Excl*   excl;
+    const float*  shiftvec;
+    const float4* gnb;
+    float4*       dnb;
+};
+
 template<bool kEwald, bool kExcl>
-__device__ __forceinline__ void adj_half(const DeviceView& v, const float2* __restrict__ nbfp_s, float2* ttab,
-                                         const float4* __restrict__ xis, const float4* __restrict__ gis,
+__device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __restrict__ xq,
+                                         const int* __restrict__ tgrid, const float2* __restrict__ nbfp_s,
+                                         float2* ttab, const float4* __restrict__ xis, const float4* __restrict__ gis,
                                          const float4* __restrict__ gnb, float4* dnb, const int cj_lane,
                                          unsigned im, unsigned wexcl, int h, int sci, bool central, int ii, int jj,
                                          float dxa[kNcl], float dya[kNcl], float dza[kNcl], float dqa[kNcl],
@@ -59,9 +72,9 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float2* __re
             continue;
         }
         const int      aj = cj * kCl + h * (kCl / kSplit) + jj;
-        const float4   xj = v.xq[aj];
+        const float4   xj = xq[aj];
         const float4   gj = gnb[aj];
-        const int      tj = v.tgrid[aj];
+        const int      tj = tgrid[aj];
         const unsigned wj = wexcl >> (jm * kNcl);
         float          djx = 0.0f, djy = 0.0f, djz = 0.0f, djq = 0.0f;
 #pragma unroll
@@ -181,6 +194,114 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float2* __re
     }
 }
 
+// One list entry: its 64 shifted i-atoms and their upstream gradients go to the
+// warp's shared-memory slots, all cj4 groups are processed, then the i-side sums
+// and the entry's type-pair table are flushed (vector reds / FP64 atomics).
+template<bool kEwald>
+__device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p, const Sci& s,
+                                          const float2* __restrict__ nbfp_s, float2* ttab, float4* xis, float4* gis,
+                                          int lane, const AdjConsts& k, float pbeta, float beta2l2, float c2b,
+                                          float b2c2b, double* gnbfp)
+{
+    const unsigned full    = 0xffffffffu;
+    const int      ii      = lane & 7;
+    const int      jj      = lane >> 3;
+    const int      nt1     = v.ntypes1;
+    const float    sx = p.shiftvec[3 * s.shift], sy = p.shiftvec[3 * s.shift + 1], sz = p.shiftvec[3 * s.shift + 2];
+    const bool     central = (s.shift == kCentral);
+    __syncwarp();
+    for (int m = lane; m < kSc; m += 32)
+    {
+        const int    a = s.sci * kSc + m;
+        const float4 x = p.xq[a];
+        const float4 g = p.gnb[a];
+        xis[m]         = make_float4(x.x + sx, x.y + sy, x.z + sz, x.w);
+        gis[m]         = make_float4(g.x, g.y, g.z, __int_as_float(p.tgrid[a]));
+    }
+    __syncwarp();
+    float dxa[kNcl], dya[kNcl], dza[kNcl], dqa[kNcl];
+#pragma unroll
+    for (int c = 0; c < kNcl; c++)
+    {
+        dxa[c] = dya[c] = dza[c] = dqa[c] = 0.0f;
+    }
+    for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
+    {
+        const int4 ime     = *reinterpret_cast<const int4*>(&p.cj4[j4].imei[0]);
+        const int  cj_lane = (lane < kJg) ? p.cj4[j4].cj[lane] : 0;
+#pragma unroll 1
+        for (int h = 0; h < kSplit; h++)
+        {
+            const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
+            const int      exi = (h == 0) ? ime.y : ime.w;
+            if (!im)
+            {
+                continue;
+            }
+            if (exi == 0)
+            {
+                adj_half<kEwald, false>(v, p.xq, p.tgrid, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h,
+                                        s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+            }
+            else
+            {
+                const unsigned wexcl = p.excl[exi].pair[lane];
+                adj_half<kEwald, true>(v, p.xq, p.tgrid, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl,
+                                       h, s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kNcl; c++)
+    {
+        float ax = dxa[c], ay = dya[c], az = dza[c], aq = dqa[c];
+        for (int o = 8; o < 32; o <<= 1)
+        {
+            ax += __shfl_xor_sync(full, ax, o);
+            ay += __shfl_xor_sync(full, ay, o);
+            az += __shfl_xor_sync(full, az, o);
+            aq += __shfl_xor_sync(full, aq, o);
+        }
+        if (jj == 0)
+        {
+            float4* dst = &p.dnb[(s.sci * kNcl + c) * kCl + ii];
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(ax), "f"(ay), "f"(az),
+                         "f"(aq)
+                         : "memory");
+        }
+    }
+    // flush the type-pair gradients of this entry into the FP64 sums
+    __syncwarp();
+    for (int m = lane; m < nt1 * nt1; m += 32)
+    {
+        const float2 t = ttab[m];
+        if (t.x != 0.0f || t.y != 0.0f)
+        {
+            atomicAdd(&gnbfp[2 * m], (double)t.x);
+            atomicAdd(&gnbfp[2 * m + 1], (double)t.y);
+            ttab[m] = make_float2(0.0f, 0.0f);
+        }
+    }
+    __syncwarp();
+}
+
+// Shared set-up of the adjoint kernels: the type table and zeroed per-warp tables.
+__device__ __forceinline__ void adj_setup(const DeviceView& v, float2* nbfp_s, float2 (*ttab_s)[kAdjMaxTypes1 * kAdjMaxTypes1])
+{
+    const int nt1  = v.ntypes1;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    for (int m = threadIdx.x; m < nt1 * nt1; m += blockDim.x)
+    {
+        nbfp_s[m] = v.nbfp[m];
+    }
+    for (int m = lane; m < nt1 * nt1; m += 32)
+    {
+        ttab_s[warp][m] = make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+}
+
 template<bool kEwald>
 __global__ void __launch_bounds__(kAdjThreads, 2)
         k_backward(DeviceView v, const float4* __restrict__ gnb, float4* dnb, double* gnbfp, int* work_counter,
@@ -196,34 +317,16 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
     __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
-    const int         nt1  = v.ntypes1;
-    const int         warp = threadIdx.x >> 5;
-    const int         lane = threadIdx.x & 31;
-    for (int m = threadIdx.x; m < nt1 * nt1; m += blockDim.x)
-    {
-        nbfp_s[m] = v.nbfp[m];
-    }
-    for (int m = lane; m < nt1 * nt1; m += 32)
-    {
-        ttab_s[warp][m] = make_float2(0.0f, 0.0f);
-    }
-    __syncthreads();
+    adj_setup(v, nbfp_s, ttab_s);
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
         return;
     }
-    const unsigned full    = 0xffffffffu;
-    const int      ii      = lane & 7;
-    const int      jj      = lane >> 3;
-    const int      numSci  = v.hdr->num_sci;
-    const float    beta    = v.beta;
-    const float    pbeta   = v.erfc_p * beta;
-    const float    beta2l2 = beta * beta * 1.4426950408889634f;
-    const float    c2b     = 1.1283791670955126f * beta;
-    const float    b2c2b   = beta * beta * c2b;
-    float4*        xis     = xis_s[warp];
-    float4*        gis     = gis_s[warp];
-    float2*        ttab    = ttab_s[warp];
+    const int     warp   = threadIdx.x >> 5;
+    const int     lane   = threadIdx.x & 31;
+    const int     numSci = v.hdr->num_sci;
+    const float   b2c2b  = v.beta * v.beta * v.c2b;
+    const AdjPtrs p      = { v.xq, v.tgrid, v.cj4, v.excl, v.shiftvec, gnb, dnb };
     for (;;)
     {
         int e = 0;
@@ -231,87 +334,155 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         {
             e = atomicAdd(work_counter, 1);
         }
-        e = __shfl_sync(full, e, 0);
+        e = __shfl_sync(0xffffffffu, e, 0);
         if (e >= numSci)
         {
             break;
         }
-        const Sci   s  = v.sci[e];
-        const float sx = v.shiftvec[3 * s.shift], sy = v.shiftvec[3 * s.shift + 1], sz = v.shiftvec[3 * s.shift + 2];
-        const bool  central = (s.shift == kCentral);
-        for (int m = lane; m < kSc; m += 32)
+        adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], lane, k, v.pbeta,
+                          v.beta2l2, v.c2b, b2c2b, gnbfp);
+    }
+}
+
+__device__ __forceinline__ int adj_find_system(const int* prefix, int nsys, int e)
+{
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= e)
         {
-            const int    a = s.sci * kSc + m;
-            const float4 x = v.xq[a];
-            const float4 g = gnb[a];
-            xis[m]         = make_float4(x.x + sx, x.y + sy, x.z + sz, x.w);
-            gis[m]         = make_float4(g.x, g.y, g.z, __int_as_float(v.tgrid[a]));
+            lo = mid;
         }
-        __syncwarp();
-        float dxa[kNcl], dya[kNcl], dza[kNcl], dqa[kNcl];
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
+        else
         {
-            dxa[c] = dya[c] = dza[c] = dqa[c] = 0.0f;
+            hi = mid - 1;
         }
-        for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
+    }
+    return lo;
+}
+
+// The adjoint over all systems of a batch (shared type table and type-pair
+// gradient sums; per-system upstream energy gradients gE[2 s], gE[2 s + 1]).
+template<bool kEwald>
+__global__ void __launch_bounds__(kAdjThreads, 2)
+        k_batch_backward(DeviceView cv, const BatchSys* __restrict__ sys, const int* __restrict__ prefix, int nsys,
+                         double* gnbfp, int* work_counter, const double* __restrict__ gE)
+{
+    __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ float4 xis_s[kAdjWarps][kSc];
+    __shared__ float4 gis_s[kAdjWarps][kSc];
+    adj_setup(cv, nbfp_s, ttab_s);
+    const int   warp  = threadIdx.x >> 5;
+    const int   lane  = threadIdx.x & 31;
+    const int   total = prefix[nsys];
+    const float b2c2b = cv.beta * cv.beta * cv.c2b;
+    for (;;)
+    {
+        int e = 0;
+        if (lane == 0)
         {
-            const int4 ime     = *reinterpret_cast<const int4*>(&v.cj4[j4].imei[0]);
-            const int  cj_lane = (lane < kJg) ? v.cj4[j4].cj[lane] : 0;
-#pragma unroll 1
-            for (int h = 0; h < kSplit; h++)
-            {
-                const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
-                const int      exi = (h == 0) ? ime.y : ime.w;
-                if (!im)
-                {
-                    continue;
-                }
-                if (exi == 0)
-                {
-                    adj_half<kEwald, false>(v, nbfp_s, ttab, xis, gis, gnb, dnb, cj_lane, im, 0u, h, s.sci, central,
-                                            ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
-                }
-                else
-                {
-                    const unsigned wexcl = v.excl[exi].pair[lane];
-                    adj_half<kEwald, true>(v, nbfp_s, ttab, xis, gis, gnb, dnb, cj_lane, im, wexcl, h, s.sci,
-                                           central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
-                }
-            }
+            e = atomicAdd(work_counter, 1);
         }
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
+        e = __shfl_sync(0xffffffffu, e, 0);
+        if (e >= total)
         {
-            float ax = dxa[c], ay = dya[c], az = dza[c], aq = dqa[c];
-            for (int o = 8; o < 32; o <<= 1)
-            {
-                ax += __shfl_xor_sync(full, ax, o);
-                ay += __shfl_xor_sync(full, ay, o);
-                az += __shfl_xor_sync(full, az, o);
-                aq += __shfl_xor_sync(full, aq, o);
-            }
-            if (jj == 0)
-            {
-                float4* dst = &dnb[(s.sci * kNcl + c) * kCl + ii];
-                asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(ax), "f"(ay), "f"(az),
-                             "f"(aq)
-                             : "memory");
-            }
+            break;
         }
-        // flush the type-pair gradients of this entry into the FP64 sums
-        __syncwarp();
-        for (int m = lane; m < nt1 * nt1; m += 32)
+        const int       sidx = adj_find_system(prefix, nsys, e);
+        const BatchSys& b    = sys[sidx];
+        AdjConsts       k{ 0.0f, 0.0f };
+        if (gE)
         {
-            const float2 t = ttab[m];
-            if (t.x != 0.0f || t.y != 0.0f)
-            {
-                atomicAdd(&gnbfp[2 * m], (double)t.x);
-                atomicAdd(&gnbfp[2 * m + 1], (double)t.y);
-                ttab[m] = make_float2(0.0f, 0.0f);
-            }
+            k.gE_lj = (float)gE[2 * sidx];
+            k.gE_c  = (float)gE[2 * sidx + 1];
         }
-        __syncwarp();
+        const AdjPtrs p = { b.xq, b.tgrid, b.cj4, b.excl, b.shiftvec, b.gnb, b.dnb };
+        adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], lane, k,
+                          cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gnbfp);
+    }
+}
+
+// Batched upstream gradients to grid order (blockIdx.y = system), outputs cleared.
+__global__ void k_batch_adj_prepare(const BatchSys* __restrict__ sys, const float* __restrict__ gF)
+{
+    const BatchSys& b = sys[blockIdx.y];
+    const int       k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= b.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const int     a = b.atom_indices[k];
+    const float*  g = gF + 3 * (size_t)(b.atom_base + (a >= 0 ? a : 0));
+    const_cast<float4*>(b.gnb)[k] = (a >= 0) ? make_float4(g[0], g[1], g[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    b.dnb[k]                      = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// Batched atom-order outputs (blockIdx.y = system), dL/dq with the self-energy term.
+__global__ void k_batch_adj_finish(DeviceView cv, const BatchSys* __restrict__ sys, const double* __restrict__ gE,
+                                   float* gx, float* gq)
+{
+    const BatchSys& b = sys[blockIdx.y];
+    const int       a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= b.n)
+    {
+        return;
+    }
+    const int    k = b.cells[a];
+    const float4 d = b.dnb[k];
+    const size_t o = (size_t)b.atom_base + a;
+    if (gx)
+    {
+        gx[3 * o]     = d.x;
+        gx[3 * o + 1] = d.y;
+        gx[3 * o + 2] = d.z;
+    }
+    if (gq)
+    {
+        const float q    = b.xq[k].w;
+        const float self = (cv.coulomb == 0) ? -2.0f * cv.epsfac * cv.beta * 0.5641895835477563f * q
+                                             : -cv.epsfac * cv.c_rf * q;
+        gq[o]            = gE ? d.w + (float)gE[2 * blockIdx.y + 1] * self : d.w;
+    }
+}
+
+// Charges of all systems (concatenated atom order) into xq.w and each system's q.
+__global__ void k_batch_set_q(const BatchSys* __restrict__ sys, const float* __restrict__ q)
+{
+    const BatchSys& b = sys[blockIdx.y];
+    const int       k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= b.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const int a = b.atom_indices[k];
+    if (a >= 0)
+    {
+        const float qa                  = q[(size_t)b.atom_base + a];
+        const_cast<float4*>(b.xq)[k].w  = qa;
+        b.q[a]                          = qa;
+    }
+}
+
+// Loss sum |F - F_target|^2 (FP64) and its gradient 2 (F - F_target) per coordinate.
+__global__ void k_match_loss(const float* __restrict__ f, const float* __restrict__ ft, size_t n3, float* gF,
+                             double* loss)
+{
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (size_t)gridDim.x * blockDim.x)
+    {
+        const float d = f[i] - ft[i];
+        gF[i]         = 2.0f * d;
+        acc += (double)d * (double)d;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    }
+    if ((threadIdx.x & 31) == 0 && acc != 0.0)
+    {
+        atomicAdd(loss, acc);
     }
 }
 
@@ -380,6 +551,46 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double
     }
     k_adj_finish<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, dnb, d_gE, d_gx, d_gq);
     return cudaGetLastError();
+}
+
+cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
+                                  int max_slots, int max_atoms, const float* d_gF, const double* d_gE,
+                                  double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s)
+{
+    const int tb = 256;
+    k_batch_adj_prepare<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_gF);
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    cudaMemsetAsync(d_gnbfp, 0, sizeof(double) * 2 * cv.ntypes1 * cv.ntypes1, s);
+    if (cv.coulomb == 0)
+    {
+        k_batch_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+    }
+    else
+    {
+        k_batch_backward<false><<<num_sms * 2, kAdjThreads, 0, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+    }
+    k_batch_adj_finish<<<dim3((max_atoms + tb - 1) / tb, nsys), tb, 0, s>>>(cv, sys, d_gE, d_gx, d_gq);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_set_q(const BatchSys* sys, int nsys, int max_slots, const float* d_q, cudaStream_t s)
+{
+    const int tb = 256;
+    k_batch_set_q<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_match_loss(const float* d_f, const float* d_ft, size_t n3, float* d_gF, double* d_loss,
+                              int num_sms, cudaStream_t s)
+{
+    cudaMemsetAsync(d_loss, 0, sizeof(double), s);
+    k_match_loss<<<num_sms * 4, 256, 0, s>>>(d_f, d_ft, n3, d_gF, d_loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_nbfp(const DeviceView& v, const float* d_nbfp, cudaStream_t s)
+{
+    return launch_set_parameters(v, nullptr, d_nbfp, s);
 }
 
 // Charges and LJ parameters for force matching: q (atom order) into xq.w and the

@@ -1339,6 +1339,14 @@ struct nbx_batch
     cudaGraphExec_t          graph      = nullptr;
     cudaStream_t             capture_stream = nullptr;  // private: capture is not allowed on legacy streams
     const void*              graph_key[4] = { nullptr, nullptr, nullptr, nullptr };
+    // adjoint / force matching
+    double*                  d_gnbfp_pad = nullptr;  // (nt+1)^2 * 2 FP64 type-pair sums
+    int*                     d_adj_counter = nullptr;
+    float*                   d_fm_f = nullptr;       // forces of the force-matching step, 3N
+    float*                   d_fm_g = nullptr;       // dL/dF, 3N
+    bool                     charges_on_device = false;
+    cudaGraphExec_t          fm_graph = nullptr;
+    const void*              fm_key[9] = { nullptr };
 };
 
 namespace
@@ -1396,6 +1404,10 @@ int batch_refresh(nbx_batch* b)
         t.n                 = v.n;
         t.atom_base         = b->offsets[i];
         t.self_energy       = v.self_energy;
+        t.self_on_device    = v.self_on_device;
+        t.gnb               = b->sys[i]->d_gnb;
+        t.dnb               = b->sys[i]->d_dnb;
+        t.q                 = const_cast<float*>(v.q);
         for (int d = 0; d < 3; d++)
         {
             t.box[d] = v.g.box[d];
@@ -1476,9 +1488,205 @@ int batch_compute(nbx_batch* b, const float* d_x, float* d_f, double* d_e, doubl
     cudaError_t e = cudaGraphLaunch(b->graph, b->stream);
     return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
 }
+// Adjoint scratch of every system and of the batch (first use), then the table.
+int batch_ensure_adjoint(nbx_batch* b)
+{
+    if (b->d_gnbfp_pad)
+    {
+        return NBX_OK;
+    }
+    if (b->cv.ntypes1 > adjoint_max_types1())
+    {
+        return batch_error(b, NBX_ERR_INVALID_INPUT, "the adjoint supports at most 15 particle types");
+    }
+    cudaError_t e = cudaSuccess;
+    for (nbx_handle* h : b->sys)
+    {
+        if (!h->d_gnb)
+        {
+            const size_t slots = (size_t)h->v.g.cells_capacity * kSc;
+            e = dalloc(h, &h->d_gnb, slots);
+            if (e == cudaSuccess) e = dalloc(h, &h->d_dnb, slots);
+            if (e == cudaSuccess) e = dalloc(h, &h->d_gnbfp, 2 * (size_t)h->v.ntypes1 * h->v.ntypes1);
+            if (e == cudaSuccess) e = dalloc(h, &h->d_adj_counter, 1);
+            if (e != cudaSuccess)
+            {
+                return batch_error(b, NBX_ERR_OUT_OF_MEMORY, "adjoint allocation");
+            }
+        }
+    }
+    const size_t n3 = 3 * (size_t)b->offsets.back();
+    e = cudaMalloc(&b->d_gnbfp_pad, sizeof(double) * 2 * b->cv.ntypes1 * b->cv.ntypes1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_adj_counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_fm_f, sizeof(float) * n3);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_fm_g, sizeof(float) * n3);
+    if (e != cudaSuccess)
+    {
+        return batch_error(b, NBX_ERR_OUT_OF_MEMORY, "adjoint allocation");
+    }
+    return b->have_list ? batch_refresh(b) : NBX_OK;
+}
+
+// From now on every system's self energy follows the charges on the device.
+int batch_charges_on_device(nbx_batch* b)
+{
+    if (b->charges_on_device)
+    {
+        return NBX_OK;
+    }
+    for (nbx_handle* h : b->sys)
+    {
+        h->v.self_on_device = 1;
+        h->v.self_energy    = 0.0;
+    }
+    b->charges_on_device = true;
+    drop_graph(b);  // the table changes
+    return b->have_list ? batch_refresh(b) : NBX_OK;
+}
+
+cudaError_t batch_backward_launch(nbx_batch* b, const float* d_gF, const double* d_gE, float* d_gx, float* d_gq,
+                                  double* d_gnbfp, cudaStream_t s)
+{
+    const int   nsys = (int)b->sys.size();
+    cudaError_t e    = launch_batch_backward(b->cv, b->d_table, b->d_prefix, nsys, b->max_slots, b->max_atoms, d_gF,
+                                             d_gE, b->d_gnbfp_pad, b->d_adj_counter, d_gx, d_gq, b->num_sms, s);
+    if (e == cudaSuccess && d_gnbfp)
+    {
+        e = launch_compact_gnbfp(b->d_gnbfp_pad, d_gnbfp, b->cv.ntypes1 - 1, s);
+    }
+    return e;
+}
+
 } // namespace
 
 extern "C" {
+
+int nbx_batch_set_parameters_device(nbx_batch* b, const float* d_q, const float* d_nbfp)
+{
+    if (!b)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    cudaSetDevice(b->device);
+    if (d_q)
+    {
+        int rc = batch_charges_on_device(b);
+        if (rc != NBX_OK)
+        {
+            return rc;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; d_nbfp && i < b->sys.size() && e == cudaSuccess; i++)
+    {
+        // every system's copy of the shared type table (the batched kernels read the first)
+        e = launch_set_parameters(b->sys[i]->v, nullptr, d_nbfp, b->stream);
+    }
+    if (e == cudaSuccess && d_q)
+    {
+        e = launch_batch_set_q(b->d_table, (int)b->sys.size(), b->max_slots, d_q, b->stream);
+    }
+    return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int nbx_batch_backward_device(nbx_batch* b, const float* d_x, const float* d_gF, const double* d_gE, float* d_gx,
+                              float* d_gq, double* d_gnbfp)
+{
+    if (!b || !d_x || !d_gF)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!b->have_list)
+    {
+        return batch_error(b, NBX_ERR_STATE, "no pair lists");
+    }
+    cudaSetDevice(b->device);
+    int rc = batch_ensure_adjoint(b);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    // coordinates into the grid layout (the kernel also clears the force buffers)
+    cudaError_t e = launch_batch_convert(b->d_table, (int)b->sys.size(), b->max_slots, d_x, b->stream);
+    if (e == cudaSuccess) e = batch_backward_launch(b, d_gF, d_gE, d_gx, d_gq, d_gnbfp, b->stream);
+    return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int nbx_batch_force_match_device(nbx_batch* b, const float* d_x, const float* d_q, const float* d_nbfp,
+                                 const float* d_ftarget, double* d_loss, float* d_gq, double* d_gnbfp, double* d_e,
+                                 double* d_vir)
+{
+    if (!b || !d_x || !d_q || !d_nbfp || !d_ftarget || !d_loss)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!b->have_list)
+    {
+        return batch_error(b, NBX_ERR_STATE, "no pair lists");
+    }
+    cudaSetDevice(b->device);
+    int rc = batch_ensure_adjoint(b);
+    if (rc == NBX_OK) rc = batch_charges_on_device(b);
+    if (rc != NBX_OK)
+    {
+        return rc;
+    }
+    const int    nsys = (int)b->sys.size();
+    const size_t n3   = 3 * (size_t)b->offsets.back();
+    auto         run  = [&](cudaStream_t s) {
+        cudaError_t e = launch_set_parameters(b->sys[0]->v, nullptr, d_nbfp, s);
+        if (e == cudaSuccess) e = launch_batch_set_q(b->d_table, nsys, b->max_slots, d_q, s);
+        if (e == cudaSuccess)
+            e = launch_batch_compute(b->cv, b->d_table, b->d_prefix, nsys, b->max_slots, b->max_atoms, d_x,
+                                     b->d_fm_f, b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, b->variant,
+                                     b->num_sms, s);
+        if (e == cudaSuccess) e = launch_match_loss(b->d_fm_f, d_ftarget, n3, b->d_fm_g, d_loss, b->num_sms, s);
+        if (e == cudaSuccess) e = batch_backward_launch(b, b->d_fm_g, nullptr, nullptr, d_gq, d_gnbfp, s);
+        return e;
+    };
+    if (!b->use_graph)
+    {
+        cudaError_t e = run(b->stream);
+        return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const void* key[9] = { d_x, d_q, d_nbfp, d_ftarget, d_loss, d_gq, d_gnbfp, d_e, d_vir };
+    if (!b->fm_graph || std::memcmp(key, b->fm_key, sizeof(key)) != 0)
+    {
+        if (b->fm_graph)
+        {
+            cudaGraphExecDestroy(b->fm_graph);
+            b->fm_graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess)
+        {
+            cudaError_t e2 = run(b->capture_stream);
+            e              = cudaStreamEndCapture(b->capture_stream, &g);
+            if (e2 != cudaSuccess)
+            {
+                e = e2;
+            }
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->fm_graph, g, 0);
+        if (g)
+        {
+            cudaGraphDestroy(g);
+        }
+        if (e != cudaSuccess)
+        {
+            if (b->fm_graph)
+            {
+                cudaGraphExecDestroy(b->fm_graph);
+            }
+            b->fm_graph = nullptr;
+            return batch_error(b, NBX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        std::memcpy(b->fm_key, key, sizeof(key));
+    }
+    cudaError_t e = cudaGraphLaunch(b->fm_graph, b->stream);
+    return e == cudaSuccess ? NBX_OK : batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
 
 const char* nbx_batch_last_error(const nbx_batch* b)
 {
@@ -1576,6 +1784,14 @@ int nbx_batch_destroy(nbx_batch* b)
         cudaStreamSynchronize(b->stream);
     }
     drop_graph(b);
+    if (b->fm_graph)
+    {
+        cudaGraphExecDestroy(b->fm_graph);
+    }
+    cudaFree(b->d_gnbfp_pad);
+    cudaFree(b->d_adj_counter);
+    cudaFree(b->d_fm_f);
+    cudaFree(b->d_fm_g);
     for (nbx_handle* h : b->sys)
     {
         nbx_destroy(h);

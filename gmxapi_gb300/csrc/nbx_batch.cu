@@ -115,6 +115,12 @@ __global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ 
     {
         const float4 xi = b.xq[b.cells[i]];
         const int    nx = (b.box[0] < cv.rlist) ? 2 : 1;
+        if (b.self_on_device)
+        {
+            // self term from the current charges (kernel_gpu_ref.cpp:154-178)
+            acc += (double)xi.w * (double)xi.w
+                   * (cv.coulomb == 0 ? -(double)cv.beta * 0.56418958354775628695 : -0.5 * (double)cv.c_rf);
+        }
         for (int k = b.excl_index[i]; k < b.excl_index[i + 1]; k++)
         {
             const int j = b.excl_list[k];
@@ -377,6 +383,13 @@ cudaError_t launch_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsi
 }
 
 // One batched step: sums (energies | fshift | virial partials | work counter)
+cudaError_t launch_batch_convert(const BatchSys* sys, int nsys, int max_slots, const float* d_x, cudaStream_t s)
+{
+    const int tb = 256;
+    k_batch_convert<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_x);
+    return cudaGetLastError();
+}
+
 // cleared with one memset, then the five kernels.
 cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
                                  int max_slots, int max_atoms, const float* d_x, float* d_f, double* sums,

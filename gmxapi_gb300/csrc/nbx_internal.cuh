@@ -172,9 +172,13 @@ struct BatchSys
     const ListHeader* hdr;
     const int*        excl_index;
     const int*        excl_list;
+    const float4*     gnb;        // adjoint: upstream force gradients in grid order
+    float4*           dnb;        // adjoint: accumulated dL/dx, dL/dq in grid order
+    float*            q;          // charges, atom order
     int               n;          // atoms
     int               atom_base;  // offset in the concatenated coordinate / force arrays
-    int               pad0, pad1;
+    int               self_on_device;  // 1: the self energy comes from the current charges
+    int               pad1;
     double            self_energy;
     float             box[3];
     float             shiftvec[kNShift * 3];
@@ -203,6 +207,13 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double
                             double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s);
 cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);
 cudaError_t launch_compact_gnbfp(const double* padded, double* out, int nt, cudaStream_t s);
+cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
+                                  int max_slots, int max_atoms, const float* d_gF, const double* d_gE,
+                                  double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s);
+cudaError_t launch_batch_convert(const BatchSys* sys, int nsys, int max_slots, const float* d_x, cudaStream_t s);
+cudaError_t launch_batch_set_q(const BatchSys* sys, int nsys, int max_slots, const float* d_q, cudaStream_t s);
+cudaError_t launch_match_loss(const float* d_f, const float* d_ft, size_t n3, float* d_gF, double* d_loss,
+                              int num_sms, cudaStream_t s);
 cudaError_t launch_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsigned* status, cudaStream_t s);
 cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
                                  int max_slots, int max_atoms, const float* d_x, float* d_f, double* sums,

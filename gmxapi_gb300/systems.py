@@ -187,6 +187,36 @@ def _clashes(x, types, dmin, edge, pairs):
     return pairs[close]
 
 
+def force_matching_specs(num_systems: int = 64, n_min: int = 2000, n_max: int = 50000, ntypes: int = 8,
+                         seed: int = 5) -> list[dict]:
+    """Arguments of ``lj_liquid`` for an ensemble of log-uniform sizes sharing one set of
+    per-type sigma / epsilon (drawn as in ``lj_liquid``)."""
+    rng = np.random.default_rng(seed)
+    sig_t = rng.uniform(0.25, 0.40, size=ntypes)
+    eps_t = rng.uniform(0.1, 1.0, size=ntypes)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=num_systems)).astype(int)
+    return [dict(n=int(n), ntypes=ntypes, seed=int(seed * 1000 + k), type_sigma=sig_t, type_epsilon=eps_t)
+            for k, n in enumerate(sizes)]
+
+
+def _lj_liquid_kwargs(kw: dict) -> System:
+    return lj_liquid(**kw)
+
+
+def force_matching_ensemble(num_systems: int = 64, n_min: int = 2000, n_max: int = 50000, ntypes: int = 8,
+                            seed: int = 5, processes: int = 1) -> list[System]:
+    """Random LJ + Coulomb liquids of log-uniform size sharing per-type sigma / epsilon;
+    positions, types and charges per system.  ``processes`` > 1 builds them in a
+    spawn-started process pool (safe after CUDA is initialised)."""
+    specs = force_matching_specs(num_systems, n_min, n_max, ntypes, seed)
+    if processes <= 1:
+        return [lj_liquid(**kw) for kw in specs]
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(processes) as pool:
+        return pool.map(_lj_liquid_kwargs, specs)
+
+
 def lj_liquid(
     n: int = 24000,
     ntypes: int = 8,
@@ -196,6 +226,8 @@ def lj_liquid(
     q_sigma: float = 0.4,
     sigma_range: tuple[float, float] = (0.25, 0.40),
     epsilon_range: tuple[float, float] = (0.1, 1.0),
+    type_sigma: np.ndarray | None = None,
+    type_epsilon: np.ndarray | None = None,
 ) -> System:
     """Random multi-type LJ + Coulomb liquid with Lorentz-Berthelot mixing.
 
@@ -203,9 +235,9 @@ def lj_liquid(
     epsilon_t ~ U(epsilon_range); charges ~ N(0, q_sigma) shifted to a zero
     total.  Positions are uniform in a cubic box at ``density``; every pair
     closer than ``min_dist_fraction * sigma_ij`` is rejected and the
-    higher-numbered atom redrawn, from 64 uniform candidates per round tested
-    against the atoms already accepted, until no such pair is left (periodic
-    k-d trees).  At 100 atoms/nm^3 a fraction of 0.8 packs beyond random close
+    higher-numbered atom redrawn, from uniform candidates tested against the
+    atoms already accepted (more candidates per round as the free volume
+    shrinks), until no such pair is left (periodic k-d trees).  At 100 atoms/nm^3 a fraction of 0.8 packs beyond random close
     packing, so it cannot finish; 0.5 is the default (packing fraction ~0.22).
     """
     from scipy.spatial import cKDTree
@@ -214,6 +246,11 @@ def lj_liquid(
     edge = (n / density) ** (1.0 / 3.0)
     sig_t = rng.uniform(*sigma_range, size=ntypes)
     eps_t = rng.uniform(*epsilon_range, size=ntypes)
+    # parameters shared by an ensemble replace the drawn ones (the draws keep the stream)
+    if type_sigma is not None:
+        sig_t = np.asarray(type_sigma, np.float64)
+    if type_epsilon is not None:
+        eps_t = np.asarray(type_epsilon, np.float64)
     types = rng.integers(0, ntypes, size=n).astype(np.int32)
     q = rng.normal(0.0, q_sigma, size=n)
     q = (q - q.mean()).astype(np.float32)
@@ -225,7 +262,7 @@ def lj_liquid(
     # first pass: of every clashing pair the higher-numbered atom is redrawn
     tree = cKDTree(x, boxsize=edge)
     redo = np.unique(_clashes(x, types, dmin, edge, tree.query_pairs(rmax, output_type="ndarray")).max(axis=1))
-    kcand, kngb = 64, 16
+    kcand, kngb = 8, 16  # candidates per atom and round: doubled while fewer than half the atoms place
     for _round in range(10000):
         if len(redo) == 0:
             break
@@ -240,6 +277,8 @@ def lj_liquid(
         ok = ~bad.any(axis=1) & ~near[:, -1]  # a full neighbour list is rejected outright
         ok = ok.reshape(len(redo), kcand)
         has = ok.any(axis=1)
+        if has.mean() < 0.5:
+            kcand = min(2 * kcand, 256)
         first = ok.argmax(axis=1)
         placed = redo[has]
         x[placed] = cand[has, first[has]]

@@ -201,6 +201,24 @@ int nbx_batch_sequential_md_step_device(nbx_batch* b, long long step, const floa
 int nbx_batch_set_graph(nbx_batch* b, int enable);
 int nbx_batch_set_kernel_variant(nbx_batch* b, int variant);
 int nbx_batch_set_prune(nbx_batch* b, int nstlist_prune, float rlist_inner);
+/* Batched adjoint (no counterpart in the reference).  d_q: all systems' charges, concatenated atom
+ * order; d_nbfp: the shared {6 C6, 12 C12} table ([num_types^2 * 2]); either may be NULL.  Once
+ * charges are set this way every system's self energy follows them. */
+int nbx_batch_set_parameters_device(nbx_batch* b, const float* d_q, const float* d_nbfp);
+/* dL/dx, dL/dq (concatenated atom order, float) and dL/dnbfp summed over all systems
+ * ([num_types^2 * 2] double) for upstream d_gF ([3N] float) and d_gE ([2 * num_systems] double
+ * {LJ, Coulomb} per system, NULL = 0); outputs may be NULL.  At most 15 particle types. */
+int nbx_batch_backward_device(nbx_batch* b, const float* d_x, const float* d_gF, const double* d_gE, float* d_gx,
+                              float* d_gq, double* d_gnbfp);
+/* One force-matching gradient step over the batch, on the current pair lists: parameters (d_q,
+ * d_nbfp as above) -> forces, energies, virials -> loss = sum |F - F_target|^2 (FP64, d_loss[1])
+ * -> adjoint -> dL/dq ([N] float) and dL/dnbfp ([num_types^2 * 2] double).  Captured into one
+ * CUDA graph (re-captured when an argument pointer changes) unless graphs are switched off.  The
+ * type table is written to the copy the batched kernels read (the first system's); the other
+ * systems' copies follow only nbx_batch_set_parameters_device. */
+int nbx_batch_force_match_device(nbx_batch* b, const float* d_x, const float* d_q, const float* d_nbfp,
+                                 const float* d_ftarget, double* d_loss, float* d_gq, double* d_gnbfp, double* d_e,
+                                 double* d_vir);
 
 /* ---- allocation-free force evaluation ---- */
 /* Inputs of nbx_compute_noalloc: the atom data and pair list in the layouts that

@@ -235,3 +235,19 @@ def test_repeat_compute_stable_and_changes_after_update():
     x2 = systems.perturb(s.x, np.random.default_rng(0), 0.001)
     f3 = calc.compute(x2)
     assert np.all(f3 != f1)
+
+
+def test_large_box_force_error_vs_fp64_on_subset():
+    """The 288,000-atom SPC box (96,000 molecules, 14.21 nm): GPU forces on a random
+    3,000-atom subset against the FP64 explicit-image sum."""
+    s = systems.water_large()
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
+                                 compute_virial_and_energy=True)
+    calc = nblib.ForceCalculator(s, opts)
+    f = calc.compute(s.x)
+    sub = np.sort(np.random.default_rng(17).choice(s.n, 3000, replace=False)).astype(np.int32)
+    beta = O.Oracle(systems.water_small(), rc=0.9, rlist=1.0).beta  # beta depends on rc and rtol only
+    f64, _ = O.fp64_allpairs(s, coulomb=0, rc=0.9, beta=beta, subset=sub)
+    err = rel_rms(f[sub], f64)
+    print(f"288k box, 3000-atom subset: rel RMS vs FP64 {err:.2e}")
+    assert err <= 1e-5
