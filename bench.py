@@ -375,10 +375,6 @@ def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    # the adjoint gradient at the current parameters, for the comparison below
-    opt.zero_grad(set_to_none=True)
-    loss_at(sig, eps, qs).backward()
-    g_adj = torch.cat([sig.grad, eps.grad, qs.grad]).detach().clone()
     losses = []
     a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
@@ -389,6 +385,10 @@ def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
     step_ms = a.elapsed_time(z) / iters
 
     # baseline: central differences of plain sequential per-system forward evaluations
+    # the adjoint gradient at the final parameters, compared with central differences there
+    opt.zero_grad(set_to_none=True)
+    loss_at(sig, eps, qs).backward()
+    g_adj = torch.cat([sig.grad, eps.grad, qs.grad]).detach().clone()
     base = torch.cat([sig.detach(), eps.detach(), qs.detach()]).clone()
     fseq = torch.empty_like(x)
 
