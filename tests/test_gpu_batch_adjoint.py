@@ -97,7 +97,7 @@ def _fp64_loss_grads(ens, sig, eps, qscale, q0, f_target):
         x = torch.tensor(s.x, dtype=torch.float64, requires_grad=True)
         q = torch.tensor(q0[off:off + s.n], dtype=torch.float64) * k64[torch.tensor(s.type, dtype=torch.long)]
         f, _ = ref.forces_energies(x, q, nbfp)
-        ft = torch.tensor(f_target[off:off + s.n], dtype=torch.float64)
+        ft = torch.tensor(f_target[3 * off:3 * (off + s.n)], dtype=torch.float64).reshape(-1, 3)
         total = total + ((f - ft) ** 2).sum()
         off += s.n
     gs, ge, gk = torch.autograd.grad(total, (s64, e64, k64))
