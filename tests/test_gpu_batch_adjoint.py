@@ -138,8 +138,8 @@ def test_force_matching_step_matches_fp64_autograd():
     l64, gs, ge, gk = _fp64_loss_grads(ens, sig, eps, np.ones(8), q0, f_target.cpu().numpy())
     print("loss", float(loss), l64, "grads", rel_rms(s_p.grad.cpu(), gs), rel_rms(e_p.grad.cpu(), ge),
           rel_rms(k_p.grad.cpu(), gk))
-    assert abs(float(loss) - l64) <= 1e-4 * l64
-    assert rel_rms(s_p.grad.cpu(), gs) < 1e-4
-    assert rel_rms(e_p.grad.cpu(), ge) < 1e-4
-    assert rel_rms(k_p.grad.cpu(), gk) < 1e-4
+    assert abs(float(loss) - l64) <= 2e-5 * l64
+    assert rel_rms(s_p.grad.cpu(), gs) < 2e-5
+    assert rel_rms(e_p.grad.cpu(), ge) < 2e-5
+    assert rel_rms(k_p.grad.cpu(), gk) < 2e-5
     m.close()
