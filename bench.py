@@ -648,8 +648,18 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched-ensemble and adjoint measurements")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-ensemble, adjoint and force-matching measurements")
+    ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching"],
+                    help="run one of the extra measurements alone and print its JSON (profiling)")
     args = ap.parse_args()
+    if args.only:
+        import torch
+
+        torch.cuda.set_device(0)
+        fn = {"ensemble": measure_ensemble, "adjoint": measure_adjoint, "force_matching": measure_force_matching}
+        print(json.dumps({args.only: fn[args.only](0)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
