@@ -823,7 +823,12 @@ int nbx_set_stream(nbx_handle* h, void* s)
     {
         return NBX_ERR_INVALID_INPUT;
     }
+    if (static_cast<cudaStream_t>(s) == h->stream)
+    {
+        return NBX_OK;
+    }
     cudaSetDevice(h->device);
+    // work queued on the previous stream finishes before the new one is used
     cudaStreamSynchronize(h->stream);
     if (h->own_stream)
     {
@@ -1836,9 +1841,14 @@ int nbx_batch_set_stream(nbx_batch* b, void* s)
     {
         return NBX_ERR_INVALID_INPUT;
     }
+    if (static_cast<cudaStream_t>(s) == b->stream)
+    {
+        return NBX_OK;
+    }
     cudaSetDevice(b->device);
+    // work queued on the previous stream finishes before the new one is used; the
+    // graphs were captured on a private stream and are launched on whichever is current
     cudaStreamSynchronize(b->stream);
-    drop_graph(b);
     if (b->own_stream)
     {
         cudaStreamDestroy(b->stream);
