@@ -121,6 +121,38 @@ class DifferentiableNonbonded:
         self.calc.close()
 
 
+class _TypeScaledCharges(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, scale, helper):
+        ctx.helper = helper
+        return (helper.q0 * scale[helper.types]).to(torch.float32)
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, g):
+        h = ctx.helper
+        # per-type sums of q0 * dL/dq over the type-sorted atoms: prefix sums, no atomics
+        v = (h.q0 * g.to(h.q0.dtype))[h.perm]
+        cs = torch.cat([v.new_zeros(1), torch.cumsum(v, 0)])
+        return cs[h.ends] - cs[h.starts], None
+
+
+class TypeScaledCharges:
+    """q_i = q0_i * scale[type_i] with a cheap backward (dL/dscale by prefix sums over the
+    atoms sorted by type, instead of a scatter of N values onto a few addresses)."""
+
+    def __init__(self, q0: torch.Tensor, types: torch.Tensor, ntypes: int):
+        self.q0 = q0.to(torch.float64)
+        self.types = types.to(torch.long)
+        self.perm = torch.argsort(self.types, stable=True)
+        counts = torch.bincount(self.types, minlength=ntypes)
+        self.ends = torch.cumsum(counts, 0)
+        self.starts = self.ends - counts
+
+    def __call__(self, scale: torch.Tensor) -> torch.Tensor:
+        return _TypeScaledCharges.apply(scale, self)
+
+
 class _BatchMatchLoss(torch.autograd.Function):
     """(q, nbfp) -> force-matching loss of a batch; one graph launch computes the loss and
     both gradients, which backward returns scaled by the upstream gradient."""

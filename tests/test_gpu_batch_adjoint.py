@@ -13,7 +13,12 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from gmxapi_gb300 import systems  # noqa: E402
-from gmxapi_gb300.adjoint import BatchForceMatcher, DifferentiableNonbonded, lorentz_berthelot_nbfp  # noqa: E402
+from gmxapi_gb300.adjoint import (  # noqa: E402
+    BatchForceMatcher,
+    DifferentiableNonbonded,
+    TypeScaledCharges,
+    lorentz_berthelot_nbfp,
+)
 from gmxapi_gb300.batch import BatchForceCalculator  # noqa: E402
 from gmxapi_gb300.nblib import CoulombType, NBKernelOptions  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
@@ -128,12 +133,11 @@ def test_force_matching_step_matches_fp64_autograd():
     s_p = torch.tensor(sig, dtype=torch.float64, device=DEV, requires_grad=True)
     e_p = torch.tensor(eps, dtype=torch.float64, device=DEV, requires_grad=True)
     k_p = torch.ones(8, dtype=torch.float64, device=DEV, requires_grad=True)
-    t_dev = torch.tensor(types, device=DEV)
-    q0_dev = torch.tensor(q0, dtype=torch.float64, device=DEV)
+    charges = TypeScaledCharges(torch.tensor(q0, device=DEV), torch.tensor(types, device=DEV), 8)
     for rep in range(2):  # second call replays the captured graph
         for p in (s_p, e_p, k_p):
             p.grad = None
-        loss = m((q0_dev * k_p[t_dev]).float(), lorentz_berthelot_nbfp(s_p, e_p))
+        loss = m(charges(k_p), lorentz_berthelot_nbfp(s_p, e_p))
         loss.backward()
     l64, gs, ge, gk = _fp64_loss_grads(ens, sig, eps, np.ones(8), q0, f_target.cpu().numpy())
     print("loss", float(loss), l64, "grads", rel_rms(s_p.grad.cpu(), gs), rel_rms(e_p.grad.cpu(), ge),
