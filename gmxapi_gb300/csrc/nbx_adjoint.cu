@@ -52,8 +52,8 @@ struct AdjPtrs
 };
 
 template<bool kEwald, bool kExcl>
-__device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __restrict__ xq,
-                                         const int* __restrict__ tgrid, const float2* __restrict__ nbfp_s,
+__device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __restrict__ jx,
+                                         const float4* __restrict__ jg, const float2* __restrict__ nbfp_s,
                                          float2* ttab, const float4* __restrict__ xis, const float4* __restrict__ gis,
                                          const float4* __restrict__ gnb, float4* dnb, const int cj_lane,
                                          unsigned im, unsigned wexcl, int h, int sci, bool central, int ii, int jj,
@@ -72,9 +72,11 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __re
             continue;
         }
         const int      aj = cj * kCl + h * (kCl / kSplit) + jj;
-        const float4   xj = xq[aj];
-        const float4   gj = gnb[aj];
-        const int      tj = tgrid[aj];
+        // the cj4 group's 32 j-atoms are staged in shared memory (slot jm * 8 + atom)
+        const int      sj = jm * kCl + h * (kCl / kSplit) + jj;
+        const float4   xj = jx[sj];
+        const float4   gj = jg[sj];
+        const int      tj = __float_as_int(gj.w);
         const unsigned wj = wexcl >> (jm * kNcl);
         float          djx = 0.0f, djy = 0.0f, djz = 0.0f, djq = 0.0f;
 #pragma unroll
@@ -200,8 +202,8 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __re
 template<bool kEwald>
 __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p, const Sci& s,
                                           const float2* __restrict__ nbfp_s, float2* ttab, float4* xis, float4* gis,
-                                          int lane, const AdjConsts& k, float pbeta, float beta2l2, float c2b,
-                                          float b2c2b, double* gnbfp)
+                                          float4* jx, float4* jg, int lane, const AdjConsts& k, float pbeta,
+                                          float beta2l2, float c2b, float b2c2b, double* gnbfp)
 {
     const unsigned full    = 0xffffffffu;
     const int      ii      = lane & 7;
@@ -225,13 +227,44 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
     {
         dxa[c] = dya[c] = dza[c] = dqa[c] = 0.0f;
     }
+    // software pipeline over the cj4 groups, as in the force kernel: the next group's
+    // record is loaded when a group starts, its 32 j-atoms after the group's first half
+    int4   rec_ime{};
+    int    rec_cj = 0;
+    float4 xr{}, gr{};
+    if (s.cj4_start < s.cj4_end)
+    {
+        rec_ime     = *reinterpret_cast<const int4*>(&p.cj4[s.cj4_start].imei[0]);
+        rec_cj      = (lane < kJg) ? p.cj4[s.cj4_start].cj[lane] : 0;
+        const int a = __shfl_sync(full, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
+        xr          = p.xq[a];
+        gr          = p.gnb[a];
+        gr.w        = __int_as_float(p.tgrid[a]);
+    }
     for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
     {
-        const int4 ime     = *reinterpret_cast<const int4*>(&p.cj4[j4].imei[0]);
-        const int  cj_lane = (lane < kJg) ? p.cj4[j4].cj[lane] : 0;
+        const int4 ime     = rec_ime;
+        const int  cj_lane = rec_cj;
+        __syncwarp();
+        jx[lane] = xr;
+        jg[lane] = gr;
+        __syncwarp();
+        const bool more = j4 + 1 < s.cj4_end;
+        if (more)
+        {
+            rec_ime = *reinterpret_cast<const int4*>(&p.cj4[j4 + 1].imei[0]);
+            rec_cj  = (lane < kJg) ? p.cj4[j4 + 1].cj[lane] : 0;
+        }
 #pragma unroll 1
         for (int h = 0; h < kSplit; h++)
         {
+            if (h == 1 && more)
+            {
+                const int a = __shfl_sync(full, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
+                xr          = p.xq[a];
+                gr          = p.gnb[a];
+                gr.w        = __int_as_float(p.tgrid[a]);
+            }
             const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
             const int      exi = (h == 0) ? ime.y : ime.w;
             if (!im)
@@ -240,14 +273,14 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
             }
             if (exi == 0)
             {
-                adj_half<kEwald, false>(v, p.xq, p.tgrid, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h,
-                                        s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                adj_half<kEwald, false>(v, jx, jg, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h, s.sci,
+                                        central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
             }
             else
             {
                 const unsigned wexcl = p.excl[exi].pair[lane];
-                adj_half<kEwald, true>(v, p.xq, p.tgrid, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl,
-                                       h, s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                adj_half<kEwald, true>(v, jx, jg, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl, h,
+                                       s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
             }
         }
     }
@@ -317,6 +350,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
     __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
+    __shared__ float4 jx_s[kAdjWarps][32];
+    __shared__ float4 jg_s[kAdjWarps][32];
     adj_setup(v, nbfp_s, ttab_s);
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
@@ -339,7 +374,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         {
             break;
         }
-        adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], lane, k, v.pbeta,
+        adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], jx_s[warp], jg_s[warp],
+                          lane, k, v.pbeta,
                           v.beta2l2, v.c2b, b2c2b, gnbfp);
     }
 }
@@ -373,6 +409,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
     __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
+    __shared__ float4 jx_s[kAdjWarps][32];
+    __shared__ float4 jg_s[kAdjWarps][32];
     adj_setup(cv, nbfp_s, ttab_s);
     const int   warp  = threadIdx.x >> 5;
     const int   lane  = threadIdx.x & 31;
@@ -399,7 +437,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
             k.gE_c  = (float)gE[2 * sidx + 1];
         }
         const AdjPtrs p = { b.xq, b.tgrid, b.cj4, b.excl, b.shiftvec, b.gnb, b.dnb };
-        adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], lane, k,
+        adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp],
+                          jx_s[warp], jg_s[warp], lane, k,
                           cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gnbfp);
     }
 }
