@@ -241,12 +241,10 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
     import torch
 
     from gmxapi_gb300 import nblib, systems
-    from gmxapi_gb300.adjoint import DifferentiableNonbonded, lorentz_berthelot_nbfp
+    from gmxapi_gb300.adjoint import DifferentiableNonbonded, lorentz_berthelot_nbfp, static_list_options
 
     s = systems.lj_liquid(n=24000, ntypes=8, seed=4)
-    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=RLIST, rcoulomb=RC,
-                                 nstlist_prune=0)
-    eng = DifferentiableNonbonded(s, opts, device=dev)
+    eng = DifferentiableNonbonded(s, static_list_options(RC), device=dev)  # fixed coordinates: list at rc
     d = torch.device("cuda", dev)
     stream = torch.cuda.current_stream(dev)
     rng = np.random.default_rng(12)
@@ -325,7 +323,7 @@ def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
     import torch
 
     from gmxapi_gb300 import nblib, systems
-    from gmxapi_gb300.adjoint import BatchForceMatcher, TypeScaledCharges, lorentz_berthelot_nbfp
+    from gmxapi_gb300.adjoint import BatchForceMatcher, TypeScaledCharges, lorentz_berthelot_nbfp, static_list_options
     from gmxapi_gb300.batch import BatchForceCalculator
 
     procs = max(1, min(16, (len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else 4)))
@@ -341,8 +339,8 @@ def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
     types = torch.cat([torch.as_tensor(s.type, dtype=torch.long) for s in ens]).to(d)
     n = int(q0.numel())
     rng = np.random.default_rng(21)
-    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=RLIST, rcoulomb=RC,
-                                 nstlist_prune=0, compute_virial_and_energy=True)
+    opts = static_list_options(RC)  # fixed frames: the list holds exactly the pairs within rc
+    opts.compute_virial_and_energy = True
     # targets at perturbed parameters
     ref = BatchForceCalculator(ens, opts, device=dev)
     ref.set_stream(stream.cuda_stream)

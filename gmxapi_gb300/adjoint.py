@@ -39,6 +39,15 @@ def lorentz_berthelot_nbfp(sigma: torch.Tensor, epsilon: torch.Tensor) -> torch.
     return torch.stack((6.0 * c6, 12.0 * c12), dim=-1)
 
 
+def static_list_options(rc: float = 0.9) -> NBKernelOptions:
+    """Options for coordinates that do not move between searches (force matching on fixed
+    frames, or a search on every call): the list radius equals the cut-off and the fresh
+    list is pruned to cluster pairs with an atom pair inside rc, so no buffer pairs are
+    computed."""
+    return NBKernelOptions(coulomb_type=CoulombType.Pme, pairlist_cutoff=rc, rcoulomb=rc, rlist_inner=rc,
+                           nstlist_prune=2)
+
+
 class _NonbondedFunction(torch.autograd.Function):
     """(x, q, nbfp) -> (forces (N, 3) float32, energies [E_lj, E_coul] float64)."""
 
@@ -88,12 +97,13 @@ class DifferentiableNonbonded:
     symmetrised before use so its gradient does not depend on which atom of a
     pair the list puts in the i-cluster.  The pair list is rebuilt from ``x``
     on every call unless ``search=False`` (then the list of the last search
-    is used, as within an nstlist interval).
+    is used); the default options list exactly the pairs within the cut-off
+    (``static_list_options``), so with moving coordinates and ``search=False``
+    pass options with a buffer (rlist > rc).
     """
 
     def __init__(self, system, options: NBKernelOptions | None = None, device: int = 0):
-        opts = options or NBKernelOptions(coulomb_type=CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
-                                          nstlist_prune=0)
+        opts = options or static_list_options()
         opts.compute_virial_and_energy = True
         self.system = system
         self.ntypes = int(system.ntypes)
@@ -185,8 +195,7 @@ class BatchForceMatcher:
     def __init__(self, systems, f_target: torch.Tensor, options: NBKernelOptions | None = None, device: int = 0):
         from .batch import BatchForceCalculator
 
-        opts = options or NBKernelOptions(coulomb_type=CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
-                                          nstlist_prune=0)
+        opts = options or static_list_options()
         opts.compute_virial_and_energy = True
         self.dev = torch.device("cuda", device)
         self.batch = BatchForceCalculator(systems, opts, device)
