@@ -189,9 +189,7 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __re
         }
         if (ii == 0)
         {
-            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(&dnb[aj]), "f"(djx), "f"(djy),
-                         "f"(djz), "f"(djq)
-                         : "memory");
+            red_add_v4(&dnb[aj], djx, djy, djz, djq);
         }
     }
 }
@@ -298,9 +296,7 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
         if (jj == 0)
         {
             float4* dst = &p.dnb[(s.sci * kNcl + c) * kCl + ii];
-            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(ax), "f"(ay), "f"(az),
-                         "f"(aq)
-                         : "memory");
+            red_add_v4(dst, ax, ay, az, aq);
         }
     }
     // flush the type-pair gradients of this entry into the FP64 sums

@@ -39,10 +39,11 @@ __device__ __forceinline__ float fast_ex2(float x)
     return r;
 }
 
-__device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float z)
+// Vector reduction into a buffer this kernel never reads back, so no memory clobber:
+// loads may be scheduled across it.
+__device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float z, float w = 0.0f)
 {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(0.0f)
-                 : "memory");
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(w));
 }
 
 // Compensated (Kahan) accumulation: sum + c carries ~2x float precision.
