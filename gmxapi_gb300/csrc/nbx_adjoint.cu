@@ -123,12 +123,7 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __re
             {
                 const float r    = r2 * rinv;
                 const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
-                float       poly = v.erfc_c[kErfcTerms - 1];
-#pragma unroll
-                for (int m = kErfcTerms - 2; m >= 0; m--)
-                {
-                    poly = fmaf(poly, t, v.erfc_c[m]);
-                }
+                const float poly = erfc_poly(t);
                 const float expm = fast_ex2(-beta2l2 * r2);
                 const float tp   = t * poly;
                 psi              = expm * fmaf(tp, rinv, c2b) * rinv2;

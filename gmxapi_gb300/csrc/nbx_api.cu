@@ -110,69 +110,6 @@ float calc_ewaldcoeff_q(float rc, float rtol)
     return beta;
 }
 
-// erfc(x) = t * P(t) * exp(-x^2) with t = 1/(1 + p x): P interpolated at the
-// Chebyshev nodes of t in [1/(1 + p xmax), 1] (x in [0, xmax]), returned as
-// monomial coefficients in t.  The substitution t makes erfc(x) exp(x^2),
-// which decays like 1/x, smooth enough for a degree-7 fit with ~1e-7
-// relative error.
-void fit_erfc(double xmax, float* p_out, float* coef)
-{
-    const double p    = 0.47;
-    const int    N    = kErfcTerms;
-    const double tmin = 1.0 / (1.0 + p * xmax);
-    const double mid = 0.5 * (1.0 + tmin), half = 0.5 * (1.0 - tmin);
-    double       cheb[kErfcTerms] = { 0 };
-    for (int k = 0; k < N; k++)
-    {
-        const double th = 3.14159265358979323846 * (k + 0.5) / N;
-        const double u  = std::cos(th);
-        const double t  = mid + half * u;
-        const double x  = (1.0 / t - 1.0) / p;
-        const double g  = std::erfc(x) * std::exp(x * x) / t;
-        for (int j = 0; j < N; j++)
-        {
-            cheb[j] += 2.0 / N * g * std::cos(j * th);
-        }
-    }
-    cheb[0] *= 0.5;
-    // Chebyshev -> monomials in u
-    double Tm[kErfcTerms][kErfcTerms] = { { 0 } };  // Tm[j][k]: coefficient of u^k in T_j
-    Tm[0][0] = 1.0;
-    Tm[1][1] = 1.0;
-    for (int j = 2; j < N; j++)
-    {
-        for (int k = 0; k < N; k++)
-        {
-            Tm[j][k] = (k > 0 ? 2.0 * Tm[j - 1][k - 1] : 0.0) - Tm[j - 2][k];
-        }
-    }
-    double mu[kErfcTerms] = { 0 };
-    for (int j = 0; j < N; j++)
-    {
-        for (int k = 0; k < N; k++)
-        {
-            mu[k] += cheb[j] * Tm[j][k];
-        }
-    }
-    // u = a t + b  ->  monomials in t
-    const double a = 1.0 / half, b = -mid / half;
-    double       mt[kErfcTerms] = { 0 };
-    for (int k = 0; k < N; k++)
-    {
-        // (a t + b)^k = sum_m C(k,m) a^m t^m b^(k-m)
-        double binom = 1.0;
-        for (int m = 0; m <= k; m++)
-        {
-            mt[m] += mu[k] * binom * std::pow(a, m) * std::pow(b, k - m);
-            binom = binom * (k - m) / (m + 1);
-        }
-    }
-    *p_out = (float)p;
-    for (int k = 0; k < N; k++)
-    {
-        coef[k] = (float)mt[k];
-    }
-}
 
 } // namespace nbx
 
@@ -552,6 +489,14 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     {
         return set_error(nullptr, NBX_ERR_INVALID_INPUT, "at most 47 particle types");
     }
+    if (opts.coulomb == NBX_COULOMB_EWALD
+        && (double)calc_ewaldcoeff_q(opts.rcoulomb, opts.ewald_rtol > 0.0f ? opts.ewald_rtol : 1e-5f)
+                           * (double)opts.rcoulomb
+                   > (double)kErfcXMax)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT,
+                         "ewald_rtol below erfc(4) = 1.5e-8 is not supported (beta * rc must be <= 4)");
+    }
     for (int i = 0; i < 3 * n; i++)
     {
         if (!std::isfinite(sys->x[i]))
@@ -641,7 +586,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
         v.sh_ewald       = opts.use_ewald_shift ? erfcf(v.beta * rc) / rc : 0.0f;
         // Ewald self energy, kernel_gpu_ref.cpp:154-178
         v.self_energy = -v.epsfac_d * (double)v.beta * 0.56418958354775628695 * qsq;
-        fit_erfc((double)v.beta * (double)rc, &v.erfc_p, v.erfc_c);
+        v.erfc_p = kErfcP;
     }
     else
     {

@@ -605,7 +605,11 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     {
         v.beta     = calc_ewaldcoeff_q(rc, a->ewald_rtol > 0.0f ? a->ewald_rtol : 1e-5f);
         v.sh_ewald = a->use_ewald_shift ? erfcf(v.beta * rc) / rc : 0.0f;
-        fit_erfc((double)v.beta * (double)rc, &v.erfc_p, v.erfc_c);
+        if ((double)v.beta * (double)rc > (double)kErfcXMax)
+        {
+            return NBX_ERR_INVALID_INPUT;
+        }
+        v.erfc_p = kErfcP;
     }
     set_pair_constants(v);
     v.self_energy    = 0.0;

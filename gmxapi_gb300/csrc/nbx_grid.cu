@@ -278,7 +278,7 @@ __device__ __forceinline__ int group_rank(float c, int a, int cnt, int gsize, bo
     return rank;
 }
 
-constexpr int kSortThreads   = 256;
+constexpr int kSortThreads   = 1024;
 constexpr int kSmemSortItems = 4096;
 
 // One block per grid column: z sort, per-slab y and x sorts, fill (fillCell).

@@ -22,6 +22,25 @@ constexpr float kFarAway = -1000000.0f;         // atomdata.cpp:146
 constexpr float kMinDist2 = 3.82e-07f;          // pairlist.h:146
 constexpr int kErfcTerms = 8;                    // degree-7 polynomial in t
 
+// erfc(x) = t P(t) exp(-x^2) with t = 1 / (1 + kErfcP x): P interpolates erfc(x) exp(x^2) / t at
+// the 8 Chebyshev nodes of t in [1 / (1 + kErfcP kErfcXMax), 1] (x in [0, kErfcXMax]), written as
+// monomial coefficients in t (float32 of the double-precision fit; relative error of the
+// expansion <= 1.6e-7 on [0, 4]).  The substitution makes erfc(x) exp(x^2), which decays like
+// 1/x, smooth enough for degree 7.  tests/test_oracle.py recomputes the fit and checks these.
+constexpr float kErfcP    = 0.47f;
+constexpr float kErfcXMax = 4.0f;  // beta * rc <= 4, i.e. ewald_rtol >= erfc(4) = 1.5e-8
+__device__ __forceinline__ float erfc_poly(float t)
+{
+    float p = 1.128007565e-02f;
+    p       = fmaf(p, t, 3.713922575e-02f);
+    p       = fmaf(p, t, -3.248904943e-01f);
+    p       = fmaf(p, t, 5.147097111e-01f);
+    p       = fmaf(p, t, -7.699845731e-02f);
+    p       = fmaf(p, t, 3.232774734e-01f);
+    p       = fmaf(p, t, 2.490737736e-01f);
+    return fmaf(p, t, 2.664087117e-01f);
+}
+
 // Device status word bits (nbx_status values are derived from these on the host).
 enum StatusBits : unsigned
 {
@@ -136,9 +155,8 @@ struct DeviceView
     double self_energy;     // Ewald / RF self term, constant for the system
     int    self_on_device;  // 1: k_excl_energy adds the self term from the charges instead
     double epsfac_d;        // 1/(4 pi eps0) in double for the energy sums
-    // erfc(x) = t * P(t) * exp(-x^2), t = 1/(1 + erfc_p x), fitted on [0, beta*rc] at set-up
+    // erfc(x) = t * P(t) * exp(-x^2), t = 1/(1 + kErfcP x) (erfc_poly), valid for beta*rc <= kErfcXMax
     float erfc_p;
-    float erfc_c[kErfcTerms];
     // derived per-pair constants (set_pair_constants), read straight from the
     // kernel parameters inside the pair loop
     float pbeta;    // erfc_p * beta
@@ -187,7 +205,6 @@ struct BatchSys
 // ---- host set-up helpers (nbx_api.cu) ----
 double one_4pi_eps0();
 float  calc_ewaldcoeff_q(float rc, float rtol);
-void   fit_erfc(double xmax, float* p_out, float* coef);
 
 // ---- launchers (one translation unit each) ----
 cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s);

@@ -157,12 +157,7 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
                 // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
                 const float r    = r2 * rinv;
                 const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
-                float       poly = v.erfc_c[kErfcTerms - 1];
-#pragma unroll
-                for (int k = kErfcTerms - 2; k >= 0; k--)
-                {
-                    poly = fmaf(poly, t, v.erfc_c[k]);
-                }
+                const float poly = erfc_poly(t);
                 const float expm = fast_ex2(-beta2l2 * r2);
                 const float tpr  = t * poly * rinv;  // erfc(beta r) / r = tpr * expm
                 // -(d/dr)(erfc(beta r)/r) r = expm (erfc/r-part + 2 beta/sqrt(pi)); exclusions drop 1/r

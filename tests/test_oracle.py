@@ -141,3 +141,42 @@ def test_balancing_splits_and_sorts_without_changing_pairs():
     o2.search()
     assert o2.balance(1) == 0
     assert len(o2.pairlist()["sci"]) == len(p0["sci"])
+
+
+def test_erfc_expansion_coefficients_match_their_fit():
+    """The force kernels' erfc(x) = t P(t) exp(-x^2) coefficients (nbx_internal.cuh erfc_poly)
+    recomputed: Chebyshev interpolation of erfc(x) exp(x^2) / t at 8 nodes of t in
+    [1 / (1 + 0.47 * 4), 1], converted to monomials in t; and the expansion's accuracy."""
+    import math
+    import os
+    import re
+
+    from scipy.special import erfc
+
+    n, p, xmax = 8, 0.47, 4.0
+    tmin = 1 / (1 + p * xmax)
+    mid, half = 0.5 * (1 + tmin), 0.5 * (1 - tmin)
+    cheb = np.zeros(n)
+    for k in range(n):
+        th = math.pi * (k + 0.5) / n
+        t = mid + half * math.cos(th)
+        x = (1 / t - 1) / p
+        g = math.erfc(x) * math.exp(x * x) / t
+        cheb += 2.0 / n * g * np.cos(np.arange(n) * th)
+    cheb[0] *= 0.5
+    mono_u = np.polynomial.chebyshev.cheb2poly(cheb)
+    mono_t = np.zeros(n)
+    for k in range(n):
+        term = np.polynomial.polynomial.polypow([-mid / half, 1 / half], k)
+        mono_t[: len(term)] += mono_u[k] * term
+    src = open(os.path.join(os.path.dirname(__file__), "..", "gmxapi_gb300", "csrc", "nbx_internal.cuh")).read()
+    body = src[src.index("float erfc_poly(float t)"):]
+    body = body[: body.index("}")]
+    lits = [float(v) for v in re.findall(r"([-+]?\d\.\d+e[-+]\d+)f", body)]
+    coef = np.array(lits[::-1])  # Horner order: highest first
+    assert len(coef) == n
+    np.testing.assert_allclose(coef, mono_t.astype(np.float32), rtol=1e-6, atol=1e-8)
+    x = np.linspace(0.0, xmax, 100001)
+    t = 1 / (1 + np.float32(p) * x)
+    approx = t * np.polyval(coef[::-1], t) * np.exp(-x * x)
+    assert (np.abs(approx - erfc(x)) / erfc(x)).max() < 2e-7
