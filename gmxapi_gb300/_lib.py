@@ -74,6 +74,8 @@ class nbx_options(C.Structure):
         ("nstlist", C.c_int),
         ("nstlist_prune", C.c_int),
         ("compute_energy", C.c_int),
+        ("vdw_modifier", C.c_int),
+        ("rvdw_switch", C.c_float),
     ]
 
 

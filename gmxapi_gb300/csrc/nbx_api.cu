@@ -445,6 +445,8 @@ void nbx_default_options(nbx_options* o)
     o->nstlist         = 10;
     o->nstlist_prune   = 0;
     o->compute_energy  = 0;
+    o->vdw_modifier    = NBX_VDW_POTSHIFT;
+    o->rvdw_switch     = 0.0f;
 }
 
 const char* nbx_last_error(const nbx_handle* h)
@@ -484,6 +486,15 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (opts.coulomb < 0 || opts.coulomb > 2)
     {
         return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown Coulomb type");
+    }
+    if (opts.vdw_modifier < 0 || opts.vdw_modifier > 3)
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown LJ modifier");
+    }
+    if ((opts.vdw_modifier == NBX_VDW_FORCESWITCH || opts.vdw_modifier == NBX_VDW_POTSWITCH)
+        && !(opts.rvdw_switch >= 0.0f && opts.rvdw_switch < opts.rcoulomb))
+    {
+        return set_error(nullptr, NBX_ERR_INVALID_INPUT, "the switch modifiers need 0 <= rvdw_switch < rc");
     }
     if (sys->num_types + 1 > 48)
     {
@@ -564,13 +575,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     v.rlist_inner2 = rin * rin;
     v.epsfac       = (float)one_4pi_eps0();
     v.epsfac_d     = one_4pi_eps0();
-    {
-        const float p3 = rc * rc * rc;
-        const float p6 = p3 * p3;
-        const float p12 = p6 * p6;
-        v.cpot6  = (float)(-1.0 / p6);
-        v.cpot12 = (float)(-1.0 / p12);
-    }
+    set_lj_modifier(v, opts.vdw_modifier, rc, opts.rvdw_switch);
     const float eps_rf = (opts.coulomb == NBX_COULOMB_CUTOFF) ? 1.0f : opts.epsilon_rf;
     v.k_rf = (eps_rf == 0) ? 1 / (2 * rc * rc * rc) : (eps_rf - 1.0f) / (2 * eps_rf + 1.0f) / (rc * rc * rc);
     v.c_rf = 1 / rc + v.k_rf * rc * rc;
@@ -987,6 +992,10 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
     if (h->v.ntypes1 > adjoint_max_types1())
     {
         return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint supports at most 15 particle types");
+    }
+    if (h->v.vdw_mod == NBX_VDW_FORCESWITCH || h->v.vdw_mod == NBX_VDW_POTSWITCH)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint takes the potential-shift or plain LJ cut-off");
     }
     cudaSetDevice(h->device);
     DeviceView& v = h->v;
@@ -1651,6 +1660,10 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
         return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "need at least one system");
     }
     *out = nullptr;
+    if (opts && (opts->vdw_modifier == NBX_VDW_FORCESWITCH || opts->vdw_modifier == NBX_VDW_POTSWITCH))
+    {
+        return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "batches take the potential-shift or plain LJ cut-off");
+    }
     for (int i = 1; i < num_systems; i++)
     {
         const nbx_system_desc& a = systems[0];

@@ -45,7 +45,7 @@ constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
 constexpr int kStageBytes     = 32 * (16 + 4);  // per warp: 32 staged j-atoms (xq, type)
 
-template<bool kEnergy, bool kEwald>
+template<bool kEnergy, bool kEwald, int kLj = 0>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
 {
     // {6*C6, 12*C12, LJ energy shift of the pair, 0} per type pair
@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         }
         const Sci     s = v.sci[e];
         const SysPtrs p = { v.xq, v.tgrid, v.fnb, v.cj4, v.excl, v.shiftvec, v.fshift };
-        process_entry<kEnergy, kEwald>(v, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2,
-                                       e_lj_acc, e_el_acc);
+        process_entry<kEnergy, kEwald, kLj>(v, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b,
+                                            k_rf2, e_lj_acc, e_el_acc);
     }
     if (kEnergy)
     {
@@ -390,7 +390,27 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     {
         cudaEventRecord(ev0, s);
     }
-    if (energy)
+    // the switch modifiers have their own instantiations; shift and plain cut-off share one
+    const int lj = (v.vdw_mod == NBX_VDW_FORCESWITCH) ? 1 : (v.vdw_mod == NBX_VDW_POTSWITCH) ? 2 : 0;
+    if (lj == 1)
+    {
+        if (energy)
+            ewald ? k_force<true, true, 1><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<true, false, 1><<<blocks, kForceThreads, smem, s>>>(v, counter);
+        else
+            ewald ? k_force<false, true, 1><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<false, false, 1><<<blocks, kForceThreads, smem, s>>>(v, counter);
+    }
+    else if (lj == 2)
+    {
+        if (energy)
+            ewald ? k_force<true, true, 2><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<true, false, 2><<<blocks, kForceThreads, smem, s>>>(v, counter);
+        else
+            ewald ? k_force<false, true, 2><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<false, false, 2><<<blocks, kForceThreads, smem, s>>>(v, counter);
+    }
+    else if (energy)
     {
         if (ewald)
         {
@@ -593,11 +613,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     v.rlist2       = a->rlist * a->rlist;
     v.epsfac       = (float)one_4pi_eps0();
     v.epsfac_d     = one_4pi_eps0();
-    {
-        const float p3 = rc * rc * rc, p6 = p3 * p3, p12 = p6 * p6;
-        v.cpot6        = (float)(-1.0 / p6);
-        v.cpot12       = (float)(-1.0 / p12);
-    }
+    set_lj_modifier(v, NBX_VDW_POTSHIFT, rc, 0.0f);
     const float eps_rf = (a->coulomb == NBX_COULOMB_CUTOFF) ? 1.0f : a->epsilon_rf;
     v.k_rf = (eps_rf == 0) ? 1 / (2 * rc * rc * rc) : (eps_rf - 1.0f) / (2 * eps_rf + 1.0f) / (rc * rc * rc);
     v.c_rf = 1 / rc + v.k_rf * rc * rc;

@@ -1,6 +1,8 @@
 // Internal declarations shared by the nbnxm_gb300 translation units.
 #pragma once
 
+#include <cmath>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -150,6 +152,13 @@ struct DeviceView
     // interaction constants
     float rc2, rlist, rlist2, rbb2, rlist_inner2;
     float beta, epsfac, k_rf, c_rf, sh_ewald, cpot6, cpot12;
+    // LJ modifier (nbx_vdw_modifier) and its constants (mdlib/forcerec.cpp:787-816):
+    // force switch F/p = r^-(p+1) + c2 r^2 + c3 r^3 for p = 6 (disp) and 12 (rep);
+    // potential switch sw = 1 + c3 rsw^3 + c4 rsw^4 + c5 rsw^5
+    int   vdw_mod;
+    float rvdw_switch;
+    float fsw_disp_c2, fsw_disp_c3, fsw_rep_c2, fsw_rep_c3;
+    float psw_c3, psw_c4, psw_c5;
     int   coulomb;
     float shiftvec[kNShift * 3];
     double self_energy;     // Ewald / RF self term, constant for the system
@@ -166,6 +175,45 @@ struct DeviceView
 };
 
 // One system of a batch, as the batched kernels see it (device table).
+// LJ modifier constants for cut-off rc (interaction_const setup, forcerec.cpp:787-872).
+inline void set_lj_modifier(DeviceView& v, int mod, float rc, float rsw)
+{
+    v.vdw_mod     = mod;
+    v.rvdw_switch = rsw;
+    v.fsw_disp_c2 = v.fsw_disp_c3 = v.fsw_rep_c2 = v.fsw_rep_c3 = 0.0f;
+    v.psw_c3 = v.psw_c4 = v.psw_c5 = 0.0f;
+    const double r = rc, s = rsw;
+    if (mod == 0)
+    {
+        v.cpot6  = (float)(-1.0 / std::pow(r, 6.0));
+        v.cpot12 = (float)(-1.0 / std::pow(r, 12.0));
+    }
+    else if (mod == 1)
+    {
+        auto fsw = [&](double p, float* c2, float* c3, float* cpot) {
+            const double d  = r - s;
+            const double k2 = ((p + 1) * s - (p + 4) * r) / (std::pow(r, p + 2) * d * d);
+            const double k3 = -((p + 1) * s - (p + 3) * r) / (std::pow(r, p + 2) * d * d * d);
+            *c2             = (float)k2;
+            *c3             = (float)k3;
+            *cpot           = (float)(-std::pow(r, -p) + p * k2 / 3 * d * d * d + p * k3 / 4 * d * d * d * d);
+        };
+        fsw(6.0, &v.fsw_disp_c2, &v.fsw_disp_c3, &v.cpot6);
+        fsw(12.0, &v.fsw_rep_c2, &v.fsw_rep_c3, &v.cpot12);
+    }
+    else
+    {
+        v.cpot6 = v.cpot12 = 0.0f;
+        if (mod == 2)
+        {
+            const double d = r - s;
+            v.psw_c3       = (float)(-10.0 / (d * d * d));
+            v.psw_c4       = (float)(15.0 / (d * d * d * d));
+            v.psw_c5       = (float)(-6.0 / (d * d * d * d * d));
+        }
+    }
+}
+
 // Fills the derived pair constants of a view whose beta / erfc fit / k_rf are set.
 inline void set_pair_constants(DeviceView& v)
 {

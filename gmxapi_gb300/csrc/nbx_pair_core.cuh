@@ -70,7 +70,7 @@ struct EntryState
 // over the 4 j-clusters stays rolled and only the loop over the 8 i-clusters
 // (register-resident i-data) is unrolled, which keeps the kernel inside the
 // instruction cache.
-template<bool kEnergy, bool kEwald, bool kExcl>
+template<bool kEnergy, bool kEwald, bool kExcl, int kLj = 0>
 __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs& p, const float4* __restrict__ nbfp_s,
                                              const float4* __restrict__ jx, const int* __restrict__ jt,
                                              EntryState& st, const int cj_lane, unsigned im, unsigned wexcl,
@@ -148,7 +148,39 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             // everything below is F r^2 until the one multiply by rinv2
             const float c12r6 = lj.y * rinv6;
             const float vdisp = lj.x * rinv6;
-            const float flj   = fmaf(c12r6, rinv6, -vdisp);  // vrep - vdisp, vrep = 12 C12 / r^12
+            float       flj   = fmaf(c12r6, rinv6, -vdisp);  // vrep - vdisp, vrep = 12 C12 / r^12
+            // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair) = (flj - vdisp)/12 + shift
+            float vlj = (kEnergy || kLj == 2) ? fmaf(flj - vdisp, 1.0f / 12.0f, lj.z) : 0.0f;
+            if (kLj != 0)
+            {
+                // force / potential switch from rvdw_switch to rc (kernel_ref_inner.h:168-200)
+                const float r   = r2 * rinv;
+                const float rsw = fmaxf(r - v.rvdw_switch, 0.0f);
+                const float rs2 = rsw * rsw;
+                if (kLj == 1)
+                {
+                    // F r += (-6C6 (c2 + c3 rsw) + 12C12 (c2' + c3' rsw)) rsw^2 r; the energy gains
+                    // the integral terms (-c2/3 - c3/4 rsw) rsw^3 of each
+                    flj = fmaf((lj.y * fmaf(v.fsw_rep_c3, rsw, v.fsw_rep_c2)
+                                - lj.x * fmaf(v.fsw_disp_c3, rsw, v.fsw_disp_c2))
+                                       * rs2,
+                               r, flj);
+                    if (kEnergy)
+                    {
+                        const float erep  = fmaf(v.fsw_rep_c3 * -0.25f, rsw, v.fsw_rep_c2 * (-1.0f / 3.0f));
+                        const float edisp = fmaf(v.fsw_disp_c3 * -0.25f, rsw, v.fsw_disp_c2 * (-1.0f / 3.0f));
+                        vlj = fmaf(lj.y * erep - lj.x * edisp, rs2 * rsw, vlj);
+                    }
+                }
+                else
+                {
+                    // sw = 1 + c3 rsw^3 + c4 rsw^4 + c5 rsw^5; F r = F r sw - r V dsw, V *= sw
+                    const float sw  = fmaf(fmaf(fmaf(v.psw_c5, rsw, v.psw_c4), rsw, v.psw_c3), rs2 * rsw, 1.0f);
+                    const float dsw = fmaf(fmaf(5.0f * v.psw_c5, rsw, 4.0f * v.psw_c4), rsw, 3.0f * v.psw_c3) * rs2;
+                    flj             = fmaf(flj, sw, -r * vlj * dsw);
+                    vlj *= sw;
+                }
+            }
             const float qq    = st.qi[c] * qje;
             float       fcr2;                                 // Coulomb F r^2 / (q_i q_j)
             float       h_el = 0.0f;  // q_i q_j h_el is the pair's Coulomb energy / epsfac
@@ -186,9 +218,7 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
                 const bool counted = kExcl ? (in_range && int_bit != 0.0f) : in_range;
                 // q_i h_ij here; q_j multiplies the j-cluster's sum
                 ej_el = fmaf(st.qi[c], counted ? h_el : 0.0f, ej_el);
-                // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair) = (flj - vdisp)/12 + shift
-                const float e_lj = fmaf(flj - vdisp, 1.0f / 12.0f, lj.z);
-                ej_lj += counted ? e_lj : 0.0f;
+                ej_lj += counted ? vlj : 0.0f;
             }
             st.fix[c] = fmaf(fscal, dx, st.fix[c]);
             st.fiy[c] = fmaf(fscal, dy, st.fiy[c]);
@@ -220,7 +250,8 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
 // One list entry: load the 64 shifted i-atoms, all its cj4 groups, then the
 // i-force, shift-force and energy reductions.  The entry's energies are added
 // to e_lj_acc / e_el_acc (per lane, FP64).
-template<bool kEnergy, bool kEwald>
+// kLj: 0 potential shift or plain cut-off, 1 force switch, 2 potential switch.
+template<bool kEnergy, bool kEwald, int kLj = 0>
 __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs& p, const Sci& s,
                                               const float4* __restrict__ nbfp_s, float4* jx, int* jt, int nt1,
                                               int lane, int ii, int jj, float rc2, float pbeta, float beta2l2,
@@ -292,13 +323,13 @@ __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs
             }
             if (exi == 0)
             {
-                process_half<kEnergy, kEwald, false>(v, p, nbfp_s, jx, jt, st, cj_lane, im, 0u, h, s.sci, central,
+                process_half<kEnergy, kEwald, false, kLj>(v, p, nbfp_s, jx, jt, st, cj_lane, im, 0u, h, s.sci, central,
                                                      ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2);
             }
             else
             {
                 const unsigned wexcl = p.excl[exi].pair[lane];
-                process_half<kEnergy, kEwald, true>(v, p, nbfp_s, jx, jt, st, cj_lane, im, wexcl, h, s.sci,
+                process_half<kEnergy, kEwald, true, kLj>(v, p, nbfp_s, jx, jt, st, cj_lane, im, wexcl, h, s.sci,
                                                     central, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2);
             }
         }

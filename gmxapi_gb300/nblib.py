@@ -27,6 +27,13 @@ class CoulombType(enum.IntEnum):
     ReactionField = 2
 
 
+class VdwModifier(enum.IntEnum):
+    PotShift = 0
+    ForceSwitch = 1
+    PotSwitch = 2
+    NoModifier = 3
+
+
 class InputException(ValueError):
     """Raised for invalid systems or options (nblib::InputException)."""
 
@@ -46,6 +53,10 @@ class NBKernelOptions:
     ewald_rtol: float = 1e-5
     epsilon_rf: float = 1.0
     use_ewald_shift: bool = False
+    #: LJ modifier (mdp vdw-modifier): potential shift (nblib), force switch, potential switch, none
+    vdw_modifier: "VdwModifier" = None
+    #: switching distance for the switch modifiers (nm)
+    rvdw_switch: float = 0.0
 
     def to_c(self) -> _lib.nbx_options:
         o = _lib.nbx_options()
@@ -60,6 +71,8 @@ class NBKernelOptions:
         o.nstlist = int(self.nstlist)
         o.nstlist_prune = int(self.nstlist_prune)
         o.compute_energy = int(bool(self.compute_virial_and_energy))
+        o.vdw_modifier = int(self.vdw_modifier if self.vdw_modifier is not None else VdwModifier.PotShift)
+        o.rvdw_switch = float(self.rvdw_switch)
         return o
 
 

@@ -71,7 +71,19 @@ typedef struct
     int   nstlist;          /* steps between searches for nbx_md_step_device (>= 1) */
     int   nstlist_prune;    /* dynamic pruning interval (0 = off); rolling over nstlist_prune/2 parts */
     int   compute_energy;   /* default energy/virial flag for nbx_compute */
+    int   vdw_modifier;     /* nbx_vdw_modifier (0 = potential shift, nblib's only choice) */
+    float rvdw_switch;      /* switching distance for the switch modifiers (nm), < rcoulomb */
 } nbx_options;
+
+/* LJ interaction modifiers (mdp vdw-modifier; interaction_const_t::vdw_modifier,
+ * mdlib/forcerec.cpp:853-872).  Batches and the adjoint take the potential shift only. */
+typedef enum
+{
+    NBX_VDW_POTSHIFT    = 0, /* potential shifted to zero at rc, force unchanged */
+    NBX_VDW_FORCESWITCH = 1, /* force switched to zero between rvdw_switch and rc */
+    NBX_VDW_POTSWITCH   = 2, /* potential switched to zero between rvdw_switch and rc */
+    NBX_VDW_NONE        = 3  /* plain cut-off */
+} nbx_vdw_modifier;
 
 typedef struct nbx_handle nbx_handle;
 

@@ -85,6 +85,11 @@ struct orc_ctx
     float rc, rlist_outer, rlist_inner;
     float beta, epsfac, k_rf, c_rf, sh_ewald;
     float cpot_disp, cpot_rep;
+    /* LJ modifier (0 potential shift, 1 force switch, 2 potential switch, 3 none) */
+    int   vdw_mod;
+    float rvdw_switch;
+    float fsw_disp_c2, fsw_disp_c3, fsw_rep_c2, fsw_rep_c3;
+    float psw_c3, psw_c4, psw_c5;
     float tab_scale;
     int tab_n;
     float* tabF;
@@ -343,6 +348,55 @@ orc_ctx* orc_create(int n, const float* x, const float* box, const float* q, con
         }
     }
     return c;
+}
+
+/* The LJ modifier constants of init_interaction_const (mdlib/forcerec.cpp:853-872):
+ * force_switch_constants (forcerec.cpp:787-801) for p = 6 and 12 and
+ * potential_switch_constants (forcerec.cpp:803-816), in double, stored as float. */
+void orc_set_vdw_modifier(orc_ctx* c, int mod, float rvdw_switch)
+{
+    const double rc = c->rc, rs = rvdw_switch, d = rc - rs;
+    c->vdw_mod      = mod;
+    c->rvdw_switch  = rvdw_switch;
+    c->fsw_disp_c2 = c->fsw_disp_c3 = c->fsw_rep_c2 = c->fsw_rep_c3 = 0;
+    c->psw_c3 = c->psw_c4 = c->psw_c5 = 0;
+    if (mod == 0)
+    {
+        c->cpot_disp = (float)(-1.0 / pow(rc, 6.0));
+        c->cpot_rep  = (float)(-1.0 / pow(rc, 12.0));
+    }
+    else if (mod == 1)
+    {
+        for (int k = 0; k < 2; k++)
+        {
+            const double p  = k == 0 ? 6.0 : 12.0;
+            const double c2 = ((p + 1) * rs - (p + 4) * rc) / (pow(rc, p + 2) * d * d);
+            const double c3 = -((p + 1) * rs - (p + 3) * rc) / (pow(rc, p + 2) * d * d * d);
+            const double cp = -pow(rc, -p) + p * c2 / 3 * d * d * d + p * c3 / 4 * d * d * d * d;
+            if (k == 0)
+            {
+                c->fsw_disp_c2 = (float)c2;
+                c->fsw_disp_c3 = (float)c3;
+                c->cpot_disp   = (float)cp;
+            }
+            else
+            {
+                c->fsw_rep_c2 = (float)c2;
+                c->fsw_rep_c3 = (float)c3;
+                c->cpot_rep   = (float)cp;
+            }
+        }
+    }
+    else
+    {
+        c->cpot_disp = c->cpot_rep = 0;
+        if (mod == 2)
+        {
+            c->psw_c3 = (float)(-10 / (d * d * d));
+            c->psw_c4 = (float)(15 / (d * d * d * d));
+            c->psw_c5 = (float)(-6 / (d * d * d * d * d));
+        }
+    }
 }
 
 static void free_grid(orc_ctx* c)
@@ -1519,7 +1573,32 @@ static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int compu
                                 const float rinvsix   = int_bit * rinvsq * rinvsq * rinvsq;
                                 const float Vvdw_disp = c6 * rinvsix;
                                 const float Vvdw_rep  = c12 * rinvsix * rinvsix;
-                                fscal += (Vvdw_rep - Vvdw_disp) * rinvsq;
+                                float       frLJ      = Vvdw_rep - Vvdw_disp;
+                                double      rswd      = 0.0;
+                                if (c->vdw_mod == 1 || c->vdw_mod == 2)
+                                {
+                                    /* kernel_ref_inner.h:168-200: switching from rvdw_switch */
+                                    const float r   = rsq * rinv;
+                                    float       rsw = r - c->rvdw_switch;
+                                    rsw             = rsw >= 0 ? rsw : 0;
+                                    rswd            = (double)rsw;
+                                    if (c->vdw_mod == 1)
+                                    {
+                                        frLJ += -c6 * (c->fsw_disp_c2 + c->fsw_disp_c3 * rsw) * rsw * rsw * r
+                                                + c12 * (c->fsw_rep_c2 + c->fsw_rep_c3 * rsw) * rsw * rsw * r;
+                                    }
+                                    else
+                                    {
+                                        const float VLJ = (Vvdw_rep + c12 * c->cpot_rep) / 12
+                                                          - (Vvdw_disp + c6 * c->cpot_disp) / 6;
+                                        const float sw  = 1 + (c->psw_c3 + (c->psw_c4 + c->psw_c5 * rsw) * rsw)
+                                                                     * rsw * rsw * rsw;
+                                        const float dsw = (3 * c->psw_c3 + (4 * c->psw_c4 + 5 * c->psw_c5 * rsw) * rsw)
+                                                          * rsw * rsw;
+                                        frLJ            = frLJ * sw - r * VLJ * dsw;
+                                    }
+                                }
+                                fscal += frLJ * rinvsq;
                                 if (computeEnergy)
                                 {
                                     /* the energy formulas of kernel_gpu_ref.cpp:286-291,327-336,
@@ -1540,8 +1619,21 @@ static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int compu
                                     }
                                     const double ir6 = ib / (r2c * r2c * r2c);
                                     vctot += vc;
-                                    Vvdwtot += ((double)c12 * ir6 * ir6 + ib * (double)c12 * (double)c->cpot_rep) / 12
-                                               - ((double)c6 * ir6 + ib * (double)c6 * (double)c->cpot_disp) / 6;
+                                    double vlj = ((double)c12 * ir6 * ir6 + ib * (double)c12 * (double)c->cpot_rep) / 12
+                                                 - ((double)c6 * ir6 + ib * (double)c6 * (double)c->cpot_disp) / 6;
+                                    if (c->vdw_mod == 1)
+                                    {
+                                        /* the switch terms' energy, masked like VLJ (kernel_ref_inner.h:179-192) */
+                                        const double s3 = rswd * rswd * rswd;
+                                        vlj += ib * (-(double)c6 * (-(double)c->fsw_disp_c2 / 3 - (double)c->fsw_disp_c3 / 4 * rswd) * s3
+                                                     + (double)c12 * (-(double)c->fsw_rep_c2 / 3 - (double)c->fsw_rep_c3 / 4 * rswd) * s3);
+                                    }
+                                    else if (c->vdw_mod == 2)
+                                    {
+                                        vlj *= 1 + ((double)c->psw_c3 + ((double)c->psw_c4 + (double)c->psw_c5 * rswd) * rswd)
+                                                           * rswd * rswd * rswd;
+                                    }
+                                    Vvdwtot += vlj;
                                 }
                             }
                             const float tx = fscal * dx, ty = fscal * dy, tz = fscal * dz;
@@ -1773,7 +1865,7 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
                        int ntypes, const float* nbfp, const int* excl_index, const int* excl_list,
                        int coulomb, double rc, double beta, double epsfac, double k_rf,
                        double c_rf, int use_ewald_shift, const int* subset, int nsub,
-                       double* f_out, double* e2)
+                       double* f_out, double* e2, int vdw_mod, double rvdw_switch)
 {
     /* wrap into the box in double */
     double* x = (double*)xmalloc(sizeof(double) * 3 * (size_t)n);
@@ -1818,7 +1910,40 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
     }
     const double rc2      = rc * rc;
     const double sh_ewald = (coulomb == ORC_COULOMB_EWALD && use_ewald_shift) ? erfc(beta * rc) / rc : 0.0;
-    const double cpot6 = -1.0 / pow(rc, 6), cpot12 = -1.0 / pow(rc, 12);
+    /* LJ modifier constants in double (forcerec.cpp:787-816), see orc_set_vdw_modifier */
+    double cpot6 = -1.0 / pow(rc, 6), cpot12 = -1.0 / pow(rc, 12);
+    double fc2[2] = { 0, 0 }, fc3[2] = { 0, 0 }, sw3 = 0, sw4 = 0, sw5 = 0;
+    {
+        const double dd = rc - rvdw_switch;
+        if (vdw_mod == 1)
+        {
+            for (int k = 0; k < 2; k++)
+            {
+                const double p = k == 0 ? 6.0 : 12.0;
+                fc2[k] = ((p + 1) * rvdw_switch - (p + 4) * rc) / (pow(rc, p + 2) * dd * dd);
+                fc3[k] = -((p + 1) * rvdw_switch - (p + 3) * rc) / (pow(rc, p + 2) * dd * dd * dd);
+                const double cp = -pow(rc, -p) + p * fc2[k] / 3 * dd * dd * dd + p * fc3[k] / 4 * dd * dd * dd * dd;
+                if (k == 0)
+                {
+                    cpot6 = cp;
+                }
+                else
+                {
+                    cpot12 = cp;
+                }
+            }
+        }
+        else if (vdw_mod == 2 || vdw_mod == 3)
+        {
+            cpot6 = cpot12 = 0;
+            if (vdw_mod == 2)
+            {
+                sw3 = -10 / (dd * dd * dd);
+                sw4 = 15 / (dd * dd * dd * dd);
+                sw5 = -6 / (dd * dd * dd * dd * dd);
+            }
+        }
+    }
     double       vlj = 0, vc = 0;
     for (int s = 0; s < nsub; s++)
     {
@@ -1900,7 +2025,23 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
                             const double c12  = nbfp[(type[i] * ntypes + type[j]) * 2 + 1] / 12.0;
                             const double ir6  = 1.0 / (r2 * r2 * r2);
                             v_lj              = c12 * (ir6 * ir6 + cpot12) - c6 * (ir6 + cpot6);
-                            fscal += (12 * c12 * ir6 * ir6 - 6 * c6 * ir6) / r2;
+                            double       frlj = 12 * c12 * ir6 * ir6 - 6 * c6 * ir6; /* F r */
+                            const double rsw  = r - rvdw_switch > 0 ? r - rvdw_switch : 0;
+                            if (vdw_mod == 1)
+                            {
+                                /* 6C6 = 6 c6, 12C12 = 12 c12 in the switch terms */
+                                frlj += (-6 * c6 * (fc2[0] + fc3[0] * rsw) + 12 * c12 * (fc2[1] + fc3[1] * rsw)) * rsw * rsw * r;
+                                v_lj += (-6 * c6 * (-fc2[0] / 3 - fc3[0] / 4 * rsw)
+                                         + 12 * c12 * (-fc2[1] / 3 - fc3[1] / 4 * rsw)) * rsw * rsw * rsw;
+                            }
+                            else if (vdw_mod == 2)
+                            {
+                                const double sw  = 1 + (sw3 + (sw4 + sw5 * rsw) * rsw) * rsw * rsw * rsw;
+                                const double dsw = (3 * sw3 + (4 * sw4 + 5 * sw5 * rsw) * rsw) * rsw * rsw;
+                                frlj             = frlj * sw - r * v_lj * dsw;
+                                v_lj *= sw;
+                            }
+                            fscal += frlj / r2;
                         }
                         for (int d = 0; d < 3; d++)
                         {

@@ -38,6 +38,9 @@ orc_ctx* orc_create(int n, const float* x, const float* box, const float* q, con
                     int coulomb, float rc, float rlist_outer, float rlist_inner,
                     float ewald_rtol, float epsilon_rf, int use_ewald_shift);
 void orc_destroy(orc_ctx* c);
+/* LJ modifier (0 potential shift (default), 1 force switch, 2 potential switch, 3 none)
+ * with its constants, mdlib/forcerec.cpp:787-872. */
+void orc_set_vdw_modifier(orc_ctx* c, int mod, float rvdw_switch);
 
 /* Replace the (in-box) coordinates used for gridding and for orc_set_x. */
 void orc_set_coordinates(orc_ctx* c, const float* x);
@@ -107,7 +110,7 @@ void orc_fp64_allpairs(int n, const float* x, const float* box, const float* q, 
                        int ntypes, const float* nbfp, const int* excl_index, const int* excl_list,
                        int coulomb, double rc, double beta, double epsfac, double k_rf,
                        double c_rf, int use_ewald_shift, const int* subset, int nsub,
-                       double* f_out, double* e2);
+                       double* f_out, double* e2, int vdw_mod, double rvdw_switch);
 
 /* nblib's 1/(4 pi eps0) in kJ mol^-1 nm e^-2 (src/gromacs/math/units.h:79) */
 double orc_one_4pi_eps0(void);

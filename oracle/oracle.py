@@ -47,6 +47,7 @@ def lib():
         L.orc_set_coordinates.argtypes = [vp, fp]
         L.orc_set_x.argtypes = [vp, fp]
         L.orc_prune.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.orc_set_vdw_modifier.argtypes = [vp, C.c_int, C.c_float]
         L.orc_balance.argtypes = [vp, C.c_int]
         L.orc_balance.restype = C.c_int
         L.orc_force.argtypes = [vp, C.c_int]
@@ -77,7 +78,7 @@ def lib():
             getattr(L, name).restype = C.POINTER(C.c_uint32)
         L.orc_fp64_allpairs.argtypes = [C.c_int, fp, fp, fp, ip, C.c_int, fp, ip, ip, C.c_int,
                                         C.c_double, C.c_double, C.c_double, C.c_double,
-                                        C.c_double, C.c_int, ip, C.c_int, dp, dp]
+                                        C.c_double, C.c_int, ip, C.c_int, dp, dp, C.c_int, C.c_double]
         L.orc_one_4pi_eps0.restype = C.c_double
         _lib = L
     return _lib
@@ -103,7 +104,7 @@ class Oracle:
     """One system in the oracle: grid, GPU-layout list, prune, force kernel."""
 
     def __init__(self, system, coulomb=COULOMB_EWALD, rc=0.9, rlist=1.0, rlist_inner=None,
-                 ewald_rtol=1e-5, epsilon_rf=1.0, use_ewald_shift=False):
+                 ewald_rtol=1e-5, epsilon_rf=1.0, use_ewald_shift=False, vdw_modifier=0, rvdw_switch=0.0):
         L = lib()
         self.system = system
         self._keep = []
@@ -123,6 +124,8 @@ class Oracle:
         self.c = L.orc_create(system.n, xp, bp, qp, tp, system.ntypes, nbp, eip, elp, coulomb,
                               rc, rlist, self.rlist_inner, ewald_rtol, epsilon_rf,
                               int(use_ewald_shift))
+        if vdw_modifier:
+            L.orc_set_vdw_modifier(self.c, int(vdw_modifier), float(rvdw_switch))
 
     def __del__(self):
         if getattr(self, "c", None):
@@ -244,7 +247,7 @@ class Oracle:
 
 
 def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
-                  use_ewald_shift=False, epsilon_rf=1.0):
+                  use_ewald_shift=False, epsilon_rf=1.0, vdw_modifier=0, rvdw_switch=0.0):
     """FP64 explicit-image forces (on ``subset``) and, for the full set, energies."""
     L = lib()
     n = system.n
@@ -277,5 +280,6 @@ def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
     L.orc_fp64_allpairs(n, xp, bp, qp, tp, system.ntypes, nbp, eip, elp, coulomb, rc,
                         0.0 if beta is None else float(beta), epsfac, k_rf, c_rf,
                         int(use_ewald_shift), sp, len(sub), f.ctypes.data_as(C.POINTER(C.c_double)),
-                        e.ctypes.data_as(C.POINTER(C.c_double)) if full else None)
+                        e.ctypes.data_as(C.POINTER(C.c_double)) if full else None, int(vdw_modifier),
+                        float(np.float32(rvdw_switch)))
     return (f, e) if full else (f, None)

@@ -251,3 +251,35 @@ def test_large_box_force_error_vs_fp64_on_subset():
     err = rel_rms(f[sub], f64)
     print(f"288k box, 3000-atom subset: rel RMS vs FP64 {err:.2e}")
     assert err <= 1e-5
+
+
+@pytest.mark.parametrize("mod", [nblib.VdwModifier.ForceSwitch, nblib.VdwModifier.PotSwitch,
+                                 nblib.VdwModifier.NoModifier])
+@pytest.mark.parametrize("name", ["water3000", "lj_liquid"])
+def test_lj_modifiers_vs_oracle(name, mod):
+    """vdw-modifier force switch / potential switch (rvdw_switch 0.7 nm) and plain cut-off:
+    forces, energies and virial against the oracle (kernel_ref_inner.h switch terms) and
+    forces against the FP64 sum."""
+    s = SYSTEMS[name]()
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=1.0, rcoulomb=0.9,
+                                 compute_virial_and_energy=True, vdw_modifier=mod, rvdw_switch=0.7)
+    calc = nblib.ForceCalculator(s, opts)
+    o = O.Oracle(s, rc=0.9, rlist=1.0, vdw_modifier=int(mod), rvdw_switch=0.7)
+    o.grid()
+    o.search()
+    o.balance(calc.list_balance()["min_ci_balanced"])
+    f = calc.compute(s.x)
+    o.force(True)
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+    eo = o.energies()
+    for k in range(2):
+        assert abs(calc.energies[k] - eo[k]) <= ENERGY_RTOL * abs(eo[k]) + 1e-9, (k, calc.energies[k], eo[k])
+    f64, _ = O.fp64_allpairs(s, rc=0.9, beta=o.beta, vdw_modifier=int(mod), rvdw_switch=0.7)
+    assert rel_rms(f, f64) <= FORCE_RTOL
+
+
+def test_switch_modifiers_rejected_where_unsupported():
+    s = systems.lj_liquid(n=600, ntypes=4, seed=3)
+    with pytest.raises(nblib.InputException):
+        nblib.ForceCalculator(s, nblib.NBKernelOptions(vdw_modifier=nblib.VdwModifier.ForceSwitch,
+                                                       rvdw_switch=1.2))

@@ -180,3 +180,23 @@ def test_erfc_expansion_coefficients_match_their_fit():
     t = 1 / (1 + np.float32(p) * x)
     approx = t * np.polyval(coef[::-1], t) * np.exp(-x * x)
     assert (np.abs(approx - erfc(x)) / erfc(x)).max() < 2e-7
+
+
+@pytest.mark.parametrize("mod", [1, 2, 3])
+def test_oracle_lj_modifiers_vs_fp64(mod):
+    """Force switch, potential switch and plain cut-off (rvdw_switch 0.7 nm) in the oracle's
+    float kernel against the FP64 explicit-image sum, on the random LJ + Coulomb liquid."""
+    s = systems.lj_liquid(n=1500, ntypes=4, seed=12)
+    o = O.Oracle(s, rc=0.9, rlist=1.0, vdw_modifier=mod, rvdw_switch=0.7)
+    o.grid()
+    o.search()
+    o.force(energy=True)
+    f64, e64 = O.fp64_allpairs(s, rc=0.9, beta=o.beta, vdw_modifier=mod, rvdw_switch=0.7)
+    assert rel_rms(o.forces(), f64) < 1e-5
+    np.testing.assert_allclose(o.energies(), e64, rtol=1e-5)
+    # the modifier changes the result relative to the potential shift
+    o0 = O.Oracle(s, rc=0.9, rlist=1.0)
+    o0.grid()
+    o0.search()
+    o0.force(energy=True)
+    assert abs(o0.energies()[0] - o.energies()[0]) > 1e-6 * abs(o0.energies()[0])
