@@ -106,7 +106,7 @@ def _fp64_loss_grads(ens, sig, eps, qscale, q0, f_target):
         total = total + ((f - ft) ** 2).sum()
         off += s.n
     gs, ge, gk = torch.autograd.grad(total, (s64, e64, k64))
-    return float(total), gs.numpy(), ge.numpy(), gk.numpy()
+    return float(total.detach()), gs.numpy(), ge.numpy(), gk.numpy()
 
 
 def test_force_matching_step_matches_fp64_autograd():
