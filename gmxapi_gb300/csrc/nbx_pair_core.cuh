@@ -122,12 +122,6 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
                 int_bit = 1.0f;
             }
             const bool in_range = kExcl ? (mask != 0.0f) : (r2 < rc2);
-            // a cluster-pair block with no atom pair inside the cut-off (about an eighth of the
-            // pruned list's blocks) contributes nothing: skip its pair terms
-            if (!__any_sync(0xffffffffu, in_range))
-            {
-                continue;
-            }
             r2         = fmaxf(r2, kMinDist2);
             float rinv = rsqrtf(r2);
             if (kEnergy)
