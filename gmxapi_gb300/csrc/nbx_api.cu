@@ -1678,6 +1678,7 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
     b->device    = device;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+    optin_batch_force_smem();
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
     b->own_stream = true;

@@ -211,9 +211,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const float    beta2l2 = cv.beta2l2;  // beta^2 * log2(e)
     const float    c2b     = cv.c2b;      // 2 beta / sqrt(pi)
     const float    k_rf2   = cv.k_rf2;
-    // per-warp stage of one cj4 group's j-atoms, after the type table
-    float4* jx = nbfp_s + nt1 * nt1 + (threadIdx.x >> 5) * 32;
-    int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;
+    // per-warp double-buffered j stage (bulk copies), after the type table
+    JStage js = stage_carve(nbfp_s, nt1 * nt1, threadIdx.x >> 5, blockDim.x >> 5);
+    stage_init(js, lane);
     for (;;)
     {
         int e = 0;
@@ -231,8 +231,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const Sci       s    = b.sci[e - prefix[sidx]];
         const SysPtrs   p    = { b.xq, b.tgrid, b.fnb, b.cj4, b.excl, b.shiftvec, fshift + (size_t)kNShift * 3 * sidx };
         double          elj = 0.0, eel = 0.0;
-        process_entry<kEnergy, kEwald>(cv, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2,
-                                       elj, eel);
+        if (!process_entry<kEnergy, kEwald>(cv, p, s, nbfp_s, js, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b, k_rf2,
+                                            elj, eel))
+        {
+            stage_timeout(js, const_cast<unsigned*>(&b.hdr->status), lane);
+            break;
+        }
         if (kEnergy)
         {
 #pragma unroll
@@ -357,8 +361,26 @@ template<bool kE, bool kW, int kT, int kM>
 void launch_batch_force_t(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys, int* ctr,
                           double* en, double* fs, int num_sms, cudaStream_t s)
 {
-    const size_t smem = sizeof(float4) * (size_t)cv.ntypes1 * cv.ntypes1 + (size_t)(kT / 32) * 32 * (16 + 4);
+    const size_t smem = sizeof(float4) * (size_t)cv.ntypes1 * cv.ntypes1 + (size_t)(kT / 32) * kStageSmemPerWarp;
     k_batch_force<kE, kW, kT, kM><<<num_sms * kM, kT, smem, s>>>(cv, sys, prefix, nsys, ctr, en, fs);
+}
+
+template<bool kE, bool kW, int kT, int kM>
+cudaError_t optin_batch_t()
+{
+    // the type table (up to 48^2 entries) and the per-warp stages may pass 48 KB
+    return cudaFuncSetAttribute(k_batch_force<kE, kW, kT, kM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(float4) * 48 * 48 + (kT / 32) * kStageSmemPerWarp));
+}
+
+template<bool kE, bool kW>
+cudaError_t optin_batch_variants()
+{
+    cudaError_t e = optin_batch_t<kE, kW, 256, 2>();
+    if (e == cudaSuccess) e = optin_batch_t<kE, kW, 128, 4>();
+    if (e == cudaSuccess) e = optin_batch_t<kE, kW, 512, 1>();
+    if (e == cudaSuccess) e = optin_batch_t<kE, kW, 64, 8>();
+    return e;
 }
 
 template<bool kE, bool kW>
@@ -431,6 +453,17 @@ cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, cons
         k_batch_finish<<<nsys, 32, 0, s>>>(sys, nsys, en, fs, vir, d_e, d_vir);
     }
     return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+// Raises the dynamic shared-memory limit of every batched force kernel (host set-up
+// before any launch or capture; the 512-thread shape with many types needs > 48 KB).
+cudaError_t optin_batch_force_smem()
+{
+    cudaError_t e = optin_batch_variants<true, true>();
+    if (e == cudaSuccess) e = optin_batch_variants<true, false>();
+    if (e == cudaSuccess) e = optin_batch_variants<false, true>();
+    if (e == cudaSuccess) e = optin_batch_variants<false, false>();
+    return e;
 }
 
 } // namespace nbx

@@ -43,7 +43,7 @@ namespace
 constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
-constexpr int kStageBytes     = 32 * (16 + 4);  // per warp: 32 staged j-atoms (xq, type)
+constexpr int kStageBytes     = kStageSmemPerWarp;  // per warp: double-buffered j stage and barriers
 
 template<bool kEnergy, bool kEwald, int kLj = 0>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
@@ -67,9 +67,9 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     const int      ii      = lane & 7;   // i-atom within the i-cluster
     const int      jj      = lane >> 3;  // j-atom within the warp half
     const int      numSci  = v.hdr->num_sci;
-    // per-warp stage of one cj4 group's j-atoms, after the type table
-    float4* jx = nbfp_s + nt1 * nt1 + (threadIdx.x >> 5) * 32;
-    int*    jt = reinterpret_cast<int*>(nbfp_s + nt1 * nt1 + (blockDim.x >> 5) * 32) + (threadIdx.x >> 5) * 32;
+    // per-warp double-buffered j stage (bulk copies), after the type table
+    JStage js = stage_carve(nbfp_s, nt1 * nt1, threadIdx.x >> 5, blockDim.x >> 5);
+    stage_init(js, lane);
     const float    rc2     = v.rc2;
     const float    beta    = v.beta;
     const float    pbeta   = v.pbeta;
@@ -92,8 +92,12 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         }
         const Sci     s = v.sci[e];
         const SysPtrs p = { v.xq, v.tgrid, v.fnb, v.cj4, v.excl, v.shiftvec, v.fshift };
-        process_entry<kEnergy, kEwald, kLj>(v, p, s, nbfp_s, jx, jt, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b,
-                                            k_rf2, e_lj_acc, e_el_acc);
+        if (!process_entry<kEnergy, kEwald, kLj>(v, p, s, nbfp_s, js, nt1, lane, ii, jj, rc2, pbeta, beta2l2, c2b,
+                                                 k_rf2, e_lj_acc, e_el_acc))
+        {
+            stage_timeout(js, &v.hdr->status, lane);
+            break;
+        }
     }
     if (kEnergy)
     {
@@ -570,6 +574,11 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         return NBX_ERR_INVALID_INPUT;
     }
     if (!(a->rcoulomb > 0.0f) || !(a->rlist >= a->rcoulomb) || a->coulomb < 0 || a->coulomb > 2)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    // the force kernel copies j-clusters with bulk copies: 16-byte aligned sources
+    if ((reinterpret_cast<uintptr_t>(a->xq) & 15u) != 0 || (reinterpret_cast<uintptr_t>(a->types) & 15u) != 0)
     {
         return NBX_ERR_INVALID_INPUT;
     }

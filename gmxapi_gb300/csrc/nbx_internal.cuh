@@ -268,6 +268,7 @@ cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
                                int fresh, int part, int nparts, cudaStream_t s);
 int         adjoint_max_types1();
+cudaError_t optin_batch_force_smem();
 cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double* d_gE, float4* gnb, float4* dnb,
                             double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s);
 cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);

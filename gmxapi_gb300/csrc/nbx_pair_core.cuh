@@ -46,6 +46,107 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(w));
 }
 
+// ---- bulk asynchronous copies (TMA engine) into a warp's shared-memory stage ----
+constexpr int      kStageTx   = kJg * kCl * (16 + 4);  // bytes per cj4 group: 32 xq + 32 types
+constexpr unsigned kMaxSpin   = 1u << 22;              // bounded wait on a stage barrier
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* m, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* m, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* m, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(m)), "r"(parity)
+            : "memory");
+    return ok != 0;
+}
+// global -> shared bulk copy completing on mbarrier m (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* m)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(m))
+                 : "memory");
+}
+
+// A warp's double-buffered j stage: two copies of one cj4 group's 32 j-atoms
+// (xq, types) and their two barriers; `uses` counts the groups staged so far
+// (buffer uses & 1, barrier parity (uses >> 1) & 1).
+struct JStage
+{
+    float4*             x;     // [2][32]
+    int*                t;     // [2][32]
+    unsigned long long* bar;   // [2]
+    unsigned            uses;
+};
+
+// Lane 0 of the warp (after __syncwarp) arms buffer b for cj4 group j4 and starts
+// its eight bulk copies (four j-clusters: 128 B of xq and 32 B of types each).
+__device__ __forceinline__ void stage_issue(const JStage& js, int b, const Cj4* cj4, int j4, const float4* xq,
+                                            const int* tgrid)
+{
+    const int4 cj = *reinterpret_cast<const int4*>(&cj4[j4].cj[0]);
+    fence_proxy_async();  // earlier shared reads of the buffer before the async writes
+    mbar_expect_tx(&js.bar[b], kStageTx);
+    const int c[kJg] = { cj.x, cj.y, cj.z, cj.w };
+#pragma unroll
+    for (int m = 0; m < kJg; m++)
+    {
+        bulk_g2s(js.x + b * 32 + m * kCl, xq + (size_t)c[m] * kCl, kCl * 16, &js.bar[b]);
+        bulk_g2s(js.t + b * 32 + m * kCl, tgrid + (size_t)c[m] * kCl, kCl * 4, &js.bar[b]);
+    }
+}
+
+// Bounded, warp-uniform wait for buffer b; false when the copies did not land.
+__device__ __forceinline__ bool stage_wait(const JStage& js, int b, unsigned parity)
+{
+    bool done = false;
+    for (unsigned it = 0; it < kMaxSpin; it++)
+    {
+        done = mbar_try_wait(&js.bar[b], parity);
+        if (__all_sync(0xffffffffu, done))
+        {
+            return true;
+        }
+    }
+    return false;
+}
+
+// Per-warp barrier set-up (lane 0), once per kernel.
+__device__ __forceinline__ void stage_init(JStage& js, int lane)
+{
+    if (lane == 0)
+    {
+        mbar_init(&js.bar[0], 1);
+        mbar_init(&js.bar[1], 1);
+        fence_mbar_init();
+    }
+    js.uses = 0;
+    __syncwarp();
+}
+
 // Compensated (Kahan) accumulation: sum + c carries ~2x float precision.
 __device__ __forceinline__ void kahan_add(float& sum, float& c, float v)
 {
@@ -252,10 +353,10 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
 // to e_lj_acc / e_el_acc (per lane, FP64).
 // kLj: 0 potential shift or plain cut-off, 1 force switch, 2 potential switch.
 template<bool kEnergy, bool kEwald, int kLj = 0>
-__device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs& p, const Sci& s,
-                                              const float4* __restrict__ nbfp_s, float4* jx, int* jt, int nt1,
-                                              int lane, int ii, int jj, float rc2, float pbeta, float beta2l2,
-                                              float c2b, float k_rf2, double& e_lj_acc, double& e_el_acc)
+__device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs& p, const Sci& s,
+                                              const float4* __restrict__ nbfp_s, JStage& js, int nt1, int lane,
+                                              int ii, int jj, float rc2, float pbeta, float beta2l2, float c2b,
+                                              float k_rf2, double& e_lj_acc, double& e_el_acc)
 {
     const unsigned full = 0xffffffffu;
     const float shx = p.shiftvec[3 * s.shift], shy = p.shiftvec[3 * s.shift + 1], shz = p.shiftvec[3 * s.shift + 2];
@@ -275,46 +376,48 @@ __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs
     }
     st.acc_el = st.cmp_el = 0.0f;
     st.acc_lj = st.cmp_lj = 0.0f;
-    // Software pipeline over the cj4 groups: the record (masks, j-clusters) of group
-    // k+1 is loaded when group k starts, its 32 j-atoms (xq, type; one per lane) after
-    // group k's first half, and they go to the warp's shared-memory stage when k+1
-    // starts, so neither load is waited for.
-    const unsigned full_m = 0xffffffffu;
+    // Pipeline over the cj4 groups: the 32 j-atoms of group k+1 are copied by the TMA
+    // engine into the other stage buffer while group k is computed; the masks and
+    // j-cluster indices of k+1 are loaded into registers ahead as well.
     int4           rec_ime{};
     int            rec_cj = 0;
-    float4         xr{};
-    int            tr = 0;
     if (s.cj4_start < s.cj4_end)
     {
-        rec_ime   = *reinterpret_cast<const int4*>(&p.cj4[s.cj4_start].imei[0]);
-        rec_cj    = (lane < kJg) ? p.cj4[s.cj4_start].cj[lane] : 0;
-        const int a = __shfl_sync(full_m, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
-        xr        = p.xq[a];
-        tr        = p.tgrid[a];
+        rec_ime = *reinterpret_cast<const int4*>(&p.cj4[s.cj4_start].imei[0]);
+        rec_cj  = (lane < kJg) ? p.cj4[s.cj4_start].cj[lane] : 0;
+        __syncwarp();
+        if (lane == 0)
+        {
+            stage_issue(js, js.uses & 1, p.cj4, s.cj4_start, p.xq, p.tgrid);
+        }
     }
     for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
     {
-        const int4 ime     = rec_ime;
-        const int  cj_lane = rec_cj;
-        __syncwarp();
-        jx[lane] = xr;
-        jt[lane] = tr;
-        __syncwarp();
-        const bool more = j4 + 1 < s.cj4_end;
+        const int4     ime     = rec_ime;
+        const int      cj_lane = rec_cj;
+        const int      b       = js.uses & 1;
+        const unsigned parity  = (js.uses >> 1) & 1;
+        const bool     more    = j4 + 1 < s.cj4_end;
         if (more)
         {
             rec_ime = *reinterpret_cast<const int4*>(&p.cj4[j4 + 1].imei[0]);
             rec_cj  = (lane < kJg) ? p.cj4[j4 + 1].cj[lane] : 0;
+            __syncwarp();  // the other buffer's last readers (group k-1) are done
+            if (lane == 0)
+            {
+                stage_issue(js, b ^ 1, p.cj4, j4 + 1, p.xq, p.tgrid);
+            }
         }
+        if (!stage_wait(js, b, parity))
+        {
+            return false;
+        }
+        js.uses++;
+        const float4* jx = js.x + b * 32;
+        const int*    jt = js.t + b * 32;
 #pragma unroll 1
         for (int h = 0; h < kSplit; h++)
         {
-            if (h == 1 && more)
-            {
-                const int a = __shfl_sync(full_m, rec_cj, lane >> 3) * kCl + (lane & (kCl - 1));
-                xr          = p.xq[a];
-                tr          = p.tgrid[a];
-            }
             const unsigned im  = (h == 0) ? (unsigned)ime.x : (unsigned)ime.z;
             const int      exi = (h == 0) ? ime.y : ime.w;
             if (!im)
@@ -376,6 +479,34 @@ __device__ __forceinline__ void process_entry(const DeviceView& v, const SysPtrs
             atomicAdd(&p.fshift[3 * s.shift + 2], (double)sfz);
         }
     }
+    return true;
+}
+
+// Per-warp j stage in a kernel's dynamic shared memory, after a table of `table_f4`
+// float4: [nwarps][64] float4 of xq, [nwarps][64] int of types, [nwarps][2] barriers.
+__device__ __forceinline__ JStage stage_carve(float4* smem, int table_f4, int warp, int nwarps)
+{
+    float4* base = smem + table_f4;
+    JStage  js;
+    js.x   = base + warp * 64;
+    js.t   = reinterpret_cast<int*>(base + nwarps * 64) + warp * 64;
+    js.bar = reinterpret_cast<unsigned long long*>(reinterpret_cast<int*>(base + nwarps * 64) + nwarps * 64) + warp * 2;
+    js.uses = 0;
+    return js;
+}
+constexpr int kStageSmemPerWarp = 64 * 16 + 64 * 4 + 2 * 8;
+
+// After a stage wait gave up: flag the timeout, give the copies in flight a bounded
+// second chance to land, then the warp leaves the kernel.
+__device__ __forceinline__ void stage_timeout(const JStage& js, unsigned* status, int lane)
+{
+    if (lane == 0)
+    {
+        atomicOr(status, (unsigned)kStatusTimeout);
+    }
+    const unsigned u = js.uses;
+    stage_wait(js, u & 1, (u >> 1) & 1);
+    stage_wait(js, (u + 1) & 1, ((u + 1) >> 1) & 1);
 }
 
 } // namespace nbx

@@ -240,8 +240,8 @@ typedef struct
     int             num_atoms;  /* N */
     int             num_slots;  /* grid slots (padded atoms) in xq / types; at most 65536 */
     int             num_sci;    /* list entries */
-    const float*    xq;         /* [4*num_slots] x, y, z, q per grid slot (fillers: far away, q = 0) */
-    const int*      types;      /* [num_slots] type per slot; fillers carry num_types (the all-zero type) */
+    const float*    xq;         /* [4*num_slots] x, y, z, q per grid slot (fillers: far away, q = 0); 16-byte aligned */
+    const int*      types;      /* [num_slots] type per slot; fillers carry num_types (the all-zero type); 16-byte aligned */
     int             num_types;  /* real types; nbfp has (num_types+1)^2 pairs */
     const float*    nbfp;       /* [(num_types+1)^2 * 2] {6*C6, 12*C12}, zero row/column for the filler type */
     const int*      cells;      /* [N] grid slot of each atom */
