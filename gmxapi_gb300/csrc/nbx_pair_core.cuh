@@ -102,21 +102,20 @@ struct JStage
     unsigned            uses;
 };
 
-// Lane 0 of the warp (after __syncwarp) arms buffer b for cj4 group j4 and starts
-// its eight bulk copies (four j-clusters: 128 B of xq and 32 B of types each).
-__device__ __forceinline__ void stage_issue(const JStage& js, int b, const Cj4* cj4, int j4, const float4* xq,
+// Lanes 0-3 of the warp (after __syncwarp), each holding one j-cluster index cj of a
+// cj4 group, start the group's bulk copies into buffer b: one warp instruction per
+// array copies all four clusters (128 B of xq and 32 B of types each).  Lane 0 arms
+// the barrier with the group's byte count.
+__device__ __forceinline__ void stage_issue(const JStage& js, int b, int lane, int cj, const float4* xq,
                                             const int* tgrid)
 {
-    const int4 cj = *reinterpret_cast<const int4*>(&cj4[j4].cj[0]);
     fence_proxy_async();  // earlier shared reads of the buffer before the async writes
-    mbar_expect_tx(&js.bar[b], kStageTx);
-    const int c[kJg] = { cj.x, cj.y, cj.z, cj.w };
-#pragma unroll
-    for (int m = 0; m < kJg; m++)
+    if (lane == 0)
     {
-        bulk_g2s(js.x + b * 32 + m * kCl, xq + (size_t)c[m] * kCl, kCl * 16, &js.bar[b]);
-        bulk_g2s(js.t + b * 32 + m * kCl, tgrid + (size_t)c[m] * kCl, kCl * 4, &js.bar[b]);
+        mbar_expect_tx(&js.bar[b], kStageTx);
     }
+    bulk_g2s(js.x + b * 32 + lane * kCl, xq + (size_t)cj * kCl, kCl * 16, &js.bar[b]);
+    bulk_g2s(js.t + b * 32 + lane * kCl, tgrid + (size_t)cj * kCl, kCl * 4, &js.bar[b]);
 }
 
 // Bounded, warp-uniform wait for buffer b; false when the copies did not land.
@@ -386,9 +385,9 @@ __device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs
         rec_ime = *reinterpret_cast<const int4*>(&p.cj4[s.cj4_start].imei[0]);
         rec_cj  = (lane < kJg) ? p.cj4[s.cj4_start].cj[lane] : 0;
         __syncwarp();
-        if (lane == 0)
+        if (lane < kJg)
         {
-            stage_issue(js, js.uses & 1, p.cj4, s.cj4_start, p.xq, p.tgrid);
+            stage_issue(js, js.uses & 1, lane, rec_cj, p.xq, p.tgrid);
         }
     }
     for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
@@ -403,9 +402,9 @@ __device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs
             rec_ime = *reinterpret_cast<const int4*>(&p.cj4[j4 + 1].imei[0]);
             rec_cj  = (lane < kJg) ? p.cj4[j4 + 1].cj[lane] : 0;
             __syncwarp();  // the other buffer's last readers (group k-1) are done
-            if (lane == 0)
+            if (lane < kJg)
             {
-                stage_issue(js, b ^ 1, p.cj4, j4 + 1, p.xq, p.tgrid);
+                stage_issue(js, b ^ 1, lane, rec_cj, p.xq, p.tgrid);
             }
         }
         if (!stage_wait(js, b, parity))
