@@ -45,6 +45,7 @@ EXPORTED = [
     "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
     "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
     "nbx_batch_set_parameters_device", "nbx_batch_backward_device", "nbx_batch_force_match_device",
+    "nbx_set_wait_test",
 ]
 
 
@@ -152,6 +153,7 @@ def load():
     L.nbx_get_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_get_phase_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_set_list_balance.argtypes = [vp, C.c_int]
+    L.nbx_set_wait_test.argtypes = [vp, C.c_int]
     L.nbx_batch_set_parameters_device.argtypes = [vp, vp, vp]
     L.nbx_batch_backward_device.argtypes = [vp] * 7
     L.nbx_batch_force_match_device.argtypes = [vp] * 10

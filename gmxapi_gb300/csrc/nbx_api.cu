@@ -1044,6 +1044,16 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
     return cuda_check(h, e, "nbx_set_parameters_device");
 }
 
+int nbx_set_wait_test(nbx_handle* h, int enable)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    h->v.wait_test_bytes = enable ? 16u : 0u;
+    return NBX_OK;
+}
+
 int nbx_set_list_balance(nbx_handle* h, int entries_per_sm)
 {
     if (!h || entries_per_sm < 0)

@@ -155,6 +155,7 @@ struct DeviceView
     // LJ modifier (nbx_vdw_modifier) and its constants (mdlib/forcerec.cpp:787-816):
     // force switch F/p = r^-(p+1) + c2 r^2 + c3 r^3 for p = 6 (disp) and 12 (rep);
     // potential switch sw = 1 + c3 rsw^3 + c4 rsw^4 + c5 rsw^5
+    unsigned wait_test_bytes;  // 0; > 0 only in the failure-detection test of the bounded stage waits
     int   vdw_mod;
     float rvdw_switch;
     float fsw_disp_c2, fsw_disp_c3, fsw_rep_c2, fsw_rep_c3;

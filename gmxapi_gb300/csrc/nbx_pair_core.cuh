@@ -47,8 +47,8 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float x, float y, float
 }
 
 // ---- bulk asynchronous copies (TMA engine) into a warp's shared-memory stage ----
-constexpr int      kStageTx   = kJg * kCl * (16 + 4);  // bytes per cj4 group: 32 xq + 32 types
-constexpr unsigned kMaxSpin   = 1u << 22;              // bounded wait on a stage barrier
+constexpr int                kStageTx       = kJg * kCl * (16 + 4);  // bytes per cj4 group: 32 xq + 32 types
+constexpr unsigned long long kStageWaitNs   = 1000000000ull;         // a stage wait gives up after 1 s
 
 __device__ __forceinline__ unsigned smem_u32(const void* p)
 {
@@ -107,30 +107,49 @@ struct JStage
 // array copies all four clusters (128 B of xq and 32 B of types each).  Lane 0 arms
 // the barrier with the group's byte count.
 __device__ __forceinline__ void stage_issue(const JStage& js, int b, int lane, int cj, const float4* xq,
-                                            const int* tgrid)
+                                            const int* tgrid, unsigned extra_tx = 0)
 {
     fence_proxy_async();  // earlier shared reads of the buffer before the async writes
     if (lane == 0)
     {
-        mbar_expect_tx(&js.bar[b], kStageTx);
+        // extra_tx > 0 (a failure-detection test only) arms the barrier for bytes that never
+        // arrive, so the bounded wait runs out
+        mbar_expect_tx(&js.bar[b], kStageTx + extra_tx);
     }
     bulk_g2s(js.x + b * 32 + lane * kCl, xq + (size_t)cj * kCl, kCl * 16, &js.bar[b]);
     bulk_g2s(js.t + b * 32 + lane * kCl, tgrid + (size_t)cj * kCl, kCl * 4, &js.bar[b]);
 }
 
-// Bounded, warp-uniform wait for buffer b; false when the copies did not land.
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded, warp-uniform wait for buffer b (1 s of wall time); false when the copies
+// did not land.
 __device__ __forceinline__ bool stage_wait(const JStage& js, int b, unsigned parity)
 {
-    bool done = false;
-    for (unsigned it = 0; it < kMaxSpin; it++)
+    if (__all_sync(0xffffffffu, mbar_try_wait(&js.bar[b], parity)))
     {
-        done = mbar_try_wait(&js.bar[b], parity);
+        return true;
+    }
+    const unsigned long long t0 = global_ns();
+    for (;;)
+    {
+        const bool done = mbar_try_wait(&js.bar[b], parity);
         if (__all_sync(0xffffffffu, done))
         {
             return true;
         }
+        // lane 0's clock decides, so every lane leaves together
+        const bool late = __shfl_sync(0xffffffffu, global_ns() - t0 > kStageWaitNs, 0);
+        if (late)
+        {
+            return false;
+        }
     }
-    return false;
 }
 
 // Per-warp barrier set-up (lane 0), once per kernel.
@@ -387,7 +406,7 @@ __device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs
         __syncwarp();
         if (lane < kJg)
         {
-            stage_issue(js, js.uses & 1, lane, rec_cj, p.xq, p.tgrid);
+            stage_issue(js, js.uses & 1, lane, rec_cj, p.xq, p.tgrid, v.wait_test_bytes);
         }
     }
     for (int j4 = s.cj4_start; j4 < s.cj4_end; j4++)
@@ -404,7 +423,7 @@ __device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs
             __syncwarp();  // the other buffer's last readers (group k-1) are done
             if (lane < kJg)
             {
-                stage_issue(js, b ^ 1, lane, rec_cj, p.xq, p.tgrid);
+                stage_issue(js, b ^ 1, lane, rec_cj, p.xq, p.tgrid, v.wait_test_bytes);
             }
         }
         if (!stage_wait(js, b, parity))

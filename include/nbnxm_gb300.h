@@ -157,6 +157,11 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * [2] search count pass, [3] search write pass, [4] prune (fresh or rolling).  ms and counts
  * are double[5] / long long[5] (either may be NULL); reset = 1 clears them. */
 int nbx_get_phase_timings(nbx_handle* h, double* ms, long long* counts, int reset);
+/* Failure-detection test hook (no counterpart in the reference): with enable = 1 the force
+ * kernel's shared-memory stage barriers wait for bytes that never arrive, so their bounded
+ * (1 s) waits give up and the next nbx_compute / nbx_synchronize returns NBX_ERR_TIMEOUT; the
+ * context stays usable.  Keep 0 outside that test. */
+int nbx_set_wait_test(nbx_handle* h, int enable);
 /* GPU list balancing (pairlist.cpp split_sci_entry / sort_sci): entries are split when the grid
  * has fewer than entries_per_sm x SMs cells (default 44, the reference's factor; 0 = never
  * split; entries are always sorted large-first).  Takes effect at the next search. */
