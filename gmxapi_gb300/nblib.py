@@ -18,7 +18,6 @@ import enum
 import numpy as np
 
 from . import _lib
-from ._lib import check
 
 
 class CoulombType(enum.IntEnum):
@@ -36,6 +35,14 @@ class VdwModifier(enum.IntEnum):
 
 class InputException(ValueError):
     """Raised for invalid systems or options (nblib::InputException)."""
+
+
+def check(code: int, handle=None):
+    """NBX_ERR_INVALID_INPUT as InputException (like nblib), other failures as NbxError."""
+    if code == _lib.NBX_ERR_INVALID_INPUT:
+        msg = _lib.load().nbx_last_error(handle)
+        raise InputException(msg.decode() if msg else "invalid input")
+    _lib.check(code, handle)
 
 
 @dataclasses.dataclass

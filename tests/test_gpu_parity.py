@@ -283,3 +283,70 @@ def test_switch_modifiers_rejected_where_unsupported():
     with pytest.raises(nblib.InputException):
         nblib.ForceCalculator(s, nblib.NBKernelOptions(vdw_modifier=nblib.VdwModifier.ForceSwitch,
                                                        rvdw_switch=1.2))
+
+
+def _water_like(x, q, types, box, excl=None):
+    n = len(x)
+    ei = np.arange(n + 1, dtype=np.int32) if excl is None else excl[0]
+    el = np.arange(n, dtype=np.int32) if excl is None else excl[1]
+    w = systems.water_small()
+    return systems.System(x=np.asarray(x, np.float32).reshape(-1, 3), box=np.asarray(box, np.float32),
+                          q=np.asarray(q, np.float32), type=np.asarray(types, np.int32), ntypes=w.ntypes,
+                          nbfp=w.nbfp, excl_index=ei, excl_list=el, name="edge")
+
+
+@pytest.mark.parametrize("coulomb", [nblib.CoulombType.Pme, nblib.CoulombType.ReactionField])
+def test_single_atom_only_self_energy(coulomb):
+    """One charged atom: no pairs, zero force, the energy is the self term alone."""
+    s = _water_like([[0.5, 0.6, 0.7]], [0.5], [0], [3.0, 3.0, 3.0])
+    calc, o = _pair(s, coulomb=coulomb)
+    f = calc.compute(s.x)
+    o.force(True)
+    assert np.all(f == 0.0)
+    np.testing.assert_allclose(calc.energies, o.energies(), rtol=1e-6, atol=1e-9)
+    assert calc.energies[1] < 0 and calc.energies[0] == 0.0
+
+
+def test_coincident_atoms_stay_finite():
+    """Two non-excluded atoms at the same position: the minimum-distance clamp keeps the
+    kernel finite (c_nbnxnMinDistanceSquared, pairlist.h:146), as in the reference."""
+    s = _water_like([[1.0, 1.0, 1.0], [1.0, 1.0, 1.0], [2.0, 2.0, 2.0]], [0.4, -0.4, 0.1], [0, 0, 1],
+                    [3.0, 3.0, 3.0])
+    calc, o = _pair(s)
+    f = calc.compute(s.x)
+    o.force(True)
+    assert np.all(np.isfinite(f)) and np.all(np.isfinite(calc.energies))
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+    np.testing.assert_allclose(calc.energies, o.energies(), rtol=1e-5)
+
+
+def test_list_grows_when_atoms_crowd_together():
+    """Coordinates squeezed into one corner octant after the first search: the search
+    count pass finds a longer list and the capacity grows before the write pass."""
+    s = systems.spc_water(300, 2.08, seed=5)
+    calc, o = _pair(s)
+    n0 = calc.sizes()["num_cj4"]
+    x = (s.x * np.float32(0.5)).astype(np.float32)
+    calc.update_pairlist(x)
+    o.set_coordinates(x)
+    o.grid()
+    o.search()
+    o.balance(calc.list_balance()["min_ci_balanced"])
+    assert calc.sizes()["num_cj4"] > n0
+    pg, po = calc.pairlist(), o.pairlist()
+    assert np.array_equal(canonical_pairs(pg["sci"], pg["cj4"], pg["excl"]),
+                          canonical_pairs(po["sci"], po["cj4"], po["excl"]))
+    f = calc.compute(x)
+    o.set_x(x)
+    o.force(False)
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+
+
+def test_far_outside_box_is_an_input_error():
+    """put_atoms_in_box bound: a coordinate more than 127 box lengths out is rejected."""
+    s = systems.spc_water(30, 1.0, seed=1)
+    calc = nblib.ForceCalculator(s)
+    x = s.x.copy()
+    x[0, 0] += 200.0
+    with pytest.raises(nblib.InputException):
+        calc.update_pairlist(x)
