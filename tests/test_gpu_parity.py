@@ -311,7 +311,7 @@ def test_coincident_charges_stay_finite():
     """Two non-excluded charges (no LJ) at the same position: the minimum-distance clamp
     (c_nbnxnMinDistanceSquared, pairlist.h:146) keeps the Coulomb terms finite, as in the
     reference.  (With LJ, 12 C12 r^-14 at the clamp overflows float in the reference too.)"""
-    s = _water_like([[1.0, 1.0, 1.0], [1.0, 1.0, 1.0], [2.0, 2.0, 2.0]], [0.4, -0.4, 0.1], [1, 1, 1],
+    s = _water_like([[1.0, 1.0, 1.0], [1.0, 1.0, 1.0], [1.5, 1.1, 1.0]], [0.4, -0.3, 0.1], [1, 1, 1],
                     [3.0, 3.0, 3.0])
     calc, o = _pair(s)
     f = calc.compute(s.x)
