@@ -321,13 +321,14 @@ def test_coincident_charges_stay_finite():
     np.testing.assert_allclose(calc.energies, o.energies(), rtol=1e-5)
 
 
-def test_list_grows_when_atoms_crowd_together():
-    """Coordinates squeezed into one corner octant after the first search: the search
-    count pass finds a longer list and the capacity grows before the write pass."""
+def test_list_grows_when_atoms_spread_out():
+    """Atoms first crowded into one corner octant, then spread over the whole box: the
+    search count pass finds a longer list and the capacity grows before the write pass."""
     s = systems.spc_water(300, 2.08, seed=5)
+    x = s.x.copy()
+    s.x = (x * np.float32(0.5)).astype(np.float32)
     calc, o = _pair(s)
     n0 = calc.sizes()["num_cj4"]
-    x = (s.x * np.float32(0.5)).astype(np.float32)
     calc.update_pairlist(x)
     o.set_coordinates(x)
     o.grid()
