@@ -46,6 +46,9 @@ EXPORTED = [
     "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
     "nbx_batch_set_parameters_device", "nbx_batch_backward_device", "nbx_batch_force_match_device",
     "nbx_set_wait_test",
+    "nbx_ewald_coefficient", "nbx_pme_grid_size", "nbx_pme_create", "nbx_pme_destroy", "nbx_pme_last_error",
+    "nbx_pme_set_stream", "nbx_pme_synchronize", "nbx_pme_get_info", "nbx_pme_compute_device",
+    "nbx_pme_splines_device", "nbx_pme_spread_device", "nbx_pme_solve_device", "nbx_pme_gather_device",
 ]
 
 
@@ -176,10 +179,26 @@ def load():
     L.nbx_batch_set_prune.argtypes = [vp, C.c_int, C.c_float]
     L.nbx_backward_device.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.nbx_set_parameters_device.argtypes = [vp, vp, vp]
+    L.nbx_ewald_coefficient.argtypes = [C.c_float, C.c_float]
+    L.nbx_ewald_coefficient.restype = C.c_float
+    L.nbx_pme_grid_size.argtypes = [fp, C.c_float, ip]
+    L.nbx_pme_create.argtypes = [fp, ip, C.c_float, C.c_float, C.c_int, C.POINTER(vp)]
+    L.nbx_pme_destroy.argtypes = [vp]
+    L.nbx_pme_last_error.argtypes = [vp]
+    L.nbx_pme_last_error.restype = C.c_char_p
+    L.nbx_pme_set_stream.argtypes = [vp, vp]
+    L.nbx_pme_synchronize.argtypes = [vp]
+    L.nbx_pme_get_info.argtypes = [vp, ip, fp]
+    L.nbx_pme_compute_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
+    L.nbx_pme_splines_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.nbx_pme_spread_device.argtypes = [vp, C.c_int, vp, vp, vp]
+    L.nbx_pme_solve_device.argtypes = [vp, vp, vp, vp]
+    L.nbx_pme_gather_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",
-                                                "nbx_batch_last_error"):
+                                                "nbx_batch_last_error", "nbx_pme_last_error",
+                                                "nbx_ewald_coefficient"):
             f.restype = C.c_int
     _lib = L
     return L

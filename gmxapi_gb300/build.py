@@ -29,6 +29,7 @@ UNITS = {
     "nbx_adjoint.cu": [],
     "nbx_balance.cu": [],
     "nbx_api.cu": [],
+    "nbx_pme.cu": [],
 }
 
 
@@ -69,7 +70,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
-        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static"])
+        # cuFFT (the PME transforms) from the toolkit that compiles the library
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static",
+             "-L", cudalib, "-lcufft", "-Xlinker", "-rpath," + cudalib])
     return LIB
 
 

@@ -1,0 +1,727 @@
+// Smooth particle-mesh Ewald: the reciprocal-space half of the Ewald sum whose
+// real-space half is the cluster-pair kernel.
+//
+// Restates, for one rectangular box on one GPU and pme_order 4, the reference's PME path:
+//  - grid sizes (calcFftGrid, src/gromacs/fft/calcgrid.cpp:63-160, with
+//    minimalPmeGridSize, src/gromacs/ewald/pme.cpp:488-500);
+//  - fractional coordinates and gridline indices (calc_interpolation_idx,
+//    src/gromacs/ewald/pme_spread.cpp:65-140 with make_gridindex_to_localindex,
+//    pme_grid.cpp:779-830 on one rank: t = n (x / L + 2), index = (int)t mod n);
+//  - the B-spline weights and derivatives (CALC_SPLINE(4), pme_spread.cpp:220-266);
+//  - spreading q theta_x theta_y theta_z onto the points index + 0..3, periodic
+//    (spread_coefficients_bsplines_thread + wrap_periodic_pmegrid);
+//  - the spline moduli (make_bspline_moduli / make_dft_mod,
+//    src/gromacs/ewald/calculate_spline_moduli.cpp:52-122);
+//  - the reciprocal solve with energy and virial (solve_pme_yzx,
+//    src/gromacs/ewald/pme_solve.cpp:332-587);
+//  - the force gather (gather_f_bsplines / do_fspline,
+//    src/gromacs/ewald/pme_gather.cpp:78-360).
+// The 3-D real<->complex transforms are cuFFT's (unnormalised both ways, like the
+// reference's).  Spreading accumulates with float atomics; the energy and the
+// virial are reduced in FP64.
+//
+// Layouts in device memory: real grid [nx][ny][nz] (z fastest); half-complex grid
+// [nx][ny][nz/2+1] of float2 (the r2c output of cuFFT), so the complex index
+// (kx, ky, kz) is the reference's (x, y, z) complex-grid cell with z halved.
+#include "../../include/nbnxm_gb300.h"
+#include "nbx_internal.cuh"
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+namespace
+{
+
+constexpr int kOrder = 4;  // pme_order (grid points per dimension and atom)
+
+struct PmeDims
+{
+    int   n[3];
+    float rec[3];  // recipbox diagonal: 1 / box edge (invertBoxMatrix, math/invertmatrix.cpp:62-64)
+};
+
+// CALC_SPLINE(4) for the fraction dr: weights th[0..3] and derivatives dth[0..3]
+__device__ __forceinline__ void bspline4(float dr, float th[4], float dth[4])
+{
+    float d0 = 1.0f - dr, d1 = dr, d2;
+    d2 = __fmul_rn(__fmul_rn(0.5f, dr), d1);
+    d1 = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(dr + 1.0f, d0), __fmul_rn(2.0f - dr, d1)));
+    d0 = __fmul_rn(__fmul_rn(0.5f, 1.0f - dr), d0);
+    dth[0] = -d0;
+    dth[1] = d0 - d1;
+    dth[2] = d1 - d2;
+    dth[3] = d2;
+    const float div = 1.0f / 3.0f;
+    th[3]           = __fmul_rn(__fmul_rn(div, dr), d2);
+    th[2]           = __fmul_rn(div, __fadd_rn(__fmul_rn(dr + 1.0f, d1), __fmul_rn(3.0f - dr, d2)));
+    th[1]           = __fmul_rn(div, __fadd_rn(__fmul_rn(dr + 2.0f, d0), __fmul_rn(2.0f - dr, d1)));
+    th[0]           = __fmul_rn(__fmul_rn(div, 1.0f - dr), d0);
+}
+
+// gridline index ((int)t mod n) and fraction of one coordinate, t = n (x / L + 2)
+__device__ __forceinline__ int interp_index(float x, float rec, int n, float* frac)
+{
+    const float t  = __fmul_rn((float)n, __fadd_rn(__fmul_rn(x, rec), 2.0f));  // c_pmeMaxUnitcellShift = 2
+    const int   ti = (int)floorf(t);  // the reference's truncation for t >= 0
+    *frac          = t - (float)ti;
+    const int i    = ti % n;
+    return i < 0 ? i + n : i;
+}
+
+struct AtomSplines
+{
+    int   i0[3];
+    float th[3][kOrder];
+    float dth[3][kOrder];
+};
+
+__device__ __forceinline__ void atom_splines(const PmeDims& d, const float* __restrict__ x, int a, AtomSplines& s)
+{
+    for (int k = 0; k < 3; k++)
+    {
+        float fr;
+        s.i0[k] = interp_index(x[3 * a + k], d.rec[k], d.n[k], &fr);
+        bspline4(fr, s.th[k], s.dth[k]);
+    }
+}
+
+__device__ __forceinline__ int wrap_once(int i, int n)
+{
+    return i >= n ? i - n : i;
+}
+
+// Spline data in the reference's test layout: idx [N][3], theta/dtheta [3][N][4].
+__global__ void k_pme_splines(PmeDims d, int natoms, const float* __restrict__ x, int* idx, float* theta,
+                              float* dtheta)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms)
+    {
+        return;
+    }
+    AtomSplines s;
+    atom_splines(d, x, a, s);
+    for (int k = 0; k < 3; k++)
+    {
+        idx[3 * a + k] = s.i0[k];
+        for (int o = 0; o < kOrder; o++)
+        {
+            theta[((size_t)k * natoms + a) * kOrder + o]  = s.th[k][o];
+            dtheta[((size_t)k * natoms + a) * kOrder + o] = s.dth[k][o];
+        }
+    }
+}
+
+// Four threads per atom (one x point each), 16 atomic adds per thread.
+__global__ void k_pme_spread(PmeDims d, int natoms, const float* __restrict__ x, const float* __restrict__ q,
+                             float* grid)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = t >> 2, ix = t & 3;
+    if (a >= natoms)
+    {
+        return;
+    }
+    const float qa = q[a];
+    if (qa == 0.0f)
+    {
+        return;
+    }
+    AtomSplines s;
+    atom_splines(d, x, a, s);
+    const int   gx = wrap_once(s.i0[0] + ix, d.n[0]);
+    const float vx = qa * s.th[0][ix];
+    int         gz[kOrder];
+    for (int iz = 0; iz < kOrder; iz++)
+    {
+        gz[iz] = wrap_once(s.i0[2] + iz, d.n[2]);
+    }
+    for (int iy = 0; iy < kOrder; iy++)
+    {
+        const int   gy  = wrap_once(s.i0[1] + iy, d.n[1]);
+        const float vxy = vx * s.th[1][iy];
+        float*      row = grid + ((size_t)gx * d.n[1] + gy) * d.n[2];
+        for (int iz = 0; iz < kOrder; iz++)
+        {
+            atomicAdd(&row[gz[iz]], vxy * s.th[2][iz]);
+        }
+    }
+}
+
+// solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
+// energy and virial terms in FP64 (energy = 0.5 sum, virial = 0.25 sum).
+__global__ void k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ bsp, float elfac, float factor,
+                            float pivol, double* sums, int energy)
+{
+    const int nzc    = d.n[2] / 2 + 1;
+    const int total  = d.n[0] * d.n[1] * nzc;
+    const int t      = blockIdx.x * blockDim.x + threadIdx.x;
+    double    acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    if (t < total)
+    {
+        const int kz = t % nzc;
+        const int ky = (t / nzc) % d.n[1];
+        const int kx = t / (nzc * d.n[1]);
+        if (kx != 0 || ky != 0 || kz != 0)
+        {
+            const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
+            const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
+            const float mhx   = (float)mx * d.rec[0];
+            const float mhy   = (float)my * d.rec[1];
+            const float mhz   = (float)kz * d.rec[2];
+            const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
+            const float by    = pivol * bsp[d.n[0] + ky];
+            const float den   = m2 * bsp[d.n[0] + d.n[1] + kz] * by * bsp[kx];
+            const float eterm = elfac / den * expf(-factor * m2);
+            float2      c     = cgrid[t];
+            if (energy)
+            {
+                const double corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5 : 1.0;
+                const double struct2 = 2.0 * ((double)c.x * c.x + (double)c.y * c.y);
+                const double ets2    = corner * (double)eterm * struct2;
+                const double m2d     = (double)m2;
+                const double vf      = ((double)factor * m2d + 1.0) * 2.0 / m2d;
+                acc[0]               = ets2;
+                acc[1]               = ets2 * vf * mhx * mhx - ets2;
+                acc[2]               = ets2 * vf * mhx * mhy;
+                acc[3]               = ets2 * vf * mhx * mhz;
+                acc[4]               = ets2 * vf * mhy * mhy - ets2;
+                acc[5]               = ets2 * vf * mhy * mhz;
+                acc[6]               = ets2 * vf * mhz * mhz - ets2;
+            }
+            c.x *= eterm;
+            c.y *= eterm;
+            cgrid[t] = c;
+        }
+    }
+    if (!energy)
+    {
+        return;
+    }
+    __shared__ double red[7][32];
+    const int         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 7; k++)
+    {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        }
+        if (lane == 0)
+        {
+            red[k][warp] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 7)
+    {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+        {
+            v += red[threadIdx.x][w];
+        }
+        if (v != 0.0)
+        {
+            atomicAdd(&sums[threadIdx.x], v);
+        }
+    }
+}
+
+// Forces from the potential grid (do_fspline + gather_f_bsplines), added to f.
+__global__ void k_pme_gather(PmeDims d, int natoms, const float* __restrict__ x, const float* __restrict__ q,
+                             const float* __restrict__ grid, float* f)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms)
+    {
+        return;
+    }
+    const float qa = q[a];
+    if (qa == 0.0f)
+    {
+        return;
+    }
+    AtomSplines s;
+    atom_splines(d, x, a, s);
+    int gz[kOrder];
+    for (int iz = 0; iz < kOrder; iz++)
+    {
+        gz[iz] = wrap_once(s.i0[2] + iz, d.n[2]);
+    }
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    for (int ix = 0; ix < kOrder; ix++)
+    {
+        const int gx = wrap_once(s.i0[0] + ix, d.n[0]);
+        for (int iy = 0; iy < kOrder; iy++)
+        {
+            const int    gy  = wrap_once(s.i0[1] + iy, d.n[1]);
+            const float* row = grid + ((size_t)gx * d.n[1] + gy) * d.n[2];
+            float        sz = 0.0f, sdz = 0.0f;
+            for (int iz = 0; iz < kOrder; iz++)
+            {
+                const float g = __ldg(&row[gz[iz]]);
+                sz            = fmaf(s.th[2][iz], g, sz);
+                sdz           = fmaf(s.dth[2][iz], g, sdz);
+            }
+            fx = fmaf(s.dth[0][ix] * s.th[1][iy], sz, fx);
+            fy = fmaf(s.th[0][ix] * s.dth[1][iy], sz, fy);
+            fz = fmaf(s.th[0][ix] * s.th[1][iy], sdz, fz);
+        }
+    }
+    f[3 * a + 0] -= qa * (fx * (float)d.n[0] * d.rec[0]);
+    f[3 * a + 1] -= qa * (fy * (float)d.n[1] * d.rec[1]);
+    f[3 * a + 2] -= qa * (fz * (float)d.n[2] * d.rec[2]);
+}
+
+__global__ void k_pme_finish(const double* sums, double* energy, double* virial)
+{
+    if (threadIdx.x != 0)
+    {
+        return;
+    }
+    if (energy)
+    {
+        energy[0] = 0.5 * sums[0];
+    }
+    if (virial)
+    {
+        virial[0] = 0.25 * sums[1];
+        virial[1] = virial[3] = 0.25 * sums[2];
+        virial[2] = virial[6] = 0.25 * sums[3];
+        virial[4]             = 0.25 * sums[4];
+        virial[5] = virial[7] = 0.25 * sums[5];
+        virial[8]             = 0.25 * sums[6];
+    }
+}
+
+// calcFftGrid for one dimension: the smallest listed size with spacing <= the target
+int fft_grid_size(float length, float spacing)
+{
+    static const int init[] = { 6, 8, 10, 12, 14, 16, 20, 24, 25, 28, 32, 36, 40, 42, 44 };
+    static const int base[] = { 45, 48, 50, 52, 54, 56, 60, 64, 70, 72, 75, 80, 81, 84 };
+    const int        ninit  = (int)(sizeof(init) / sizeof(init[0]));
+    const int        nbase  = (int)(sizeof(base) / sizeof(base[0]));
+    const int        nmin   = std::max((int)((double)(length / spacing) + 0.999), 2 * (kOrder - 1));
+    int              i      = ninit - 1;
+    if (init[i] >= nmin)
+    {
+        while (i > 0 && init[i - 1] >= nmin)
+        {
+            i--;
+        }
+        return init[i];
+    }
+    int fac2 = 1;
+    i        = nbase - 1;
+    while (fac2 * base[i] < nmin)
+    {
+        fac2 *= 2;
+    }
+    int n = 0;
+    do
+    {
+        const int attempt = fac2 * base[i];
+        if (((attempt % 4 == 0 && attempt != 140) || attempt == 90) && attempt >= nmin)
+        {
+            n = attempt;
+        }
+        i--;
+    } while (i > 0);
+    return n;
+}
+
+// make_bspline_moduli + make_dft_mod for pme_order 4 (spline order 3)
+void bspline_moduli(int n, float* mod)
+{
+    const int splineOrder  = kOrder - 1;
+    double    data[kOrder] = { 1.0, 0.0, 0.0, 0.0 };
+    for (int k = 2; k <= splineOrder; k++)
+    {
+        const double div = 1.0 / k;
+        for (int m = k - 1; m > 0; m--)
+        {
+            data[m] = div * ((k - m) * data[m - 1] + (m + 1) * data[m]);
+        }
+        data[0] = div * data[0];
+    }
+    for (int i = 0; i < n; i++)
+    {
+        double sc = 0.0, ss = 0.0;
+        for (int j = 0; j < splineOrder; j++)
+        {
+            const double arg = (2.0 * 3.14159265358979323846 * i * (j + 1)) / n;
+            sc += data[j] * std::cos(arg);
+            ss += data[j] * std::sin(arg);
+        }
+        mod[i] = (float)(sc * sc + ss * ss);
+    }
+    if (splineOrder % 2 == 0 && n % 2 == 0)
+    {
+        mod[n / 2] = (mod[n / 2 - 1] + mod[n / 2 + 1]) * 0.5f;
+    }
+}
+
+thread_local std::string g_pme_error;
+
+} // namespace
+
+struct nbx_pme
+{
+    int          device     = 0;
+    cudaStream_t stream     = nullptr;
+    bool         own_stream = false;
+    PmeDims      d{};
+    float        box[3]    = { 0, 0, 0 };
+    float        beta      = 0.0f;
+    float        epsilon_r = 1.0f;
+    float*       grid      = nullptr;  // real grid [nx][ny][nz]
+    float2*      cgrid     = nullptr;  // half-complex grid [nx][ny][nz/2+1]
+    float*       bsp       = nullptr;  // spline moduli x | y | z
+    double*      sums      = nullptr;  // energy + 6 virial terms
+    cufftHandle  r2c = 0, c2r = 0;
+    bool         plan_r2c = false, plan_c2r = false;
+    std::string  err;
+};
+
+namespace
+{
+
+int pme_error(nbx_pme* p, int code, const std::string& msg)
+{
+    (p ? p->err : g_pme_error) = msg;
+    return code;
+}
+
+int cuda_status(nbx_pme* p, cudaError_t e)
+{
+    return e == cudaSuccess ? NBX_OK : pme_error(p, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+size_t real_points(const nbx_pme* p)
+{
+    return (size_t)p->d.n[0] * p->d.n[1] * p->d.n[2];
+}
+
+size_t complex_points(const nbx_pme* p)
+{
+    return (size_t)p->d.n[0] * p->d.n[1] * (p->d.n[2] / 2 + 1);
+}
+
+cudaError_t launch_spread(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* grid)
+{
+    cudaError_t e = cudaMemsetAsync(grid, 0, sizeof(float) * real_points(p), p->stream);
+    if (e == cudaSuccess && natoms > 0)
+    {
+        k_pme_spread<<<(int)((4LL * natoms + 255) / 256), 256, 0, p->stream>>>(p->d, natoms, d_x, d_q, grid);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+cudaError_t launch_solve(nbx_pme* p, float2* cgrid, double* d_energy, double* d_virial)
+{
+    const bool   energy = d_energy || d_virial;
+    const double vol    = (double)p->box[0] * p->box[1] * p->box[2];
+    // elfac = ONE_4PI_EPS0 / epsilon_r, factor = pi^2 / beta^2 (pme_solve.cpp:341,354), in float like `real`
+    const float elfac  = (float)nbx::one_4pi_eps0() / p->epsilon_r;
+    const float factor = (float)(M_PI * M_PI) / (p->beta * p->beta);
+    const float pivol  = (float)M_PI * (float)vol;
+    cudaError_t e      = cudaSuccess;
+    if (energy)
+    {
+        e = cudaMemsetAsync(p->sums, 0, sizeof(double) * 8, p->stream);
+    }
+    if (e == cudaSuccess)
+    {
+        const int nc = (int)complex_points(p);
+        k_pme_solve<<<(nc + 255) / 256, 256, 0, p->stream>>>(p->d, cgrid, p->bsp, elfac, factor, pivol, p->sums,
+                                                              energy ? 1 : 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && energy)
+    {
+        k_pme_finish<<<1, 32, 0, p->stream>>>(p->sums, d_energy, d_virial);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+cudaError_t launch_gather(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* grid, float* d_f)
+{
+    if (natoms == 0)
+    {
+        return cudaSuccess;
+    }
+    k_pme_gather<<<(natoms + 127) / 128, 128, 0, p->stream>>>(p->d, natoms, d_x, d_q, grid, d_f);
+    return cudaGetLastError();
+}
+
+bool atoms_ok(int natoms, const void* a, const void* b)
+{
+    return natoms >= 0 && (natoms == 0 || (a && b));
+}
+
+} // namespace
+
+extern "C" {
+
+float nbx_ewald_coefficient(float rcoulomb, float ewald_rtol)
+{
+    if (!(rcoulomb > 0.0f))
+    {
+        return 0.0f;
+    }
+    return nbx::calc_ewaldcoeff_q(rcoulomb, ewald_rtol > 0.0f ? ewald_rtol : 1e-5f);
+}
+
+int nbx_pme_grid_size(const float* box, float spacing, int* n)
+{
+    if (!box || !n || !(spacing > 0.0f))
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null argument or non-positive spacing");
+    }
+    for (int k = 0; k < 3; k++)
+    {
+        if (!(box[k] > 0.0f))
+        {
+            return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "box edges must be positive");
+        }
+        n[k] = fft_grid_size(box[k], spacing);
+    }
+    return NBX_OK;
+}
+
+const char* nbx_pme_last_error(const nbx_pme* p)
+{
+    return p ? p->err.c_str() : g_pme_error.c_str();
+}
+
+int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float epsilon_r, int device, nbx_pme** out)
+{
+    if (!box || !grid || !out || !(ewaldcoeff_q > 0.0f))
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null argument or non-positive Ewald coefficient");
+    }
+    *out = nullptr;
+    for (int k = 0; k < 3; k++)
+    {
+        if (!(box[k] > 0.0f) || grid[k] < 2 * (kOrder - 1) || grid[k] > 4096)
+        {
+            return pme_error(nullptr, NBX_ERR_INVALID_INPUT,
+                             "box edges must be positive and grid sizes in [6, 4096] (minimalPmeGridSize)");
+        }
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    {
+        cudaGetLastError();
+        return pme_error(nullptr, NBX_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev)
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "device index out of range");
+    }
+    cudaSetDevice(device);
+    nbx_pme* p   = new nbx_pme();
+    p->device    = device;
+    p->beta      = ewaldcoeff_q;
+    p->epsilon_r = epsilon_r > 0.0f ? epsilon_r : 1.0f;
+    for (int k = 0; k < 3; k++)
+    {
+        p->box[k]   = box[k];
+        p->d.n[k]   = grid[k];
+        p->d.rec[k] = 1.0f / box[k];
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    p->own_stream = e == cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&p->grid, sizeof(float) * real_points(p));
+    if (e == cudaSuccess) e = cudaMalloc(&p->cgrid, sizeof(float2) * complex_points(p));
+    if (e == cudaSuccess) e = cudaMalloc(&p->bsp, sizeof(float) * (grid[0] + grid[1] + grid[2]));
+    if (e == cudaSuccess) e = cudaMalloc(&p->sums, sizeof(double) * 8);
+    if (e == cudaSuccess)
+    {
+        std::vector<float> mod(grid[0] + grid[1] + grid[2]);
+        bspline_moduli(grid[0], mod.data());
+        bspline_moduli(grid[1], mod.data() + grid[0]);
+        bspline_moduli(grid[2], mod.data() + grid[0] + grid[1]);
+        e = cudaMemcpy(p->bsp, mod.data(), sizeof(float) * mod.size(), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess)
+    {
+        const std::string msg = cudaGetErrorString(e);
+        nbx_pme_destroy(p);
+        return pme_error(nullptr, NBX_ERR_OUT_OF_MEMORY, "PME allocation: " + msg);
+    }
+    p->plan_r2c = cufftPlan3d(&p->r2c, grid[0], grid[1], grid[2], CUFFT_R2C) == CUFFT_SUCCESS;
+    p->plan_c2r = p->plan_r2c && cufftPlan3d(&p->c2r, grid[0], grid[1], grid[2], CUFFT_C2R) == CUFFT_SUCCESS;
+    if (!p->plan_c2r)
+    {
+        nbx_pme_destroy(p);
+        return pme_error(nullptr, NBX_ERR_CUDA, "cuFFT plan creation failed");
+    }
+    cufftSetStream(p->r2c, p->stream);
+    cufftSetStream(p->c2r, p->stream);
+    *out = p;
+    return NBX_OK;
+}
+
+int nbx_pme_destroy(nbx_pme* p)
+{
+    if (!p)
+    {
+        return NBX_OK;
+    }
+    cudaSetDevice(p->device);
+    if (p->stream)
+    {
+        cudaStreamSynchronize(p->stream);
+    }
+    if (p->plan_r2c)
+    {
+        cufftDestroy(p->r2c);
+    }
+    if (p->plan_c2r)
+    {
+        cufftDestroy(p->c2r);
+    }
+    cudaFree(p->grid);
+    cudaFree(p->cgrid);
+    cudaFree(p->bsp);
+    cudaFree(p->sums);
+    if (p->own_stream)
+    {
+        cudaStreamDestroy(p->stream);
+    }
+    delete p;
+    return NBX_OK;
+}
+
+int nbx_pme_set_stream(nbx_pme* p, void* s)
+{
+    if (!p)
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null handle");
+    }
+    if (static_cast<cudaStream_t>(s) == p->stream)
+    {
+        return NBX_OK;
+    }
+    cudaSetDevice(p->device);
+    cudaStreamSynchronize(p->stream);
+    if (p->own_stream)
+    {
+        cudaStreamDestroy(p->stream);
+    }
+    p->stream     = static_cast<cudaStream_t>(s);
+    p->own_stream = false;
+    cufftSetStream(p->r2c, p->stream);
+    cufftSetStream(p->c2r, p->stream);
+    return NBX_OK;
+}
+
+int nbx_pme_get_info(const nbx_pme* p, int* grid, float* ewaldcoeff_q)
+{
+    if (!p)
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null handle");
+    }
+    for (int k = 0; k < 3 && grid; k++)
+    {
+        grid[k] = p->d.n[k];
+    }
+    if (ewaldcoeff_q)
+    {
+        *ewaldcoeff_q = p->beta;
+    }
+    return NBX_OK;
+}
+
+int nbx_pme_splines_device(nbx_pme* p, int natoms, const float* d_x, int* d_idx, float* d_theta, float* d_dtheta)
+{
+    if (!p || !atoms_ok(natoms, d_x, d_idx) || (natoms > 0 && (!d_theta || !d_dtheta)))
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument or negative atom count");
+    }
+    cudaSetDevice(p->device);
+    if (natoms == 0)
+    {
+        return NBX_OK;
+    }
+    k_pme_splines<<<(natoms + 127) / 128, 128, 0, p->stream>>>(p->d, natoms, d_x, d_idx, d_theta, d_dtheta);
+    return cuda_status(p, cudaGetLastError());
+}
+
+int nbx_pme_spread_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_grid)
+{
+    if (!p || !atoms_ok(natoms, d_x, d_q) || !d_grid)
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument or negative atom count");
+    }
+    cudaSetDevice(p->device);
+    return cuda_status(p, launch_spread(p, natoms, d_x, d_q, d_grid));
+}
+
+int nbx_pme_solve_device(nbx_pme* p, void* d_cgrid, double* d_energy, double* d_virial)
+{
+    if (!p || !d_cgrid)
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument");
+    }
+    cudaSetDevice(p->device);
+    return cuda_status(p, launch_solve(p, static_cast<float2*>(d_cgrid), d_energy, d_virial));
+}
+
+int nbx_pme_gather_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* d_grid, float* d_f)
+{
+    if (!p || !atoms_ok(natoms, d_x, d_q) || !d_grid || (natoms > 0 && !d_f))
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument or negative atom count");
+    }
+    cudaSetDevice(p->device);
+    return cuda_status(p, launch_gather(p, natoms, d_x, d_q, d_grid, d_f));
+}
+
+int nbx_pme_compute_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_f, double* d_energy,
+                           double* d_virial)
+{
+    if (!p || !atoms_ok(natoms, d_x, d_q) || (natoms > 0 && !d_f))
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument or negative atom count");
+    }
+    cudaSetDevice(p->device);
+    cudaError_t e = launch_spread(p, natoms, d_x, d_q, p->grid);
+    if (e != cudaSuccess)
+    {
+        return cuda_status(p, e);
+    }
+    if (cufftExecR2C(p->r2c, p->grid, reinterpret_cast<cufftComplex*>(p->cgrid)) != CUFFT_SUCCESS)
+    {
+        return pme_error(p, NBX_ERR_CUDA, "cuFFT real-to-complex transform failed");
+    }
+    e = launch_solve(p, p->cgrid, d_energy, d_virial);
+    if (e != cudaSuccess)
+    {
+        return cuda_status(p, e);
+    }
+    if (cufftExecC2R(p->c2r, reinterpret_cast<cufftComplex*>(p->cgrid), p->grid) != CUFFT_SUCCESS)
+    {
+        return pme_error(p, NBX_ERR_CUDA, "cuFFT complex-to-real transform failed");
+    }
+    return cuda_status(p, launch_gather(p, natoms, d_x, d_q, p->grid, d_f));
+}
+
+int nbx_pme_synchronize(nbx_pme* p)
+{
+    if (!p)
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null handle");
+    }
+    cudaSetDevice(p->device);
+    return cuda_status(p, cudaStreamSynchronize(p->stream));
+}
+
+} // extern "C"

@@ -153,6 +153,33 @@ def water_large(seed: int = 2) -> System:
     return spc_water(96000, 14.21, seed)
 
 
+#: Madelung constant of the rock-salt lattice, referred to the nearest-neighbour distance
+MADELUNG_ROCK_SALT = 1.747564594633182
+
+
+def rock_salt(cells: int = 4, nn_distance: float = 0.282) -> System:
+    """A perfect rock-salt crystal of unit charges: `cells`^3 conventional cubic cells
+    (8 ions each, lattice constant 2 * nn_distance), no Lennard-Jones, no exclusions
+    but self.  Its electrostatic energy is -N/2 * MADELUNG_ROCK_SALT / nn_distance
+    (times 1/(4 pi eps0)) and the force on every ion is zero."""
+    g = np.arange(2 * cells, dtype=np.float64)
+    idx = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
+    x = (idx + 0.25) * nn_distance
+    q = np.where(idx.sum(1) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    n = x.shape[0]
+    return System(
+        x=x.astype(np.float32),
+        box=np.full(3, 2 * cells * nn_distance, dtype=np.float32),
+        q=q,
+        type=np.zeros(n, np.int32),
+        ntypes=1,
+        nbfp=np.zeros(2, np.float32),
+        excl_index=np.arange(n + 1, dtype=np.int32),
+        excl_list=np.arange(n, dtype=np.int32),
+        name=f"rocksalt{n}",
+    )
+
+
 def uneven_ensemble(
     num_systems: int = 256, seed: int = 3, n_min: int = 500, n_max: int = 20000
 ) -> list[System]:

@@ -278,6 +278,52 @@ typedef struct
 int nbx_compute_noalloc(const nbx_noalloc_args* args, float* d_f, double* d_energies, double* d_virial,
                         void* cuda_stream);
 
+/* ---- smooth PME, reciprocal space (the long-range half of the Ewald sum) ---- */
+/* Rectangular boxes, pme_order 4, one GPU, charges only (no LJ-PME, no free-energy
+ * grids).  The real-space half is nbx_compute* with coulomb = NBX_COULOMB_EWALD and
+ * the same Ewald coefficient.  Device layouts: real grid [nx][ny][nz] floats (z
+ * fastest); half-complex grid [nx][ny][nz/2+1] of {re, im} float pairs. */
+typedef struct nbx_pme nbx_pme;
+
+/* Replaces calc_ewaldcoeff_q (src/gromacs/ewald/ewald_utils.h:68): the Ewald
+ * coefficient beta with erfc(beta rc) = ewald_rtol (<= 0 means 1e-5); 0 for rc <= 0. */
+float nbx_ewald_coefficient(float rcoulomb, float ewald_rtol);
+
+/* Replaces calcFftGrid (src/gromacs/fft/calcgrid.h:46) with minGridPointsPerDim =
+ * 2 (pme_order - 1): grid sizes n[3] for box edges box[3] and the largest spacing. */
+int nbx_pme_grid_size(const float* box, float spacing, int* n);
+
+/* Replaces gmx_pme_init (src/gromacs/ewald/pme.h:140): box[3] edges (nm), grid[3]
+ * sizes (6..4096 each), the Ewald coefficient, epsilon_r (<= 0 means 1). */
+int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float epsilon_r, int device, nbx_pme** out);
+/* Replaces gmx_pme_destroy (src/gromacs/ewald/pme.h:168). */
+int         nbx_pme_destroy(nbx_pme* p);
+const char* nbx_pme_last_error(const nbx_pme* p);
+int         nbx_pme_set_stream(nbx_pme* p, void* cuda_stream);
+int         nbx_pme_synchronize(nbx_pme* p);
+/* grid[3] sizes and the Ewald coefficient (either may be NULL). */
+int nbx_pme_get_info(const nbx_pme* p, int* grid, float* ewaldcoeff_q);
+
+/* Replaces gmx_pme_do (src/gromacs/ewald/pme.h:181) for the Coulomb grid: spreads the
+ * charges d_q[N] at d_x[3N] (device, atom order, any image within two box lengths of
+ * the unit cell), solves, and ADDS the reciprocal-space forces to d_f[3N].  d_energy
+ * (double[1]) and d_virial (double[9]) may be NULL; when either is given the solve
+ * sums the energy and virial (FP64).  Asynchronous on the handle's stream. */
+int nbx_pme_compute_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_f, double* d_energy,
+                           double* d_virial);
+
+/* The stages of nbx_pme_compute_device one at a time, as the reference's PME tests
+ * drive them (src/gromacs/ewald/tests/pmetestcommon.h: pmePerformSplineAndSpread,
+ * pmePerformSolve, pmePerformGather):
+ *  splines: gridline indices d_idx[N][3], weights d_theta[3][N][4], derivatives d_dtheta[3][N][4];
+ *  spread:  overwrites the real grid d_grid with the spread charges;
+ *  solve:   scales the half-complex grid d_cgrid in place, optional energy / virial;
+ *  gather:  adds the forces interpolated from the real grid d_grid to d_f. */
+int nbx_pme_splines_device(nbx_pme* p, int natoms, const float* d_x, int* d_idx, float* d_theta, float* d_dtheta);
+int nbx_pme_spread_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_grid);
+int nbx_pme_solve_device(nbx_pme* p, void* d_cgrid, double* d_energy, double* d_virial);
+int nbx_pme_gather_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* d_grid, float* d_f);
+
 #ifdef __cplusplus
 }
 #endif
