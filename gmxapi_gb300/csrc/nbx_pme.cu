@@ -17,8 +17,9 @@
 //  - the force gather (gather_f_bsplines / do_fspline,
 //    src/gromacs/ewald/pme_gather.cpp:78-360).
 // The 3-D real<->complex transforms are cuFFT's (unnormalised both ways, like the
-// reference's).  Spreading accumulates with float atomics; the energy and the
-// virial are reduced in FP64.
+// reference's).  Spreading accumulates with float atomics (16-byte vector reductions
+// when nz is a multiple of 4); the energy and the virial terms are summed per warp in
+// float and across the grid in FP64.
 //
 // Layouts in device memory: real grid [nx][ny][nz] (z fastest); half-complex grid
 // [nx][ny][nz/2+1] of float2 (the r2c output of cuFFT), so the complex index
@@ -30,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -116,7 +118,39 @@ __global__ void k_pme_splines(PmeDims d, int natoms, const float* __restrict__ x
     }
 }
 
-// Four threads per atom (one x point each), 16 atomic adds per thread.
+__device__ __forceinline__ void red_add_v4(float* addr, float a, float b, float c, float d)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d));
+}
+
+// The four z points gz0..gz0+3 of one (x, y) grid row as 16-byte vector reductions:
+// with nz a multiple of 4 (and a 16-byte aligned grid) they fall in the aligned blocks
+// [gz0 & ~3, +4) and the next one (periodic), which receive the weights shifted by gz0 & 3.
+__device__ __forceinline__ void spread_row_v4(float* row, int gz0, int nz, const float w[4])
+{
+    const int a  = gz0 & 3;
+    float*    pa = row + (gz0 - a);
+    float*    pb = row + (gz0 - a + 4 == nz ? 0 : gz0 - a + 4);
+    switch (a)
+    {
+        case 0: red_add_v4(pa, w[0], w[1], w[2], w[3]); break;
+        case 1:
+            red_add_v4(pa, 0.0f, w[0], w[1], w[2]);
+            red_add_v4(pb, w[3], 0.0f, 0.0f, 0.0f);
+            break;
+        case 2:
+            red_add_v4(pa, 0.0f, 0.0f, w[0], w[1]);
+            red_add_v4(pb, w[2], w[3], 0.0f, 0.0f);
+            break;
+        default:
+            red_add_v4(pa, 0.0f, 0.0f, 0.0f, w[0]);
+            red_add_v4(pb, w[1], w[2], w[3], 0.0f);
+            break;
+    }
+}
+
+// Four threads per atom (one x point each); each adds its 4 x 4 (y, z) weights.
+template<bool kVec>
 __global__ void k_pme_spread(PmeDims d, int natoms, const float* __restrict__ x, const float* __restrict__ q,
                              float* grid)
 {
@@ -145,27 +179,52 @@ __global__ void k_pme_spread(PmeDims d, int natoms, const float* __restrict__ x,
         const int   gy  = wrap_once(s.i0[1] + iy, d.n[1]);
         const float vxy = vx * s.th[1][iy];
         float*      row = grid + ((size_t)gx * d.n[1] + gy) * d.n[2];
+        float       w[kOrder];
         for (int iz = 0; iz < kOrder; iz++)
         {
-            atomicAdd(&row[gz[iz]], vxy * s.th[2][iz]);
+            w[iz] = vxy * s.th[2][iz];
+        }
+        if (kVec)
+        {
+            spread_row_v4(row, s.i0[2], d.n[2], w);
+        }
+        else
+        {
+            for (int iz = 0; iz < kOrder; iz++)
+            {
+                atomicAdd(&row[gz[iz]], w[iz]);
+            }
         }
     }
 }
 
+constexpr int kSolveThreads   = 256;
+constexpr int kSolveMaxBlocks = 4096;  // one point per thread up to 1M points, grid-stride above
+// With energies, 2 blocks per SM (grid-stride): each block adds once to the completion
+// counter, and thousands of same-address atomics would serialise in L2.
+constexpr int kSolveEnergyBlocksPerSm = 2;
+
 // solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
-// energy and virial terms in FP64 (energy = 0.5 sum, virial = 0.25 sum).
-__global__ void k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ bsp, float elfac, float factor,
-                            float pivol, double* sums, int energy)
+// energy and virial terms (energy = 0.5 sum, virial = 0.25 sum).  Per-point terms and
+// per-thread / per-warp sums are float (the reference sums them in `real`); each block
+// writes its 7 sums in FP64 to partials[block][8] and the last block to finish sums the
+// partials in FP64 (no same-address atomics on the sums).
+__global__ void __launch_bounds__(kSolveThreads) k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ bsp,
+                                                             float elfac, float factor, float pivol, double* partials,
+                                                             unsigned int* done, double* energy_out,
+                                                             double* virial_out)
 {
-    const int nzc    = d.n[2] / 2 + 1;
-    const int total  = d.n[0] * d.n[1] * nzc;
-    const int t      = blockIdx.x * blockDim.x + threadIdx.x;
-    double    acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
-    if (t < total)
+    const bool energy = energy_out || virial_out;
+    const int  nzc    = d.n[2] / 2 + 1;
+    const int  total  = d.n[0] * d.n[1] * nzc;
+    float      acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    // (kx, ky, kz) of t, advanced by the grid stride with carries instead of divisions
+    const int t0     = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    int       kz = t0 % nzc, ky = (t0 / nzc) % d.n[1], kx = t0 / (nzc * d.n[1]);
+    const int sz = stride % nzc, sy = (stride / nzc) % d.n[1], sx = stride / (nzc * d.n[1]);
+    for (int t = t0; t < total; t += stride)
     {
-        const int kz = t % nzc;
-        const int ky = (t / nzc) % d.n[1];
-        const int kx = t / (nzc * d.n[1]);
         if (kx != 0 || ky != 0 || kz != 0)
         {
             const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
@@ -180,33 +239,92 @@ __global__ void k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ 
             float2      c     = cgrid[t];
             if (energy)
             {
-                const double corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5 : 1.0;
-                const double struct2 = 2.0 * ((double)c.x * c.x + (double)c.y * c.y);
-                const double ets2    = corner * (double)eterm * struct2;
-                const double m2d     = (double)m2;
-                const double vf      = ((double)factor * m2d + 1.0) * 2.0 / m2d;
-                acc[0]               = ets2;
-                acc[1]               = ets2 * vf * mhx * mhx - ets2;
-                acc[2]               = ets2 * vf * mhx * mhy;
-                acc[3]               = ets2 * vf * mhx * mhz;
-                acc[4]               = ets2 * vf * mhy * mhy - ets2;
-                acc[5]               = ets2 * vf * mhy * mhz;
-                acc[6]               = ets2 * vf * mhz * mhz - ets2;
+                const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
+                const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
+                const float ets2    = corner * eterm * struct2;
+                const float ets2vf  = ets2 * ((factor * m2 + 1.0f) * 2.0f / m2);
+                acc[0] += ets2;
+                acc[1] += ets2vf * mhx * mhx - ets2;
+                acc[2] += ets2vf * mhx * mhy;
+                acc[3] += ets2vf * mhx * mhz;
+                acc[4] += ets2vf * mhy * mhy - ets2;
+                acc[5] += ets2vf * mhy * mhz;
+                acc[6] += ets2vf * mhz * mhz - ets2;
             }
             c.x *= eterm;
             c.y *= eterm;
             cgrid[t] = c;
         }
+        kz += sz;
+        int carry = 0;
+        if (kz >= nzc)
+        {
+            kz -= nzc;
+            carry = 1;
+        }
+        ky += sy + carry;
+        carry = 0;
+        if (ky >= d.n[1])
+        {
+            ky -= d.n[1];
+            carry = 1;
+        }
+        kx += sx + carry;
     }
     if (!energy)
     {
         return;
     }
-    __shared__ double red[7][32];
+    __shared__ double red[7][kSolveThreads / 32];
+    __shared__ bool   last;
     const int         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = 0; k < 7; k++)
     {
-        double v = acc[k];
+        float v = acc[k];
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        }
+        if (lane == 0)
+        {
+            red[k][warp] = (double)v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 7)
+    {
+        double v = 0.0;
+        for (int w = 0; w < kSolveThreads / 32; w++)
+        {
+            v += red[threadIdx.x][w];
+        }
+        partials[blockIdx.x * 8 + threadIdx.x] = v;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last)
+    {
+        return;
+    }
+    // the last block: FP64 sum of every block's partials
+    __threadfence();
+    double sum[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    {
+        for (int k = 0; k < 7; k++)
+        {
+            sum[k] += __ldcg(&partials[b * 8 + k]);
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < 7; k++)
+    {
+        double v = sum[k];
         for (int o = 16; o > 0; o >>= 1)
         {
             v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -217,17 +335,31 @@ __global__ void k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ 
         }
     }
     __syncthreads();
-    if (threadIdx.x < 7)
+    if (threadIdx.x == 0)
     {
-        double v = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+        double tot[7];
+        for (int k = 0; k < 7; k++)
         {
-            v += red[threadIdx.x][w];
+            tot[k] = 0.0;
+            for (int w = 0; w < kSolveThreads / 32; w++)
+            {
+                tot[k] += red[k][w];
+            }
         }
-        if (v != 0.0)
+        if (energy_out)
         {
-            atomicAdd(&sums[threadIdx.x], v);
+            energy_out[0] = 0.5 * tot[0];
         }
+        if (virial_out)
+        {
+            virial_out[0]                 = 0.25 * tot[1];
+            virial_out[1] = virial_out[3] = 0.25 * tot[2];
+            virial_out[2] = virial_out[6] = 0.25 * tot[3];
+            virial_out[4]                 = 0.25 * tot[4];
+            virial_out[5] = virial_out[7] = 0.25 * tot[5];
+            virial_out[8]                 = 0.25 * tot[6];
+        }
+        *done = 0u;  // ready for the next solve on this stream
     }
 }
 
@@ -275,27 +407,6 @@ __global__ void k_pme_gather(PmeDims d, int natoms, const float* __restrict__ x,
     f[3 * a + 0] -= qa * (fx * (float)d.n[0] * d.rec[0]);
     f[3 * a + 1] -= qa * (fy * (float)d.n[1] * d.rec[1]);
     f[3 * a + 2] -= qa * (fz * (float)d.n[2] * d.rec[2]);
-}
-
-__global__ void k_pme_finish(const double* sums, double* energy, double* virial)
-{
-    if (threadIdx.x != 0)
-    {
-        return;
-    }
-    if (energy)
-    {
-        energy[0] = 0.5 * sums[0];
-    }
-    if (virial)
-    {
-        virial[0] = 0.25 * sums[1];
-        virial[1] = virial[3] = 0.25 * sums[2];
-        virial[2] = virial[6] = 0.25 * sums[3];
-        virial[4]             = 0.25 * sums[4];
-        virial[5] = virial[7] = 0.25 * sums[5];
-        virial[8]             = 0.25 * sums[6];
-    }
 }
 
 // calcFftGrid for one dimension: the smallest listed size with spacing <= the target
@@ -381,7 +492,9 @@ struct nbx_pme
     float*       grid      = nullptr;  // real grid [nx][ny][nz]
     float2*      cgrid     = nullptr;  // half-complex grid [nx][ny][nz/2+1]
     float*       bsp       = nullptr;  // spline moduli x | y | z
-    double*      sums      = nullptr;  // energy + 6 virial terms
+    double*      sums      = nullptr;  // solve partials [kSolveMaxBlocks][8]: energy + 6 virial terms
+    unsigned*    done      = nullptr;  // blocks of the running solve that have written their partials
+    int          num_sms   = 1;
     cufftHandle  r2c = 0, c2r = 0;
     bool         plan_r2c = false, plan_c2r = false;
     std::string  err;
@@ -414,40 +527,36 @@ size_t complex_points(const nbx_pme* p)
 cudaError_t launch_spread(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* grid)
 {
     cudaError_t e = cudaMemsetAsync(grid, 0, sizeof(float) * real_points(p), p->stream);
-    if (e == cudaSuccess && natoms > 0)
+    if (e != cudaSuccess || natoms == 0)
     {
-        k_pme_spread<<<(int)((4LL * natoms + 255) / 256), 256, 0, p->stream>>>(p->d, natoms, d_x, d_q, grid);
-        e = cudaGetLastError();
+        return e;
     }
-    return e;
+    const int  blocks = (int)((4LL * natoms + 255) / 256);
+    const bool vec    = p->d.n[2] % 4 == 0 && (reinterpret_cast<uintptr_t>(grid) & 15) == 0;
+    if (vec)
+    {
+        k_pme_spread<true><<<blocks, 256, 0, p->stream>>>(p->d, natoms, d_x, d_q, grid);
+    }
+    else
+    {
+        k_pme_spread<false><<<blocks, 256, 0, p->stream>>>(p->d, natoms, d_x, d_q, grid);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_solve(nbx_pme* p, float2* cgrid, double* d_energy, double* d_virial)
 {
-    const bool   energy = d_energy || d_virial;
-    const double vol    = (double)p->box[0] * p->box[1] * p->box[2];
+    const double vol = (double)p->box[0] * p->box[1] * p->box[2];
     // elfac = ONE_4PI_EPS0 / epsilon_r, factor = pi^2 / beta^2 (pme_solve.cpp:341,354), in float like `real`
-    const float elfac  = (float)nbx::one_4pi_eps0() / p->epsilon_r;
-    const float factor = (float)(M_PI * M_PI) / (p->beta * p->beta);
-    const float pivol  = (float)M_PI * (float)vol;
-    cudaError_t e      = cudaSuccess;
-    if (energy)
-    {
-        e = cudaMemsetAsync(p->sums, 0, sizeof(double) * 8, p->stream);
-    }
-    if (e == cudaSuccess)
-    {
-        const int nc = (int)complex_points(p);
-        k_pme_solve<<<(nc + 255) / 256, 256, 0, p->stream>>>(p->d, cgrid, p->bsp, elfac, factor, pivol, p->sums,
-                                                              energy ? 1 : 0);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess && energy)
-    {
-        k_pme_finish<<<1, 32, 0, p->stream>>>(p->sums, d_energy, d_virial);
-        e = cudaGetLastError();
-    }
-    return e;
+    const float elfac   = (float)nbx::one_4pi_eps0() / p->epsilon_r;
+    const float factor  = (float)(M_PI * M_PI) / (p->beta * p->beta);
+    const float pivol   = (float)M_PI * (float)vol;
+    const int   nc      = (int)complex_points(p);
+    const int   cap     = (d_energy || d_virial) ? kSolveEnergyBlocksPerSm * p->num_sms : kSolveMaxBlocks;
+    const int   nblocks = std::max(1, std::min((nc + kSolveThreads - 1) / kSolveThreads, cap));
+    k_pme_solve<<<nblocks, kSolveThreads, 0, p->stream>>>(p->d, cgrid, p->bsp, elfac, factor, pivol, p->sums,
+                                                          p->done, d_energy, d_virial);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_gather(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* grid, float* d_f)
@@ -541,7 +650,10 @@ int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float 
     if (e == cudaSuccess) e = cudaMalloc(&p->grid, sizeof(float) * real_points(p));
     if (e == cudaSuccess) e = cudaMalloc(&p->cgrid, sizeof(float2) * complex_points(p));
     if (e == cudaSuccess) e = cudaMalloc(&p->bsp, sizeof(float) * (grid[0] + grid[1] + grid[2]));
-    if (e == cudaSuccess) e = cudaMalloc(&p->sums, sizeof(double) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&p->sums, sizeof(double) * 8 * kSolveMaxBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&p->done, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(p->done, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess)
     {
         std::vector<float> mod(grid[0] + grid[1] + grid[2]);
@@ -592,6 +704,7 @@ int nbx_pme_destroy(nbx_pme* p)
     cudaFree(p->cgrid);
     cudaFree(p->bsp);
     cudaFree(p->sums);
+    cudaFree(p->done);
     if (p->own_stream)
     {
         cudaStreamDestroy(p->stream);
