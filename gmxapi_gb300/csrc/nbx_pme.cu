@@ -200,9 +200,9 @@ __global__ void k_pme_spread(PmeDims d, int natoms, const float* __restrict__ x,
 
 constexpr int kSolveThreads   = 256;
 constexpr int kSolveMaxBlocks = 4096;  // one point per thread up to 1M points, grid-stride above
-// With energies, 2 blocks per SM (grid-stride): each block adds once to the completion
+// With energies, 4 blocks per SM (grid-stride): each block adds once to the completion
 // counter, and thousands of same-address atomics would serialise in L2.
-constexpr int kSolveEnergyBlocksPerSm = 2;
+constexpr int kSolveEnergyBlocksPerSm = 4;
 
 // solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
 // energy and virial terms (energy = 0.5 sum, virial = 0.25 sum).  Per-point terms and
