@@ -615,6 +615,46 @@ def measure_pme(dev: int, calc=None, frames=None, flush=None, stream=None, steps
     }
 
 
+def measure_md(dev: int, steps: int = 200, warmup: int = 20) -> dict:
+    """GPU-resident MD steps (nbx_md_run_device): cluster-pair LJ + Ewald real space, PME
+    reciprocal space and leap-frog on one stream, for 296,352 argon-like atoms with charges
+    +-0.3 e (fcc start at 120 K, box 22.08 nm, rc 0.9, rlist 1.0, nstlist 10, PME grid at
+    0.12 nm, dt 2 fs), energies every 100 steps.  Reports the step time and the NVE drift."""
+    import torch
+
+    from gmxapi_gb300 import md, nblib, systems
+
+    s = systems.lj_fcc(cells=42, lattice=0.5256, charge=0.3, seed=1)
+    rng = np.random.default_rng(2)
+    v0 = (rng.standard_normal((s.n, 3)) * math.sqrt(0.00831446 * 120.0 / systems.ARGON_MASS)).astype(np.float32)
+    opts = nblib.NBKernelOptions(pairlist_cutoff=1.0, rcoulomb=0.9, nstlist=10, compute_virial_and_energy=True)
+    run = md.MdRunner(s, np.full(s.n, systems.ARGON_MASS, np.float32), opts, dt=0.002, velocities=v0, pme=True,
+                      fourier_spacing=PME_SPACING, device=dev)
+    run.run(warmup, nstcalcenergy=warmup)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    a.record(run.stream)
+    rows = run.run(steps, nstcalcenergy=100)
+    b.record(run.stream)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) * 1e3
+    ms = a.elapsed_time(b)
+    etot = rows.sum(axis=1)
+    out = {
+        "atoms": s.n, "box_nm": float(s.box[0]), "pme_grid": list(run.pme.grid), "steps": steps,
+        "ms_per_step": ms / steps, "wall_ms_per_step": wall / steps,
+        "ns_per_day": 0.002 * steps / (ms * 1e-3) * 86400 / 1000,
+        "atom_steps_per_s": s.n * steps / (ms * 1e-3),
+        "energy_rows": rows.tolist(),
+        "drift_kj_mol": float(etot[-1] - etot[0]), "mean_ekin_kj_mol": float(rows[:, 3].mean()),
+        "note": "device-timed over the whole loop (searches every 10 steps included); ns/day at dt 2 fs",
+    }
+    run.close()
+    return out
+
+
 def workload_config() -> dict:
     return {"workload": "spc_water_288k", "atoms": 288000, "box_nm": 14.21, "rc_nm": RC, "rlist_nm": RLIST,
             "rlist_inner_nm": RLIST_INNER, "nstlist": NSTLIST, "nstlist_prune": NSTPRUNE,
@@ -728,6 +768,7 @@ def run_ours(args) -> None:
     adjoint = measure_adjoint(dev) if not args.no_extras else None
     force_matching = measure_force_matching(dev) if not args.no_extras else None
     pme_block = measure_pme(dev, calc, frames, flush, stream) if not args.no_extras else None
+    md_block = measure_md(dev) if not args.no_extras else None
 
     peak = measure_fp32_peak(dev)
     pairs_avg = 0.5 * (pairs0 + pairs1)
@@ -764,6 +805,8 @@ def run_ours(args) -> None:
         line["force_matching"] = force_matching
     if pme_block is not None:
         line["pme"] = pme_block
+    if md_block is not None:
+        line["md"] = md_block
     print(json.dumps(line))
 
 
@@ -775,7 +818,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-ensemble, adjoint and force-matching measurements")
-    ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching", "pme"],
+    ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching", "pme", "md"],
                     help="run one of the extra measurements alone and print its JSON (profiling)")
     args = ap.parse_args()
     if args.only:
@@ -783,7 +826,7 @@ def main():
 
         torch.cuda.set_device(0)
         fn = {"ensemble": measure_ensemble, "adjoint": measure_adjoint, "force_matching": measure_force_matching,
-              "pme": measure_pme}
+              "pme": measure_pme, "md": measure_md}
         print(json.dumps({args.only: fn[args.only](0)}))
         return
     if args.impl == "reference":

@@ -49,6 +49,9 @@ EXPORTED = [
     "nbx_ewald_coefficient", "nbx_pme_grid_size", "nbx_pme_create", "nbx_pme_destroy", "nbx_pme_last_error",
     "nbx_pme_set_stream", "nbx_pme_synchronize", "nbx_pme_get_info", "nbx_pme_compute_device",
     "nbx_pme_splines_device", "nbx_pme_spread_device", "nbx_pme_solve_device", "nbx_pme_gather_device",
+    "nbx_get_options", "nbx_set_force_accumulate", "nbx_leapfrog_create", "nbx_leapfrog_destroy",
+    "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
+    "nbx_md_run_device",
 ]
 
 
@@ -194,11 +197,21 @@ def load():
     L.nbx_pme_spread_device.argtypes = [vp, C.c_int, vp, vp, vp]
     L.nbx_pme_solve_device.argtypes = [vp, vp, vp, vp]
     L.nbx_pme_gather_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.nbx_get_options.argtypes = [vp, C.POINTER(nbx_options)]
+    L.nbx_set_force_accumulate.argtypes = [vp, C.c_int]
+    L.nbx_leapfrog_create.argtypes = [C.c_int, fp, fp, C.c_int, C.POINTER(vp)]
+    L.nbx_leapfrog_destroy.argtypes = [vp]
+    L.nbx_leapfrog_last_error.argtypes = [vp]
+    L.nbx_leapfrog_last_error.restype = C.c_char_p
+    L.nbx_leapfrog_set_stream.argtypes = [vp, vp]
+    L.nbx_leapfrog_integrate.argtypes = [vp, C.c_float, fp, fp, fp]
+    L.nbx_leapfrog_integrate_device.argtypes = [vp, C.c_float, vp, vp, vp, vp]
+    L.nbx_md_run_device.argtypes = [vp, vp, vp, C.c_longlong, C.c_int, C.c_float, vp, vp, vp, vp, C.c_int, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",
                                                 "nbx_batch_last_error", "nbx_pme_last_error",
-                                                "nbx_ewald_coefficient"):
+                                                "nbx_ewald_coefficient", "nbx_leapfrog_last_error"):
             f.restype = C.c_int
     _lib = L
     return L

@@ -30,6 +30,7 @@ UNITS = {
     "nbx_balance.cu": [],
     "nbx_api.cu": [],
     "nbx_pme.cu": [],
+    "nbx_md.cu": [],
 }
 
 

@@ -824,7 +824,11 @@ int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, doubl
     {
         return rc;
     }
+    // host arrays: forces are overwritten (GmxForceCalculator::compute), whatever nbx_set_force_accumulate says
+    const int accumulate = h->v.accumulate_f;
+    h->v.accumulate_f    = 0;
     rc = compute_async(h, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    h->v.accumulate_f = accumulate;
     if (rc != NBX_OK)
     {
         return rc;
@@ -950,7 +954,10 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
     {
         return rc;
     }
+    const int accumulate = h->v.accumulate_f;  // host arrays: forces are overwritten
+    h->v.accumulate_f    = 0;
     rc = nbx_md_step_device(h, step, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    h->v.accumulate_f = accumulate;
     if (rc != NBX_OK)
     {
         return rc;
@@ -1051,6 +1058,26 @@ int nbx_set_wait_test(nbx_handle* h, int enable)
         return NBX_ERR_INVALID_INPUT;
     }
     h->v.wait_test_bytes = enable ? 16u : 0u;
+    return NBX_OK;
+}
+
+int nbx_get_options(const nbx_handle* h, nbx_options* out)
+{
+    if (!h || !out)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    *out = h->opts;
+    return NBX_OK;
+}
+
+int nbx_set_force_accumulate(nbx_handle* h, int enable)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    h->v.accumulate_f = enable ? 1 : 0;
     return NBX_OK;
 }
 

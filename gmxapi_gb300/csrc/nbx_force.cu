@@ -244,9 +244,18 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
         {
             const int    k  = v.cells[a];
             const float4 fa = v.fnb[k];
-            f[3 * a]        = fa.x;
-            f[3 * a + 1]    = fa.y;
-            f[3 * a + 2]    = fa.z;
+            if (v.accumulate_f)
+            {
+                f[3 * a] += fa.x;
+                f[3 * a + 1] += fa.y;
+                f[3 * a + 2] += fa.z;
+            }
+            else
+            {
+                f[3 * a]     = fa.x;
+                f[3 * a + 1] = fa.y;
+                f[3 * a + 2] = fa.z;
+            }
             if (do_virial)
             {
                 const float4 xa   = v.xq[k];

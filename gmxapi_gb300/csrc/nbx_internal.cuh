@@ -173,6 +173,9 @@ struct DeviceView
     float beta2l2;  // beta^2 log2(e)
     float c2b;      // 2 beta / sqrt(pi)
     float k_rf2;    // 2 k_rf
+    // 1: k_reduce_f adds the nonbonded forces to the caller's buffer
+    // (nbnxn_gpu_add_nbat_f_to_f_kernel<accumulateForce = true>); 0: overwrites it
+    int accumulate_f;
 };
 
 // One system of a batch, as the batched kernels see it (device table).

@@ -225,6 +225,10 @@ class ForceCalculator:
         check(_lib.load().nbx_get_timings(self.h, C.byref(ms), cnt, int(reset)), self.h)
         return float(ms.value), int(cnt[0]), int(cnt[1])
 
+    def set_force_accumulate(self, enable: bool):
+        """Device calls add the nonbonded forces to the force buffer instead of overwriting it."""
+        check(_lib.load().nbx_set_force_accumulate(self.h, int(bool(enable))), self.h)
+
     def set_list_balance(self, entries_per_sm: int):
         """Entries per SM below which long list entries are split (0: never); next search."""
         check(_lib.load().nbx_set_list_balance(self.h, int(entries_per_sm)), self.h)

@@ -153,6 +153,38 @@ def water_large(seed: int = 2) -> System:
     return spc_water(96000, 14.21, seed)
 
 
+ARGON_SIGMA, ARGON_EPSILON, ARGON_MASS = 0.3405, 0.996, 39.948
+
+
+def lj_fcc(cells: int = 6, lattice: float = 0.5256, charge: float = 0.0, seed: int = 0) -> System:
+    """Argon-like Lennard-Jones atoms on an fcc lattice (4 per cubic cell of edge `lattice`),
+    one type; with `charge` > 0 half of the atoms (seeded choice) carry +charge and half -charge.
+    A relaxed starting structure for MD (no overlaps), unlike the random liquids."""
+    rng = np.random.default_rng(seed)
+    g = np.arange(cells, dtype=np.float64)
+    corners = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 1, 3)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])[None] + 0.25
+    x = ((corners + basis).reshape(-1, 3) * lattice).astype(np.float32)
+    n = x.shape[0]
+    q = np.zeros(n, np.float32)
+    if charge > 0:
+        sign = np.ones(n)
+        sign[rng.permutation(n)[: n // 2]] = -1.0
+        q = (sign * charge).astype(np.float32)
+    c6, c12 = lj_c6_c12(ARGON_SIGMA, ARGON_EPSILON)
+    return System(
+        x=x,
+        box=np.full(3, cells * lattice, dtype=np.float32),
+        q=q,
+        type=np.zeros(n, np.int32),
+        ntypes=1,
+        nbfp=nbfp_from_c6c12(np.array([[c6]]), np.array([[c12]])),
+        excl_index=np.arange(n + 1, dtype=np.int32),
+        excl_list=np.arange(n, dtype=np.int32),
+        name=f"ljfcc{n}",
+    )
+
+
 #: Madelung constant of the rock-salt lattice, referred to the nearest-neighbour distance
 MADELUNG_ROCK_SALT = 1.747564594633182
 

@@ -165,6 +165,13 @@ int nbx_set_wait_test(nbx_handle* h, int enable);
 /* GPU list balancing (pairlist.cpp split_sci_entry / sort_sci): entries are split when the grid
  * has fewer than entries_per_sm x SMs cells (default 44, the reference's factor; 0 = never
  * split; entries are always sorted large-first).  Takes effect at the next search. */
+/* The options the handle was created with. */
+int nbx_get_options(const nbx_handle* h, nbx_options* out);
+/* 1: nbx_compute_device / nbx_md_step_device ADD the nonbonded forces to d_f (mdrun's
+ * nbnxn_gpu_add_nbat_f_to_f_kernel with accumulateForce, nbnxm_buffer_ops_kernels.cuh:134),
+ * e.g. after bonded or PME forces; 0 (default): they overwrite d_f.  The host-array calls
+ * (nbx_compute, nbx_md_step) always overwrite. */
+int nbx_set_force_accumulate(nbx_handle* h, int enable);
 int nbx_set_list_balance(nbx_handle* h, int entries_per_sm);
 /* out[4] = {min_ci_balanced, split target in cluster pairs (0: none), entries before
  * splitting, entries after} of the current list. */
@@ -323,6 +330,34 @@ int nbx_pme_splines_device(nbx_pme* p, int natoms, const float* d_x, int* d_idx,
 int nbx_pme_spread_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_grid);
 int nbx_pme_solve_device(nbx_pme* p, void* d_cgrid, double* d_energy, double* d_virial);
 int nbx_pme_gather_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* d_grid, float* d_f);
+
+/* ---- GPU-resident MD steps: leap-frog and the step loop ---- */
+typedef struct nbx_leapfrog nbx_leapfrog;
+
+/* Replaces nblib::LeapFrog::LeapFrog (api/nblib/integrator.h:71): inverse masses inv_mass[N]
+ * (host, finite, >= 0) and the rectangular box edges box[3]. */
+int         nbx_leapfrog_create(int num_atoms, const float* inv_mass, const float* box, int device,
+                                nbx_leapfrog** out);
+int         nbx_leapfrog_destroy(nbx_leapfrog* p);
+const char* nbx_leapfrog_last_error(const nbx_leapfrog* p);
+int         nbx_leapfrog_set_stream(nbx_leapfrog* p, void* cuda_stream);
+/* Replaces nblib::LeapFrog::integrate (api/nblib/integrator.h:84): v += f dt / m; x += v dt;
+ * put_atoms_in_box.  Host arrays [3N], updated in place. */
+int nbx_leapfrog_integrate(nbx_leapfrog* p, float dt, float* x, float* v, const float* f);
+/* The same on device arrays, asynchronous on the handle's stream; d_ekin (double[1], may be
+ * NULL) receives 0.5 (KE(t - dt/2) + KE(t + dt/2)), summed in FP64. */
+int nbx_leapfrog_integrate_device(nbx_leapfrog* p, float dt, float* d_x, float* d_v, const float* d_f,
+                                  double* d_ekin);
+
+/* num_steps GPU-resident MD steps from first_step (mdrun's do_force + update, sim_util.cpp):
+ * nonbonded forces with the handle's search / rolling-prune schedule (nbx_md_step_device),
+ * PME forces added when pme is not NULL (charges d_q[N]), leap-frog update of d_x / d_v;
+ * atoms are put in the box only on the update before a search step.  All on h's stream.
+ * Every nstcalcenergy steps (counted from first_step) a row of d_energies receives
+ * {E_LJ, E_Coulomb real space, E_Coulomb reciprocal, E_kin} (FP64; E_kin as in
+ * nbx_leapfrog_integrate_device); d_energies may be NULL. */
+int nbx_md_run_device(nbx_handle* h, nbx_pme* pme, nbx_leapfrog* lf, long long first_step, int num_steps, float dt,
+                      float* d_x, float* d_v, float* d_f, const float* d_q, int nstcalcenergy, double* d_energies);
 
 #ifdef __cplusplus
 }
