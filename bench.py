@@ -618,13 +618,13 @@ def measure_pme(dev: int, calc=None, frames=None, flush=None, stream=None, steps
 def measure_md(dev: int, steps: int = 200, warmup: int = 20) -> dict:
     """GPU-resident MD steps (nbx_md_run_device): cluster-pair LJ + Ewald real space, PME
     reciprocal space and leap-frog on one stream, for 296,352 argon-like atoms with charges
-    +-0.3 e (fcc start at 120 K, box 22.08 nm, rc 0.9, rlist 1.0, nstlist 10, PME grid at
+    +-0.1 e (fcc start at 120 K, box 22.08 nm, rc 0.9, rlist 1.0, nstlist 10, PME grid at
     0.12 nm, dt 2 fs), energies every 100 steps.  Reports the step time and the NVE drift."""
     import torch
 
     from gmxapi_gb300 import md, nblib, systems
 
-    s = systems.lj_fcc(cells=42, lattice=0.5256, charge=0.3, seed=1)
+    s = systems.lj_fcc(cells=42, lattice=0.5256, charge=0.1, seed=1)
     rng = np.random.default_rng(2)
     v0 = (rng.standard_normal((s.n, 3)) * math.sqrt(0.00831446 * 120.0 / systems.ARGON_MASS)).astype(np.float32)
     opts = nblib.NBKernelOptions(pairlist_cutoff=1.0, rcoulomb=0.9, nstlist=10, compute_virial_and_energy=True)

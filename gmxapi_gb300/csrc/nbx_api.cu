@@ -1081,6 +1081,16 @@ int nbx_set_force_accumulate(nbx_handle* h, int enable)
     return NBX_OK;
 }
 
+int nbx_get_force_accumulate(const nbx_handle* h, int* enabled)
+{
+    if (!h || !enabled)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    *enabled = h->v.accumulate_f;
+    return NBX_OK;
+}
+
 int nbx_set_list_balance(nbx_handle* h, int entries_per_sm)
 {
     if (!h || entries_per_sm < 0)

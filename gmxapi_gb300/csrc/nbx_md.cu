@@ -195,6 +195,13 @@ int launch_leapfrog(nbx_leapfrog* p, float dt, float* d_x, float* d_v, const flo
 
 } // namespace
 
+namespace
+{
+int run_steps(nbx_handle* h, nbx_pme* pme, nbx_leapfrog* lf, long long first_step, int num_steps, float dt,
+              float* d_x, float* d_v, float* d_f, const float* d_q, int nstcalcenergy, double* d_energies,
+              int nstlist, int natoms, void* s);
+} // namespace
+
 extern "C" {
 
 const char* nbx_leapfrog_last_error(const nbx_leapfrog* p)
@@ -395,6 +402,26 @@ int nbx_md_run_device(nbx_handle* h, nbx_pme* pme, nbx_leapfrog* lf, long long f
         return rc;
     }
     const int nstlist = std::max(1, opts.nstlist);
+    // each step starts a fresh force buffer: the nonbonded forces overwrite it
+    int accumulate = 0;
+    nbx_get_force_accumulate(h, &accumulate);
+    nbx_set_force_accumulate(h, 0);
+    rc = run_steps(h, pme, lf, first_step, num_steps, dt, d_x, d_v, d_f, d_q, nstcalcenergy, d_energies, nstlist,
+                   natoms, s);
+    nbx_set_force_accumulate(h, accumulate);
+    return rc;
+}
+
+} // extern "C"
+
+namespace
+{
+
+int run_steps(nbx_handle* h, nbx_pme* pme, nbx_leapfrog* lf, long long first_step, int num_steps, float dt,
+              float* d_x, float* d_v, float* d_f, const float* d_q, int nstcalcenergy, double* d_energies,
+              int nstlist, int natoms, void* s)
+{
+    int rc = NBX_OK;
     for (int k = 0; k < num_steps; k++)
     {
         const long long step   = first_step + k;
@@ -424,4 +451,4 @@ int nbx_md_run_device(nbx_handle* h, nbx_pme* pme, nbx_leapfrog* lf, long long f
     return NBX_OK;
 }
 
-} // extern "C"
+} // namespace

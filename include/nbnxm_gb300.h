@@ -172,6 +172,7 @@ int nbx_get_options(const nbx_handle* h, nbx_options* out);
  * e.g. after bonded or PME forces; 0 (default): they overwrite d_f.  The host-array calls
  * (nbx_compute, nbx_md_step) always overwrite. */
 int nbx_set_force_accumulate(nbx_handle* h, int enable);
+int nbx_get_force_accumulate(const nbx_handle* h, int* enabled);
 int nbx_set_list_balance(nbx_handle* h, int entries_per_sm);
 /* out[4] = {min_ci_balanced, split target in cluster pairs (0: none), entries before
  * splitting, entries after} of the current list. */
@@ -350,8 +351,9 @@ int nbx_leapfrog_integrate_device(nbx_leapfrog* p, float dt, float* d_x, float* 
                                   double* d_ekin);
 
 /* num_steps GPU-resident MD steps from first_step (mdrun's do_force + update, sim_util.cpp):
- * nonbonded forces with the handle's search / rolling-prune schedule (nbx_md_step_device),
- * PME forces added when pme is not NULL (charges d_q[N]), leap-frog update of d_x / d_v;
+ * nonbonded forces with the handle's search / rolling-prune schedule (nbx_md_step_device)
+ * written to d_f (overwriting, whatever nbx_set_force_accumulate says), PME forces added when
+ * pme is not NULL (charges d_q[N]), leap-frog update of d_x / d_v;
  * atoms are put in the box only on the update before a search step.  All on h's stream.
  * Every nstcalcenergy steps (counted from first_step) a row of d_energies receives
  * {E_LJ, E_Coulomb real space, E_Coulomb reciprocal, E_kin} (FP64; E_kin as in
