@@ -51,7 +51,8 @@ EXPORTED = [
     "nbx_pme_splines_device", "nbx_pme_spread_device", "nbx_pme_solve_device", "nbx_pme_gather_device",
     "nbx_get_options", "nbx_set_force_accumulate", "nbx_get_force_accumulate", "nbx_leapfrog_create", "nbx_leapfrog_destroy",
     "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
-    "nbx_md_run_device",
+    "nbx_md_run_device", "nbx_fep_enable", "nbx_fep_set_lambda", "nbx_fep_get_energies", "nbx_fep_energies_device",
+    "nbx_fep_disable",
 ]
 
 
@@ -108,6 +109,22 @@ class nbx_noalloc_args(C.Structure):
         ("ewald_rtol", C.c_float),
         ("epsilon_rf", C.c_float),
         ("use_ewald_shift", C.c_int),
+    ]
+
+
+class nbx_fep_desc(C.Structure):
+    _fields_ = [
+        ("num_perturbed", C.c_int),
+        ("perturbed", C.POINTER(C.c_int)),
+        ("qB", C.POINTER(C.c_float)),
+        ("typeB", C.POINTER(C.c_int)),
+        ("lambda_coul", C.c_float),
+        ("lambda_vdw", C.c_float),
+        ("alpha_vdw", C.c_float),
+        ("alpha_coul", C.c_float),
+        ("lambda_power", C.c_int),
+        ("sigma6_def", C.c_float),
+        ("sigma6_min", C.c_float),
     ]
 
 
@@ -207,12 +224,19 @@ def load():
     L.nbx_leapfrog_set_stream.argtypes = [vp, vp]
     L.nbx_leapfrog_integrate.argtypes = [vp, C.c_float, fp, fp, fp]
     L.nbx_leapfrog_integrate_device.argtypes = [vp, C.c_float, vp, vp, vp, vp]
+    L.nbx_fep_enable.argtypes = [vp, C.POINTER(nbx_fep_desc)]
+    L.nbx_fep_set_lambda.argtypes = [vp, C.c_float, C.c_float]
+    L.nbx_fep_get_energies.argtypes = [vp, dp]
+    L.nbx_fep_energies_device.argtypes = [vp]
+    L.nbx_fep_energies_device.restype = vp
+    L.nbx_fep_disable.argtypes = [vp]
     L.nbx_md_run_device.argtypes = [vp, vp, vp, C.c_longlong, C.c_int, C.c_float, vp, vp, vp, vp, C.c_int, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",
                                                 "nbx_batch_last_error", "nbx_pme_last_error",
-                                                "nbx_ewald_coefficient", "nbx_leapfrog_last_error"):
+                                                "nbx_ewald_coefficient", "nbx_leapfrog_last_error",
+                                                "nbx_fep_energies_device"):
             f.restype = C.c_int
     _lib = L
     return L

@@ -31,6 +31,7 @@ UNITS = {
     "nbx_api.cu": [],
     "nbx_pme.cu": [],
     "nbx_md.cu": [],
+    "nbx_fep.cu": [],
 }
 
 

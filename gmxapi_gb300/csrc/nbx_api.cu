@@ -70,6 +70,16 @@ struct nbx_handle
     long long   phase_count[5] = { 0, 0, 0, 0, 0 };
     long long   force_launches = 0;
     long long   launches = 0;
+    // free-energy perturbation (nbx_fep_*): the perturbed atoms leave the cluster path
+    bool           fep_on       = false;
+    FepView        fep{};
+    float*         d_fep_q      = nullptr;  // [2N]: state A | state B charges
+    int*           d_fep_t      = nullptr;  // [2N]: state A | state B types
+    int*           d_fep_list   = nullptr;  // [N] perturbed atoms
+    unsigned char* d_fep_pert   = nullptr;  // [N]
+    double*        d_fep_sums   = nullptr;  // [4]
+    double         self_energy_all = 0.0;    // the self energy with every atom, restored on disable
+    int            fep_power       = 1;
 };
 
 namespace nbx
@@ -401,6 +411,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
     }
     // the events bracket the force kernel alone
     if (e == cudaSuccess) e = launch_force(v, energy, h->stream, h->num_sms, e0, e1);
+    if (e == cudaSuccess && h->fep_on) e = launch_fep(v, h->fep, energy, h->stream);
     if (h->timing)
     {
         h->ev_pending.push_back({ e0, e1, 0 });
@@ -426,6 +437,55 @@ bool valid_box(const float* box)
         }
     }
     return true;
+}
+
+} // namespace
+
+namespace
+{
+
+// lambda factors of nb_free_energy.cpp:356-388 (sc-r-power 6)
+void set_fep_lambda(FepView& f, float lam_c, float lam_v, int power)
+{
+    const float lfc[2] = { 1.0f - lam_c, lam_c }, lfv[2] = { 1.0f - lam_v, lam_v }, dlf[2] = { -1.0f, 1.0f };
+    for (int i = 0; i < 2; i++)
+    {
+        f.lfc[i]     = lfc[i];
+        f.lfv[i]     = lfv[i];
+        f.lfac_c[i]  = power == 2 ? (1 - lfc[i]) * (1 - lfc[i]) : (1 - lfc[i]);
+        f.dlfac_c[i] = dlf[i] * power / 6.0f * (power == 2 ? (1 - lfc[i]) : 1.0f);
+        f.lfac_v[i]  = power == 2 ? (1 - lfv[i]) * (1 - lfv[i]) : (1 - lfv[i]);
+        f.dlfac_v[i] = dlf[i] * power / 6.0f * (power == 2 ? (1 - lfv[i]) : 1.0f);
+    }
+}
+
+double self_energy_of(const DeviceView& v, const std::vector<float>& q)
+{
+    double qsq = 0.0;
+    for (float c : q)
+    {
+        qsq += (double)c * (double)c;
+    }
+    return v.coulomb == NBX_COULOMB_EWALD ? -v.epsfac_d * (double)v.beta * 0.56418958354775628695 * qsq
+                                          : -v.epsfac_d * 0.5 * (double)v.c_rf * qsq;
+}
+
+int fep_restore(nbx_handle* h)
+{
+    DeviceView& v = h->v;
+    const int   n = h->n;
+    cudaError_t e = cudaMemcpyAsync(const_cast<float*>(v.q), h->d_fep_q, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                                    h->stream);
+    if (e == cudaSuccess)
+    {
+        e = cudaMemcpyAsync(const_cast<int*>(v.type), h->d_fep_t, sizeof(int) * n, cudaMemcpyDeviceToDevice,
+                            h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    v.self_energy = h->self_energy_all;
+    h->fep_on     = false;
+    h->have_list  = false;
+    return cuda_check(h, e, "free-energy restore");
 }
 
 } // namespace
@@ -996,6 +1056,10 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
     {
         return set_error(h, NBX_ERR_STATE, "no pair list");
     }
+    if (h->fep_on)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint does not cover perturbed atoms");
+    }
     if (h->v.ntypes1 > adjoint_max_types1())
     {
         return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint supports at most 15 particle types");
@@ -1039,6 +1103,10 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
     {
         return NBX_ERR_INVALID_INPUT;
     }
+    if (h->fep_on)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "parameters cannot change while perturbed atoms are set");
+    }
     cudaSetDevice(h->device);
     if (d_q)
     {
@@ -1059,6 +1127,189 @@ int nbx_set_wait_test(nbx_handle* h, int enable)
     }
     h->v.wait_test_bytes = enable ? 16u : 0u;
     return NBX_OK;
+}
+
+int nbx_fep_enable(nbx_handle* h, const nbx_fep_desc* d)
+{
+    if (!h || !d || d->num_perturbed < 0 || d->num_perturbed > h->n
+        || (d->num_perturbed > 0 && (!d->perturbed || !d->qB || !d->typeB)))
+    {
+        return h ? set_error(h, NBX_ERR_INVALID_INPUT, "null argument or bad perturbed-atom count")
+                 : NBX_ERR_INVALID_INPUT;
+    }
+    DeviceView& v = h->v;
+    if (d->lambda_power != 1 && d->lambda_power != 2)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "sc-power must be 1 or 2");
+    }
+    if (!(d->alpha_vdw >= 0.0f) || !(d->alpha_coul >= 0.0f) || !(d->sigma6_def > 0.0f) || !(d->sigma6_min > 0.0f))
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "soft-core alpha must be >= 0 and sigma^6 > 0");
+    }
+    if (v.vdw_mod != NBX_VDW_POTSHIFT && v.vdw_mod != NBX_VDW_NONE)
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "perturbed atoms take the potential-shift or plain LJ cut-off");
+    }
+    for (int k = 0; k < 3; k++)
+    {
+        if (v.g.box[k] < 2.0f * v.rlist)
+        {
+            return set_error(h, NBX_ERR_INVALID_INPUT, "perturbed atoms need box edges of at least 2 rlist");
+        }
+    }
+    const int          n  = h->n;
+    const int          nt = v.ntypes1 - 1;
+    std::vector<char>  seen(n, 0);
+    for (int k = 0; k < d->num_perturbed; k++)
+    {
+        const int a = d->perturbed[k];
+        if (a < 0 || a >= n || seen[a] || d->typeB[k] < 0 || d->typeB[k] >= nt || !std::isfinite(d->qB[k]))
+        {
+            return set_error(h, NBX_ERR_INVALID_INPUT, "perturbed atoms: bad or repeated index, type or charge");
+        }
+        seen[a] = 1;
+    }
+    cudaSetDevice(h->device);
+    if (h->fep_on)
+    {
+        int rc = fep_restore(h);
+        if (rc != NBX_OK)
+        {
+            return rc;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!h->d_fep_q)
+    {
+        e = dalloc(h, &h->d_fep_q, 2 * (size_t)n);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_fep_t, 2 * (size_t)n);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_fep_list, (size_t)n);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_fep_pert, (size_t)n);
+        if (e == cudaSuccess) e = dalloc(h, &h->d_fep_sums, 4);
+        if (e != cudaSuccess)
+        {
+            return set_error(h, NBX_ERR_OUT_OF_MEMORY, "free-energy buffers");
+        }
+    }
+    // state A = the topology's charges and types (on the device)
+    std::vector<float> q(2 * (size_t)n);
+    std::vector<int>   t(2 * (size_t)n);
+    e = cudaMemcpyAsync(q.data(), v.q, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t.data(), v.type, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess)
+    {
+        return cuda_check(h, e, "free-energy setup");
+    }
+    std::copy(q.begin(), q.begin() + n, q.begin() + n);
+    std::copy(t.begin(), t.begin() + n, t.begin() + n);
+    std::vector<unsigned char> pert(n, 0);
+    std::vector<float>         qm(q.begin(), q.begin() + n);
+    std::vector<int>           tm(t.begin(), t.begin() + n);
+    for (int k = 0; k < d->num_perturbed; k++)
+    {
+        const int a = d->perturbed[k];
+        q[n + a]    = d->qB[k];
+        t[n + a]    = d->typeB[k];
+        pert[a]     = 1;
+        qm[a]       = 0.0f;  // masked out of the cluster path (atomdata_mask_fep)
+        tm[a]       = nt;    // the all-zero type
+    }
+    h->self_energy_all = self_energy_of(v, std::vector<float>(q.begin(), q.begin() + n));
+    e = cudaMemcpyAsync(h->d_fep_q, q.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_fep_t, t.data(), sizeof(int) * 2 * n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && d->num_perturbed > 0)
+    {
+        e = cudaMemcpyAsync(h->d_fep_list, d->perturbed, sizeof(int) * d->num_perturbed, cudaMemcpyHostToDevice,
+                            h->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_fep_pert, pert.data(), n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+    {
+        e = cudaMemcpyAsync(const_cast<float*>(v.q), qm.data(), sizeof(float) * n, cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemcpyAsync(const_cast<int*>(v.type), tm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess)
+    {
+        return cuda_check(h, e, "free-energy setup");
+    }
+    FepView& f     = h->fep;
+    f.np           = d->num_perturbed;
+    f.plist        = h->d_fep_list;
+    f.pert         = h->d_fep_pert;
+    f.qA           = h->d_fep_q;
+    f.qB           = h->d_fep_q + n;
+    f.tA           = h->d_fep_t;
+    f.tB           = h->d_fep_t + n;
+    f.alpha_c      = d->alpha_coul;
+    f.alpha_v      = d->alpha_vdw;
+    f.sigma6_def   = d->sigma6_def;
+    f.sigma6_min   = d->sigma6_min;
+    f.soft         = (d->alpha_coul != 0.0f || d->alpha_vdw != 0.0f) ? 1 : 0;
+    f.sums         = h->d_fep_sums;
+    h->fep_power   = d->lambda_power;
+    set_fep_lambda(f, d->lambda_coul, d->lambda_vdw, d->lambda_power);
+    v.self_energy  = self_energy_of(v, qm);
+    h->fep_on      = true;
+    h->have_list   = false;  // the next search fills the masked charges and types into the grid
+    return NBX_OK;
+}
+
+int nbx_fep_set_lambda(nbx_handle* h, float lambda_coul, float lambda_vdw)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->fep_on)
+    {
+        return set_error(h, NBX_ERR_STATE, "no perturbed atoms set");
+    }
+    if (!(lambda_coul >= 0.0f && lambda_coul <= 1.0f && lambda_vdw >= 0.0f && lambda_vdw <= 1.0f))
+    {
+        return set_error(h, NBX_ERR_INVALID_INPUT, "lambda must lie in [0, 1]");
+    }
+    set_fep_lambda(h->fep, lambda_coul, lambda_vdw, h->fep_power);
+    return NBX_OK;
+}
+
+int nbx_fep_get_energies(nbx_handle* h, double* out)
+{
+    if (!h || !out)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->fep_on)
+    {
+        return set_error(h, NBX_ERR_STATE, "no perturbed atoms set");
+    }
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaMemcpyAsync(out, h->d_fep_sums, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return cuda_check(h, e, "free-energy energies");
+}
+
+const double* nbx_fep_energies_device(nbx_handle* h)
+{
+    return (h && h->fep_on) ? h->d_fep_sums : nullptr;
+}
+
+int nbx_fep_disable(nbx_handle* h)
+{
+    if (!h)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    if (!h->fep_on)
+    {
+        return NBX_OK;
+    }
+    cudaSetDevice(h->device);
+    return fep_restore(h);
 }
 
 int nbx_get_options(const nbx_handle* h, nbx_options* out)

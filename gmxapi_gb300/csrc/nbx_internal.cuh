@@ -259,6 +259,26 @@ double one_4pi_eps0();
 float  calc_ewaldcoeff_q(float rc, float rtol);
 
 // ---- launchers (one translation unit each) ----
+// Free-energy (perturbed) pairs: what the perturbed-pair kernel needs besides the DeviceView.
+// The perturbed atoms are masked out of the cluster path (charge 0, all-zero LJ type), so every
+// pair with a perturbed atom is computed here, once.
+struct FepView
+{
+    int                  np;     // perturbed atoms
+    const int*           plist;  // [np] original indices
+    const unsigned char* pert;   // [N] 1 for perturbed atoms
+    const float*         qA;     // [N] state-A charges (unscaled)
+    const float*         qB;     // [N] state-B charges (= qA for unperturbed atoms)
+    const int*           tA;     // [N] state-A types
+    const int*           tB;     // [N] state-B types (= tA for unperturbed atoms)
+    // lambda factors per state {A, B} (nb_free_energy.cpp:356-388)
+    float lfc[2], lfv[2], lfac_c[2], dlfac_c[2], lfac_v[2], dlfac_v[2];
+    float alpha_c, alpha_v, sigma6_def, sigma6_min;
+    int   soft;  // soft-core on (alpha_c or alpha_v non-zero)
+    double* sums;  // [4]: V_Coulomb, V_LJ, dV/dlambda_Coulomb, dV/dlambda_LJ of the perturbed pairs
+};
+
+cudaError_t launch_fep(const DeviceView& v, const FepView& fp, bool energy, cudaStream_t s);
 cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s);
 cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s);
 cudaError_t launch_search(const DeviceView& v, cudaStream_t s);

@@ -233,6 +233,46 @@ class ForceCalculator:
         """Entries per SM below which long list entries are split (0: never); next search."""
         check(_lib.load().nbx_set_list_balance(self.h, int(entries_per_sm)), self.h)
 
+    # ---- free-energy perturbation (nb_free_energy.cpp, dispatched from kerneldispatch.cpp:458-567) ----
+    def set_free_energy(self, perturbed, qB, typeB, lambda_coul: float = 0.0, lambda_vdw: float = 0.0,
+                        alpha_vdw: float = 0.5, alpha_coul: float = 0.5, sc_power: int = 1,
+                        sc_sigma: float = 0.3, sc_sigma_min: float | None = None, x=None):
+        """Perturb `perturbed` atoms between their topology state (A) and charges qB / types typeB
+        (B); the list is rebuilt at x (default: the coordinates the calculator was built with)."""
+        self._fep_p = np.ascontiguousarray(perturbed, np.int32)
+        self._fep_q = np.ascontiguousarray(qB, np.float32)
+        self._fep_t = np.ascontiguousarray(typeB, np.int32)
+        if not (self._fep_p.shape == self._fep_q.shape == self._fep_t.shape):
+            raise InputException("perturbed, qB and typeB differ in length")
+        d = _lib.nbx_fep_desc()
+        d.num_perturbed = int(self._fep_p.shape[0])
+        d.perturbed = _iptr(self._fep_p)
+        d.qB = _fptr(self._fep_q)
+        d.typeB = _iptr(self._fep_t)
+        d.lambda_coul = float(lambda_coul)
+        d.lambda_vdw = float(lambda_vdw)
+        d.alpha_vdw = float(alpha_vdw)
+        d.alpha_coul = float(alpha_coul)
+        d.lambda_power = int(sc_power)
+        d.sigma6_def = float(sc_sigma) ** 6
+        d.sigma6_min = float(sc_sigma if sc_sigma_min is None else sc_sigma_min) ** 6
+        check(_lib.load().nbx_fep_enable(self.h, C.byref(d)), self.h)
+        self.update_pairlist(self._x if x is None else x)
+
+    def set_lambda(self, lambda_coul: float, lambda_vdw: float | None = None):
+        lv = lambda_coul if lambda_vdw is None else lambda_vdw
+        check(_lib.load().nbx_fep_set_lambda(self.h, float(lambda_coul), float(lv)), self.h)
+
+    def free_energy_terms(self) -> dict:
+        """{V_coul, V_lj, dvdl_coul, dvdl_lj} of the perturbed pairs from the last evaluation with energies."""
+        out = np.zeros(4)
+        check(_lib.load().nbx_fep_get_energies(self.h, out.ctypes.data_as(C.POINTER(C.c_double))), self.h)
+        return {"V_coul": out[0], "V_lj": out[1], "dvdl_coul": out[2], "dvdl_lj": out[3]}
+
+    def clear_free_energy(self, x=None):
+        check(_lib.load().nbx_fep_disable(self.h), self.h)
+        self.update_pairlist(self._x if x is None else x)
+
     def list_balance(self) -> dict:
         o = np.zeros(4, np.int32)
         check(_lib.load().nbx_get_list_balance(self.h, _iptr(o)), self.h)

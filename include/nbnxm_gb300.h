@@ -195,6 +195,41 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
  * memory (either may be NULL); the list is kept.  The self energy then follows the new charges. */
 int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nbfp);
 
+/* ---- free-energy perturbation of some atoms (the perturbed-pair kernel) ---- */
+/* Replaces the free-energy path of the nonbonded step: nb_free_energy_kernel
+ * (src/gromacs/gmxlib/nonbonded/nb_free_energy.cpp:200-850) as dispatched from
+ * kerneldispatch.cpp:458-567.  Perturbed atoms interpolate between state A (the topology's
+ * charge and type) and state B with lambda_coul / lambda_vdw, with Beutler soft-core
+ * (sc-r-power 6).  Ewald or reaction-field Coulomb; potential-shift or plain LJ cut-off. */
+typedef struct
+{
+    int          num_perturbed;
+    const int*   perturbed;    /* [P] atom indices */
+    const float* qB;           /* [P] state-B charges */
+    const int*   typeB;        /* [P] state-B types (< num_types) */
+    float        lambda_coul;  /* initial lambdas, in [0, 1] */
+    float        lambda_vdw;
+    float        alpha_vdw;    /* sc-alpha for LJ and Coulomb (0: no soft-core) */
+    float        alpha_coul;
+    int          lambda_power; /* sc-power: 1 or 2 */
+    float        sigma6_def;   /* sc-sigma^6 for pairs without C6 or C12 */
+    float        sigma6_min;   /* lower bound of sigma^6 */
+} nbx_fep_desc;
+
+/* Masks the perturbed atoms out of the cluster path and computes every pair with a perturbed
+ * atom in the perturbed-pair kernel from then on (energies include its lambda-weighted terms).
+ * Needs box edges >= 2 rlist.  The next call must search (nbx_search_device, nbx_update_pairlist
+ * or the search step of nbx_md_step_device). */
+int nbx_fep_enable(nbx_handle* h, const nbx_fep_desc* desc);
+int nbx_fep_set_lambda(nbx_handle* h, float lambda_coul, float lambda_vdw);
+/* out[4] = {V_Coulomb, V_LJ, dV/dlambda_Coulomb, dV/dlambda_LJ} of the perturbed pairs (with their
+ * self terms) from the last evaluation with energies; synchronises the handle's stream. */
+int nbx_fep_get_energies(nbx_handle* h, double* out);
+/* The same four FP64 values in device memory (valid after the evaluation on the handle's stream). */
+const double* nbx_fep_energies_device(nbx_handle* h);
+/* Back to the plain topology (the next call must search again). */
+int nbx_fep_disable(nbx_handle* h);
+
 /* ---- batched ensembles ---- */
 /* Many independent systems (uneven sizes, shared types / nbfp / options) evaluated together:
  * per-system grids and lists, one persistent force launch over all list entries, per-system

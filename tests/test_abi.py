@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "nbnxm_gb300.h")).read()
-    decl = r"^(?:const\s+)?(?:int|void|char|float)\s*\*?\s*(nbx_[a-z0-9_]+)\s*\("
+    decl = r"^(?:const\s+)?(?:int|void|char|float|double)\s*\*?\s*(nbx_[a-z0-9_]+)\s*\("
     return sorted(set(re.findall(decl, text, flags=re.M)))
 
 
