@@ -655,6 +655,58 @@ def measure_md(dev: int, steps: int = 200, warmup: int = 20) -> dict:
     return out
 
 
+def measure_fep(dev: int, num_perturbed: int = 256, steps: int = 20) -> dict:
+    """The perturbed-pair (free-energy) kernel on the 288k-atom water box: num_perturbed atoms
+    (seeded choice) change charge and become uncharged in state B, soft-core alpha 0.5,
+    lambda 0.5.  Times the force + energy evaluation with and without the perturbation (the
+    list is the same size: perturbed atoms stay in the cluster lists with zero parameters)."""
+    import torch
+
+    from gmxapi_gb300 import nblib, systems
+
+    s = systems.water_large()
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=RLIST, rcoulomb=RC,
+                                 compute_virial_and_energy=True)
+    calc = nblib.ForceCalculator(s, opts, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    calc.set_stream(stream.cuda_stream)
+    x = torch.from_numpy(s.x.reshape(-1)).to(f"cuda:{dev}")
+    f = torch.zeros_like(x)
+    ev = torch.zeros(11, dtype=torch.float64, device=x.device)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=x.device)
+
+    def timed():
+        for _ in range(3):
+            calc.compute_device(x.data_ptr(), f.data_ptr(), ev.data_ptr(), ev[2:].data_ptr())
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            calc.compute_device(x.data_ptr(), f.data_ptr(), ev.data_ptr(), ev[2:].data_ptr())
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    calc.search_device(x.data_ptr())
+    plain = timed()
+    rng = np.random.default_rng(11)
+    pert = np.sort(rng.choice(s.n, num_perturbed, replace=False)).astype(np.int32)
+    calc.set_free_energy(pert, np.zeros(num_perturbed, np.float32), s.type[pert], lambda_coul=0.5,
+                         lambda_vdw=0.5)
+    calc.search_device(x.data_ptr())
+    with_fep = timed()
+    terms = calc.free_energy_terms()
+    calc.close()
+    return {"atoms": s.n, "perturbed": num_perturbed, "ms_plain": plain, "ms_with_perturbed": with_fep,
+            "overhead_ms": with_fep - plain, "lambda": 0.5, "terms": terms,
+            "note": "force + energy + virial evaluation, L2 flushed between evaluations; the "
+                    "perturbed pairs run in one block per perturbed atom after the cluster kernel"}
+
+
 def workload_config() -> dict:
     return {"workload": "spc_water_288k", "atoms": 288000, "box_nm": 14.21, "rc_nm": RC, "rlist_nm": RLIST,
             "rlist_inner_nm": RLIST_INNER, "nstlist": NSTLIST, "nstlist_prune": NSTPRUNE,
@@ -769,6 +821,7 @@ def run_ours(args) -> None:
     force_matching = measure_force_matching(dev) if not args.no_extras else None
     pme_block = measure_pme(dev, calc, frames, flush, stream) if not args.no_extras else None
     md_block = measure_md(dev) if not args.no_extras else None
+    fep_block = measure_fep(dev) if not args.no_extras else None
 
     peak = measure_fp32_peak(dev)
     pairs_avg = 0.5 * (pairs0 + pairs1)
@@ -807,6 +860,8 @@ def run_ours(args) -> None:
         line["pme"] = pme_block
     if md_block is not None:
         line["md"] = md_block
+    if fep_block is not None:
+        line["free_energy"] = fep_block
     print(json.dumps(line))
 
 
@@ -818,7 +873,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-ensemble, adjoint and force-matching measurements")
-    ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching", "pme", "md"],
+    ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching", "pme", "md", "fep"],
                     help="run one of the extra measurements alone and print its JSON (profiling)")
     args = ap.parse_args()
     if args.only:
@@ -826,7 +881,7 @@ def main():
 
         torch.cuda.set_device(0)
         fn = {"ensemble": measure_ensemble, "adjoint": measure_adjoint, "force_matching": measure_force_matching,
-              "pme": measure_pme, "md": measure_md}
+              "pme": measure_pme, "md": measure_md, "fep": measure_fep}
         print(json.dumps({args.only: fn[args.only](0)}))
         return
     if args.impl == "reference":

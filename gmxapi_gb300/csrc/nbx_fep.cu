@@ -8,8 +8,8 @@
 //
 // The reference runs this on the CPU over a separate perturbed-pair list built by the search.
 // Here the perturbed atoms are masked out of the cluster path (charge 0, all-zero LJ type; their
-// self terms leave the handle's self energy) and one warp per perturbed atom finds its partners
-// in the grid columns within rlist of it (minimum image: the box is at least 2 rlist), computes
+// self terms leave the handle's self energy) and one block per perturbed atom finds its partners
+// in the grid cells within rlist of it (minimum image: the box is at least 2 rlist), computes
 // each pair once (a pair of two perturbed atoms by the lower index) and adds the forces to the
 // grid-order force buffer before the reduction, the i-forces per periodic shift to the shift
 // forces (so the virial follows), energies and dV/dlambda in FP64.
@@ -22,7 +22,7 @@ namespace nbx
 namespace
 {
 
-constexpr int kFepWarps   = 4;
+constexpr int kFepWarps   = 8;
 constexpr int kFepMaxExcl = 64;  // exclusions of one perturbed atom kept in shared memory
 
 struct FepAcc
@@ -232,98 +232,119 @@ __device__ __forceinline__ int min_image(const DeviceView& v, float4 xi, float4 
     return shift_index(-n[0], -n[1], -n[2]);
 }
 
+// One block per perturbed atom.  Its warps take the grid columns within rlist in turn; in a
+// column the lanes test 32 cells' z ranges (bbcz, periodic) at once and the warp then walks the
+// 64 slots of each cell in range (2 per lane).  The i-force is added once per warp, the shift
+// forces and energies once per block.
 template<bool kEwald>
 __global__ void __launch_bounds__(kFepWarps * 32) k_fep(DeviceView v, FepView fp, int energy)
 {
-    __shared__ float fsh[kFepWarps][kNShift * 3];
-    __shared__ int   exl[kFepWarps][kFepMaxExcl];
-    const int        lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int        w    = blockIdx.x * kFepWarps + wib;
-    for (int k = lane; k < kNShift * 3; k += 32)
+    __shared__ float  fsh[kNShift * 3];
+    __shared__ int    exl[kFepMaxExcl];
+    __shared__ double esum[kFepWarps][4];
+    const int         lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < kNShift * 3; k += blockDim.x)
     {
-        fsh[wib][k] = 0.0f;
+        fsh[k] = 0.0f;
     }
-    __syncwarp();
-    FepAcc acc{ 0.0f, 0.0f, 0.0f, 0.0f };
-    if (w < fp.np)
+    const int    ai  = fp.plist[blockIdx.x];
+    const int    si  = v.cells[ai];
+    const float4 xi  = v.xq[si];
+    const float  qAi = v.epsfac * fp.qA[ai], qBi = v.epsfac * fp.qB[ai];
+    const int    tAi = fp.tA[ai], tBi = fp.tB[ai];
+    const int    e0 = v.excl_index[ai], e1 = v.excl_index[ai + 1];
+    const int    nex = min(e1 - e0, kFepMaxExcl);
+    for (int k = threadIdx.x; k < nex; k += blockDim.x)
     {
-        const int    ai  = fp.plist[w];
-        const int    si  = v.cells[ai];
-        const float4 xi  = v.xq[si];
-        const float  qAi = v.epsfac * fp.qA[ai], qBi = v.epsfac * fp.qB[ai];
-        const int    tAi = fp.tA[ai], tBi = fp.tB[ai];
-        const int    e0 = v.excl_index[ai], e1 = v.excl_index[ai + 1];
-        const int    nex = min(e1 - e0, kFepMaxExcl);
-        for (int k = lane; k < nex; k += 32)
-        {
-            exl[wib][k] = v.excl_list[e0 + k];
-        }
-        __syncwarp();
-        float fi[3] = { 0.0f, 0.0f, 0.0f };
+        exl[k] = v.excl_list[e0 + k];
+    }
+    __syncthreads();
+    FepAcc acc{ 0.0f, 0.0f, 0.0f, 0.0f };
+    float  fi[3] = { 0.0f, 0.0f, 0.0f };
 
-        // grid columns within rlist of the atom (periodic; all columns once when the range wraps)
-        const float rl  = v.rlist;
-        const int   ncx = v.g.ncx, ncy = v.g.ncy;
-        int         cx0 = (int)floorf((xi.x - rl) * v.g.ics[0]);
-        int         cx1 = (int)floorf((xi.x + rl) * v.g.ics[0]);
-        int         cy0 = (int)floorf((xi.y - rl) * v.g.ics[1]);
-        int         cy1 = (int)floorf((xi.y + rl) * v.g.ics[1]);
-        int         nxc = cx1 - cx0 + 1, nyc = cy1 - cy0 + 1;
-        if (nxc >= ncx)
+    // one pair: j at grid slot `slot`, atom aj, not excluded, not the atom itself
+    auto pair = [&](int slot, int aj) {
+        float       d[3];
+        const int   sh  = min_image(v, xi, v.xq[slot], d);
+        const float rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (rsq >= v.rc2)
         {
-            cx0 = 0;
-            nxc = ncx;
+            return;
         }
-        if (nyc >= ncy)
+        const int    tAj   = fp.tA[aj], tBj = fp.tB[aj];
+        const float  qq[2] = { qAi * fp.qA[aj], qBi * fp.qB[aj] };
+        const float2 nb[2] = { v.nbfp[tAi * v.ntypes1 + tAj], v.nbfp[tBi * v.ntypes1 + tBj] };
+        const float  F     = fep_pair<kEwald>(v, fp, rsq, qq, nb, acc);
+        const float  tx = F * d[0], ty = F * d[1], tz = F * d[2];
+        fi[0] += tx;
+        fi[1] += ty;
+        fi[2] += tz;
+        red_v4(&v.fnb[slot], -tx, -ty, -tz);
+        if (energy && sh >= 0)
         {
-            cy0 = 0;
-            nyc = ncy;
+            atomicAdd(&fsh[3 * sh + 0], tx);
+            atomicAdd(&fsh[3 * sh + 1], ty);
+            atomicAdd(&fsh[3 * sh + 2], tz);
         }
-        for (int ix = 0; ix < nxc; ix++)
+    };
+
+    // grid columns within rlist of the atom (periodic; every column once when the range wraps)
+    const float rl  = v.rlist;
+    const int   ncx = v.g.ncx, ncy = v.g.ncy;
+    int         cx0 = (int)floorf((xi.x - rl) * v.g.ics[0]);
+    int         nxc = (int)floorf((xi.x + rl) * v.g.ics[0]) - cx0 + 1;
+    int         cy0 = (int)floorf((xi.y - rl) * v.g.ics[1]);
+    int         nyc = (int)floorf((xi.y + rl) * v.g.ics[1]) - cy0 + 1;
+    if (nxc >= ncx)
+    {
+        cx0 = 0;
+        nxc = ncx;
+    }
+    if (nyc >= ncy)
+    {
+        cy0 = 0;
+        nyc = ncy;
+    }
+    const float Lz = v.g.box[2];
+    for (int c = wib; c < nxc * nyc; c += kFepWarps)
+    {
+        const int cx   = ((cx0 + c / nyc) % ncx + ncx) % ncx;
+        const int cy   = ((cy0 + c % nyc) % ncy + ncy) % ncy;
+        const int col  = cx * ncy + cy;
+        const int c0   = v.cxy_ind[col], c1 = v.cxy_ind[col + 1];
+        for (int cb = c0; cb < c1; cb += 32)
         {
-            const int cx = ((cx0 + ix) % ncx + ncx) % ncx;
-            for (int iy = 0; iy < nyc; iy++)
+            bool near = false;
+            if (cb + lane < c1)
             {
-                const int cy  = ((cy0 + iy) % ncy + ncy) % ncy;
-                const int col = cx * ncy + cy;
-                const int s1  = v.cxy_ind[col + 1] * kSc;
-                for (int slot = v.cxy_ind[col] * kSc + lane; slot < s1; slot += 32)
+                const float2 z = v.bbcz[cb + lane];
+                for (int k = -1; k <= 1; k++)
                 {
-                    const int aj = v.atom_indices[slot];
-                    if (aj < 0 || aj == ai || (fp.pert[aj] && aj < ai))
+                    near |= (z.y + k * Lz >= xi.z - rl) && (z.x + k * Lz <= xi.z + rl);
+                }
+            }
+            unsigned todo = __ballot_sync(0xffffffffu, near);
+            while (todo)
+            {
+                const int cell = cb + __ffs(todo) - 1;
+                todo &= todo - 1;
+                for (int k = lane; k < kSc; k += 32)
+                {
+                    const int slot = cell * kSc + k;
+                    const int aj   = v.atom_indices[slot];
+                    if (aj < 0 || aj == ai || (fp.pert[aj] && aj < ai)
+                        || excluded_from(aj, exl, nex, v.excl_list, e0, e1))
                     {
                         continue;
                     }
-                    if (excluded_from(aj, exl[wib], nex, v.excl_list, e0, e1))
-                    {
-                        continue;
-                    }
-                    float     d[3];
-                    const int sh  = min_image(v, xi, v.xq[slot], d);
-                    const float rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-                    if (rsq >= v.rc2)
-                    {
-                        continue;
-                    }
-                    const int    tAj   = fp.tA[aj], tBj = fp.tB[aj];
-                    const float  qq[2] = { qAi * fp.qA[aj], qBi * fp.qB[aj] };
-                    const float2 nb[2] = { v.nbfp[tAi * v.ntypes1 + tAj], v.nbfp[tBi * v.ntypes1 + tBj] };
-                    const float  F     = fep_pair<kEwald>(v, fp, rsq, qq, nb, acc);
-                    const float  tx = F * d[0], ty = F * d[1], tz = F * d[2];
-                    fi[0] += tx;
-                    fi[1] += ty;
-                    fi[2] += tz;
-                    red_v4(&v.fnb[slot], -tx, -ty, -tz);
-                    if (energy && sh >= 0)
-                    {
-                        atomicAdd(&fsh[wib][3 * sh + 0], tx);
-                        atomicAdd(&fsh[wib][3 * sh + 1], ty);
-                        atomicAdd(&fsh[wib][3 * sh + 2], tz);
-                    }
+                    pair(slot, aj);
                 }
             }
         }
-        // excluded pairs within rc
+    }
+    // excluded pairs within rc, and the self pair (warp 0)
+    if (wib == 0)
+    {
         for (int k = e0 + lane; k < e1; k += 32)
         {
             const int aj = v.excl_list[k];
@@ -348,15 +369,15 @@ __global__ void __launch_bounds__(kFepWarps * 32) k_fep(DeviceView v, FepView fp
             red_v4(&v.fnb[sj], -tx, -ty, -tz);
             if (energy && sh >= 0)
             {
-                atomicAdd(&fsh[wib][3 * sh + 0], tx);
-                atomicAdd(&fsh[wib][3 * sh + 1], ty);
-                atomicAdd(&fsh[wib][3 * sh + 2], tz);
+                atomicAdd(&fsh[3 * sh + 0], tx);
+                atomicAdd(&fsh[3 * sh + 1], ty);
+                atomicAdd(&fsh[3 * sh + 2], tz);
             }
         }
-        // the self pair: half of the r = 0 excluded term (:696-706)
+        // half of the r = 0 excluded term (nb_free_energy.cpp:696-706)
         if (lane == 0)
         {
-            const float vself = kEwald ? v.c2b : v.c_rf;
+            const float vself  = kEwald ? v.c2b : v.c_rf;
             const float qqs[2] = { qAi * fp.qA[ai], qBi * fp.qB[ai] };
 #pragma unroll
             for (int s = 0; s < 2; s++)
@@ -366,30 +387,22 @@ __global__ void __launch_bounds__(kFepWarps * 32) k_fep(DeviceView v, FepView fp
                 acc.dc -= 0.5f * dlf * qqs[s] * vself;
             }
         }
+    }
 #pragma unroll
-        for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 3; k++)
+    {
+        for (int o = 16; o > 0; o >>= 1)
         {
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                fi[k] += __shfl_xor_sync(0xffffffffu, fi[k], o);
-            }
-        }
-        if (lane == 0)
-        {
-            red_v4(&v.fnb[si], fi[0], fi[1], fi[2]);
+            fi[k] += __shfl_xor_sync(0xffffffffu, fi[k], o);
         }
     }
-    __syncwarp();
+    if (lane == 0 && (fi[0] != 0.0f || fi[1] != 0.0f || fi[2] != 0.0f))
+    {
+        red_v4(&v.fnb[si], fi[0], fi[1], fi[2]);
+    }
     if (!energy)
     {
         return;
-    }
-    for (int k = lane; k < kNShift * 3; k += 32)
-    {
-        if (fsh[wib][k] != 0.0f)
-        {
-            atomicAdd(&v.fshift[k], (double)fsh[wib][k]);
-        }
     }
     double e[4] = { acc.vc, acc.vv, acc.dc, acc.dv };
 #pragma unroll
@@ -399,14 +412,30 @@ __global__ void __launch_bounds__(kFepWarps * 32) k_fep(DeviceView v, FepView fp
         {
             e[k] += __shfl_xor_sync(0xffffffffu, e[k], o);
         }
-    }
-    if (lane == 0 && w < fp.np)
-    {
-        atomicAdd(&v.energy[1], e[0]);
-        atomicAdd(&v.energy[0], e[1]);
-        for (int k = 0; k < 4; k++)
+        if (lane == 0)
         {
-            atomicAdd(&fp.sums[k], e[k]);
+            esum[wib][k] = e[k];
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kNShift * 3; k += blockDim.x)
+    {
+        if (fsh[k] != 0.0f)
+        {
+            atomicAdd(&v.fshift[k], (double)fsh[k]);
+        }
+    }
+    if (threadIdx.x < 4)
+    {
+        double t = 0.0;
+        for (int w = 0; w < kFepWarps; w++)
+        {
+            t += esum[w][threadIdx.x];
+        }
+        atomicAdd(&fp.sums[threadIdx.x], t);
+        if (threadIdx.x < 2)
+        {
+            atomicAdd(&v.energy[1 - threadIdx.x], t);  // V_Coulomb -> energy[1], V_LJ -> energy[0]
         }
     }
 }
@@ -420,14 +449,13 @@ cudaError_t launch_fep(const DeviceView& v, const FepView& fp, bool energy, cuda
     {
         return e;
     }
-    const int blocks = (fp.np + kFepWarps - 1) / kFepWarps;
     if (v.coulomb == 0)
     {
-        k_fep<true><<<blocks, kFepWarps * 32, 0, s>>>(v, fp, energy ? 1 : 0);
+        k_fep<true><<<fp.np, kFepWarps * 32, 0, s>>>(v, fp, energy ? 1 : 0);
     }
     else
     {
-        k_fep<false><<<blocks, kFepWarps * 32, 0, s>>>(v, fp, energy ? 1 : 0);
+        k_fep<false><<<fp.np, kFepWarps * 32, 0, s>>>(v, fp, energy ? 1 : 0);
     }
     return cudaGetLastError();
 }
