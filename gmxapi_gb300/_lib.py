@@ -52,7 +52,7 @@ EXPORTED = [
     "nbx_get_options", "nbx_set_force_accumulate", "nbx_get_force_accumulate", "nbx_leapfrog_create", "nbx_leapfrog_destroy",
     "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
     "nbx_md_run_device", "nbx_fep_enable", "nbx_fep_set_lambda", "nbx_fep_get_energies", "nbx_fep_energies_device",
-    "nbx_fep_disable",
+    "nbx_fep_disable", "nbx_pme_create_lj", "nbx_ewald_coefficient_lj",
 ]
 
 
@@ -84,6 +84,7 @@ class nbx_options(C.Structure):
         ("compute_energy", C.c_int),
         ("vdw_modifier", C.c_int),
         ("rvdw_switch", C.c_float),
+        ("ewald_rtol_lj", C.c_float),
     ]
 
 
@@ -204,6 +205,9 @@ def load():
     L.nbx_pme_grid_size.argtypes = [fp, C.c_float, ip]
     L.nbx_pme_create.argtypes = [fp, ip, C.c_float, C.c_float, C.c_int, C.POINTER(vp)]
     L.nbx_pme_destroy.argtypes = [vp]
+    L.nbx_pme_create_lj.argtypes = [fp, ip, C.c_float, C.c_int, C.POINTER(vp)]
+    L.nbx_ewald_coefficient_lj.argtypes = [C.c_float, C.c_float]
+    L.nbx_ewald_coefficient_lj.restype = C.c_float
     L.nbx_pme_last_error.argtypes = [vp]
     L.nbx_pme_last_error.restype = C.c_char_p
     L.nbx_pme_set_stream.argtypes = [vp, vp]
@@ -236,7 +240,7 @@ def load():
         if f.restype is C.c_int or name not in ("nbx_default_options", "nbx_last_error", "nbx_get_stream",
                                                 "nbx_batch_last_error", "nbx_pme_last_error",
                                                 "nbx_ewald_coefficient", "nbx_leapfrog_last_error",
-                                                "nbx_fep_energies_device"):
+                                                "nbx_fep_energies_device", "nbx_ewald_coefficient_lj"):
             f.restype = C.c_int
     _lib = L
     return L

@@ -507,6 +507,7 @@ void nbx_default_options(nbx_options* o)
     o->compute_energy  = 0;
     o->vdw_modifier    = NBX_VDW_POTSHIFT;
     o->rvdw_switch     = 0.0f;
+    o->ewald_rtol_lj   = 1e-3f;
 }
 
 const char* nbx_last_error(const nbx_handle* h)
@@ -547,7 +548,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     {
         return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown Coulomb type");
     }
-    if (opts.vdw_modifier < 0 || opts.vdw_modifier > 3)
+    if (opts.vdw_modifier < 0 || opts.vdw_modifier > NBX_VDW_LJPME)
     {
         return set_error(nullptr, NBX_ERR_INVALID_INPUT, "unknown LJ modifier");
     }
@@ -636,6 +637,27 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     v.epsfac       = (float)one_4pi_eps0();
     v.epsfac_d     = one_4pi_eps0();
     set_lj_modifier(v, opts.vdw_modifier, rc, opts.rvdw_switch);
+    if (opts.vdw_modifier == NBX_VDW_LJPME)
+    {
+        // LJ-PME real space: the potential-shift constants of the plain part plus the grid terms
+        // (forcerec.cpp:703-716, kernel_ref_outer.h:182-189); the self energy of the grid part
+        // sum_i 0.5 (6 C6_ii) / 6 beta^6 / 6 (kernel_ref_outer.h:307-313)
+        set_lj_modifier(v, NBX_VDW_POTSHIFT, rc, 0.0f);
+        v.vdw_mod         = NBX_VDW_LJPME;
+        const float bl    = nbx_ewald_coefficient_lj(rc, opts.ewald_rtol_lj);
+        const float crc2  = (bl * rc) * (bl * rc);
+        v.lje_coeff2      = bl * bl;
+        v.lje_coeff6_6    = v.lje_coeff2 * v.lje_coeff2 * v.lje_coeff2 / 6.0f;
+        v.sh_lj_ewald     = (std::exp(-crc2) * (1 + crc2 + 0.5f * crc2 * crc2) - 1) / (rc * rc * rc * rc * rc * rc);
+        double self_lj    = 0.0;
+        const int nt      = sys->num_types;
+        for (int i = 0; i < n; i++)
+        {
+            const int t = sys->type[i];
+            self_lj += 0.5 * (double)sys->nbfp[2 * (t * nt + t)] / 6.0 * (double)v.lje_coeff6_6;
+        }
+        v.self_energy_lj = self_lj;
+    }
     const float eps_rf = (opts.coulomb == NBX_COULOMB_CUTOFF) ? 1.0f : opts.epsilon_rf;
     v.k_rf = (eps_rf == 0) ? 1 / (2 * rc * rc * rc) : (eps_rf - 1.0f) / (2 * eps_rf + 1.0f) / (rc * rc * rc);
     v.c_rf = 1 / rc + v.k_rf * rc * rc;
@@ -1064,7 +1086,7 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
     {
         return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint supports at most 15 particle types");
     }
-    if (h->v.vdw_mod == NBX_VDW_FORCESWITCH || h->v.vdw_mod == NBX_VDW_POTSWITCH)
+    if (h->v.vdw_mod == NBX_VDW_FORCESWITCH || h->v.vdw_mod == NBX_VDW_POTSWITCH || h->v.vdw_mod == NBX_VDW_LJPME)
     {
         return set_error(h, NBX_ERR_INVALID_INPUT, "the adjoint takes the potential-shift or plain LJ cut-off");
     }
@@ -1958,7 +1980,8 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
         return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "need at least one system");
     }
     *out = nullptr;
-    if (opts && (opts->vdw_modifier == NBX_VDW_FORCESWITCH || opts->vdw_modifier == NBX_VDW_POTSWITCH))
+    if (opts && (opts->vdw_modifier == NBX_VDW_FORCESWITCH || opts->vdw_modifier == NBX_VDW_POTSWITCH
+                 || opts->vdw_modifier == NBX_VDW_LJPME))
     {
         return batch_error(nullptr, NBX_ERR_INVALID_INPUT, "batches take the potential-shift or plain LJ cut-off");
     }

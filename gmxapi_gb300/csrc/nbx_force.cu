@@ -48,14 +48,21 @@ constexpr int kStageBytes     = kStageSmemPerWarp;  // per warp: double-buffered
 template<bool kEnergy, bool kEwald, int kLj = 0>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
 {
-    // {6*C6, 12*C12, LJ energy shift of the pair, 0} per type pair
+    // {6*C6, 12*C12, LJ energy shift of the pair, LJ-PME grid 6*C6 (geometric)} per type pair
     extern __shared__ float4 nbfp_s[];
     const int nt1 = v.ntypes1;
     for (int k = threadIdx.x; k < nt1 * nt1; k += blockDim.x)
     {
         const float2 p = v.nbfp[k];
+        // LJ-PME grid: sqrt(6 C6_ii) sqrt(6 C6_jj), the reference's nbfp_comb product (geometric rule)
+        float c6grid = 0.0f;
+        if (kLj == 3)
+        {
+            const int ti = k / nt1, tj = k % nt1;
+            c6grid       = sqrtf(v.nbfp[ti * nt1 + ti].x) * sqrtf(v.nbfp[tj * nt1 + tj].x);
+        }
         // (12C12 cpot12)/12 - (6C6 cpot6)/6 (kernel_gpu_ref.cpp:327-336)
-        nbfp_s[k] = make_float4(p.x, p.y, p.y * v.cpot12 * (1.0f / 12.0f) - p.x * v.cpot6 * (1.0f / 6.0f), 0.0f);
+        nbfp_s[k] = make_float4(p.x, p.y, p.y * v.cpot12 * (1.0f / 12.0f) - p.x * v.cpot6 * (1.0f / 6.0f), c6grid);
     }
     __syncthreads();
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
@@ -143,11 +150,15 @@ __constant__ double kErfSeries[16] = {
 
 __global__ void k_excl_energy(DeviceView v)
 {
-    const int i   = blockIdx.x * blockDim.x + threadIdx.x;
-    double    acc = 0.0;
+    const int i      = blockIdx.x * blockDim.x + threadIdx.x;
+    double    acc    = 0.0;
+    double    acc_lj = 0.0;  // LJ-PME: the grid part of excluded pairs
+    const bool ljpme = v.vdw_mod == NBX_VDW_LJPME;
     if (i < v.n)
     {
         const float4 xi  = v.xq[v.cells[i]];
+        const int    nt1 = v.ntypes1;
+        const float  sci = ljpme ? sqrtf(v.nbfp[v.type[i] * (nt1 + 1)].x) : 0.0f;
         if (v.self_on_device)
         {
             // self term, kernel_gpu_ref.cpp:154-178 (acc is scaled by epsfac below)
@@ -207,6 +218,15 @@ __global__ void k_excl_energy(DeviceView v)
                             h = (double)v.k_rf * r2d - (double)v.c_rf;
                         }
                         acc += (double)xi.w * (double)xj.w * h;
+                        if (ljpme)
+                        {
+                            // c6grid / 6 r^-6 (1 - e^-b (1 + b + b^2/2)), b = beta_lj^2 r^2
+                            const int    tj     = v.type[j];
+                            const double c6grid = (double)(sci * sqrtf(v.nbfp[tj * (nt1 + 1)].x));
+                            const double b      = (double)v.lje_coeff2 * r2d;
+                            const double ir6    = 1.0 / (r2d * r2d * r2d);
+                            acc_lj += c6grid / 6.0 * ir6 * (1.0 - exp(-b) * (1.0 + b + 0.5 * b * b));
+                        }
                     }
                 }
             }
@@ -215,10 +235,15 @@ __global__ void k_excl_energy(DeviceView v)
     for (int o = 16; o > 0; o >>= 1)
     {
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        acc_lj += __shfl_xor_sync(0xffffffffu, acc_lj, o);
     }
     if ((threadIdx.x & 31) == 0 && acc != 0.0)
     {
         atomicAdd(&v.energy[1], acc * v.epsfac_d);
+    }
+    if ((threadIdx.x & 31) == 0 && acc_lj != 0.0)
+    {
+        atomicAdd(&v.energy[0], acc_lj);
     }
 }
 
@@ -311,7 +336,7 @@ __global__ void k_finish(DeviceView v, double* d_energies, double* d_virial)
     const int t = threadIdx.x;
     if (d_energies && t < 2)
     {
-        d_energies[t] = v.energy[t] + (t == 1 ? v.self_energy : 0.0);
+        d_energies[t] = v.energy[t] + (t == 1 ? v.self_energy : v.self_energy_lj);
     }
     if (d_virial && t < 9)
     {
@@ -404,8 +429,20 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
         cudaEventRecord(ev0, s);
     }
     // the switch modifiers have their own instantiations; shift and plain cut-off share one
-    const int lj = (v.vdw_mod == NBX_VDW_FORCESWITCH) ? 1 : (v.vdw_mod == NBX_VDW_POTSWITCH) ? 2 : 0;
-    if (lj == 1)
+    const int lj = (v.vdw_mod == NBX_VDW_FORCESWITCH) ? 1
+                   : (v.vdw_mod == NBX_VDW_POTSWITCH) ? 2
+                   : (v.vdw_mod == NBX_VDW_LJPME)     ? 3
+                                                       : 0;
+    if (lj == 3)
+    {
+        if (energy)
+            ewald ? k_force<true, true, 3><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<true, false, 3><<<blocks, kForceThreads, smem, s>>>(v, counter);
+        else
+            ewald ? k_force<false, true, 3><<<blocks, kForceThreads, smem, s>>>(v, counter)
+                  : k_force<false, false, 3><<<blocks, kForceThreads, smem, s>>>(v, counter);
+    }
+    else if (lj == 1)
     {
         if (energy)
             ewald ? k_force<true, true, 1><<<blocks, kForceThreads, smem, s>>>(v, counter)

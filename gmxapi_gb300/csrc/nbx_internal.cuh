@@ -173,6 +173,10 @@ struct DeviceView
     float beta2l2;  // beta^2 log2(e)
     float c2b;      // 2 beta / sqrt(pi)
     float k_rf2;    // 2 k_rf
+    // LJ-PME real space (vdw_mod NBX_VDW_LJPME): beta_lj^2, beta_lj^6 / 6, the grid potential's
+    // shift at rc (forcerec.cpp:711-712) and the LJ self energy sum_i C6_ii beta^6 / 12
+    float  lje_coeff2, lje_coeff6_6, sh_lj_ewald;
+    double self_energy_lj;
     // 1: k_reduce_f adds the nonbonded forces to the caller's buffer
     // (nbnxn_gpu_add_nbat_f_to_f_kernel<accumulateForce = true>); 0: overwrites it
     int accumulate_f;

@@ -250,7 +250,7 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             }
             const float  rinv2 = rinv * rinv;
             float4       lj;
-            if (kEnergy)
+            if (kEnergy || kLj == 3)
             {
                 lj = nbfp_s[st.ti[c] + tj];
             }
@@ -259,7 +259,8 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
                 const float2 l2 = *reinterpret_cast<const float2*>(&nbfp_s[st.ti[c] + tj]);
                 lj              = make_float4(l2.x, l2.y, 0.0f, 0.0f);
             }
-            float rinv6 = rinv2 * rinv2 * rinv2;
+            float       rinv6    = rinv2 * rinv2 * rinv2;
+            const float rinv6_nm = rinv6;  // LJ-PME: the grid part also acts on excluded pairs
             if (kExcl)
             {
                 rinv6 *= int_bit;
@@ -270,7 +271,22 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
             float       flj   = fmaf(c12r6, rinv6, -vdisp);  // vrep - vdisp, vrep = 12 C12 / r^12
             // LJ energy: vrep/12 - vdisp/6 + (shift constant of this type pair) = (flj - vdisp)/12 + shift
             float vlj = (kEnergy || kLj == 2) ? fmaf(flj - vdisp, 1.0f / 12.0f, lj.z) : 0.0f;
-            if (kLj != 0)
+            if (kLj == 3)
+            {
+                // LJ-PME, geometric grid c6grid = lj.w (kernel_ref_inner.h:204-252): subtract the grid
+                // part c6grid (1 - e^-b (1 + b + b^2/2)) / r^6, b = beta_lj^2 r^2, from F r and V
+                const float cr2  = v.lje_coeff2 * r2;
+                const float expm = fast_ex2(-1.4426950408889634f * cr2);
+                const float poly = fmaf(0.5f * cr2, cr2, 1.0f + cr2);
+                flj              = fmaf(lj.w, rinv6_nm - expm * fmaf(rinv6_nm, poly, v.lje_coeff6_6), flj);
+                if (kEnergy)
+                {
+                    // the grid potential's shift only for pairs that interact
+                    vlj = fmaf(lj.w * (1.0f / 6.0f), fmaf(rinv6_nm, 1.0f - expm * poly, int_bit * v.sh_lj_ewald),
+                               vlj);
+                }
+            }
+            else if (kLj != 0)
             {
                 // force / potential switch from rvdw_switch to rc (kernel_ref_inner.h:168-200)
                 const float r   = r2 * rinv;
@@ -369,7 +385,7 @@ __device__ __forceinline__ void process_half(const DeviceView& v, const SysPtrs&
 // One list entry: load the 64 shifted i-atoms, all its cj4 groups, then the
 // i-force, shift-force and energy reductions.  The entry's energies are added
 // to e_lj_acc / e_el_acc (per lane, FP64).
-// kLj: 0 potential shift or plain cut-off, 1 force switch, 2 potential switch.
+// kLj: 0 potential shift or plain cut-off, 1 force switch, 2 potential switch, 3 LJ-PME (grid part).
 template<bool kEnergy, bool kEwald, int kLj = 0>
 __device__ __forceinline__ bool process_entry(const DeviceView& v, const SysPtrs& p, const Sci& s,
                                               const float4* __restrict__ nbfp_s, JStage& js, int nt1, int lane,

@@ -204,77 +204,12 @@ constexpr int kSolveMaxBlocks = 4096;  // one point per thread up to 1M points, 
 // counter, and thousands of same-address atomics would serialise in L2.
 constexpr int kSolveEnergyBlocksPerSm = 4;
 
-// solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
-// energy and virial terms (energy = 0.5 sum, virial = 0.25 sum).  Per-point terms and
-// per-thread / per-warp sums are float (the reference sums them in `real`); each block
-// writes its 7 sums in FP64 to partials[block][8] and the last block to finish sums the
-// partials in FP64 (no same-address atomics on the sums).
-__global__ void __launch_bounds__(kSolveThreads) k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ bsp,
-                                                             float elfac, float factor, float pivol, double* partials,
-                                                             unsigned int* done, double* energy_out,
-                                                             double* virial_out)
+// The solve's energy / virial sums: per warp in float, per block in FP64 into partials[block][8];
+// the last block to finish (completion counter) adds the partials in FP64 and writes
+// energy = 0.5 sum, virial = 0.25 sum.
+__device__ void solve_finish(const float acc[7], double* partials, unsigned int* done, double* energy_out,
+                             double* virial_out)
 {
-    const bool energy = energy_out || virial_out;
-    const int  nzc    = d.n[2] / 2 + 1;
-    const int  total  = d.n[0] * d.n[1] * nzc;
-    float      acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
-    // (kx, ky, kz) of t, advanced by the grid stride with carries instead of divisions
-    const int t0     = blockIdx.x * blockDim.x + threadIdx.x;
-    const int stride = gridDim.x * blockDim.x;
-    int       kz = t0 % nzc, ky = (t0 / nzc) % d.n[1], kx = t0 / (nzc * d.n[1]);
-    const int sz = stride % nzc, sy = (stride / nzc) % d.n[1], sx = stride / (nzc * d.n[1]);
-    for (int t = t0; t < total; t += stride)
-    {
-        if (kx != 0 || ky != 0 || kz != 0)
-        {
-            const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
-            const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
-            const float mhx   = (float)mx * d.rec[0];
-            const float mhy   = (float)my * d.rec[1];
-            const float mhz   = (float)kz * d.rec[2];
-            const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
-            const float by    = pivol * bsp[d.n[0] + ky];
-            const float den   = m2 * bsp[d.n[0] + d.n[1] + kz] * by * bsp[kx];
-            const float eterm = elfac / den * expf(-factor * m2);
-            float2      c     = cgrid[t];
-            if (energy)
-            {
-                const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
-                const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
-                const float ets2    = corner * eterm * struct2;
-                const float ets2vf  = ets2 * ((factor * m2 + 1.0f) * 2.0f / m2);
-                acc[0] += ets2;
-                acc[1] += ets2vf * mhx * mhx - ets2;
-                acc[2] += ets2vf * mhx * mhy;
-                acc[3] += ets2vf * mhx * mhz;
-                acc[4] += ets2vf * mhy * mhy - ets2;
-                acc[5] += ets2vf * mhy * mhz;
-                acc[6] += ets2vf * mhz * mhz - ets2;
-            }
-            c.x *= eterm;
-            c.y *= eterm;
-            cgrid[t] = c;
-        }
-        kz += sz;
-        int carry = 0;
-        if (kz >= nzc)
-        {
-            kz -= nzc;
-            carry = 1;
-        }
-        ky += sy + carry;
-        carry = 0;
-        if (ky >= d.n[1])
-        {
-            ky -= d.n[1];
-            carry = 1;
-        }
-        kx += sx + carry;
-    }
-    if (!energy)
-    {
-        return;
-    }
     __shared__ double red[7][kSolveThreads / 32];
     __shared__ bool   last;
     const int         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -360,6 +295,151 @@ __global__ void __launch_bounds__(kSolveThreads) k_pme_solve(PmeDims d, float2* 
             virial_out[8]                 = 0.25 * tot[6];
         }
         *done = 0u;  // ready for the next solve on this stream
+    }
+}
+
+// solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
+// energy and virial terms (energy = 0.5 sum, virial = 0.25 sum).  Per-point terms and
+// per-thread / per-warp sums are float (the reference sums them in `real`); each block
+// writes its 7 sums in FP64 to partials[block][8] and the last block to finish sums the
+// partials in FP64 (no same-address atomics on the sums).
+__global__ void __launch_bounds__(kSolveThreads) k_pme_solve(PmeDims d, float2* cgrid, const float* __restrict__ bsp,
+                                                             float elfac, float factor, float pivol, double* partials,
+                                                             unsigned int* done, double* energy_out,
+                                                             double* virial_out)
+{
+    const bool energy = energy_out || virial_out;
+    const int  nzc    = d.n[2] / 2 + 1;
+    const int  total  = d.n[0] * d.n[1] * nzc;
+    float      acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    // (kx, ky, kz) of t, advanced by the grid stride with carries instead of divisions
+    const int t0     = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    int       kz = t0 % nzc, ky = (t0 / nzc) % d.n[1], kx = t0 / (nzc * d.n[1]);
+    const int sz = stride % nzc, sy = (stride / nzc) % d.n[1], sx = stride / (nzc * d.n[1]);
+    for (int t = t0; t < total; t += stride)
+    {
+        if (kx != 0 || ky != 0 || kz != 0)
+        {
+            const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
+            const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
+            const float mhx   = (float)mx * d.rec[0];
+            const float mhy   = (float)my * d.rec[1];
+            const float mhz   = (float)kz * d.rec[2];
+            const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
+            const float by    = pivol * bsp[d.n[0] + ky];
+            const float den   = m2 * bsp[d.n[0] + d.n[1] + kz] * by * bsp[kx];
+            const float eterm = elfac / den * expf(-factor * m2);
+            float2      c     = cgrid[t];
+            if (energy)
+            {
+                const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
+                const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
+                const float ets2    = corner * eterm * struct2;
+                const float ets2vf  = ets2 * ((factor * m2 + 1.0f) * 2.0f / m2);
+                acc[0] += ets2;
+                acc[1] += ets2vf * mhx * mhx - ets2;
+                acc[2] += ets2vf * mhx * mhy;
+                acc[3] += ets2vf * mhx * mhz;
+                acc[4] += ets2vf * mhy * mhy - ets2;
+                acc[5] += ets2vf * mhy * mhz;
+                acc[6] += ets2vf * mhz * mhz - ets2;
+            }
+            c.x *= eterm;
+            c.y *= eterm;
+            cgrid[t] = c;
+        }
+        kz += sz;
+        int carry = 0;
+        if (kz >= nzc)
+        {
+            kz -= nzc;
+            carry = 1;
+        }
+        ky += sy + carry;
+        carry = 0;
+        if (ky >= d.n[1])
+        {
+            ky -= d.n[1];
+            carry = 1;
+        }
+        kx += sx + carry;
+    }
+    if (energy)
+    {
+        solve_finish(acc, partials, done, energy_out, virial_out);
+    }
+}
+
+// solve_pme_lj_yzx, geometric combination rule (one grid; pme_solve.cpp:588-915): the
+// dispersion influence function eterm = -((1 - 2 b) e^-b + 2 b sqrt(pi) sqrt(b) erfc(sqrt(b))) / D,
+// b = pi^2 m^2 / beta_lj^2, D = B_x B_y B_z 3 V / (pi^1.5 beta_lj^3); the k = 0 element is
+// scaled too.  Energy and virial sums as in k_pme_solve.
+__global__ void __launch_bounds__(kSolveThreads) k_pme_solve_lj(PmeDims d, float2* cgrid,
+                                                                const float* __restrict__ bsp, float factor,
+                                                                float by_pref, double* partials, unsigned int* done,
+                                                                double* energy_out, double* virial_out)
+{
+    const bool energy = energy_out || virial_out;
+    const int  nzc    = d.n[2] / 2 + 1;
+    const int  total  = d.n[0] * d.n[1] * nzc;
+    float      acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    const int  t0     = blockIdx.x * blockDim.x + threadIdx.x;
+    const int  stride = gridDim.x * blockDim.x;
+    int        kz = t0 % nzc, ky = (t0 / nzc) % d.n[1], kx = t0 / (nzc * d.n[1]);
+    const int  sz = stride % nzc, sy = (stride / nzc) % d.n[1], sx = stride / (nzc * d.n[1]);
+    for (int t = t0; t < total; t += stride)
+    {
+        const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
+        const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
+        const float mhx   = (float)mx * d.rec[0];
+        const float mhy   = (float)my * d.rec[1];
+        const float mhz   = (float)kz * d.rec[2];
+        const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
+        const float den   = bsp[d.n[0] + d.n[1] + kz] * (by_pref * bsp[d.n[0] + ky]) * bsp[kx];
+        const float b     = factor * m2;
+        const float e1    = expf(-b);
+        const float mk    = sqrtf(b);
+        const float e2    = 1.7724538509055159f * mk * erfcf(mk);
+        const float eterm = -((1.0f - 2.0f * b) * e1 + 2.0f * b * e2) / den;
+        float2      c     = cgrid[t];
+        if (energy)
+        {
+            const float vterm   = 3.0f * (-e1 + e2) / den;
+            const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
+            const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
+            const float ets2    = corner * eterm * struct2;
+            const float ets2vf  = corner * 2.0f * factor * vterm * struct2;
+            acc[0] += ets2;
+            acc[1] += ets2vf * mhx * mhx - ets2;
+            acc[2] += ets2vf * mhx * mhy;
+            acc[3] += ets2vf * mhx * mhz;
+            acc[4] += ets2vf * mhy * mhy - ets2;
+            acc[5] += ets2vf * mhy * mhz;
+            acc[6] += ets2vf * mhz * mhz - ets2;
+        }
+        c.x *= eterm;
+        c.y *= eterm;
+        cgrid[t] = c;
+        kz += sz;
+        int carry = 0;
+        if (kz >= nzc)
+        {
+            kz -= nzc;
+            carry = 1;
+        }
+        ky += sy + carry;
+        carry = 0;
+        if (ky >= d.n[1])
+        {
+            ky -= d.n[1];
+            carry = 1;
+        }
+        kx += sx + carry;
+    }
+    if (energy)
+    {
+        solve_finish(acc, partials, done, energy_out, virial_out);
     }
 }
 
@@ -489,6 +569,7 @@ struct nbx_pme
     float        box[3]    = { 0, 0, 0 };
     float        beta      = 0.0f;
     float        epsilon_r = 1.0f;
+    int          lj        = 0;  // 1: the Lennard-Jones (dispersion) grid, coefficients sqrt(C6)
     float*       grid      = nullptr;  // real grid [nx][ny][nz]
     float2*      cgrid     = nullptr;  // half-complex grid [nx][ny][nz/2+1]
     float*       bsp       = nullptr;  // spline moduli x | y | z
@@ -546,14 +627,23 @@ cudaError_t launch_spread(nbx_pme* p, int natoms, const float* d_x, const float*
 
 cudaError_t launch_solve(nbx_pme* p, float2* cgrid, double* d_energy, double* d_virial)
 {
-    const double vol = (double)p->box[0] * p->box[1] * p->box[2];
-    // elfac = ONE_4PI_EPS0 / epsilon_r, factor = pi^2 / beta^2 (pme_solve.cpp:341,354), in float like `real`
-    const float elfac   = (float)nbx::one_4pi_eps0() / p->epsilon_r;
-    const float factor  = (float)(M_PI * M_PI) / (p->beta * p->beta);
-    const float pivol   = (float)M_PI * (float)vol;
-    const int   nc      = (int)complex_points(p);
-    const int   cap     = (d_energy || d_virial) ? kSolveEnergyBlocksPerSm * p->num_sms : kSolveMaxBlocks;
-    const int   nblocks = std::max(1, std::min((nc + kSolveThreads - 1) / kSolveThreads, cap));
+    const double vol     = (double)p->box[0] * p->box[1] * p->box[2];
+    const int    nc      = (int)complex_points(p);
+    const int    cap     = (d_energy || d_virial) ? kSolveEnergyBlocksPerSm * p->num_sms : kSolveMaxBlocks;
+    const int    nblocks = std::max(1, std::min((nc + kSolveThreads - 1) / kSolveThreads, cap));
+    // factor = pi^2 / beta^2 (pme_solve.cpp:341,602), in float like `real`
+    const float  factor  = (float)(M_PI * M_PI) / (p->beta * p->beta);
+    if (p->lj)
+    {
+        // by = 3 V B_y / (pi sqrt(pi) beta^3) (pme_solve.cpp:664)
+        const float by_pref = (float)(3.0 * vol / (M_PI * std::sqrt(M_PI) * (double)p->beta * p->beta * p->beta));
+        k_pme_solve_lj<<<nblocks, kSolveThreads, 0, p->stream>>>(p->d, cgrid, p->bsp, factor, by_pref, p->sums,
+                                                                 p->done, d_energy, d_virial);
+        return cudaGetLastError();
+    }
+    // elfac = ONE_4PI_EPS0 / epsilon_r (pme_solve.cpp:354)
+    const float elfac = (float)nbx::one_4pi_eps0() / p->epsilon_r;
+    const float pivol = (float)M_PI * (float)vol;
     k_pme_solve<<<nblocks, kSolveThreads, 0, p->stream>>>(p->d, cgrid, p->bsp, elfac, factor, pivol, p->sums,
                                                           p->done, d_energy, d_virial);
     return cudaGetLastError();
@@ -679,6 +769,52 @@ int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float 
     cufftSetStream(p->c2r, p->stream);
     *out = p;
     return NBX_OK;
+}
+
+int nbx_pme_create_lj(const float* box, const int* grid, float ewaldcoeff_lj, int device, nbx_pme** out)
+{
+    const int rc = nbx_pme_create(box, grid, ewaldcoeff_lj, 1.0f, device, out);
+    if (rc == NBX_OK)
+    {
+        (*out)->lj = 1;
+    }
+    return rc;
+}
+
+float nbx_ewald_coefficient_lj(float rvdw, float ewald_rtol_lj)
+{
+    // calc_ewaldcoeff_lj (ewald/ewald_utils.cpp:76-115): exp(-x^2)(1 + x^2 + x^4/2) = rtol, x = beta rc
+    if (!(rvdw > 0.0f))
+    {
+        return 0.0f;
+    }
+    const float rtol = ewald_rtol_lj > 0.0f ? ewald_rtol_lj : 1e-3f;
+    auto        f    = [rvdw](float beta) {
+        const float x2 = (beta * rvdw) * (beta * rvdw);
+        return std::exp(-x2) * (1.0f + x2 + x2 * x2 / 2.0f);
+    };
+    float beta = 5.0f;
+    int   i    = 0;
+    do
+    {
+        i++;
+        beta *= 2.0f;
+    } while (f(beta) > rtol);
+    const int n    = i + 60;
+    float     low  = 0.0f, high = beta;
+    for (i = 0; i < n; i++)
+    {
+        beta = (low + high) / 2.0f;
+        if (f(beta) > rtol)
+        {
+            low = beta;
+        }
+        else
+        {
+            high = beta;
+        }
+    }
+    return beta;
 }
 
 int nbx_pme_destroy(nbx_pme* p)

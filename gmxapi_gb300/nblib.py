@@ -31,6 +31,8 @@ class VdwModifier(enum.IntEnum):
     ForceSwitch = 1
     PotSwitch = 2
     NoModifier = 3
+    #: LJ-PME real space (vdwtype PME, geometric grid) with the potential shift
+    LjPme = 4
 
 
 class InputException(ValueError):
@@ -64,6 +66,8 @@ class NBKernelOptions:
     vdw_modifier: "VdwModifier" = None
     #: switching distance for the switch modifiers (nm)
     rvdw_switch: float = 0.0
+    #: LJ-PME (vdw_modifier LJPME): erfc-like tolerance of the LJ Ewald coefficient at rc
+    ewald_rtol_lj: float = 1e-3
 
     def to_c(self) -> _lib.nbx_options:
         o = _lib.nbx_options()
@@ -80,6 +84,7 @@ class NBKernelOptions:
         o.compute_energy = int(bool(self.compute_virial_and_energy))
         o.vdw_modifier = int(self.vdw_modifier if self.vdw_modifier is not None else VdwModifier.PotShift)
         o.rvdw_switch = float(self.rvdw_switch)
+        o.ewald_rtol_lj = float(self.ewald_rtol_lj)
         return o
 
 

@@ -35,6 +35,11 @@ def ewald_coefficient(rcoulomb: float, ewald_rtol: float = 1e-5) -> float:
     return float(_lib.load().nbx_ewald_coefficient(float(rcoulomb), float(ewald_rtol)))
 
 
+def ewald_coefficient_lj(rvdw: float, ewald_rtol_lj: float = 1e-3) -> float:
+    """beta_lj with exp(-x^2)(1 + x^2 + x^4/2) = ewald_rtol_lj, x = beta_lj rvdw (calc_ewaldcoeff_lj)."""
+    return float(_lib.load().nbx_ewald_coefficient_lj(float(rvdw), float(ewald_rtol_lj)))
+
+
 def grid_size(box, spacing: float = 0.12) -> tuple[int, int, int]:
     """PME grid sizes for the box edges and the largest grid spacing (calcFftGrid)."""
     b = (C.c_float * 3)(*[float(v) for v in box])
@@ -44,22 +49,32 @@ def grid_size(box, spacing: float = 0.12) -> tuple[int, int, int]:
 
 
 class Pme:
-    """The Coulomb PME grid of one rectangular box (pme_order 4) on one GPU."""
+    """One PME grid of a rectangular box (pme_order 4) on one GPU: Coulomb (charges), or with
+    ``lj=True`` the LJ-PME dispersion grid (geometric rule; coefficients sqrt(C6_ii), the
+    reference's sqrt_c6A)."""
 
     def __init__(self, box, grid=None, ewald_coeff: float | None = None, *, rcoulomb: float = 1.0,
                  ewald_rtol: float = 1e-5, fourier_spacing: float = 0.12, epsilon_r: float = 1.0,
-                 device: int = 0):
+                 device: int = 0, lj: bool = False, ewald_rtol_lj: float = 1e-3):
         self.box = tuple(float(v) for v in box)
         if len(self.box) != 3:
             raise InputException("rectangular boxes only: three edge lengths")
         self.grid = tuple(int(v) for v in grid) if grid is not None else grid_size(self.box, fourier_spacing)
-        self.beta = float(ewald_coeff) if ewald_coeff is not None else ewald_coefficient(rcoulomb, ewald_rtol)
+        self.lj = bool(lj)
+        if ewald_coeff is not None:
+            self.beta = float(ewald_coeff)
+        else:
+            self.beta = (ewald_coefficient_lj(rcoulomb, ewald_rtol_lj) if self.lj
+                         else ewald_coefficient(rcoulomb, ewald_rtol))
         self.epsilon_r = float(epsilon_r)
         self.device = device
         b = (C.c_float * 3)(*self.box)
         n = (C.c_int * 3)(*self.grid)
         h = C.c_void_p()
-        _check(_lib.load().nbx_pme_create(b, n, self.beta, self.epsilon_r, device, C.byref(h)))
+        if self.lj:
+            _check(_lib.load().nbx_pme_create_lj(b, n, self.beta, device, C.byref(h)))
+        else:
+            _check(_lib.load().nbx_pme_create(b, n, self.beta, self.epsilon_r, device, C.byref(h)))
         self.h = h
         self.energy = 0.0
         self.virial = np.zeros((3, 3))

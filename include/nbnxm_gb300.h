@@ -73,6 +73,7 @@ typedef struct
     int   compute_energy;   /* default energy/virial flag for nbx_compute */
     int   vdw_modifier;     /* nbx_vdw_modifier (0 = potential shift, nblib's only choice) */
     float rvdw_switch;      /* switching distance for the switch modifiers (nm), < rcoulomb */
+    float ewald_rtol_lj;    /* LJ-PME: the LJ Ewald coefficient from rtol (<= 0: 1e-3, the mdp default) */
 } nbx_options;
 
 /* LJ interaction modifiers (mdp vdw-modifier; interaction_const_t::vdw_modifier,
@@ -82,7 +83,11 @@ typedef enum
     NBX_VDW_POTSHIFT    = 0, /* potential shifted to zero at rc, force unchanged */
     NBX_VDW_FORCESWITCH = 1, /* force switched to zero between rvdw_switch and rc */
     NBX_VDW_POTSWITCH   = 2, /* potential switched to zero between rvdw_switch and rc */
-    NBX_VDW_NONE        = 3  /* plain cut-off */
+    NBX_VDW_NONE        = 3, /* plain cut-off */
+    NBX_VDW_LJPME       = 4  /* LJ-PME real space (vdwtype PME, geometric grid) with the potential shift:
+                                the grid part c6grid (1 - e^-b (1 + b + b^2/2)) / r^6, b = beta_lj^2 r^2, is
+                                subtracted (kernel_ref_inner.h:204-252); the reciprocal part is
+                                nbx_pme_create_lj */
 } nbx_vdw_modifier;
 
 typedef struct nbx_handle nbx_handle;
@@ -339,6 +344,14 @@ int nbx_pme_grid_size(const float* box, float spacing, int* n);
 /* Replaces gmx_pme_init (src/gromacs/ewald/pme.h:140): box[3] edges (nm), grid[3]
  * sizes (6..4096 each), the Ewald coefficient, epsilon_r (<= 0 means 1). */
 int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float epsilon_r, int device, nbx_pme** out);
+/* The Lennard-Jones (dispersion) grid of LJ-PME with the geometric combination rule: the same
+ * handle and calls, with the per-atom coefficients sqrt(C6_ii) in place of the charges (the
+ * reference's sqrt_c6A, mdlib/mdatoms.cpp:444) and solve_pme_lj_yzx (pme_solve.cpp:588-915);
+ * energies and virials are the dispersion energy and virial. */
+int nbx_pme_create_lj(const float* box, const int* grid, float ewaldcoeff_lj, int device, nbx_pme** out);
+/* Replaces calc_ewaldcoeff_lj (src/gromacs/ewald/ewald_utils.h): beta with
+ * exp(-x^2)(1 + x^2 + x^4/2) = ewald_rtol_lj, x = beta rvdw (<= 0 means 1e-3). */
+float nbx_ewald_coefficient_lj(float rvdw, float ewald_rtol_lj);
 /* Replaces gmx_pme_destroy (src/gromacs/ewald/pme.h:168). */
 int         nbx_pme_destroy(nbx_pme* p);
 const char* nbx_pme_last_error(const nbx_pme* p);

@@ -1865,8 +1865,15 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
                        int ntypes, const float* nbfp, const int* excl_index, const int* excl_list,
                        int coulomb, double rc, double beta, double epsfac, double k_rf,
                        double c_rf, int use_ewald_shift, const int* subset, int nsub,
-                       double* f_out, double* e2, int vdw_mod, double rvdw_switch)
+                       double* f_out, double* e2, int vdw_mod, double rvdw_switch, double beta_lj)
 {
+    /* vdw_mod 4: LJ-PME real space with the geometric grid (kernel_ref_inner.h:204-252): the
+     * potential-shift LJ plus, for every pair within rc (excluded ones included), the grid part
+     * c6grid (1 - e^-b (1 + b + b^2/2)) / r^6, b = beta_lj^2 r^2, with its shift sh_lj_ewald
+     * (forcerec.cpp:711-712) on interacting pairs, and the self term C6_ii beta_lj^6 / 12. */
+    const double bl2 = beta_lj * beta_lj, bl6_6 = bl2 * bl2 * bl2 / 6.0;
+    const double crc2 = bl2 * rc * rc;
+    const double sh_lj_ewald = vdw_mod == 4 ? (exp(-crc2) * (1 + crc2 + 0.5 * crc2 * crc2) - 1) / pow(rc, 6) : 0.0;
     /* wrap into the box in double */
     double* x = (double*)xmalloc(sizeof(double) * 3 * (size_t)n);
     for (int i = 0; i < n; i++)
@@ -2019,6 +2026,19 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
                                 fscal = qq * (-2 * k_rf);
                             }
                         }
+                        if (vdw_mod == 4)
+                        {
+                            /* the grid part, geometric: sqrt(6 C6_ii) sqrt(6 C6_jj) / 6 (float factors) */
+                            const double c6g = (double)(sqrtf(nbfp[(type[i] * ntypes + type[i]) * 2])
+                                                        * sqrtf(nbfp[(type[j] * ntypes + type[j]) * 2]))
+                                               / 6.0;
+                            const double ir6  = 1.0 / (r2 * r2 * r2);
+                            const double b    = bl2 * r2;
+                            const double em   = exp(-b);
+                            const double poly = 1.0 + b + 0.5 * b * b;
+                            fscal += 6.0 * c6g * (ir6 - em * (ir6 * poly + bl6_6)) / r2;
+                            vlj += 0.5 * c6g * (ir6 * (1.0 - em * poly) + (excl ? 0.0 : sh_lj_ewald));
+                        }
                         if (!excl)
                         {
                             const double c6   = nbfp[(type[i] * ntypes + type[j]) * 2] / 6.0;
@@ -2056,6 +2076,10 @@ void orc_fp64_allpairs(int n, const float* xin, const float* box, const float* q
         for (int d = 0; d < 3; d++)
         {
             f_out[s * 3 + d] = fi[d];
+        }
+        if (vdw_mod == 4)
+        {
+            vlj += 0.5 * (double)nbfp[(type[i] * ntypes + type[i]) * 2] / 6.0 * bl6_6;
         }
         if (coulomb == ORC_COULOMB_EWALD)
         {

@@ -110,7 +110,7 @@ void orc_fp64_allpairs(int n, const float* x, const float* box, const float* q, 
                        int ntypes, const float* nbfp, const int* excl_index, const int* excl_list,
                        int coulomb, double rc, double beta, double epsfac, double k_rf,
                        double c_rf, int use_ewald_shift, const int* subset, int nsub,
-                       double* f_out, double* e2, int vdw_mod, double rvdw_switch);
+                       double* f_out, double* e2, int vdw_mod, double rvdw_switch, double beta_lj);
 
 /* nblib's 1/(4 pi eps0) in kJ mol^-1 nm e^-2 (src/gromacs/math/units.h:79) */
 double orc_one_4pi_eps0(void);

@@ -78,7 +78,8 @@ def lib():
             getattr(L, name).restype = C.POINTER(C.c_uint32)
         L.orc_fp64_allpairs.argtypes = [C.c_int, fp, fp, fp, ip, C.c_int, fp, ip, ip, C.c_int,
                                         C.c_double, C.c_double, C.c_double, C.c_double,
-                                        C.c_double, C.c_int, ip, C.c_int, dp, dp, C.c_int, C.c_double]
+                                        C.c_double, C.c_int, ip, C.c_int, dp, dp, C.c_int, C.c_double,
+                                        C.c_double]
         L.orc_one_4pi_eps0.restype = C.c_double
         _lib = L
     return _lib
@@ -247,8 +248,9 @@ class Oracle:
 
 
 def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
-                  use_ewald_shift=False, epsilon_rf=1.0, vdw_modifier=0, rvdw_switch=0.0):
-    """FP64 explicit-image forces (on ``subset``) and, for the full set, energies."""
+                  use_ewald_shift=False, epsilon_rf=1.0, vdw_modifier=0, rvdw_switch=0.0, beta_lj=0.0):
+    """FP64 explicit-image forces (on ``subset``) and, for the full set, energies.
+    vdw_modifier 4 is LJ-PME real space (geometric grid) with the LJ Ewald coefficient beta_lj."""
     L = lib()
     n = system.n
     epsfac = L.orc_one_4pi_eps0()
@@ -281,5 +283,5 @@ def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
                         0.0 if beta is None else float(beta), epsfac, k_rf, c_rf,
                         int(use_ewald_shift), sp, len(sub), f.ctypes.data_as(C.POINTER(C.c_double)),
                         e.ctypes.data_as(C.POINTER(C.c_double)) if full else None, int(vdw_modifier),
-                        float(np.float32(rvdw_switch)))
+                        float(np.float32(rvdw_switch)), float(beta_lj))
     return (f, e) if full else (f, None)

@@ -15,6 +15,8 @@ cites the reference code it restates (paths inside the GROMACS source tree):
 - ``spread``: spread_coefficients_bsplines_thread + wrap_periodic_pmegrid: atom a adds
   q theta_x theta_y theta_z to points (index + 0..3) mod n.
 - ``solve``: solve_pme_yzx, src/gromacs/ewald/pme_solve.cpp:332-587.
+- ``solve_lj``: solve_pme_lj_yzx with the geometric combination rule (one grid),
+  src/gromacs/ewald/pme_solve.cpp:588-915.
 - ``gather``: gather_f_bsplines / do_fspline, src/gromacs/ewald/pme_gather.cpp:78-360.
 - ``compute``: gmx_pme_do's Coulomb path (spread -> r2c FFT -> solve -> c2r FFT ->
   gather), src/gromacs/ewald/pme.cpp:1002-1300, with unnormalised transforms.
@@ -201,6 +203,50 @@ def solve(cgrid: np.ndarray, n, box, beta: float, epsilon_r: float = 1.0, bsp=No
     return c * eterm, energy, vir
 
 
+def solve_lj(cgrid: np.ndarray, n, box, beta_lj: float, bsp=None):
+    """solve_pme_lj_yzx, geometric combination (one grid; pme_solve.cpp:588-915): the
+    dispersion influence function, energy (0.5 sum) and virial (0.25 sum).  Unlike the
+    Coulomb solve, the k = 0 element is scaled too."""
+    if bsp is None:
+        bsp = [bspline_moduli(n[d]) for d in range(3)]
+    nx, ny, nz = n
+    nzc = nz // 2 + 1
+    kx = np.arange(nx)
+    ky = np.arange(ny)
+    kz = np.arange(nzc)
+    mx = np.where(kx < (nx + 1) // 2, kx, kx - nx).astype(np.float64)
+    my = np.where(ky < (ny + 1) // 2, ky, ky - ny).astype(np.float64)
+    rec = [1.0 / float(np.float32(b)) for b in box]
+    mhx = (mx * rec[0])[:, None, None] * np.ones((1, ny, nzc))
+    mhy = (my * rec[1])[None, :, None] * np.ones((nx, 1, nzc))
+    mhz = (kz * rec[2])[None, None, :] * np.ones((nx, ny, 1))
+    m2 = mhx * mhx + mhy * mhy + mhz * mhz
+    vol = float(np.float32(box[0])) * float(np.float32(box[1])) * float(np.float32(box[2]))
+    factor = np.pi * np.pi / (beta_lj * beta_lj)
+    by = 3.0 * vol * bsp[1] / (np.pi * math.sqrt(np.pi) * beta_lj ** 3)
+    denom = bsp[2][:nzc][None, None, :] * by[None, :, None] * bsp[0][:, None, None]
+    t1 = np.exp(-factor * m2)
+    mk = np.sqrt(factor * m2)
+    from scipy.special import erfc as _erfc
+
+    t2 = math.sqrt(math.pi) * mk * _erfc(mk)
+    m2k = factor * m2
+    eterm = -((1.0 - 2.0 * m2k) * t1 + 2.0 * m2k * t2) / denom
+    vterm = 3.0 * (-t1 + t2) / denom
+    c = np.asarray(cgrid, dtype=np.complex128)
+    struct2 = 2.0 * (c.real ** 2 + c.imag ** 2)
+    corner = np.where((kz == 0) | (kz == (nz + 1) // 2), 0.5, 1.0)[None, None, :]
+    ets2 = corner * eterm * struct2
+    ets2vf = corner * 2.0 * factor * vterm * struct2
+    energy = 0.5 * ets2.sum()
+    mh = (mhx, mhy, mhz)
+    vir = np.zeros((3, 3))
+    for a in range(3):
+        for b in range(a + 1):
+            vir[a, b] = vir[b, a] = 0.25 * (ets2vf * mh[b] * mh[a] - (ets2 if a == b else 0.0)).sum()
+    return c * eterm, energy, vir
+
+
 def gather(grid, idx, theta, dtheta, q, n, box) -> np.ndarray:
     """Reciprocal-space forces [N, 3] (not added to anything)."""
     q = np.asarray(q, dtype=np.float64)
@@ -214,13 +260,17 @@ def gather(grid, idx, theta, dtheta, q, n, box) -> np.ndarray:
     return -q[:, None] * f
 
 
-def compute(x, q, box, n, beta: float, epsilon_r: float = 1.0, single: bool = True):
-    """Forces [N,3], energy and virial of the PME reciprocal part (gmx_pme_do, Coulomb)."""
+def compute(x, q, box, n, beta: float, epsilon_r: float = 1.0, single: bool = True, lj: bool = False):
+    """Forces [N,3], energy and virial of the PME reciprocal part (gmx_pme_do): the Coulomb grid,
+    or with lj=True the LJ-PME dispersion grid (q = sqrt(C6_ii), beta = beta_lj, geometric)."""
     n = tuple(int(v) for v in n)
     idx, theta, dtheta = splines(x, box, n, single)
     grid = spread(idx, theta, q, n)
     cgrid = np.fft.rfftn(grid)
-    cgrid, energy, vir = solve(cgrid, n, box, beta, epsilon_r)
+    if lj:
+        cgrid, energy, vir = solve_lj(cgrid, n, box, beta)
+    else:
+        cgrid, energy, vir = solve(cgrid, n, box, beta, epsilon_r)
     pot = np.fft.irfftn(cgrid, s=n, axes=(0, 1, 2)) * (n[0] * n[1] * n[2])  # unnormalised inverse
     f = gather(pot, idx, theta, dtheta, q, n, box)
     return f, energy, vir

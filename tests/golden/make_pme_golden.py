@@ -147,6 +147,24 @@ def main(ref_root: str) -> None:
                 })
     out["solve"] = solve
 
+    # the Lennard-Jones (geometric) solver on the same inputs: method index 1 of SaneInput and
+    # DifferentEpsilonR (beta_lj 0.7), every case of DifferentEwaldCoeffLJ (beta_lj 2.35)
+    solve_lj = []
+    for prefix, beta_lj, nmeth, meth in (("SaneInput", 0.7, 2, 1), ("DifferentEwaldCoeffLJ", 2.35, 1, 0),
+                                         ("DifferentEpsilonR", 0.7, 2, 1)):
+        for gi, grid in enumerate(sgrids):
+            for vi, vals in enumerate(cgrids):
+                index = ((0 * 2 + gi) * 2 + vi) * nmeth + meth  # box 0
+                root = _root(os.path.join(rdir, f"{prefix}_PmeSolveTest_ReproducesOutputs_{index}.xml"))
+                energy = float(root.find("Real[@Name='Energy']").text)
+                vir = _cells(root.find("Matrix[@Name='Virial']"))
+                solve_lj.append({
+                    "case": prefix, "file_index": index, "box": [sboxes[0][0], sboxes[0][4], sboxes[0][8]],
+                    "grid": grid, "beta_lj": beta_lj, "input": vals,
+                    "output": _cells(root.find("NonZeroGridValues")), "energy": energy, "virial": vir,
+                })
+    out["solve_lj"] = solve_lj
+
     # ---- gather: Combine(boxes, orders 3..5, grid sizes, grids, atom counts 1, 2, 13) ----
     text = open(os.path.join(tdir, "pmegathertest.cpp")).read()
     gboxes = _boxes(text)

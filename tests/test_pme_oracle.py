@@ -161,3 +161,46 @@ def test_exact_forces_are_the_energy_gradient():
         ep = P.ewald_reciprocal_exact(xp, q, box, 3.12, [20, 20, 20])[0]
         em = P.ewald_reciprocal_exact(xm, q, box, 3.12, [20, 20, 20])[0]
         assert -(ep - em) / (2 * h) == pytest.approx(f[i, d], rel=1e-5, abs=1e-3)
+
+
+def test_lj_solve_matches_reference_data(golden):
+    assert len(golden["solve_lj"]) == 12
+    for case in golden["solve_lj"]:
+        out, energy, vir = P.solve_lj(_complex_grid(case), tuple(case["grid"]), case["box"], case["beta_lj"])
+        for key, val in case["output"].items():
+            parts = key.split()
+            v = out[int(parts[1]), int(parts[2]), int(parts[3])]
+            got = v.real if parts[4] == "re" else v.imag
+            assert got == pytest.approx(val, rel=1e-10, abs=1e-300)
+        assert energy == pytest.approx(case["energy"], rel=1e-10)
+        for key, val in case["virial"].items():
+            _, a, b = key.split()
+            assert vir[int(a), int(b)] == pytest.approx(val, rel=1e-9, abs=1e-12 * abs(case["energy"]))
+
+
+def test_lj_pme_reproduces_the_fcc_lattice_energy():
+    """LJ-PME real space (FP64 all-pairs, geometric grid) + the dispersion grid on an argon fcc
+    crystal: the untruncated lattice sums 0.5 N (C12 A12 / a^12 - C6 A6 / a^6), A6 = 14.45392,
+    A12 = 12.13188, less the repulsion's potential shift inside rc."""
+    from gmxapi_gb300 import build, systems
+
+    build.build()
+    from gmxapi_gb300 import pme as pm
+    from oracle import oracle as O
+
+    s = systems.lj_fcc(cells=6, lattice=0.5256, charge=0.0, seed=0)
+    rc = 0.9
+    bl = pm.ewald_coefficient_lj(rc, 1e-3)
+    f_real, e_real = O.fp64_allpairs(s, rc=rc, beta=3.47, vdw_modifier=4, beta_lj=bl)
+    nb = np.asarray(s.nbfp).reshape(-1, 2)
+    c6, c12 = float(nb[0, 0]) / 6.0, float(nb[0, 1]) / 12.0
+    box = [float(b) for b in s.box]
+    f_rec, e_rec, _ = P.compute(s.x, np.full(s.n, np.sqrt(c6)), box, (40, 40, 40), bl, single=False, lj=True)
+    a = 0.5256 / np.sqrt(2.0)
+    d = s.x[0] - s.x
+    d -= np.round(d / s.box) * s.box
+    r = np.sqrt((d * d).sum(1))
+    n_rc = int(np.sum((r > 0) & (r < rc)))
+    expect = 0.5 * s.n * (c12 * 12.13188 / a ** 12 - c6 * 14.45392 / a ** 6) - 0.5 * s.n * n_rc * c12 / rc ** 12
+    assert e_real[0] + e_rec == pytest.approx(expect, rel=2e-5)
+    assert np.abs(f_real + f_rec).max() < 1e-2  # lattice sites are force-free
