@@ -82,15 +82,19 @@ def test_lj_solve_matches_reference_data():
         p.solve_device(dc.data_ptr(), e.data_ptr(), v.data_ptr())
         p.synchronize()
         out = dc.cpu().numpy().astype(np.float64)
+        # the influence function cancels to O(1/b) e^-b at large b, so far-tail values carry float
+        # error; like the reference's solver test, tolerances scale with max(1, largest value) for
+        # the grid, 10 for the energy and 1000 for the virial (pmesolvetest.cpp)
+        scale = max([1.0] + [abs(v_) for v_ in case["output"].values()])
         for key, val in case["output"].items():
             parts = key.split()
             got = out[int(parts[1]), int(parts[2]), int(parts[3]), 0 if parts[4] == "re" else 1]
-            assert got == pytest.approx(val, rel=1e-5, abs=1e-30)
-        assert e.item() == pytest.approx(case["energy"], rel=1e-5)
+            assert got == pytest.approx(val, rel=1e-5, abs=1e-6 * scale)
+        assert e.item() == pytest.approx(case["energy"], rel=1e-5, abs=1e-6 * 10.0)
         vir = v.cpu().numpy().reshape(3, 3)
         for key, val in case["virial"].items():
             _, a, b = key.split()
-            assert vir[int(a), int(b)] == pytest.approx(val, rel=1e-5, abs=1e-6 * abs(case["energy"]))
+            assert vir[int(a), int(b)] == pytest.approx(val, rel=1e-5, abs=1e-6 * 1000.0)
         p.close()
 
 
