@@ -129,11 +129,29 @@ __global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ 
                 continue;
             }
             const float4 xj = b.xq[b.cells[j]];
-            for (int tz = -1; tz <= 1; tz++)
+            // one image per dimension whose box edge is at least 2 rc: the nearest
+            int         lo[3], hi[3];
+            const float xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
+            const float rc    = sqrtf(cv.rc2);
+            for (int d = 0; d < 3; d++)
             {
-                for (int ty = -1; ty <= 1; ty++)
+                const int lim = d == 0 ? nx : 1;
+                if (b.box[d] >= 2.0f * rc)
                 {
-                    for (int tx = -nx; tx <= nx; tx++)
+                    const int t = min(max((int)rintf(xd[d] / b.box[d]), -lim), lim);
+                    lo[d] = hi[d] = t;
+                }
+                else
+                {
+                    lo[d] = -lim;
+                    hi[d] = lim;
+                }
+            }
+            for (int tz = lo[2]; tz <= hi[2]; tz++)
+            {
+                for (int ty = lo[1]; ty <= hi[1]; ty++)
+                {
+                    for (int tx = lo[0]; tx <= hi[0]; tx++)
                     {
                         const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
                         const float dx = (xi.x + b.shiftvec[3 * s]) - xj.x;

@@ -166,6 +166,9 @@ __global__ void k_excl_energy(DeviceView v)
                    * (v.coulomb == 0 ? -(double)v.beta * 0.56418958354775628695 : -0.5 * (double)v.c_rf);
         }
         const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
+        // a box edge of at least 2 rc leaves one image within rc in that dimension: the nearest
+        // (same shift-vector arithmetic as the full image loop, so the same float results)
+        const float  rc  = sqrtf(v.rc2);
         for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
         {
             const int j = v.excl_list[k];
@@ -173,12 +176,28 @@ __global__ void k_excl_energy(DeviceView v)
             {
                 continue;
             }
-            const float4 xj = v.xq[v.cells[j]];
-            for (int tz = -1; tz <= 1; tz++)
+            const float4 xj  = v.xq[v.cells[j]];
+            int          lo[3], hi[3];
+            const float  xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
+            for (int d = 0; d < 3; d++)
             {
-                for (int ty = -1; ty <= 1; ty++)
+                const int lim = d == 0 ? nx : 1;
+                if (v.g.box[d] >= 2.0f * rc)
                 {
-                    for (int tx = -nx; tx <= nx; tx++)
+                    const int t = min(max((int)rintf(xd[d] / v.g.box[d]), -lim), lim);
+                    lo[d] = hi[d] = t;
+                }
+                else
+                {
+                    lo[d] = -lim;
+                    hi[d] = lim;
+                }
+            }
+            for (int tz = lo[2]; tz <= hi[2]; tz++)
+            {
+                for (int ty = lo[1]; ty <= hi[1]; ty++)
+                {
+                    for (int tx = lo[0]; tx <= hi[0]; tx++)
                     {
                         const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
                         const float dx = (xi.x + v.shiftvec[3 * s]) - xj.x;
