@@ -86,24 +86,6 @@ __global__ void k_batch_convert(const BatchSys* __restrict__ sys, const float* _
     }
 }
 
-__constant__ double kBatchErfSeries[16] = {
-    1.0,
-    1.0 / 3.0,
-    1.0 / 10.0,
-    1.0 / 42.0,
-    1.0 / 216.0,
-    1.0 / 1320.0,
-    1.0 / 9360.0,
-    1.0 / 75600.0,
-    1.0 / 685440.0,
-    1.0 / 6894720.0,
-    1.0 / 76204800.0,
-    1.0 / 918086400.0,
-    1.0 / 11975040000.0,
-    1.0 / 168129561600.0,
-    1.0 / 2528170444800.0,
-    1.0 / 40537905408000.0,
-};
 
 // Excluded-pair Coulomb energies in FP64 per system (see k_excl_energy).
 __global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ sys, double* energies)
@@ -111,6 +93,7 @@ __global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ 
     const BatchSys& b   = sys[blockIdx.y];
     const int       i   = blockIdx.x * blockDim.x + threadIdx.x;
     double          acc = 0.0;
+    double          acc_s = 0.0;  // Ewald: sum of q_i q_j S(beta^2 r^2), scaled below
     if (i < b.n && !(b.hdr->status & kStatusGridOverflow))
     {
         const float4 xi = b.xq[b.cells[i]];
@@ -162,37 +145,34 @@ __global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ 
                         {
                             continue;
                         }
-                        const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
-                        double       h;
+                        const double qq = (double)xi.w * (double)xj.w;
                         if (cv.coulomb == 0)
                         {
                             const double bb = (double)cv.beta;
-                            const double w  = bb * bb * r2d;
+                            const double w  = bb * bb * (double)r2;
                             if (w <= 1.0)
                             {
-                                double sum = 0.0;
-                                for (int t = 15; t >= 0; t--)
-                                {
-                                    sum = fma(sum, -w, kBatchErfSeries[t]);
-                                }
-                                h = -bb * 1.1283791670955125739 * sum;
+                                acc_s = fma(qq, erf_over_x_series(w), acc_s);
                             }
                             else
                             {
-                                const double rd = sqrt(r2d);
-                                h               = -erf(bb * rd) / rd;
+                                const double rd = sqrt(fmax((double)dx * dx + (double)dy * dy + (double)dz * dz,
+                                                            (double)kMinDist2));
+                                acc -= qq * erf(bb * rd) / rd;
                             }
                         }
                         else
                         {
-                            h = (double)cv.k_rf * r2d - (double)cv.c_rf;
+                            const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz,
+                                                    (double)kMinDist2);
+                            acc += qq * ((double)cv.k_rf * r2d - (double)cv.c_rf);
                         }
-                        acc += (double)xi.w * (double)xj.w * h;
                     }
                 }
             }
         }
     }
+    acc += acc_s * (-(double)cv.beta * 1.1283791670955125739);
     for (int o = 16; o > 0; o >>= 1)
     {
         acc += __shfl_xor_sync(0xffffffffu, acc, o);

@@ -33,6 +33,7 @@
 #include "nbx_internal.cuh"
 #include "nbx_pair_core.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace nbx
@@ -44,6 +45,150 @@ constexpr int kForceThreads   = 256;
 constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
 constexpr int kStageBytes     = kStageSmemPerWarp;  // per warp: double-buffered j stage and barriers
+
+// Coulomb energy of the excluded pairs within rc, summed in FP64 (Ewald: the
+// series of erf(x)/x with its tail in float, erf_over_x_series), from the exclusion
+// lists: every excluded pair i < j and every periodic image of it with
+// r^2 < rc^2 in the pair kernel's float arithmetic, i.e. exactly the
+// excluded pairs the list-based kernel sees (the half list holds each image
+// pair once).  Ewald: -q_i q_j erf(beta r)/r; RF: q_i q_j (k_rf r^2 - c_rf)
+// (kernel_gpu_ref.cpp:259-291 with int_bit = 0).  Energies only.
+
+constexpr int kExclThreads      = 256;
+constexpr int kExclBlocksPerSm = 4;
+constexpr int kExclChunkAtoms  = 128;  // atoms per exclusion work item of k_force (4 per lane)
+
+// The excluded pairs (j > i) and the self term of atom i: Coulomb terms into acc (scaled by
+// epsfac by the caller), the Ewald series sums into acc_s (scaled by -beta 2/sqrt(pi) by the
+// caller), the LJ-PME grid part into acc_lj.
+__device__ __forceinline__ void excl_atom(const DeviceView& v, int i, bool ljpme, double beta2, double& acc,
+                                          double& acc_s, double& acc_lj)
+{
+    const float4 xi  = v.xq[v.cells[i]];
+    const double qi  = (double)xi.w;
+    const int    nt1 = v.ntypes1;
+    const float  sci = ljpme ? sqrtf(v.nbfp[v.type[i] * (nt1 + 1)].x) : 0.0f;
+    if (v.self_on_device)
+    {
+        // self term, kernel_gpu_ref.cpp:154-178 (acc is scaled by epsfac by the caller)
+        acc += (double)xi.w * (double)xi.w
+               * (v.coulomb == 0 ? -(double)v.beta * 0.56418958354775628695 : -0.5 * (double)v.c_rf);
+    }
+    const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
+    // a box edge of at least 2 rc leaves one image within rc in that dimension: the nearest
+    // (same shift-vector arithmetic as the full image loop, so the same float results)
+    const float  rc  = sqrtf(v.rc2);
+    for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
+    {
+        const int j = v.excl_list[k];
+        if (j <= i)
+        {
+            continue;
+        }
+        const float4 xj  = v.xq[v.cells[j]];
+        int          lo[3], hi[3];
+        const float  xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
+        for (int d = 0; d < 3; d++)
+        {
+            const int lim = d == 0 ? nx : 1;
+            if (v.g.box[d] >= 2.0f * rc)
+            {
+                const int t = min(max((int)rintf(xd[d] / v.g.box[d]), -lim), lim);
+                lo[d] = hi[d] = t;
+            }
+            else
+            {
+                lo[d] = -lim;
+                hi[d] = lim;
+            }
+        }
+        for (int tz = lo[2]; tz <= hi[2]; tz++)
+        {
+            for (int ty = lo[1]; ty <= hi[1]; ty++)
+            {
+                for (int tx = lo[0]; tx <= hi[0]; tx++)
+                {
+                    const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
+                    const float dx = (xi.x + v.shiftvec[3 * s]) - xj.x;
+                    const float dy = (xi.y + v.shiftvec[3 * s + 1]) - xj.y;
+                    const float dz = (xi.z + v.shiftvec[3 * s + 2]) - xj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (!(r2 < v.rc2))
+                    {
+                        continue;
+                    }
+                    const double qq  = qi * (double)xj.w;
+                    // r^2 in FP64 from the float differences, only where the series is not used
+                    auto r2_fp64 = [&]() {
+                        return fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
+                    };
+                    if (v.coulomb == 0)
+                    {
+                        // -erf(beta r)/r = -beta 2/sqrt(pi) S(beta^2 r^2); excluded pairs are
+                        // short (beta r <= 1), so S comes from its series (the factor is
+                        // applied once per thread by the caller).  w from the float r^2: its rounding
+                        // differs from pair to pair and averages out in the sum.
+                        const double w = beta2 * (double)r2;
+                        if (w <= 1.0)
+                        {
+                            acc_s = fma(qq, erf_over_x_series(w), acc_s);
+                        }
+                        else
+                        {
+                            const double rd = sqrt(r2_fp64());
+                            acc -= qq * erf((double)v.beta * rd) / rd;
+                        }
+                    }
+                    else
+                    {
+                        acc += qq * ((double)v.k_rf * r2_fp64() - (double)v.c_rf);
+                    }
+                    if (ljpme)
+                    {
+                        // c6grid / 6 r^-6 (1 - e^-b (1 + b + b^2/2)), b = beta_lj^2 r^2
+                        const int    tj     = v.type[j];
+                        const double c6grid = (double)(sci * sqrtf(v.nbfp[tj * (nt1 + 1)].x));
+                        const double r2d    = r2_fp64();
+                        const double b      = (double)v.lje_coeff2 * r2d;
+                        const double ir6    = 1.0 / (r2d * r2d * r2d);
+                        acc_lj += c6grid / 6.0 * ir6 * (1.0 - exp(-b) * (1.0 + b + 0.5 * b * b));
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Work item t of k_force's queue: list entries E and exclusion chunks C interleaved, one chunk
+// after every E / C entries (the chunks' FP64 and gather work then overlaps other warps' pair
+// work instead of running as a separate launch); idx is the entry or the chunk.
+__device__ __forceinline__ bool item_is_chunk(int t, int E, int C, int& idx)
+{
+    if (C == 0)
+    {
+        idx = t;
+        return false;
+    }
+    const int s = E / C;
+    if (s >= 1)
+    {
+        const int q = t / (s + 1), r = t - q * (s + 1);
+        if (q < C)
+        {
+            idx = (r == s) ? q : q * s + r;
+            return r == s;
+        }
+        idx = C * s + (t - C * (s + 1));
+        return false;
+    }
+    if (t < 2 * E)
+    {
+        idx = t >> 1;
+        return (t & 1) != 0;
+    }
+    idx = E + (t - 2 * E);
+    return true;
+}
 
 template<bool kEnergy, bool kEwald, int kLj = 0>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
@@ -85,17 +230,34 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     const float    k_rf2   = v.k_rf2;
 
     double e_lj_acc = 0.0, e_el_acc = 0.0;
+    // excluded-pair and self energies as work items of this queue (LJ-PME keeps its own kernel)
+    const int numChunks = (kEnergy && kLj != 3) ? v.excl_chunks : 0;
+    double    excl_s    = 0.0;  // Ewald series sums of the exclusion items (scaled at the end)
     for (;;)
     {
-        int e = 0;
+        int t = 0;
         if (lane == 0)
         {
-            e = atomicAdd(work_counter, 1);
+            t = atomicAdd(work_counter, 1);
         }
-        e = __shfl_sync(full, e, 0);
-        if (e >= numSci)
+        t = __shfl_sync(full, t, 0);
+        if (t >= numSci + numChunks)
         {
             break;
+        }
+        int e;
+        if (item_is_chunk(t, numSci, numChunks, e))
+        {
+            if (kEnergy && kLj != 3)
+            {
+                const double beta2 = (double)v.beta * (double)v.beta;
+                for (int i = e * kExclChunkAtoms + lane; i < min(v.n, (e + 1) * kExclChunkAtoms); i += 32)
+                {
+                    double dummy_lj = 0.0;
+                    excl_atom(v, i, false, beta2, e_el_acc, excl_s, dummy_lj);
+                }
+            }
+            continue;
         }
         const Sci     s = v.sci[e];
         const SysPtrs p = { v.xq, v.tgrid, v.fnb, v.cj4, v.excl, v.shiftvec, v.fshift };
@@ -108,6 +270,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     }
     if (kEnergy)
     {
+        e_el_acc += excl_s * (-(double)v.beta * 1.1283791670955125739);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
         {
@@ -122,154 +285,62 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     }
 }
 
-// Coulomb energy of the excluded pairs within rc, in FP64, from the exclusion
-// lists: every excluded pair i < j and every periodic image of it with
-// r^2 < rc^2 in the pair kernel's float arithmetic, i.e. exactly the
-// excluded pairs the list-based kernel sees (the half list holds each image
-// pair once).  Ewald: -q_i q_j erf(beta r)/r; RF: q_i q_j (k_rf r^2 - c_rf)
-// (kernel_gpu_ref.cpp:259-291 with int_bit = 0).  Energies only.
-// 1/(n! (2n+1)), n = 0..15
-__constant__ double kErfSeries[16] = {
-    1.0,
-    1.0 / 3.0,
-    1.0 / 10.0,
-    1.0 / 42.0,
-    1.0 / 216.0,
-    1.0 / 1320.0,
-    1.0 / 9360.0,
-    1.0 / 75600.0,
-    1.0 / 685440.0,
-    1.0 / 6894720.0,
-    1.0 / 76204800.0,
-    1.0 / 918086400.0,
-    1.0 / 11975040000.0,
-    1.0 / 168129561600.0,
-    1.0 / 2528170444800.0,
-    1.0 / 40537905408000.0,
-};
-
-__global__ void k_excl_energy(DeviceView v)
+__global__ void __launch_bounds__(kExclThreads) k_excl_energy(DeviceView v)
 {
-    const int i      = blockIdx.x * blockDim.x + threadIdx.x;
     double    acc    = 0.0;
     double    acc_lj = 0.0;  // LJ-PME: the grid part of excluded pairs
+    double    acc_s  = 0.0;  // Ewald: sum of q_i q_j S(beta^2 r^2) over excluded pairs
     const bool ljpme = v.vdw_mod == NBX_VDW_LJPME;
-    if (i < v.n)
+    const double beta2 = (double)v.beta * (double)v.beta;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x)
     {
-        const float4 xi  = v.xq[v.cells[i]];
-        const int    nt1 = v.ntypes1;
-        const float  sci = ljpme ? sqrtf(v.nbfp[v.type[i] * (nt1 + 1)].x) : 0.0f;
-        if (v.self_on_device)
-        {
-            // self term, kernel_gpu_ref.cpp:154-178 (acc is scaled by epsfac below)
-            acc += (double)xi.w * (double)xi.w
-                   * (v.coulomb == 0 ? -(double)v.beta * 0.56418958354775628695 : -0.5 * (double)v.c_rf);
-        }
-        const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
-        // a box edge of at least 2 rc leaves one image within rc in that dimension: the nearest
-        // (same shift-vector arithmetic as the full image loop, so the same float results)
-        const float  rc  = sqrtf(v.rc2);
-        for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
-        {
-            const int j = v.excl_list[k];
-            if (j <= i)
-            {
-                continue;
-            }
-            const float4 xj  = v.xq[v.cells[j]];
-            int          lo[3], hi[3];
-            const float  xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
-            for (int d = 0; d < 3; d++)
-            {
-                const int lim = d == 0 ? nx : 1;
-                if (v.g.box[d] >= 2.0f * rc)
-                {
-                    const int t = min(max((int)rintf(xd[d] / v.g.box[d]), -lim), lim);
-                    lo[d] = hi[d] = t;
-                }
-                else
-                {
-                    lo[d] = -lim;
-                    hi[d] = lim;
-                }
-            }
-            for (int tz = lo[2]; tz <= hi[2]; tz++)
-            {
-                for (int ty = lo[1]; ty <= hi[1]; ty++)
-                {
-                    for (int tx = lo[0]; tx <= hi[0]; tx++)
-                    {
-                        const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
-                        const float dx = (xi.x + v.shiftvec[3 * s]) - xj.x;
-                        const float dy = (xi.y + v.shiftvec[3 * s + 1]) - xj.y;
-                        const float dz = (xi.z + v.shiftvec[3 * s + 2]) - xj.z;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        if (!(r2 < v.rc2))
-                        {
-                            continue;
-                        }
-                        const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
-                        double       h;
-                        if (v.coulomb == 0)
-                        {
-                            // erf(x)/x = 2/sqrt(pi) sum_n (-x^2)^n / (n! (2n+1)); 16 terms reach
-                            // double precision for x <= 1 (excluded pairs are short), no
-                            // square root or division needed
-                            const double b = (double)v.beta;
-                            const double w = b * b * r2d;
-                            if (w <= 1.0)
-                            {
-                                double sum = 0.0;
-                                for (int k = 15; k >= 0; k--)
-                                {
-                                    sum = fma(sum, -w, kErfSeries[k]);
-                                }
-                                h = -b * 1.1283791670955125739 * sum;
-                            }
-                            else
-                            {
-                                const double rd = sqrt(r2d);
-                                h               = -erf(b * rd) / rd;
-                            }
-                        }
-                        else
-                        {
-                            h = (double)v.k_rf * r2d - (double)v.c_rf;
-                        }
-                        acc += (double)xi.w * (double)xj.w * h;
-                        if (ljpme)
-                        {
-                            // c6grid / 6 r^-6 (1 - e^-b (1 + b + b^2/2)), b = beta_lj^2 r^2
-                            const int    tj     = v.type[j];
-                            const double c6grid = (double)(sci * sqrtf(v.nbfp[tj * (nt1 + 1)].x));
-                            const double b      = (double)v.lje_coeff2 * r2d;
-                            const double ir6    = 1.0 / (r2d * r2d * r2d);
-                            acc_lj += c6grid / 6.0 * ir6 * (1.0 - exp(-b) * (1.0 + b + 0.5 * b * b));
-                        }
-                    }
-                }
-            }
-        }
+        excl_atom(v, i, ljpme, beta2, acc, acc_s, acc_lj);
     }
+    acc += acc_s * (-(double)v.beta * 1.1283791670955125739);
+    // warp, then block sums: one atomic per block and sum (a few hundred blocks), not one per
+    // warp, because same-address FP64 atomics serialise in L2
+    __shared__ double part[2][kExclThreads / 32];
     for (int o = 16; o > 0; o >>= 1)
     {
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
         acc_lj += __shfl_xor_sync(0xffffffffu, acc_lj, o);
     }
-    if ((threadIdx.x & 31) == 0 && acc != 0.0)
+    if ((threadIdx.x & 31) == 0)
     {
-        atomicAdd(&v.energy[1], acc * v.epsfac_d);
+        part[0][threadIdx.x >> 5] = acc;
+        part[1][threadIdx.x >> 5] = acc_lj;
     }
-    if ((threadIdx.x & 31) == 0 && acc_lj != 0.0)
+    __syncthreads();
+    if (threadIdx.x < 2)
     {
-        atomicAdd(&v.energy[0], acc_lj);
+        double t = 0.0;
+        for (int w = 0; w < kExclThreads / 32; w++)
+        {
+            t += part[threadIdx.x][w];
+        }
+        if (t != 0.0)
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicAdd(&v.energy[1], t * v.epsfac_d);
+            }
+            else
+            {
+                atomicAdd(&v.energy[0], t);
+            }
+        }
     }
+}
+
+int excl_blocks(int n, int num_sms)
+{
+    return std::max(1, std::min((n + kExclThreads - 1) / kExclThreads, kExclBlocksPerSm * num_sms));
 }
 
 // f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k: each
 // thread gathers kReduceAtoms atoms and sums their x (x) f in float, the
 // partial sums are reduced in FP64.
-constexpr int kReduceAtoms = 8;
+constexpr int kReduceAtoms = 4;
 
 __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
 {
@@ -279,32 +350,39 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
     {
         w[k] = 0.0f;
     }
+    // all gathers first, then the stores: stores through f may alias the loads, so loads
+    // written after a store would wait for it
     const int a0 = (blockIdx.x * blockDim.x) * kReduceAtoms + threadIdx.x;
+    int       ks[kReduceAtoms];
 #pragma unroll
     for (int r = 0; r < kReduceAtoms; r++)
     {
         const int a = a0 + r * blockDim.x;
-        if (a < v.n)
+        ks[r]       = a < v.n ? v.cells[a] : -1;
+    }
+    float4 fa[kReduceAtoms], xa[kReduceAtoms];
+#pragma unroll
+    for (int r = 0; r < kReduceAtoms; r++)
+    {
+        if (ks[r] >= 0)
         {
-            const int    k  = v.cells[a];
-            const float4 fa = v.fnb[k];
-            if (v.accumulate_f)
-            {
-                f[3 * a] += fa.x;
-                f[3 * a + 1] += fa.y;
-                f[3 * a + 2] += fa.z;
-            }
-            else
-            {
-                f[3 * a]     = fa.x;
-                f[3 * a + 1] = fa.y;
-                f[3 * a + 2] = fa.z;
-            }
+            fa[r] = v.fnb[ks[r]];
             if (do_virial)
             {
-                const float4 xa   = v.xq[k];
-                const float  xv[3] = { xa.x, xa.y, xa.z };
-                const float  fv[3] = { fa.x, fa.y, fa.z };
+                xa[r] = v.xq[ks[r]];
+            }
+        }
+    }
+    if (do_virial)
+    {
+        // the virial of the nonbonded forces only (before any accumulation into f)
+#pragma unroll
+        for (int r = 0; r < kReduceAtoms; r++)
+        {
+            if (ks[r] >= 0)
+            {
+                const float xv[3] = { xa[r].x, xa[r].y, xa[r].z };
+                const float fv[3] = { fa[r].x, fa[r].y, fa[r].z };
 #pragma unroll
                 for (int p = 0; p < 3; p++)
                 {
@@ -315,6 +393,42 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
                     }
                 }
             }
+        }
+    }
+    if (v.accumulate_f)
+    {
+        float old[kReduceAtoms][3];
+#pragma unroll
+        for (int r = 0; r < kReduceAtoms; r++)
+        {
+            if (ks[r] >= 0)
+            {
+                const int a = a0 + r * blockDim.x;
+                old[r][0]   = f[3 * a];
+                old[r][1]   = f[3 * a + 1];
+                old[r][2]   = f[3 * a + 2];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kReduceAtoms; r++)
+        {
+            if (ks[r] >= 0)
+            {
+                fa[r].x += old[r][0];
+                fa[r].y += old[r][1];
+                fa[r].z += old[r][2];
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kReduceAtoms; r++)
+    {
+        if (ks[r] >= 0)
+        {
+            const int a  = a0 + r * blockDim.x;
+            f[3 * a]     = fa[r].x;
+            f[3 * a + 1] = fa[r].y;
+            f[3 * a + 2] = fa[r].z;
         }
     }
     if (!do_virial)
@@ -439,9 +553,17 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     const int    blocks = num_sms * kForceMinBlocks;
     const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1 + kStageBytes * (kForceThreads / 32);
     const bool   ewald  = (v.coulomb == 0);
-    if (energy)
+    // the energy flavours take the excluded-pair and self energies as work items, except LJ-PME
+    // (its excluded pairs need the FP64 grid term: a separate kernel)
+    DeviceView kv = v;
+    kv.excl_chunks = 0;
+    if (energy && v.vdw_mod == NBX_VDW_LJPME)
     {
-        k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
+        k_excl_energy<<<excl_blocks(v.n, num_sms), kExclThreads, 0, s>>>(v);
+    }
+    else if (energy)
+    {
+        kv.excl_chunks = (v.n + kExclChunkAtoms - 1) / kExclChunkAtoms;
     }
     if (ev0)
     {
@@ -455,50 +577,50 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     if (lj == 3)
     {
         if (energy)
-            ewald ? k_force<true, true, 3><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<true, false, 3><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<true, true, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<true, false, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         else
-            ewald ? k_force<false, true, 3><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<false, false, 3><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<false, true, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<false, false, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter);
     }
     else if (lj == 1)
     {
         if (energy)
-            ewald ? k_force<true, true, 1><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<true, false, 1><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<true, true, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<true, false, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         else
-            ewald ? k_force<false, true, 1><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<false, false, 1><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<false, true, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<false, false, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter);
     }
     else if (lj == 2)
     {
         if (energy)
-            ewald ? k_force<true, true, 2><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<true, false, 2><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<true, true, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<true, false, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         else
-            ewald ? k_force<false, true, 2><<<blocks, kForceThreads, smem, s>>>(v, counter)
-                  : k_force<false, false, 2><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            ewald ? k_force<false, true, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter)
+                  : k_force<false, false, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter);
     }
     else if (energy)
     {
         if (ewald)
         {
-            k_force<true, true><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            k_force<true, true><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         }
         else
         {
-            k_force<true, false><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            k_force<true, false><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         }
     }
     else
     {
         if (ewald)
         {
-            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         }
         else
         {
-            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, counter);
+            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(kv, counter);
         }
     }
     if (ev1)
@@ -730,7 +852,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         int*         ctr    = &v.hdr->work_counter;
         if (energy)
         {
-            k_excl_energy<<<(v.n + 255) / 256, 256, 0, s>>>(v);
+            k_excl_energy<<<excl_blocks(v.n, num_sms), kExclThreads, 0, s>>>(v);
             if (v.coulomb == 0)
             {
                 k_force<true, true><<<blocks, kForceThreads, smem, s>>>(v, ctr);

@@ -43,6 +43,29 @@ __device__ __forceinline__ float erfc_poly(float t)
     return fmaf(p, t, 2.664087117e-01f);
 }
 
+// sqrt(pi)/2 erf(x)/x for w = x^2 <= 1, from its Maclaurin series sum_n (-w)^n / (n! (2n+1)):
+// 1 - w/3 in FP64 and the tail w^2 sum_{n>=2} in float (terms n <= 13; the first dropped term is
+// 1.1e-13 at w = 1).  The tail is at most 0.1 of the result, so its float rounding stays below
+// 1e-8 relative, and the FP64 part is three operations (FP64 issues at a small fraction of the
+// FP32 rate).  wd is w in FP64; the float tail uses w rounded to float.
+__device__ __forceinline__ double erf_over_x_series(double wd)
+{
+    const float w = (float)wd;
+    float       r = 5.94779391e-12f;  // 1/(13! 27)
+    r             = fmaf(r, -w, 8.35070277e-11f);
+    r             = fmaf(r, -w, 1.08922216e-09f);
+    r             = fmaf(r, -w, 1.31225333e-08f);
+    r             = fmaf(r, -w, 1.45038527e-07f);
+    r             = fmaf(r, -w, 1.45891693e-06f);
+    r             = fmaf(r, -w, 1.32275136e-05f);
+    r             = fmaf(r, -w, 1.06837608e-04f);
+    r             = fmaf(r, -w, 7.57575734e-04f);
+    r             = fmaf(r, -w, 4.62962966e-03f);
+    r             = fmaf(r, -w, 2.38095243e-02f);
+    r             = fmaf(r, -w, 1.00000001e-01f);  // 1/(2! 5)
+    return fma(wd, -1.0 / 3.0, 1.0) + (double)(w * w * r);
+}
+
 // Device status word bits (nbx_status values are derived from these on the host).
 enum StatusBits : unsigned
 {
@@ -180,6 +203,9 @@ struct DeviceView
     // 1: k_reduce_f adds the nonbonded forces to the caller's buffer
     // (nbnxn_gpu_add_nbat_f_to_f_kernel<accumulateForce = true>); 0: overwrites it
     int accumulate_f;
+    // > 0: the energy flavours of k_force also compute the excluded-pair and self energies, as
+    // this many work items of kExclChunkAtoms atoms interleaved with the list entries
+    int excl_chunks;
 };
 
 // One system of a batch, as the batched kernels see it (device table).
