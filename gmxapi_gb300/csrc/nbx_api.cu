@@ -51,6 +51,7 @@ struct nbx_handle
     double* d_out = nullptr;  // energies[2] + virial[9]
     unsigned long long* d_count = nullptr;
     ListHeader* h_hdr = nullptr;  // pinned copy for reading sizes
+    double*     h_out = nullptr;  // pinned copy of the energies and virial (11 doubles)
     // adjoint scratch, allocated on the first backward call
     float4* d_gnb   = nullptr;
     float4* d_dnb   = nullptr;
@@ -427,6 +428,22 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
     return cuda_check(h, e, "compute");
 }
 
+// The device address of a host array the GPU can access directly (pinned memory mapped
+// into the device's address space, e.g. cudaHostAlloc / cudaMallocHost under unified
+// addressing), or nullptr: then the array is staged by copies.  Kernels then read the
+// coordinates from and write the forces to host memory over the host link, overlapping
+// the transfer with the kernels that use it.
+void* mapped_device_ptr(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 bool valid_box(const float* box)
 {
     for (int d = 0; d < 3; d++)
@@ -782,6 +799,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (e == cudaSuccess) e = dalloc(h, &h->d_out, 11);
     if (e == cudaSuccess) e = dalloc(h, &h->d_count, 1);
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_hdr, sizeof(ListHeader));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_out, 11 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpyAsync(q, sys->q, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(t, sys->type, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ei, sys->excl_index, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream);
@@ -831,6 +849,7 @@ int nbx_destroy(nbx_handle* h)
     if (h->h_hdr)
     {
         cudaFreeHost(h->h_hdr);
+        cudaFreeHost(h->h_out);
     }
     for (auto& p : h->ev_pending)
     {
@@ -900,26 +919,32 @@ int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, doubl
     }
     cudaSetDevice(h->device);
     const size_t bytes = sizeof(float) * 3 * h->n;
-    cudaError_t  e     = cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream);
-    int          rc    = cuda_check(h, e, "nbx_compute H2D");
-    if (rc != NBX_OK)
+    // mapped pinned arrays are read / written by the kernels in place; others are copied
+    const float* d_x = static_cast<const float*>(mapped_device_ptr(x));
+    float*       d_f = static_cast<float*>(mapped_device_ptr(f));
+    if (!d_x)
     {
-        return rc;
+        const int rc = cuda_check(h, cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream),
+                                  "nbx_compute H2D");
+        if (rc != NBX_OK)
+        {
+            return rc;
+        }
+        d_x = h->d_x;
     }
     // host arrays: forces are overwritten (GmxForceCalculator::compute), whatever nbx_set_force_accumulate says
     const int accumulate = h->v.accumulate_f;
     h->v.accumulate_f    = 0;
-    rc = compute_async(h, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    int rc = compute_async(h, d_x, d_f ? d_f : h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
     h->v.accumulate_f = accumulate;
     if (rc != NBX_OK)
     {
         return rc;
     }
-    e = cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
-    double hout[11];
+    cudaError_t e = d_f ? cudaSuccess : cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess && (energies || virial))
     {
-        e = cudaMemcpyAsync(hout, h->d_out, sizeof(hout), cudaMemcpyDeviceToHost, h->stream);
+        e = cudaMemcpyAsync(h->h_out, h->d_out, 11 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->h_hdr, h->v.hdr, sizeof(ListHeader), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -929,12 +954,12 @@ int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, doubl
     }
     if (energies)
     {
-        energies[0] = hout[0];
-        energies[1] = hout[1];
+        energies[0] = h->h_out[0];
+        energies[1] = h->h_out[1];
     }
     if (virial)
     {
-        std::memcpy(virial, hout + 2, 9 * sizeof(double));
+        std::memcpy(virial, h->h_out + 2, 9 * sizeof(double));
     }
     return status_to_error(h, h->h_hdr->status);
 }
@@ -1030,25 +1055,34 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
     }
     cudaSetDevice(h->device);
     const size_t bytes = sizeof(float) * 3 * h->n;
-    cudaError_t  e     = cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream);
-    int          rc    = cuda_check(h, e, "nbx_md_step H2D");
-    if (rc != NBX_OK)
+    // mapped pinned arrays are read / written by the kernels in place, except the
+    // coordinates of a search step (the gridding passes read them several times)
+    const bool   search = !h->have_list || step % std::max(1, h->opts.nstlist) == 0;
+    const float* d_x    = search ? nullptr : static_cast<const float*>(mapped_device_ptr(x));
+    float*       d_f    = static_cast<float*>(mapped_device_ptr(f));
+    if (!d_x)
     {
-        return rc;
+        const int rc = cuda_check(h, cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream),
+                                  "nbx_md_step H2D");
+        if (rc != NBX_OK)
+        {
+            return rc;
+        }
+        d_x = h->d_x;
     }
     const int accumulate = h->v.accumulate_f;  // host arrays: forces are overwritten
     h->v.accumulate_f    = 0;
-    rc = nbx_md_step_device(h, step, h->d_x, h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
+    int rc = nbx_md_step_device(h, step, d_x, d_f ? d_f : h->d_f, energies ? h->d_out : nullptr,
+                                virial ? h->d_out + 2 : nullptr);
     h->v.accumulate_f = accumulate;
     if (rc != NBX_OK)
     {
         return rc;
     }
-    double hout[11];
-    e = cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e = d_f ? cudaSuccess : cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess && (energies || virial))
     {
-        e = cudaMemcpyAsync(hout, h->d_out, sizeof(hout), cudaMemcpyDeviceToHost, h->stream);
+        e = cudaMemcpyAsync(h->h_out, h->d_out, 11 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if ((rc = cuda_check(h, e, "nbx_md_step D2H")) != NBX_OK)
@@ -1057,12 +1091,12 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
     }
     if (energies)
     {
-        energies[0] = hout[0];
-        energies[1] = hout[1];
+        energies[0] = h->h_out[0];
+        energies[1] = h->h_out[1];
     }
     if (virial)
     {
-        std::memcpy(virial, hout + 2, 9 * sizeof(double));
+        std::memcpy(virial, h->h_out + 2, 9 * sizeof(double));
     }
     return NBX_OK;
 }

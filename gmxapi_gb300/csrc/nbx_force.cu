@@ -229,10 +229,15 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     const float    c2b     = v.c2b;      // 2 beta / sqrt(pi)
     const float    k_rf2   = v.k_rf2;
 
-    double e_lj_acc = 0.0, e_el_acc = 0.0;
+    // per-lane FP64 energy sums, in shared memory: they change once per entry, and registers
+    // are what the pair loop is short of
+    __shared__ double e_acc_s[2][kForceThreads];
+    double&           e_lj_acc = e_acc_s[0][threadIdx.x];
+    double&           e_el_acc = e_acc_s[1][threadIdx.x];
+    e_lj_acc                   = 0.0;
+    e_el_acc                   = 0.0;
     // excluded-pair and self energies as work items of this queue (LJ-PME keeps its own kernel)
     const int numChunks = (kEnergy && kLj != 3) ? v.excl_chunks : 0;
-    double    excl_s    = 0.0;  // Ewald series sums of the exclusion items (scaled at the end)
     for (;;)
     {
         int t = 0;
@@ -250,12 +255,14 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
         {
             if (kEnergy && kLj != 3)
             {
-                const double beta2 = (double)v.beta * (double)v.beta;
+                const double beta2  = (double)v.beta * (double)v.beta;
+                double       excl_s = 0.0;  // Ewald series sums of this item
                 for (int i = e * kExclChunkAtoms + lane; i < min(v.n, (e + 1) * kExclChunkAtoms); i += 32)
                 {
                     double dummy_lj = 0.0;
                     excl_atom(v, i, false, beta2, e_el_acc, excl_s, dummy_lj);
                 }
+                e_el_acc = fma(excl_s, -(double)v.beta * 1.1283791670955125739, e_el_acc);
             }
             continue;
         }
@@ -270,17 +277,17 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
     }
     if (kEnergy)
     {
-        e_el_acc += excl_s * (-(double)v.beta * 1.1283791670955125739);
+        double elj = e_lj_acc, eel = e_el_acc;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
         {
-            e_lj_acc += __shfl_xor_sync(full, e_lj_acc, o);
-            e_el_acc += __shfl_xor_sync(full, e_el_acc, o);
+            elj += __shfl_xor_sync(full, elj, o);
+            eel += __shfl_xor_sync(full, eel, o);
         }
         if (lane == 0)
         {
-            atomicAdd(&v.energy[0], e_lj_acc);
-            atomicAdd(&v.energy[1], e_el_acc * v.epsfac_d);
+            atomicAdd(&v.energy[0], elj);
+            atomicAdd(&v.energy[1], eel * v.epsfac_d);
         }
     }
 }
@@ -340,9 +347,10 @@ int excl_blocks(int n, int num_sms)
 // f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k: each
 // thread gathers kReduceAtoms atoms and sums their x (x) f in float, the
 // partial sums are reduced in FP64.
-constexpr int kReduceAtoms = 4;
+constexpr int kReduceAtoms   = 4;
+constexpr int kReduceThreads = 256;
 
-__global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
 {
     float w[9];
 #pragma unroll
@@ -352,12 +360,12 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
     }
     // all gathers first, then the stores: stores through f may alias the loads, so loads
     // written after a store would wait for it
-    const int a0 = (blockIdx.x * blockDim.x) * kReduceAtoms + threadIdx.x;
+    const int a0 = (blockIdx.x * kReduceThreads) * kReduceAtoms + threadIdx.x;
     int       ks[kReduceAtoms];
 #pragma unroll
     for (int r = 0; r < kReduceAtoms; r++)
     {
-        const int a = a0 + r * blockDim.x;
+        const int a = a0 + r * kReduceThreads;
         ks[r]       = a < v.n ? v.cells[a] : -1;
     }
     float4 fa[kReduceAtoms], xa[kReduceAtoms];
@@ -395,40 +403,36 @@ __global__ void k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
             }
         }
     }
-    if (v.accumulate_f)
-    {
-        float old[kReduceAtoms][3];
-#pragma unroll
-        for (int r = 0; r < kReduceAtoms; r++)
-        {
-            if (ks[r] >= 0)
-            {
-                const int a = a0 + r * blockDim.x;
-                old[r][0]   = f[3 * a];
-                old[r][1]   = f[3 * a + 1];
-                old[r][2]   = f[3 * a + 2];
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < kReduceAtoms; r++)
-        {
-            if (ks[r] >= 0)
-            {
-                fa[r].x += old[r][0];
-                fa[r].y += old[r][1];
-                fa[r].z += old[r][2];
-            }
-        }
-    }
+    // stage the block's forces in shared memory, then write them as contiguous floats:
+    // whole sectors also when f is host memory written over the host link
+    __shared__ float sf[3 * kReduceThreads * kReduceAtoms];
 #pragma unroll
     for (int r = 0; r < kReduceAtoms; r++)
     {
         if (ks[r] >= 0)
         {
-            const int a  = a0 + r * blockDim.x;
-            f[3 * a]     = fa[r].x;
-            f[3 * a + 1] = fa[r].y;
-            f[3 * a + 2] = fa[r].z;
+            const int j   = threadIdx.x + r * kReduceThreads;
+            sf[3 * j]     = fa[r].x;
+            sf[3 * j + 1] = fa[r].y;
+            sf[3 * j + 2] = fa[r].z;
+        }
+    }
+    __syncthreads();
+    const int base  = blockIdx.x * kReduceThreads * kReduceAtoms;
+    const int count = 3 * min(kReduceThreads * kReduceAtoms, v.n - base);
+    float*    fb    = f + 3 * (size_t)base;
+    if (v.accumulate_f)
+    {
+        for (int i = threadIdx.x; i < count; i += kReduceThreads)
+        {
+            fb[i] += sf[i];
+        }
+    }
+    else
+    {
+        for (int i = threadIdx.x; i < count; i += kReduceThreads)
+        {
+            fb[i] = sf[i];
         }
     }
     if (!do_virial)
@@ -636,8 +640,8 @@ cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* /*d_x*
     {
         cudaMemsetAsync(v.virial, 0, sizeof(double) * 9, s);
     }
-    const int tb = 256;
-    k_reduce_f<<<(v.n + tb * kReduceAtoms - 1) / (tb * kReduceAtoms), tb, 0, s>>>(v, d_f, virial ? 1 : 0);
+    const int per_block = kReduceThreads * kReduceAtoms;
+    k_reduce_f<<<(v.n + per_block - 1) / per_block, kReduceThreads, 0, s>>>(v, d_f, virial ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -870,7 +874,8 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         {
             k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
-        k_reduce_f<<<(v.n + 256 * kReduceAtoms - 1) / (256 * kReduceAtoms), 256, 0, s>>>(v, d_f, d_virial ? 1 : 0);
+        k_reduce_f<<<(v.n + kReduceThreads * kReduceAtoms - 1) / (kReduceThreads * kReduceAtoms), kReduceThreads, 0, s>>>(
+                v, d_f, d_virial ? 1 : 0);
         if (energy)
         {
             k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);

@@ -416,27 +416,29 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsign
 
 // nbnxn_atomdata_copy_x_to_nbat_x (atomdata.cpp:1018-1073), plus the box
 // shift each atom received at the last search so that coordinates which left
-// the box since then stay consistent with the grid and the list.
+// the box since then stay consistent with the grid and the list.  One thread per
+// atom: x is read in atom order (coalesced, also when it is host memory read over
+// the host link) and each atom's xq slot is rewritten, keeping its charge.
 __global__ void k_convert_x(DeviceView v, const float* __restrict__ x)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= v.hdr->num_cells * kSc)
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= v.n)
     {
         return;
     }
-    const int a = v.atom_indices[k];
-    if (a >= 0)
+    const int k = v.cells[a];
+    if ((unsigned)k >= (unsigned)(v.g.cells_capacity * kSc))
     {
-        const float4 old  = v.xq[k];
-        const int    code = v.image[a];
-        float        c[3];
-        for (int d = 0; d < 3; d++)
-        {
-            const int s = (int)(signed char)((code >> (8 * d)) & 0xff);
-            c[d]        = (s == 0) ? x[3 * a + d] : x[3 * a + d] + (float)s * v.g.box[d];
-        }
-        v.xq[k] = make_float4(c[0], c[1], c[2], old.w);
+        return;
     }
+    const int code = v.image[a];
+    float     c[3];
+    for (int d = 0; d < 3; d++)
+    {
+        const int s = (int)(signed char)((code >> (8 * d)) & 0xff);
+        c[d]        = (s == 0) ? x[3 * a + d] : x[3 * a + d] + (float)s * v.g.box[d];
+    }
+    v.xq[k] = make_float4(c[0], c[1], c[2], v.xq[k].w);
 }
 
 } // namespace
@@ -459,9 +461,8 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
 
 cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s)
 {
-    const int tb    = 256;
-    const int total = v.g.cells_capacity * kSc;
-    k_convert_x<<<(total + tb - 1) / tb, tb, 0, s>>>(v, d_x);
+    const int tb = 256;
+    k_convert_x<<<v.n > 0 ? (v.n + tb - 1) / tb : 1, tb, 0, s>>>(v, d_x);
     return cudaGetLastError();
 }
 
