@@ -841,11 +841,14 @@ def run_ours(args) -> None:
                      "kernel": "nbx::k_force<energy, ewald>",
                      "note": f"{FLOPS_PER_PAIR_VF} flops per computed pair (nrnb.cpp:106) x "
                              f"{pairs_avg:.4g} computed pairs / {avg_force_ms:.4f} ms average launch; "
+                             "the launch also holds the excluded-pair and self energy work items; "
                              "peak = measured FFMA probe of this run (of measured); traffic = DRAM bytes "
                              "per launch from ncu"},
         "cpu_baseline": cpu_baseline_port(),
         "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": n * 12,
-                "d2h_bytes_per_step": n * 12 + 11 * 8},
+                "d2h_bytes_per_step": n * 12 + 11 * 8,
+                "transfer": "nbx_md_step on pinned host arrays: the kernels read x and write f, E, "
+                            "virial in place over the host link (search steps copy x)"},
         "gpu_launches": launches,
         "clocks": clocks,
     }

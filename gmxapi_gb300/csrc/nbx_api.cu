@@ -52,6 +52,7 @@ struct nbx_handle
     unsigned long long* d_count = nullptr;
     ListHeader* h_hdr = nullptr;  // pinned copy for reading sizes
     double*     h_out = nullptr;  // pinned copy of the energies and virial (11 doubles)
+    double*     d_hout = nullptr; // h_out's device address when the device can write it directly
     // adjoint scratch, allocated on the first backward call
     float4* d_gnb   = nullptr;
     float4* d_dnb   = nullptr;
@@ -800,6 +801,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (e == cudaSuccess) e = dalloc(h, &h->d_count, 1);
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_hdr, sizeof(ListHeader));
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_out, 11 * sizeof(double));
+    if (e == cudaSuccess) h->d_hout = static_cast<double*>(mapped_device_ptr(h->h_out));
     if (e == cudaSuccess) e = cudaMemcpyAsync(q, sys->q, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(t, sys->type, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ei, sys->excl_index, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream);
@@ -1072,15 +1074,18 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
     }
     const int accumulate = h->v.accumulate_f;  // host arrays: forces are overwritten
     h->v.accumulate_f    = 0;
-    int rc = nbx_md_step_device(h, step, d_x, d_f ? d_f : h->d_f, energies ? h->d_out : nullptr,
-                                virial ? h->d_out + 2 : nullptr);
+    // energies and virial: written by the finishing kernel into the pinned h_out when the
+    // device can address it, else copied there
+    double* d_out = h->d_hout ? h->d_hout : h->d_out;
+    int     rc    = nbx_md_step_device(h, step, d_x, d_f ? d_f : h->d_f, energies ? d_out : nullptr,
+                                       virial ? d_out + 2 : nullptr);
     h->v.accumulate_f = accumulate;
     if (rc != NBX_OK)
     {
         return rc;
     }
     cudaError_t e = d_f ? cudaSuccess : cudaMemcpyAsync(f, h->d_f, bytes, cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess && (energies || virial))
+    if (e == cudaSuccess && (energies || virial) && !h->d_hout)
     {
         e = cudaMemcpyAsync(h->h_out, h->d_out, 11 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     }

@@ -18,7 +18,7 @@ namespace nbx
 namespace
 {
 
-constexpr int kPruneWarps = 4;
+constexpr int kPruneWarps = 8;
 
 // Prunes one list entry (block-cooperative): the shifted i-atoms go to shared
 // memory, each warp takes cj4 groups of the entry.
@@ -38,9 +38,23 @@ __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer,
         xib[k]         = make_float4(x.x + sx, x.y + sy, x.z + sz, 0.0f);
     }
     __syncthreads();
+    // the next group's record and outer masks are loaded while the current one is tested
+    Cj4  c4n{};
+    uint2 outn{};
+    if (s.cj4_start + warp < s.cj4_end)
+    {
+        c4n  = cj4[s.cj4_start + warp];
+        outn = fresh ? uint2{} : reinterpret_cast<const uint2*>(imask_outer)[s.cj4_start + warp];
+    }
     for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
     {
-        const Cj4 c4 = cj4[j4];
+        const Cj4   c4  = c4n;
+        const uint2 out = outn;
+        if (j4 + kPruneWarps < s.cj4_end)
+        {
+            c4n  = cj4[j4 + kPruneWarps];
+            outn = fresh ? uint2{} : reinterpret_cast<const uint2*>(imask_outer)[j4 + kPruneWarps];
+        }
         for (int w = 0; w < kSplit; w++)
         {
             unsigned full_m, check, nw;
@@ -52,7 +66,7 @@ __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer,
             }
             else
             {
-                full_m = imask_outer[2 * j4 + w];
+                full_m = w == 0 ? out.x : out.y;
                 nw     = c4.imei[w].imask;
                 check  = nw ^ full_m;
             }
