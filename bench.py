@@ -37,8 +37,8 @@ SIGMA_STEP = 0.002
 # Ewald-analytic + LJ flops per pair with energies (src/gromacs/gmxlib/nrnb.cpp:106)
 FLOPS_PER_PAIR_VF = 107
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_force launch on this workload, from an
-# ncu --set full capture (list + coordinates; forces stay in L2)
-FORCE_KERNEL_DRAM_BYTES = 21.54e6
+# ncu --set full capture (list, coordinates and the exclusion items' lists; forces stay in L2)
+FORCE_KERNEL_DRAM_BYTES = 27.38e6
 
 
 def useful_pairs(n: int, box) -> float:
