@@ -2074,7 +2074,8 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
     b->sums_bytes     = sizeof(double) * (2 + kNShift * 3 + 9) * nsys + 64;
     if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(BatchSys) * nsys);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_table, sizeof(BatchSys) * nsys);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(int) * (nsys + 1));
+    // entry prefix sums, then the exclusion work items' prefix sums (k_batch_prefix)
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(int) * 2 * (nsys + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_sums, b->sums_bytes);
     if (e != cudaSuccess)

@@ -34,19 +34,23 @@ __device__ __forceinline__ int find_system(const int* prefix, int nsys, int e)
     return lo;
 }
 
-// Entry prefix sums over the systems' lists (after every search); systems
-// whose list or grid overflowed contribute no entries and are flagged.
+// Entry prefix sums over the systems' lists (after every search), prefix[0..nsys], and the
+// prefix sums of their exclusion work items (kExclChunkAtoms atoms each),
+// prefix[nsys + 1 .. 2 nsys + 1]; systems whose list or grid overflowed contribute neither
+// and are flagged.
 __global__ void k_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsigned* status)
 {
     if (threadIdx.x != 0)
     {
         return;
     }
-    int      run = 0;
+    int*     chunk_prefix = prefix + nsys + 1;
+    int      run = 0, run_c = 0;
     unsigned st  = 0;
     for (int s = 0; s < nsys; s++)
     {
-        prefix[s]            = run;
+        prefix[s]          = run;
+        chunk_prefix[s]    = run_c;
         const ListHeader* h = sys[s].hdr;
         if (h->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
         {
@@ -54,9 +58,11 @@ __global__ void k_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsig
             continue;
         }
         run += h->num_sci;
+        run_c += (sys[s].n + kExclChunkAtoms - 1) / kExclChunkAtoms;
     }
-    prefix[nsys] = run;
-    *status      = st;
+    prefix[nsys]       = run;
+    chunk_prefix[nsys] = run_c;
+    *status            = st;
 }
 
 // nbnxn_atomdata_copy_x_to_nbat_x for all systems (blockIdx.y = system); also
@@ -87,99 +93,37 @@ __global__ void k_batch_convert(const BatchSys* __restrict__ sys, const float* _
 }
 
 
-// Excluded-pair Coulomb energies in FP64 per system (see k_excl_energy).
-__global__ void k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ sys, double* energies)
+// Excluded-pair Coulomb energies and self terms in FP64 for all systems: one warp per work
+// item of kExclChunkAtoms atoms (the item prefix sums of k_batch_prefix), one wave of blocks,
+// one FP64 atomic per item into its system's energy.
+__global__ void __launch_bounds__(256) k_batch_excl_energy(DeviceView cv, const BatchSys* __restrict__ sys,
+                                                           const int* __restrict__ prefix, int nsys,
+                                                           double* energies)
 {
-    const BatchSys& b   = sys[blockIdx.y];
-    const int       i   = blockIdx.x * blockDim.x + threadIdx.x;
-    double          acc = 0.0;
-    double          acc_s = 0.0;  // Ewald: sum of q_i q_j S(beta^2 r^2), scaled below
-    if (i < b.n && !(b.hdr->status & kStatusGridOverflow))
+    const int* chunk_prefix = prefix + nsys + 1;
+    const int  total        = chunk_prefix[nsys];
+    const int  lane         = threadIdx.x & 31;
+    const int  nwarps       = (gridDim.x * blockDim.x) >> 5;
+    const double beta2      = (double)cv.beta * (double)cv.beta;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < total; c += nwarps)
     {
-        const float4 xi = b.xq[b.cells[i]];
-        const int    nx = (b.box[0] < cv.rlist) ? 2 : 1;
-        if (b.self_on_device)
+        const int       cs = find_system(chunk_prefix, nsys, c);
+        const BatchSys& b  = sys[cs];
+        const int       a0 = (c - chunk_prefix[cs]) * kExclChunkAtoms;
+        double          acc = 0.0, acc_s = 0.0, acc_lj = 0.0;
+        for (int i = a0 + lane; i < min(b.n, a0 + kExclChunkAtoms); i += 32)
         {
-            // self term from the current charges (kernel_gpu_ref.cpp:154-178)
-            acc += (double)xi.w * (double)xi.w
-                   * (cv.coulomb == 0 ? -(double)cv.beta * 0.56418958354775628695 : -0.5 * (double)cv.c_rf);
+            excl_atom(cv, b, i, false, beta2, acc, acc_s, acc_lj);
         }
-        for (int k = b.excl_index[i]; k < b.excl_index[i + 1]; k++)
+        acc += acc_s * (-(double)cv.beta * 1.1283791670955125739);
+        for (int o = 16; o > 0; o >>= 1)
         {
-            const int j = b.excl_list[k];
-            if (j <= i)
-            {
-                continue;
-            }
-            const float4 xj = b.xq[b.cells[j]];
-            // one image per dimension whose box edge is at least 2 rc: the nearest
-            int         lo[3], hi[3];
-            const float xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
-            const float rc    = sqrtf(cv.rc2);
-            for (int d = 0; d < 3; d++)
-            {
-                const int lim = d == 0 ? nx : 1;
-                if (b.box[d] >= 2.0f * rc)
-                {
-                    const int t = min(max((int)rintf(xd[d] / b.box[d]), -lim), lim);
-                    lo[d] = hi[d] = t;
-                }
-                else
-                {
-                    lo[d] = -lim;
-                    hi[d] = lim;
-                }
-            }
-            for (int tz = lo[2]; tz <= hi[2]; tz++)
-            {
-                for (int ty = lo[1]; ty <= hi[1]; ty++)
-                {
-                    for (int tx = lo[0]; tx <= hi[0]; tx++)
-                    {
-                        const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
-                        const float dx = (xi.x + b.shiftvec[3 * s]) - xj.x;
-                        const float dy = (xi.y + b.shiftvec[3 * s + 1]) - xj.y;
-                        const float dz = (xi.z + b.shiftvec[3 * s + 2]) - xj.z;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        if (!(r2 < cv.rc2))
-                        {
-                            continue;
-                        }
-                        const double qq = (double)xi.w * (double)xj.w;
-                        if (cv.coulomb == 0)
-                        {
-                            const double bb = (double)cv.beta;
-                            const double w  = bb * bb * (double)r2;
-                            if (w <= 1.0)
-                            {
-                                acc_s = fma(qq, erf_over_x_series(w), acc_s);
-                            }
-                            else
-                            {
-                                const double rd = sqrt(fmax((double)dx * dx + (double)dy * dy + (double)dz * dz,
-                                                            (double)kMinDist2));
-                                acc -= qq * erf(bb * rd) / rd;
-                            }
-                        }
-                        else
-                        {
-                            const double r2d = fmax((double)dx * dx + (double)dy * dy + (double)dz * dz,
-                                                    (double)kMinDist2);
-                            acc += qq * ((double)cv.k_rf * r2d - (double)cv.c_rf);
-                        }
-                    }
-                }
-            }
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
         }
-    }
-    acc += acc_s * (-(double)cv.beta * 1.1283791670955125739);
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    }
-    if ((threadIdx.x & 31) == 0 && acc != 0.0)
-    {
-        atomicAdd(&energies[2 * blockIdx.y + 1], acc * cv.epsfac_d);
+        if (lane == 0 && acc != 0.0)
+        {
+            atomicAdd(&energies[2 * cs + 1], acc * cv.epsfac_d);
+        }
     }
 }
 
@@ -426,8 +370,7 @@ cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, cons
     k_batch_convert<<<gconv, tb, 0, s>>>(sys, d_x);
     if (energy)
     {
-        dim3 gex((max_atoms + tb - 1) / tb, nsys);
-        k_batch_excl_energy<<<gex, tb, 0, s>>>(cv, sys, en);
+        k_batch_excl_energy<<<num_sms * 8, 256, 0, s>>>(cv, sys, prefix, nsys, en);
     }
     const bool ewald = (cv.coulomb == 0);
     if (energy)

@@ -46,149 +46,8 @@ constexpr int kForceMinBlocks = 2;
 constexpr int kMaxTypes1      = 48;  // types + dummy held in shared memory (36 KB)
 constexpr int kStageBytes     = kStageSmemPerWarp;  // per warp: double-buffered j stage and barriers
 
-// Coulomb energy of the excluded pairs within rc, summed in FP64 (Ewald: the
-// series of erf(x)/x with its tail in float, erf_over_x_series), from the exclusion
-// lists: every excluded pair i < j and every periodic image of it with
-// r^2 < rc^2 in the pair kernel's float arithmetic, i.e. exactly the
-// excluded pairs the list-based kernel sees (the half list holds each image
-// pair once).  Ewald: -q_i q_j erf(beta r)/r; RF: q_i q_j (k_rf r^2 - c_rf)
-// (kernel_gpu_ref.cpp:259-291 with int_bit = 0).  Energies only.
-
 constexpr int kExclThreads      = 256;
 constexpr int kExclBlocksPerSm = 4;
-constexpr int kExclChunkAtoms  = 128;  // atoms per exclusion work item of k_force (4 per lane)
-
-// The excluded pairs (j > i) and the self term of atom i: Coulomb terms into acc (scaled by
-// epsfac by the caller), the Ewald series sums into acc_s (scaled by -beta 2/sqrt(pi) by the
-// caller), the LJ-PME grid part into acc_lj.
-__device__ __forceinline__ void excl_atom(const DeviceView& v, int i, bool ljpme, double beta2, double& acc,
-                                          double& acc_s, double& acc_lj)
-{
-    const float4 xi  = v.xq[v.cells[i]];
-    const double qi  = (double)xi.w;
-    const int    nt1 = v.ntypes1;
-    const float  sci = ljpme ? sqrtf(v.nbfp[v.type[i] * (nt1 + 1)].x) : 0.0f;
-    if (v.self_on_device)
-    {
-        // self term, kernel_gpu_ref.cpp:154-178 (acc is scaled by epsfac by the caller)
-        acc += (double)xi.w * (double)xi.w
-               * (v.coulomb == 0 ? -(double)v.beta * 0.56418958354775628695 : -0.5 * (double)v.c_rf);
-    }
-    const int    nx  = (v.g.box[0] < v.rlist) ? 2 : 1;
-    // a box edge of at least 2 rc leaves one image within rc in that dimension: the nearest
-    // (same shift-vector arithmetic as the full image loop, so the same float results)
-    const float  rc  = sqrtf(v.rc2);
-    for (int k = v.excl_index[i]; k < v.excl_index[i + 1]; k++)
-    {
-        const int j = v.excl_list[k];
-        if (j <= i)
-        {
-            continue;
-        }
-        const float4 xj  = v.xq[v.cells[j]];
-        int          lo[3], hi[3];
-        const float  xd[3] = { xj.x - xi.x, xj.y - xi.y, xj.z - xi.z };
-        for (int d = 0; d < 3; d++)
-        {
-            const int lim = d == 0 ? nx : 1;
-            if (v.g.box[d] >= 2.0f * rc)
-            {
-                const int t = min(max((int)rintf(xd[d] / v.g.box[d]), -lim), lim);
-                lo[d] = hi[d] = t;
-            }
-            else
-            {
-                lo[d] = -lim;
-                hi[d] = lim;
-            }
-        }
-        for (int tz = lo[2]; tz <= hi[2]; tz++)
-        {
-            for (int ty = lo[1]; ty <= hi[1]; ty++)
-            {
-                for (int tx = lo[0]; tx <= hi[0]; tx++)
-                {
-                    const int   s  = 5 * (3 * (tz + 1) + ty + 1) + tx + 2;
-                    const float dx = (xi.x + v.shiftvec[3 * s]) - xj.x;
-                    const float dy = (xi.y + v.shiftvec[3 * s + 1]) - xj.y;
-                    const float dz = (xi.z + v.shiftvec[3 * s + 2]) - xj.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (!(r2 < v.rc2))
-                    {
-                        continue;
-                    }
-                    const double qq  = qi * (double)xj.w;
-                    // r^2 in FP64 from the float differences, only where the series is not used
-                    auto r2_fp64 = [&]() {
-                        return fmax((double)dx * dx + (double)dy * dy + (double)dz * dz, (double)kMinDist2);
-                    };
-                    if (v.coulomb == 0)
-                    {
-                        // -erf(beta r)/r = -beta 2/sqrt(pi) S(beta^2 r^2); excluded pairs are
-                        // short (beta r <= 1), so S comes from its series (the factor is
-                        // applied once per thread by the caller).  w from the float r^2: its rounding
-                        // differs from pair to pair and averages out in the sum.
-                        const double w = beta2 * (double)r2;
-                        if (w <= 1.0)
-                        {
-                            acc_s = fma(qq, erf_over_x_series(w), acc_s);
-                        }
-                        else
-                        {
-                            const double rd = sqrt(r2_fp64());
-                            acc -= qq * erf((double)v.beta * rd) / rd;
-                        }
-                    }
-                    else
-                    {
-                        acc += qq * ((double)v.k_rf * r2_fp64() - (double)v.c_rf);
-                    }
-                    if (ljpme)
-                    {
-                        // c6grid / 6 r^-6 (1 - e^-b (1 + b + b^2/2)), b = beta_lj^2 r^2
-                        const int    tj     = v.type[j];
-                        const double c6grid = (double)(sci * sqrtf(v.nbfp[tj * (nt1 + 1)].x));
-                        const double r2d    = r2_fp64();
-                        const double b      = (double)v.lje_coeff2 * r2d;
-                        const double ir6    = 1.0 / (r2d * r2d * r2d);
-                        acc_lj += c6grid / 6.0 * ir6 * (1.0 - exp(-b) * (1.0 + b + 0.5 * b * b));
-                    }
-                }
-            }
-        }
-    }
-}
-
-// Work item t of k_force's queue: list entries E and exclusion chunks C interleaved, one chunk
-// after every E / C entries (the chunks' FP64 and gather work then overlaps other warps' pair
-// work instead of running as a separate launch); idx is the entry or the chunk.
-__device__ __forceinline__ bool item_is_chunk(int t, int E, int C, int& idx)
-{
-    if (C == 0)
-    {
-        idx = t;
-        return false;
-    }
-    const int s = E / C;
-    if (s >= 1)
-    {
-        const int q = t / (s + 1), r = t - q * (s + 1);
-        if (q < C)
-        {
-            idx = (r == s) ? q : q * s + r;
-            return r == s;
-        }
-        idx = C * s + (t - C * (s + 1));
-        return false;
-    }
-    if (t < 2 * E)
-    {
-        idx = t >> 1;
-        return (t & 1) != 0;
-    }
-    idx = E + (t - 2 * E);
-    return true;
-}
 
 template<bool kEnergy, bool kEwald, int kLj = 0>
 __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(DeviceView v, int* work_counter)
@@ -260,7 +119,7 @@ __global__ void __launch_bounds__(kForceThreads, kForceMinBlocks) k_force(Device
                 for (int i = e * kExclChunkAtoms + lane; i < min(v.n, (e + 1) * kExclChunkAtoms); i += 32)
                 {
                     double dummy_lj = 0.0;
-                    excl_atom(v, i, false, beta2, e_el_acc, excl_s, dummy_lj);
+                    excl_atom(v, v, i, false, beta2, e_el_acc, excl_s, dummy_lj);
                 }
                 e_el_acc = fma(excl_s, -(double)v.beta * 1.1283791670955125739, e_el_acc);
             }
@@ -301,7 +160,7 @@ __global__ void __launch_bounds__(kExclThreads) k_excl_energy(DeviceView v)
     const double beta2 = (double)v.beta * (double)v.beta;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x)
     {
-        excl_atom(v, i, ljpme, beta2, acc, acc_s, acc_lj);
+        excl_atom(v, v, i, ljpme, beta2, acc, acc_s, acc_lj);
     }
     acc += acc_s * (-(double)v.beta * 1.1283791670955125739);
     // warp, then block sums: one atomic per block and sum (a few hundred blocks), not one per
