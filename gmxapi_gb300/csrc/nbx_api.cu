@@ -404,7 +404,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
 {
     DeviceView& v      = h->v;
     const bool  energy = (d_e != nullptr) || (d_vir != nullptr);
-    cudaError_t e      = launch_convert_x(v, d_x, h->stream);
+    cudaError_t e      = launch_convert_x(v, d_x, h->stream, true);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (h->timing)
     {
@@ -422,10 +422,9 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
             collect_timings(h, false);
         }
     }
-    if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_x, d_vir != nullptr, h->stream);
-    if (e == cudaSuccess && energy) e = launch_finish_energy(v, d_e, d_vir, h->stream);
+    if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_e, d_vir, h->stream);
     h->force_launches += 1;
-    h->launches += 3 + (energy ? 2 : 0);
+    h->launches += 3 + (v.vdw_mod == NBX_VDW_LJPME && energy ? 1 : 0) + (h->fep_on ? 1 : 0);
     return cuda_check(h, e, "compute");
 }
 

@@ -203,13 +203,35 @@ int excl_blocks(int n, int num_sms)
     return std::max(1, std::min((n + kExclThreads - 1) / kExclThreads, kExclBlocksPerSm * num_sms));
 }
 
+// energies += self terms; virial = -1/2 (sum x (x) f + sum shift (x) fshift)
+// (mdlib/sim_util.cpp:157-176, calcvir.cpp:103-145).  Threads t < 9 of one block; the sums are
+// read past L1 (other blocks of the calling kernel added to them).
+__device__ __forceinline__ void finish_sums(const DeviceView& v, double* d_energies, double* d_virial, int t)
+{
+    if (d_energies && t < 2)
+    {
+        d_energies[t] = __ldcg(&v.energy[t]) + (t == 1 ? v.self_energy : v.self_energy_lj);
+    }
+    if (d_virial && t < 9)
+    {
+        const int p = t / 3, q = t % 3;
+        double    s = __ldcg(&v.virial[t]);
+        for (int sh = 0; sh < kNShift; sh++)
+        {
+            s += (double)v.shiftvec[3 * sh + p] * __ldcg(&v.fshift[3 * sh + q]);
+        }
+        d_virial[t] = -0.5 * s;
+    }
+}
+
 // f[a] = fnb[cells[a]] (atomdata.cpp:1181-1228) and sum_k x_k (x) f_k: each
 // thread gathers kReduceAtoms atoms and sums their x (x) f in float, the
 // partial sums are reduced in FP64.
 constexpr int kReduceAtoms   = 4;
 constexpr int kReduceThreads = 256;
 
-__global__ void __launch_bounds__(kReduceThreads) k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial)
+__global__ void __launch_bounds__(kReduceThreads)
+        k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial, double* d_energies, double* d_virial)
 {
     float w[9];
 #pragma unroll
@@ -294,34 +316,51 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_f(DeviceView v, float
             fb[i] = sf[i];
         }
     }
-    if (!do_virial)
+    if (do_virial)
+    {
+        __shared__ double ws[9][32];
+        const int         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int k = 0; k < 9; k++)
+        {
+            double t = (double)w[k];
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                t += __shfl_xor_sync(0xffffffffu, t, o);
+            }
+            if (lane == 0)
+            {
+                ws[k][warp] = t;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 9)
+        {
+            double t = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++)
+            {
+                t += ws[threadIdx.x][k];
+            }
+            atomicAdd(&v.virial[threadIdx.x], t);
+            __threadfence();
+        }
+    }
+    if (!d_energies && !d_virial)
     {
         return;
     }
-    __shared__ double ws[9][32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 9; k++)
+    // the last block to finish writes the energies and the virial (no separate launch)
+    __shared__ int last;
+    __syncthreads();
+    if (threadIdx.x == 0)
     {
-        double t = (double)w[k];
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            t += __shfl_xor_sync(0xffffffffu, t, o);
-        }
-        if (lane == 0)
-        {
-            ws[k][warp] = t;
-        }
+        last = atomicAdd(reinterpret_cast<unsigned*>(&v.hdr->work_counter2), 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (threadIdx.x < 9)
+    if (last)
     {
-        double t = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++)
-        {
-            t += ws[threadIdx.x][k];
-        }
-        atomicAdd(&v.virial[threadIdx.x], t);
+        __threadfence();
+        finish_sums(v, d_energies, d_virial, threadIdx.x);
     }
 }
 
@@ -329,21 +368,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_f(DeviceView v, float
 // (mdlib/sim_util.cpp:157-176, calcvir.cpp:103-145).
 __global__ void k_finish(DeviceView v, double* d_energies, double* d_virial)
 {
-    const int t = threadIdx.x;
-    if (d_energies && t < 2)
-    {
-        d_energies[t] = v.energy[t] + (t == 1 ? v.self_energy : v.self_energy_lj);
-    }
-    if (d_virial && t < 9)
-    {
-        const int p = t / 3, q = t % 3;
-        double    s = v.virial[t];
-        for (int sh = 0; sh < kNShift; sh++)
-        {
-            s += (double)v.shiftvec[3 * sh + p] * v.fshift[3 * sh + q];
-        }
-        d_virial[t] = -0.5 * s;
-    }
+    finish_sums(v, d_energies, d_virial, threadIdx.x);
 }
 
 __global__ void k_pair_count(DeviceView v, unsigned long long* out)
@@ -408,11 +433,9 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     {
         return cudaErrorInvalidValue;
     }
+    // the accumulators (grid forces, shift forces, energies, work queue) were cleared by the
+    // coordinate conversion of this evaluation (launch_convert_x with clear)
     int* counter = &v.hdr->work_counter;
-    cudaMemsetAsync(counter, 0, sizeof(int), s);
-    cudaMemsetAsync(v.fnb, 0, sizeof(float4) * (size_t)v.g.cells_capacity * kSc, s);
-    cudaMemsetAsync(v.fshift, 0, sizeof(double) * kNShift * 3, s);
-    cudaMemsetAsync(v.energy, 0, sizeof(double) * 2, s);
     const int    blocks = num_sms * kForceMinBlocks;
     const size_t smem   = sizeof(float4) * (size_t)v.ntypes1 * v.ntypes1 + kStageBytes * (kForceThreads / 32);
     const bool   ewald  = (v.coulomb == 0);
@@ -493,20 +516,10 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, const float* /*d_x*/, bool virial, cudaStream_t s)
+cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, double* d_e, double* d_vir, cudaStream_t s)
 {
-    if (virial)
-    {
-        cudaMemsetAsync(v.virial, 0, sizeof(double) * 9, s);
-    }
     const int per_block = kReduceThreads * kReduceAtoms;
-    k_reduce_f<<<(v.n + per_block - 1) / per_block, kReduceThreads, 0, s>>>(v, d_f, virial ? 1 : 0);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_finish_energy(const DeviceView& v, double* d_energies, double* d_virial, cudaStream_t s)
-{
-    k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);
+    k_reduce_f<<<(v.n + per_block - 1) / per_block, kReduceThreads, 0, s>>>(v, d_f, d_vir ? 1 : 0, d_e, d_vir);
     return cudaGetLastError();
 }
 
@@ -734,7 +747,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
             k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
         k_reduce_f<<<(v.n + kReduceThreads * kReduceAtoms - 1) / (kReduceThreads * kReduceAtoms), kReduceThreads, 0, s>>>(
-                v, d_f, d_virial ? 1 : 0);
+                v, d_f, d_virial ? 1 : 0, nullptr, nullptr);
         if (energy)
         {
             k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);

@@ -15,6 +15,8 @@
 // pair list, is bit-identical to the reference's.
 #include "nbx_internal.cuh"
 
+#include <algorithm>
+
 #include <cfloat>
 
 namespace nbx
@@ -419,9 +421,40 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsign
 // the box since then stay consistent with the grid and the list.  One thread per
 // atom: x is read in atom order (coalesced, also when it is host memory read over
 // the host link) and each atom's xq slot is rewritten, keeping its charge.
-__global__ void k_convert_x(DeviceView v, const float* __restrict__ x)
+// clear: also zero what a force evaluation accumulates into (the grid-order forces,
+// shift forces, energies, virial, the work queue and the reduction's completion
+// counter), in place of separate memsets before the force kernel.
+__global__ void k_convert_x(DeviceView v, const float* __restrict__ x, int clear)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (clear)
+    {
+        if (t < v.g.cells_capacity * kSc)
+        {
+            v.fnb[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        if (blockIdx.x == 0)
+        {
+            for (int k = threadIdx.x; k < kNShift * 3; k += blockDim.x)
+            {
+                v.fshift[k] = 0.0;
+            }
+            if (threadIdx.x < 2)
+            {
+                v.energy[threadIdx.x] = 0.0;
+            }
+            if (threadIdx.x < 9)
+            {
+                v.virial[threadIdx.x] = 0.0;
+            }
+            if (threadIdx.x == 0)
+            {
+                v.hdr->work_counter  = 0;
+                v.hdr->work_counter2 = 0;
+            }
+        }
+    }
+    const int a = t;
     if (a >= v.n)
     {
         return;
@@ -459,10 +492,11 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s)
+cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s, bool clear)
 {
-    const int tb = 256;
-    k_convert_x<<<v.n > 0 ? (v.n + tb - 1) / tb : 1, tb, 0, s>>>(v, d_x);
+    const int tb      = 256;
+    const int threads = clear ? std::max(v.n, v.g.cells_capacity * kSc) : v.n;
+    k_convert_x<<<threads > 0 ? (threads + tb - 1) / tb : 1, tb, 0, s>>>(v, d_x, clear ? 1 : 0);
     return cudaGetLastError();
 }
 
