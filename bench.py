@@ -53,6 +53,20 @@ def dist_env():
     return world, rank, local
 
 
+def replica_throughput(total_ms: float, units_per_step: float, steps: int, world: int, device=None):
+    """Whole-job throughput of `world` independent replicas (one per GPU, no data-path collective):
+    the slowest rank's timed region (max over ranks) and world x units x steps / that time.  The
+    only collective is this max over the default process group (NCCL on GPUs, gloo in the CPU test)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * units_per_step * steps / (total_ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
 
@@ -773,12 +787,8 @@ def run_ours(args) -> None:
     force_ms, force_launches, launches = calc.timings(reset=True)
     calc.set_timing(False)
     pairs1 = calc.pair_count()
-    if world > 1:
-        t = torch.tensor([total_ms], device=frames.device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
     up = useful_pairs(n, s.box)
-    value = world * up * args.steps / (total_ms * 1e-3)
+    total_ms, value = replica_throughput(total_ms, up, args.steps, world, frames.device)
 
     # e2e: the same schedule through the C ABI with host arrays (pinned), H2D x and D2H f/E/virial per step
     hx = frames.cpu().pin_memory()
