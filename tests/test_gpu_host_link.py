@@ -60,3 +60,24 @@ def test_compute_with_mapped_host_arrays_matches_staged_copies():
     assert np.allclose(b.energies, a.energies, rtol=1e-9, atol=0.0)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("pinned", ["x", "f"])
+def test_one_mapped_array_and_one_pageable(pinned):
+    """Each host array takes its own route: in place when mapped, copied otherwise."""
+    s = systems.spc_water(1000, 3.104, seed=13)
+    a = nblib.ForceCalculator(s, _opts())
+    b = nblib.ForceCalculator(s, _opts())
+    x = s.x.astype(np.float32)
+    xt, xp = _pinned(x)
+    ft, fp = _pinned(np.zeros_like(x))
+    for step in range(12):
+        fa = a.md_step(step, x, energies=True)
+        if pinned == "x":
+            fb = b.md_step(step, xp, energies=True)
+        else:
+            fb = b.md_step(step, x, forces=fp, energies=True)
+        assert rel_rms(fb.astype(np.float64), fa.astype(np.float64)) <= 1e-6, step
+        assert np.allclose(b.energies, a.energies, rtol=1e-9, atol=0.0), step
+    a.close()
+    b.close()
