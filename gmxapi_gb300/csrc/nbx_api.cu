@@ -53,6 +53,8 @@ struct nbx_handle
     ListHeader* h_hdr = nullptr;  // pinned copy for reading sizes
     double*     h_out = nullptr;  // pinned copy of the energies and virial (11 doubles)
     double*     d_hout = nullptr; // h_out's device address when the device can write it directly
+    bool        x_host = false;   // this call's coordinates / forces are host memory used in place
+    bool        f_host = false;
     // adjoint scratch, allocated on the first backward call
     float4* d_gnb   = nullptr;
     float4* d_dnb   = nullptr;
@@ -404,7 +406,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
 {
     DeviceView& v      = h->v;
     const bool  energy = (d_e != nullptr) || (d_vir != nullptr);
-    cudaError_t e      = launch_convert_x(v, d_x, h->stream, true);
+    cudaError_t e      = launch_convert_x(v, d_x, h->stream, true, h->x_host);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (h->timing)
     {
@@ -422,7 +424,7 @@ int compute_async(nbx_handle* h, const float* d_x, float* d_f, double* d_e, doub
             collect_timings(h, false);
         }
     }
-    if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_e, d_vir, h->stream);
+    if (e == cudaSuccess) e = launch_reduce_f(v, d_f, d_e, d_vir, h->stream, h->f_host);
     h->force_launches += 1;
     h->launches += 3 + (v.vdw_mod == NBX_VDW_LJPME && energy ? 1 : 0) + (h->fep_on ? 1 : 0);
     return cuda_check(h, e, "compute");
@@ -936,8 +938,11 @@ int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, doubl
     // host arrays: forces are overwritten (GmxForceCalculator::compute), whatever nbx_set_force_accumulate says
     const int accumulate = h->v.accumulate_f;
     h->v.accumulate_f    = 0;
+    h->x_host = d_x != h->d_x;
+    h->f_host = d_f != nullptr;
     int rc = compute_async(h, d_x, d_f ? d_f : h->d_f, energies ? h->d_out : nullptr, virial ? h->d_out + 2 : nullptr);
     h->v.accumulate_f = accumulate;
+    h->x_host = h->f_host = false;
     if (rc != NBX_OK)
     {
         return rc;
@@ -1076,9 +1081,12 @@ int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double*
     // energies and virial: written by the finishing kernel into the pinned h_out when the
     // device can address it, else copied there
     double* d_out = h->d_hout ? h->d_hout : h->d_out;
+    h->x_host     = d_x != h->d_x;
+    h->f_host     = d_f != nullptr;
     int     rc    = nbx_md_step_device(h, step, d_x, d_f ? d_f : h->d_f, energies ? d_out : nullptr,
                                        virial ? d_out + 2 : nullptr);
     h->v.accumulate_f = accumulate;
+    h->x_host = h->f_host = false;
     if (rc != NBX_OK)
     {
         return rc;

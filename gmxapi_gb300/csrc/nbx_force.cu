@@ -231,7 +231,7 @@ constexpr int kReduceAtoms   = 4;
 constexpr int kReduceThreads = 256;
 
 __global__ void __launch_bounds__(kReduceThreads)
-        k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial, double* d_energies, double* d_virial)
+        k_reduce_f(DeviceView v, float* __restrict__ f, int do_virial, double* d_energies, double* d_virial, int stage)
 {
     float w[9];
 #pragma unroll
@@ -284,36 +284,65 @@ __global__ void __launch_bounds__(kReduceThreads)
             }
         }
     }
-    // stage the block's forces in shared memory, then write them as contiguous floats:
-    // whole sectors also when f is host memory written over the host link
-    __shared__ float sf[3 * kReduceThreads * kReduceAtoms];
+    if (stage)
+    {
+        // the block's forces through shared memory, written as contiguous floats: whole
+        // sectors when f is host memory written over the host link
+        __shared__ float sf[3 * kReduceThreads * kReduceAtoms];
 #pragma unroll
-    for (int r = 0; r < kReduceAtoms; r++)
-    {
-        if (ks[r] >= 0)
+        for (int r = 0; r < kReduceAtoms; r++)
         {
-            const int j   = threadIdx.x + r * kReduceThreads;
-            sf[3 * j]     = fa[r].x;
-            sf[3 * j + 1] = fa[r].y;
-            sf[3 * j + 2] = fa[r].z;
+            if (ks[r] >= 0)
+            {
+                const int j   = threadIdx.x + r * kReduceThreads;
+                sf[3 * j]     = fa[r].x;
+                sf[3 * j + 1] = fa[r].y;
+                sf[3 * j + 2] = fa[r].z;
+            }
         }
-    }
-    __syncthreads();
-    const int base  = blockIdx.x * kReduceThreads * kReduceAtoms;
-    const int count = 3 * min(kReduceThreads * kReduceAtoms, v.n - base);
-    float*    fb    = f + 3 * (size_t)base;
-    if (v.accumulate_f)
-    {
+        __syncthreads();
+        const int base  = blockIdx.x * kReduceThreads * kReduceAtoms;
+        const int count = 3 * min(kReduceThreads * kReduceAtoms, v.n - base);
+        float*    fb    = f + 3 * (size_t)base;
         for (int i = threadIdx.x; i < count; i += kReduceThreads)
         {
-            fb[i] += sf[i];
+            fb[i] = v.accumulate_f ? fb[i] + sf[i] : sf[i];
         }
     }
     else
     {
-        for (int i = threadIdx.x; i < count; i += kReduceThreads)
+        if (v.accumulate_f)
         {
-            fb[i] = sf[i];
+            float old[kReduceAtoms][3];
+#pragma unroll
+            for (int r = 0; r < kReduceAtoms; r++)
+            {
+                if (ks[r] >= 0)
+                {
+                    const int a = a0 + r * kReduceThreads;
+                    old[r][0]   = f[3 * a];
+                    old[r][1]   = f[3 * a + 1];
+                    old[r][2]   = f[3 * a + 2];
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kReduceAtoms; r++)
+            {
+                fa[r].x += old[r][0];
+                fa[r].y += old[r][1];
+                fa[r].z += old[r][2];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kReduceAtoms; r++)
+        {
+            if (ks[r] >= 0)
+            {
+                const int a  = a0 + r * kReduceThreads;
+                f[3 * a]     = fa[r].x;
+                f[3 * a + 1] = fa[r].y;
+                f[3 * a + 2] = fa[r].z;
+            }
         }
     }
     if (do_virial)
@@ -360,7 +389,32 @@ __global__ void __launch_bounds__(kReduceThreads)
     if (last)
     {
         __threadfence();
-        finish_sums(v, d_energies, d_virial, threadIdx.x);
+        // the shift-force part of the virial, sum_s shift_s (x) fshift_s: 9 x 45 products over
+        // the whole block, summed in shared memory
+        __shared__ double sv[9];
+        if (threadIdx.x < 9)
+        {
+            sv[threadIdx.x] = d_virial ? __ldcg(&v.virial[threadIdx.x]) : 0.0;
+        }
+        __syncthreads();
+        if (d_virial)
+        {
+            for (int i = threadIdx.x; i < 9 * kNShift; i += kReduceThreads)
+            {
+                const int c = i / kNShift, sh = i - c * kNShift;
+                atomicAdd(&sv[c], (double)v.shiftvec[3 * sh + c / 3] * __ldcg(&v.fshift[3 * sh + c % 3]));
+            }
+        }
+        __syncthreads();
+        if (d_energies && threadIdx.x < 2)
+        {
+            d_energies[threadIdx.x] = __ldcg(&v.energy[threadIdx.x])
+                                      + (threadIdx.x == 1 ? v.self_energy : v.self_energy_lj);
+        }
+        if (d_virial && threadIdx.x < 9)
+        {
+            d_virial[threadIdx.x] = -0.5 * sv[threadIdx.x];
+        }
     }
 }
 
@@ -516,10 +570,11 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, double* d_e, double* d_vir, cudaStream_t s)
+cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, double* d_e, double* d_vir, cudaStream_t s, bool stage)
 {
     const int per_block = kReduceThreads * kReduceAtoms;
-    k_reduce_f<<<(v.n + per_block - 1) / per_block, kReduceThreads, 0, s>>>(v, d_f, d_vir ? 1 : 0, d_e, d_vir);
+    k_reduce_f<<<(v.n + per_block - 1) / per_block, kReduceThreads, 0, s>>>(v, d_f, d_vir ? 1 : 0, d_e, d_vir,
+                                                                           stage ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -747,7 +802,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
             k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
         }
         k_reduce_f<<<(v.n + kReduceThreads * kReduceAtoms - 1) / (kReduceThreads * kReduceAtoms), kReduceThreads, 0, s>>>(
-                v, d_f, d_virial ? 1 : 0, nullptr, nullptr);
+                v, d_f, d_virial ? 1 : 0, nullptr, nullptr, 0);
         if (energy)
         {
             k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);

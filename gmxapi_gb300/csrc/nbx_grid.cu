@@ -418,13 +418,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsign
 
 // nbnxn_atomdata_copy_x_to_nbat_x (atomdata.cpp:1018-1073), plus the box
 // shift each atom received at the last search so that coordinates which left
-// the box since then stay consistent with the grid and the list.  One thread per
-// atom: x is read in atom order (coalesced, also when it is host memory read over
-// the host link) and each atom's xq slot is rewritten, keeping its charge.
+// the box since then stay consistent with the grid and the list.
+// atom_order 0: one thread per grid slot (coalesced xq, x gathered by atom index),
+// for coordinates in device memory; 1: one thread per atom (coalesced x, xq written
+// by slot), for coordinates read from host memory over the host link.
 // clear: also zero what a force evaluation accumulates into (the grid-order forces,
 // shift forces, energies, virial, the work queue and the reduction's completion
 // counter), in place of separate memsets before the force kernel.
-__global__ void k_convert_x(DeviceView v, const float* __restrict__ x, int clear)
+__global__ void k_convert_x(DeviceView v, const float* __restrict__ x, int clear, int atom_order)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (clear)
@@ -454,24 +455,42 @@ __global__ void k_convert_x(DeviceView v, const float* __restrict__ x, int clear
             }
         }
     }
-    const int a = t;
-    if (a >= v.n)
+    int a, k;
+    if (atom_order)
     {
-        return;
+        a = t;
+        if (a >= v.n)
+        {
+            return;
+        }
+        k = v.cells[a];
+        if ((unsigned)k >= (unsigned)(v.g.cells_capacity * kSc))
+        {
+            return;
+        }
     }
-    const int k = v.cells[a];
-    if ((unsigned)k >= (unsigned)(v.g.cells_capacity * kSc))
+    else
     {
-        return;
+        k = t;
+        if (k >= v.hdr->num_cells * kSc)
+        {
+            return;
+        }
+        a = v.atom_indices[k];
+        if (a < 0)
+        {
+            return;
+        }
     }
-    const int code = v.image[a];
-    float     c[3];
+    const float4 old  = v.xq[k];
+    const int    code = v.image[a];
+    float        c[3];
     for (int d = 0; d < 3; d++)
     {
         const int s = (int)(signed char)((code >> (8 * d)) & 0xff);
         c[d]        = (s == 0) ? x[3 * a + d] : x[3 * a + d] + (float)s * v.g.box[d];
     }
-    v.xq[k] = make_float4(c[0], c[1], c[2], v.xq[k].w);
+    v.xq[k] = make_float4(c[0], c[1], c[2], old.w);
 }
 
 } // namespace
@@ -492,11 +511,12 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s, bool clear)
+cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s, bool clear, bool atom_order)
 {
     const int tb      = 256;
-    const int threads = clear ? std::max(v.n, v.g.cells_capacity * kSc) : v.n;
-    k_convert_x<<<threads > 0 ? (threads + tb - 1) / tb : 1, tb, 0, s>>>(v, d_x, clear ? 1 : 0);
+    const int items   = atom_order ? v.n : v.g.cells_capacity * kSc;
+    const int threads = clear ? std::max(items, v.g.cells_capacity * kSc) : items;
+    k_convert_x<<<threads > 0 ? (threads + tb - 1) / tb : 1, tb, 0, s>>>(v, d_x, clear ? 1 : 0, atom_order ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -311,15 +311,19 @@ struct FepView
 cudaError_t launch_fep(const DeviceView& v, const FepView& fp, bool energy, cudaStream_t s);
 cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStream_t s);
 // clear: also zero the force-evaluation accumulators (grid forces, shift forces, energies,
-// virial, work queue) for the next launch_force / launch_reduce_f
-cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s, bool clear = false);
+// virial, work queue) for the next launch_force / launch_reduce_f; atom_order: read x in atom
+// order (x in host memory read over the host link)
+cudaError_t launch_convert_x(const DeviceView& v, const float* d_x, cudaStream_t s, bool clear = false,
+                             bool atom_order = false);
 cudaError_t launch_search(const DeviceView& v, cudaStream_t s);
 cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s);
 cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, cudaEvent_t ev0 = nullptr,
                          cudaEvent_t ev1 = nullptr);
 // forces to atom order (+ virial); with d_e / d_vir the last block also finishes the energies
 // and virial (the accumulators must have been cleared by launch_convert_x(clear))
-cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, double* d_e, double* d_vir, cudaStream_t s);
+// (stage: write the forces through shared memory as contiguous floats, for f in host memory)
+cudaError_t launch_reduce_f(const DeviceView& v, float* d_f, double* d_e, double* d_vir, cudaStream_t s,
+                            bool stage = false);
 cudaError_t launch_pair_count(const DeviceView& v, unsigned long long* d_out, cudaStream_t s);
 cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
