@@ -112,15 +112,20 @@ def _liquid():
     return s, masses
 
 
-@pytest.mark.parametrize("with_pme", [True, False])
-def test_md_run_matches_oracle(md, with_pme):
+@pytest.mark.parametrize("with_pme,prune", [(True, False), (False, False), (True, True)])
+def test_md_run_matches_oracle(md, with_pme, prune):
+    """prune: dynamic pruning to rlist_inner 0.92 every 4 steps (2 rolling parts), against the
+    oracle's unpruned list: pruning drops only pairs that stay beyond rc, so the trajectory is the
+    same."""
     from gmxapi_gb300 import nblib
     from gmxapi_gb300 import pme as pm
 
     s, masses = _liquid()
     rng = np.random.default_rng(4)
     v0 = (rng.standard_normal((s.n, 3)) * np.sqrt(0.00831446 * 120.0 / 39.948)).astype(np.float32)
-    opts = nblib.NBKernelOptions(pairlist_cutoff=1.0, rcoulomb=0.9, nstlist=10, compute_virial_and_energy=True)
+    extra = {"rlist_inner": 0.92, "nstlist_prune": 4} if prune else {}
+    opts = nblib.NBKernelOptions(pairlist_cutoff=1.0, rcoulomb=0.9, nstlist=10, compute_virial_and_energy=True,
+                                 **extra)
     run = md.MdRunner(s, masses, opts, dt=0.002, velocities=v0, pme=with_pme)
     rows = run.run(20, nstcalcenergy=1)
     box = [float(b) for b in s.box]
