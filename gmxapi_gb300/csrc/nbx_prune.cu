@@ -18,10 +18,14 @@ namespace nbx
 namespace
 {
 
-constexpr int kPruneWarps = 8;
+// warps per list entry: 8 for the rolling pass (few bits per group to test, latency-bound on the
+// group records), 4 for the fresh pass (every bit tested, compute-bound)
+constexpr int kPruneWarpsRolling = 8;
+constexpr int kPruneWarpsFresh   = 4;
 
 // Prunes one list entry (block-cooperative): the shifted i-atoms go to shared
 // memory, each warp takes cj4 groups of the entry.
+template<int kPruneWarps>
 __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
                             const float* shiftvec, float outer2, float inner2, int fresh, float4* xib)
 {
@@ -113,6 +117,7 @@ __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer,
     }
 }
 
+template<int kPruneWarps>
 __global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fresh, int part, int nparts)
 {
     __shared__ float4 xib[kSc];
@@ -124,13 +129,15 @@ __global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fr
     // entries part, part + nparts, ... (all entries for a fresh list)
     for (int e = part + blockIdx.x * nparts; e < numSci; e += gridDim.x * nparts)
     {
-        prune_entry(v.sci[e], v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2, v.rlist_inner2, fresh, xib);
+        prune_entry<kPruneWarps>(v.sci[e], v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2, v.rlist_inner2, fresh,
+                                 xib);
     }
 }
 
 // The same prune over a batch of systems: global entry index -> system by a
 // search of the entry prefix sums; entries whose index within their system is
 // part (mod nparts) are pruned.
+template<int kPruneWarps>
 __global__ void __launch_bounds__(32 * kPruneWarps)
         k_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2, int fresh,
                       int part, int nparts)
@@ -158,7 +165,7 @@ __global__ void __launch_bounds__(32 * kPruneWarps)
             continue;
         }
         const BatchSys& b = sys[lo];
-        prune_entry(b.sci[local], b.cj4, b.imask_outer, b.xq, b.shiftvec, outer2, inner2, fresh, xib);
+        prune_entry<kPruneWarps>(b.sci[local], b.cj4, b.imask_outer, b.xq, b.shiftvec, outer2, inner2, fresh, xib);
     }
 }
 
@@ -167,8 +174,16 @@ __global__ void __launch_bounds__(32 * kPruneWarps)
 cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2,
                                int fresh, int part, int nparts, cudaStream_t s)
 {
-    k_batch_prune<<<152 * 8, 32 * kPruneWarps, 0, s>>>(sys, entry_prefix, nsys, outer2, inner2, fresh, part,
-                                                         fresh ? 1 : nparts);
+    if (fresh)
+    {
+        k_batch_prune<kPruneWarpsFresh><<<152 * 8, 32 * kPruneWarpsFresh, 0, s>>>(sys, entry_prefix, nsys, outer2,
+                                                                                 inner2, fresh, part, 1);
+    }
+    else
+    {
+        k_batch_prune<kPruneWarpsRolling><<<152 * 8, 32 * kPruneWarpsRolling, 0, s>>>(sys, entry_prefix, nsys, outer2,
+                                                                                     inner2, fresh, part, nparts);
+    }
     return cudaGetLastError();
 }
 
@@ -180,7 +195,14 @@ cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, c
         nparts = 1;
     }
     // enough blocks for ~8 per SM; entries beyond are picked up by the grid-stride loop
-    k_prune<<<152 * 8, 32 * kPruneWarps, 0, s>>>(v, fresh, part, nparts);
+    if (fresh)
+    {
+        k_prune<kPruneWarpsFresh><<<152 * 8, 32 * kPruneWarpsFresh, 0, s>>>(v, fresh, part, nparts);
+    }
+    else
+    {
+        k_prune<kPruneWarpsRolling><<<152 * 8, 32 * kPruneWarpsRolling, 0, s>>>(v, fresh, part, nparts);
+    }
     return cudaGetLastError();
 }
 
