@@ -87,6 +87,14 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "50"], stdout=self.fh, stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler has produced its first line (start-up ~0.1 s)
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+                self.fh.flush()
+                if os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.01)
+            self.skip = sum(1 for _ in open(self.path))
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -105,7 +113,10 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        lines = open(self.path).readlines()
+        # the lines written before the timed region began are dropped, unless nothing came after
+        timed = lines[getattr(self, "skip", 0):] or lines[-1:]
+        for line in timed:
             p = [t.strip() for t in line.split(",")]
             if len(p) < 9:
                 continue
