@@ -517,16 +517,44 @@ __global__ void k_match_loss(const float* __restrict__ f, const float* __restric
 }
 
 // Upstream force gradients to grid order; clears the output accumulators.
-__global__ void k_adj_prepare(DeviceView v, const float* __restrict__ gF, float4* gnb, float4* dnb)
+// Per grid slot: the coordinates of this evaluation into xq (as k_convert_x, with the box shifts of
+// the last search) when x is given, the upstream force gradient in grid order, a cleared dL/dx
+// accumulator; block 0 also clears the work queue and the FP64 type-pair gradient table (in place
+// of separate memsets).
+__global__ void k_adj_prepare(DeviceView v, const float* __restrict__ x, const float* __restrict__ gF, float4* gnb,
+                              float4* dnb, int* counter, double* gnbfp, int n_gnbfp)
 {
+    if (blockIdx.x == 0)
+    {
+        for (int i = threadIdx.x; i < n_gnbfp; i += blockDim.x)
+        {
+            gnbfp[i] = 0.0;
+        }
+        if (threadIdx.x == 0)
+        {
+            *counter = 0;
+        }
+    }
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= v.hdr->num_cells * kSc)
     {
         return;
     }
     const int a = v.atom_indices[k];
-    gnb[k]      = (a >= 0) ? make_float4(gF[3 * a], gF[3 * a + 1], gF[3 * a + 2], 0.0f) : make_float4(0, 0, 0, 0);
-    dnb[k]      = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (x && a >= 0)
+    {
+        const float4 old  = v.xq[k];
+        const int    code = v.image[a];
+        float        c[3];
+        for (int d = 0; d < 3; d++)
+        {
+            const int sh = (int)(signed char)((code >> (8 * d)) & 0xff);
+            c[d]         = (sh == 0) ? x[3 * a + d] : x[3 * a + d] + (float)sh * v.g.box[d];
+        }
+        v.xq[k] = make_float4(c[0], c[1], c[2], old.w);
+    }
+    gnb[k] = (a >= 0) ? make_float4(gF[3 * a], gF[3 * a + 1], gF[3 * a + 2], 0.0f) : make_float4(0, 0, 0, 0);
+    dnb[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // Atom-order outputs; dL/dq also gets the self-energy term.
@@ -563,14 +591,14 @@ int adjoint_max_types1()
     return kAdjMaxTypes1;
 }
 
-cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double* d_gE, float4* gnb, float4* dnb,
-                            double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s)
+cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* d_gF, const double* d_gE,
+                            float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
+                            int num_sms, cudaStream_t s)
 {
     const int tb    = 256;
     const int slots = v.g.cells_capacity * kSc;
-    k_adj_prepare<<<(slots + tb - 1) / tb, tb, 0, s>>>(v, d_gF, gnb, dnb);
-    cudaMemsetAsync(counter, 0, sizeof(int), s);
-    cudaMemsetAsync(d_gnbfp, 0, sizeof(double) * 2 * v.ntypes1 * v.ntypes1, s);
+    k_adj_prepare<<<(slots + tb - 1) / tb, tb, 0, s>>>(v, d_x, d_gF, gnb, dnb, counter, d_gnbfp,
+                                                       2 * v.ntypes1 * v.ntypes1);
     if (v.coulomb == 0)
     {
         k_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);

@@ -1151,17 +1151,14 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
             return cuda_check(h, e, "adjoint allocation");
         }
     }
-    e = launch_convert_x(v, d_x, h->stream);
-    if (e == cudaSuccess)
-    {
-        e = launch_backward(v, d_gF, d_gE, h->d_gnb, h->d_dnb, h->d_gnbfp, h->d_adj_counter, d_gx, d_gq, h->num_sms,
-                            h->stream);
-    }
+    // the coordinate conversion is part of the preparation kernel
+    e = launch_backward(v, d_x, d_gF, d_gE, h->d_gnb, h->d_dnb, h->d_gnbfp, h->d_adj_counter, d_gx, d_gq,
+                        h->num_sms, h->stream);
     if (e == cudaSuccess && d_gnbfp)
     {
         e = launch_compact_gnbfp(h->d_gnbfp, d_gnbfp, v.ntypes1 - 1, h->stream);
     }
-    h->launches += 4 + (d_gnbfp ? 1 : 0);
+    h->launches += 3 + (d_gnbfp ? 1 : 0);
     return cuda_check(h, e, "nbx_backward_device");
 }
 

@@ -330,8 +330,10 @@ cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int
                                int fresh, int part, int nparts, cudaStream_t s);
 int         adjoint_max_types1();
 cudaError_t optin_batch_force_smem();
-cudaError_t launch_backward(const DeviceView& v, const float* d_gF, const double* d_gE, float4* gnb, float4* dnb,
-                            double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s);
+// d_x: coordinates converted into xq by the preparation kernel (nullptr: xq is current)
+cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* d_gF, const double* d_gE,
+                            float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
+                            int num_sms, cudaStream_t s);
 cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);
 cudaError_t launch_compact_gnbfp(const double* padded, double* out, int nt, cudaStream_t s);
 cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
