@@ -435,8 +435,21 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
 }
 
 // Batched upstream gradients to grid order (blockIdx.y = system), outputs cleared.
-__global__ void k_batch_adj_prepare(const BatchSys* __restrict__ sys, const float* __restrict__ gF)
+__global__ void k_batch_adj_prepare(const BatchSys* __restrict__ sys, const float* __restrict__ gF, int* counter,
+                                    double* gnbfp, int n_gnbfp)
 {
+    // block (0, 0) also clears the work queue and the FP64 type-pair gradient table
+    if (blockIdx.x == 0 && blockIdx.y == 0)
+    {
+        for (int i = threadIdx.x; i < n_gnbfp; i += blockDim.x)
+        {
+            gnbfp[i] = 0.0;
+        }
+        if (threadIdx.x == 0)
+        {
+            *counter = 0;
+        }
+    }
     const BatchSys& b = sys[blockIdx.y];
     const int       k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= b.hdr->num_cells * kSc)
@@ -616,9 +629,8 @@ cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, con
                                   double* d_gnbfp, int* counter, float* d_gx, float* d_gq, int num_sms, cudaStream_t s)
 {
     const int tb = 256;
-    k_batch_adj_prepare<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_gF);
-    cudaMemsetAsync(counter, 0, sizeof(int), s);
-    cudaMemsetAsync(d_gnbfp, 0, sizeof(double) * 2 * cv.ntypes1 * cv.ntypes1, s);
+    k_batch_adj_prepare<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_gF, counter, d_gnbfp,
+                                                                             2 * cv.ntypes1 * cv.ntypes1);
     if (cv.coulomb == 0)
     {
         k_batch_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
