@@ -322,15 +322,46 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
         torch.cuda.synchronize()
         return a.elapsed_time(z) / steps
 
+    def graph_timed(fn):
+        """Device time of `steps` calls captured in one CUDA graph (no host launch gaps: the
+        24,000-atom entries are short enough for Python and launch overhead to dominate)."""
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        side = torch.cuda.Stream(d)
+        eng.calc.set_stream(side.cuda_stream)
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=side):
+                for _ in range(steps):
+                    fn()
+            for _ in range(2):
+                g.replay()
+            torch.cuda.synchronize()
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            g.replay()
+            z.record(stream)
+            torch.cuda.synchronize()
+            return a.elapsed_time(z) / steps
+        finally:
+            eng.calc.set_stream(stream.cuda_stream)
+
     fwd_ms = timed(forward)
     step_ms = timed(grad_step)
-    fwd_entry_ms = timed(forward_only)
-    bwd_ms = timed(backward_only)
+    fwd_call_ms = timed(forward_only)
+    bwd_call_ms = timed(backward_only)
+    try:
+        fwd_entry_ms, bwd_ms, entry_timing = graph_timed(forward_only), graph_timed(backward_only), "graph"
+    except Exception as exc:  # capture unavailable: the per-call times stand
+        fwd_entry_ms, bwd_ms, entry_timing = fwd_call_ms, bwd_call_ms, f"per call ({type(exc).__name__})"
     eng.close()
     return {"workload": "random LJ+Coulomb liquid, 24000 atoms, 8 types, Lorentz-Berthelot, "
                         "rejection at 0.5 sigma (seed 4)", "atoms": s.n, "steps": steps,
             "forward_ms": fwd_ms, "gradient_step_ms": step_ms, "forward_entry_ms": fwd_entry_ms,
             "backward_entry_ms": bwd_ms, "adjoint_cost_vs_forward": bwd_ms / fwd_entry_ms,
+            "entry_timing": entry_timing, "forward_entry_call_ms": fwd_call_ms,
+            "backward_entry_call_ms": bwd_call_ms,
             "gradient_step_vs_forward": step_ms / fwd_ms,
             "gradient_steps_per_s": 1e3 / step_ms,
             "note": "forward = the autograd forward (parameter upload, F+E); forward entry = C-ABI F+E "
