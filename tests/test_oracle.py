@@ -200,3 +200,40 @@ def test_oracle_lj_modifiers_vs_fp64(mod):
     o0.search()
     o0.force(energy=True)
     assert abs(o0.energies()[0] - o.energies()[0]) > 1e-6 * abs(o0.energies()[0])
+
+
+def test_erf_series_coefficients_and_accuracy():
+    """The excluded-pair energies' sqrt(pi)/2 erf(x)/x = 1 - w/3 + w^2 R(w) (nbx_internal.cuh
+    erf_over_x_series, w = x^2 <= 1): the float coefficients of R are 1/(n! (2n+1)) for n = 2..13
+    rounded to float32, and the hybrid evaluation (1 - w/3 in FP64, the tail in float32 with
+    fused multiply-adds) stays within 1.5e-8 relative of the exact function."""
+    import math
+    import os
+    import re
+
+    from scipy.special import erf
+
+    src = open(os.path.join(os.path.dirname(__file__), "..", "gmxapi_gb300", "csrc", "nbx_internal.cuh")).read()
+    body = src[src.index("double erf_over_x_series(double wd)"):]
+    body = body[: body.index("return")]
+    lits = [float(v.rstrip("f")) for v in re.findall(r"[-+]?\d+\.\d+e[-+]\d+f", body)]
+    want = [1.0 / (math.factorial(n) * (2 * n + 1)) for n in range(13, 1, -1)]
+    assert len(lits) == len(want)
+    for got, w in zip(lits, want):
+        assert np.float32(got) == np.float32(w)
+    c = [np.float32(v) for v in lits]
+
+    def fma32(a, b, d):  # a float32 fused multiply-add, rounded once
+        return np.float32(np.float64(a) * np.float64(b) + np.float64(d))
+
+    worst = 0.0
+    for wd in np.linspace(1e-6, 1.0, 4001):
+        w = np.float32(wd)
+        r = c[0]
+        for k in c[1:]:
+            r = fma32(r, -w, k)
+        s = (1.0 - wd / 3.0) + float(np.float32(np.float32(w * w) * r))  # FP64 part: fma on the GPU
+        x = math.sqrt(wd)
+        exact = erf(x) / x * math.sqrt(math.pi) / 2
+        worst = max(worst, abs(s - exact) / exact)
+    assert worst <= 1.5e-8, worst
