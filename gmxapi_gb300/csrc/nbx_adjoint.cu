@@ -294,7 +294,8 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
             red_add_v4(dst, ax, ay, az, aq);
         }
     }
-    // flush the type-pair gradients of this entry into the FP64 sums
+    // flush the type-pair gradients of this entry into the block's FP64 sums (shared memory;
+    // added to the global sums once per block at the end)
     __syncwarp();
     for (int m = lane; m < nt1 * nt1; m += 32)
     {
@@ -310,20 +311,37 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
 }
 
 // Shared set-up of the adjoint kernels: the type table and zeroed per-warp tables.
-__device__ __forceinline__ void adj_setup(const DeviceView& v, float2* nbfp_s, float2 (*ttab_s)[kAdjMaxTypes1 * kAdjMaxTypes1])
+__device__ __forceinline__ void adj_setup(const DeviceView& v, float2* nbfp_s, float2 (*ttab_s)[kAdjMaxTypes1 * kAdjMaxTypes1],
+                                          double* gsum_s)
 {
     const int nt1  = v.ntypes1;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     for (int m = threadIdx.x; m < nt1 * nt1; m += blockDim.x)
     {
-        nbfp_s[m] = v.nbfp[m];
+        nbfp_s[m]         = v.nbfp[m];
+        gsum_s[2 * m]     = 0.0;
+        gsum_s[2 * m + 1] = 0.0;
     }
     for (int m = lane; m < nt1 * nt1; m += 32)
     {
         ttab_s[warp][m] = make_float2(0.0f, 0.0f);
     }
     __syncthreads();
+}
+
+// The block's FP64 type-pair gradient sums into the global ones (one atomic per non-zero element
+// and block instead of one per element and list entry).
+__device__ __forceinline__ void adj_flush(const double* gsum_s, double* gnbfp, int n)
+{
+    __syncthreads();
+    for (int m = threadIdx.x; m < n; m += blockDim.x)
+    {
+        if (gsum_s[m] != 0.0)
+        {
+            atomicAdd(&gnbfp[m], gsum_s[m]);
+        }
+    }
 }
 
 template<bool kEwald>
@@ -338,12 +356,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         k.gE_c  = (float)gE[1];
     }
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
     __shared__ float4 jg_s[kAdjWarps][32];
-    adj_setup(v, nbfp_s, ttab_s);
+    adj_setup(v, nbfp_s, ttab_s, gsum_s);
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
         return;
@@ -367,8 +386,9 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         }
         adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], jx_s[warp], jg_s[warp],
                           lane, k, v.pbeta,
-                          v.beta2l2, v.c2b, b2c2b, gnbfp);
+                          v.beta2l2, v.c2b, b2c2b, gsum_s);
     }
+    adj_flush(gsum_s, gnbfp, 2 * v.ntypes1 * v.ntypes1);
 }
 
 __device__ __forceinline__ int adj_find_system(const int* prefix, int nsys, int e)
@@ -397,12 +417,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
                          double* gnbfp, int* work_counter, const double* __restrict__ gE)
 {
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
+    __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
     __shared__ float4 jg_s[kAdjWarps][32];
-    adj_setup(cv, nbfp_s, ttab_s);
+    adj_setup(cv, nbfp_s, ttab_s, gsum_s);
     const int   warp  = threadIdx.x >> 5;
     const int   lane  = threadIdx.x & 31;
     const int   total = prefix[nsys];
@@ -430,8 +451,9 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         const AdjPtrs p = { b.xq, b.tgrid, b.cj4, b.excl, b.shiftvec, b.gnb, b.dnb };
         adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp],
                           jx_s[warp], jg_s[warp], lane, k,
-                          cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gnbfp);
+                          cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gsum_s);
     }
+    adj_flush(gsum_s, gnbfp, 2 * cv.ntypes1 * cv.ntypes1);
 }
 
 // Batched upstream gradients to grid order (blockIdx.y = system), outputs cleared.
