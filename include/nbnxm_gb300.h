@@ -112,7 +112,9 @@ int nbx_update_pairlist(nbx_handle* h, const float* x);
 /* Replaces ForceCalculator::compute (api/nblib/forcecalculator.cpp:57-60 ->
  * GmxForceCalculator::compute, gmxcalculator.cpp:70-83): convertCoordinates ->
  * nonbonded kernel -> atomdata_add_nbat_f_to_f.  Host arrays; forces are overwritten.
- * energies (double[2]) and virial (double[9]) may be NULL. */
+ * energies (double[2]) and virial (double[9]) may be NULL.  An array in pinned host memory mapped
+ * into the device's address space (cudaMallocHost, cudaHostAlloc, cudaHostRegister) is read or
+ * written by the kernels in place; other host memory is staged through device buffers. */
 int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, double* virial);
 
 /* ---- device-resident interface (pointers into device memory, asynchronous on the handle's stream) ---- */
@@ -132,7 +134,8 @@ int nbx_compute_device(nbx_handle* h, const float* d_x, float* d_f, double* d_en
 int nbx_md_step_device(nbx_handle* h, long long step, const float* d_x, float* d_f, double* d_energies,
                        double* d_virial);
 int nbx_synchronize(nbx_handle* h);
-/* nbx_md_step_device with host arrays (H2D of x and D2H of f / energies / virial inside the call). */
+/* nbx_md_step_device with host arrays (x in, f / energies / virial out, inside the call; mapped
+ * pinned arrays are used in place as in nbx_compute, except x on search steps, which is copied). */
 int nbx_md_step(nbx_handle* h, long long step, const float* x, float* f, double* energies, double* virial);
 
 /* ---- layout export, for parity checks against the nbnxm layout ---- */
