@@ -389,20 +389,27 @@ __global__ void __launch_bounds__(kReduceThreads)
     if (last)
     {
         __threadfence();
-        // the shift-force part of the virial, sum_s shift_s (x) fshift_s: 9 x 45 products over
-        // the whole block, summed in shared memory
+        // the shift-force part of the virial, sum_s shift_s (x) fshift_s: one warp per component
+        // (8 warps, component 8 on warp 0), the 45 shifts over the lanes, a shuffle reduction
         __shared__ double sv[9];
-        if (threadIdx.x < 9)
-        {
-            sv[threadIdx.x] = d_virial ? __ldcg(&v.virial[threadIdx.x]) : 0.0;
-        }
-        __syncthreads();
         if (d_virial)
         {
-            for (int i = threadIdx.x; i < 9 * kNShift; i += kReduceThreads)
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            for (int c = warp; c < 9; c += kReduceThreads / 32)
             {
-                const int c = i / kNShift, sh = i - c * kNShift;
-                atomicAdd(&sv[c], (double)v.shiftvec[3 * sh + c / 3] * __ldcg(&v.fshift[3 * sh + c % 3]));
+                double t = 0.0;
+                for (int sh = lane; sh < kNShift; sh += 32)
+                {
+                    t += (double)v.shiftvec[3 * sh + c / 3] * __ldcg(&v.fshift[3 * sh + c % 3]);
+                }
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    t += __shfl_xor_sync(0xffffffffu, t, o);
+                }
+                if (lane == 0)
+                {
+                    sv[c] = t + __ldcg(&v.virial[c]);
+                }
             }
         }
         __syncthreads();
