@@ -24,8 +24,13 @@
 //    self-pair logic; energies are accumulated with compensated sums of
 //    q_i (q_j h(r)) (no single rounded q_i q_j per type pair, whose error
 //    would be systematic) and reduced in FP64; the Coulomb energies of
-//    excluded pairs come from k_excl_energy, in FP64 (rigid molecules repeat
-//    the same pair geometry, so their float rounding would not average out);
+//    excluded pairs and the self terms are summed in FP64 (rigid molecules
+//    repeat the same pair geometry, so their float rounding would not average
+//    out) by work items of 128 atoms interleaved with the list entries in the
+//    same queue (k_excl_energy, a separate kernel, only for LJ-PME);
+//  - a force evaluation is three launches: k_convert_x (clears the
+//    accumulators), k_force, k_reduce_f (its last block writes the energies
+//    and the virial);
 //  - j forces are reduced over the 8 i-lanes with shuffles and added with one
 //    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
 //    until the entry ends; shift forces and energies are reduced in FP64.
