@@ -2,7 +2,8 @@
 //
 // Each system keeps its own grid and pair list (built by the single-system
 // search); one step for the whole batch is six launches, independent of the
-// number of systems: coordinate conversion, FP64 exclusion energies, one
+// number of systems: clearing the sums, coordinate conversion, FP64 exclusion
+// energies (one wave of warps over 128-atom items of all systems), one
 // persistent force kernel over the concatenated entry space of all systems
 // (an entry finds its system by searching the entry prefix sums), the force
 // gather + virial, and the per-system energy / virial finish.  The sequence
