@@ -768,6 +768,17 @@ def measure_fep(dev: int, num_perturbed: int = 256, steps: int = 20) -> dict:
                     "perturbed pairs run in one block per perturbed atom after the cluster kernel"}
 
 
+def schedule_counts(first: int, steps: int) -> tuple[int, int]:
+    """Searches and rolling-prune passes the step schedule runs in steps [first, first + steps):
+    a search where step % nstlist == 0, otherwise one rolling-prune part (of nstlist_prune / 2)
+    at every second step of list age (nbx_md_step_device, pairlistsets.h:106-114), so every
+    entry is pruned once per nstlist_prune steps."""
+    sched = range(first, first + steps)
+    searches = sum(1 for t in sched if t % NSTLIST == 0)
+    prunes = sum(1 for t in sched if t % NSTLIST != 0 and (t % NSTLIST) % 2 == 0)
+    return searches, prunes
+
+
 def workload_config() -> dict:
     return {"workload": "spc_water_288k", "atoms": 288000, "box_nm": 14.21, "rc_nm": RC, "rlist_nm": RLIST,
             "rlist_inner_nm": RLIST_INNER, "nstlist": NSTLIST, "nstlist_prune": NSTPRUNE,
@@ -796,6 +807,11 @@ def run_ours(args) -> None:
     stream = torch.cuda.current_stream(dev)
     calc.set_stream(stream.cuda_stream)
     total = args.warmup + args.steps
+    # schedule steps: the timed window starts on a search step (step % nstlist == 0), so it holds
+    # ceil(K / nstlist) searches, and the warm-up steps run the rolling prunes just before it
+    t0 = NSTLIST * -(-args.warmup // NSTLIST)
+    sched0 = t0 - args.warmup
+    searches, prunes = schedule_counts(t0, args.steps)
     # coordinate frames: a Gaussian random walk, resident in HBM before timing
     gen = torch.Generator(device=f"cuda:{dev}").manual_seed(1234 + rank)
     frames = torch.empty((total, n * 3), dtype=torch.float32, device=f"cuda:{dev}")
@@ -807,7 +823,7 @@ def run_ours(args) -> None:
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=frames.device)  # 256 MB > L2
 
     def step(t):
-        calc.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), ev.data_ptr(), ev[2:].data_ptr())
+        calc.md_step_device(sched0 + t, frames[t].data_ptr(), f.data_ptr(), ev.data_ptr(), ev[2:].data_ptr())
 
     for t in range(args.warmup):
         step(t)
@@ -852,7 +868,7 @@ def run_ours(args) -> None:
     dp = C.POINTER(C.c_double)
 
     def hstep(t):
-        _lib.check(L.nbx_md_step(calc2.h, t, C.cast(hx[t].data_ptr(), fp), C.cast(hf.data_ptr(), fp),
+        _lib.check(L.nbx_md_step(calc2.h, sched0 + t, C.cast(hx[t].data_ptr(), fp), C.cast(hf.data_ptr(), fp),
                                  he.ctypes.data_as(dp), hv.ctypes.data_as(dp)), calc2.h)
 
     for t in range(args.warmup):
@@ -890,7 +906,8 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SPC water)",
-        "config": workload_config(),
+        "config": dict(workload_config(), timed_schedule_steps=[t0, t0 + args.steps - 1],
+                       searches_in_timed_window=searches, rolling_prunes_in_timed_window=prunes),
         "force_evals_per_s": world * args.steps / (total_ms * 1e-3),
         "pairs_computed_per_eval": pairs_avg, "useful_pairs_per_eval": up,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

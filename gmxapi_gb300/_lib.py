@@ -38,7 +38,7 @@ EXPORTED = [
     "nbx_compute", "nbx_set_stream", "nbx_get_stream", "nbx_search_device", "nbx_prune_device",
     "nbx_compute_device", "nbx_md_step_device", "nbx_synchronize", "nbx_get_sizes", "nbx_get_grid",
     "nbx_get_pairlist", "nbx_get_pair_counts", "nbx_measure_fp32_peak", "nbx_md_step",
-    "nbx_set_timing", "nbx_get_timings", "nbx_compute_noalloc",
+    "nbx_set_timing", "nbx_get_timings", "nbx_compute_noalloc", "nbx_noalloc_status", "nbx_noalloc_set_wait_test",
     "nbx_batch_create", "nbx_batch_destroy", "nbx_batch_last_error", "nbx_batch_atoms", "nbx_batch_set_stream",
     "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
@@ -183,6 +183,8 @@ def load():
     L.nbx_batch_force_match_device.argtypes = [vp] * 10
     L.nbx_get_list_balance.argtypes = [vp, ip]
     L.nbx_compute_noalloc.argtypes = [C.POINTER(nbx_noalloc_args), vp, vp, vp, vp]
+    L.nbx_noalloc_status.argtypes = [vp]
+    L.nbx_noalloc_set_wait_test.argtypes = [C.c_int]
     L.nbx_batch_create.argtypes = [C.c_int, C.POINTER(nbx_system_desc), C.POINTER(nbx_options), C.c_int,
                                    C.POINTER(vp)]
     L.nbx_batch_destroy.argtypes = [vp]

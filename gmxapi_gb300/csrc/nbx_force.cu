@@ -490,6 +490,57 @@ __global__ void k_fma_probe(float* out, int iters)
     }
 }
 
+// Dynamic shared memory beyond the 48 KB default needs a per-kernel opt-in (type tables of more
+// than 45 types with the per-warp stages and the static energy sums); the attribute is a property
+// of the kernel in the current device's context, so it is set whenever the launch needs it.
+template<class Kernel>
+cudaError_t force_smem_optin(Kernel kernel, size_t smem)
+{
+    if (smem + sizeof(double) * 2 * kForceThreads <= 48 * 1024)
+    {
+        return cudaSuccess;
+    }
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template<bool kEnergy, bool kEwald, int kLj>
+void launch_k_force(const DeviceView& v, int blocks, size_t smem, cudaStream_t s, int* counter)
+{
+    if (force_smem_optin(k_force<kEnergy, kEwald, kLj>, smem) != cudaSuccess)
+    {
+        return;  // the launch error is reported by cudaGetLastError
+    }
+    k_force<kEnergy, kEwald, kLj><<<blocks, kForceThreads, smem, s>>>(v, counter);
+}
+
+// Marks the outputs of an allocation-free evaluation whose device status word is non-zero (a
+// bounded stage wait gave up, or a capacity check failed): every force component, the energies
+// and the virial become NaN, so a failed evaluation cannot pass for a correct one.
+__global__ void k_noalloc_check(const ListHeader* hdr, float* f, int n3, double* d_energies, double* d_virial)
+{
+    if (__ldcg(&hdr->status) == 0u)
+    {
+        return;
+    }
+    const float nan = __int_as_float(0x7fc00000);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x)
+    {
+        f[i] = nan;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 9)
+    {
+        const double dnan = __longlong_as_double(0x7ff8000000000000ll);
+        if (d_energies && threadIdx.x < 2)
+        {
+            d_energies[threadIdx.x] = dnan;
+        }
+        if (d_virial)
+        {
+            d_virial[threadIdx.x] = dnan;
+        }
+    }
+}
+
 } // namespace
 
 cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, cudaEvent_t ev0,
@@ -526,55 +577,19 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
                    : (v.vdw_mod == NBX_VDW_POTSWITCH) ? 2
                    : (v.vdw_mod == NBX_VDW_LJPME)     ? 3
                                                        : 0;
-    if (lj == 3)
-    {
-        if (energy)
-            ewald ? k_force<true, true, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<true, false, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        else
-            ewald ? k_force<false, true, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<false, false, 3><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-    }
-    else if (lj == 1)
-    {
-        if (energy)
-            ewald ? k_force<true, true, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<true, false, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        else
-            ewald ? k_force<false, true, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<false, false, 1><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-    }
-    else if (lj == 2)
-    {
-        if (energy)
-            ewald ? k_force<true, true, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<true, false, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        else
-            ewald ? k_force<false, true, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter)
-                  : k_force<false, false, 2><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-    }
-    else if (energy)
-    {
-        if (ewald)
-        {
-            k_force<true, true><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        }
-        else
-        {
-            k_force<true, false><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        }
-    }
-    else
-    {
-        if (ewald)
-        {
-            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        }
-        else
-        {
-            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(kv, counter);
-        }
-    }
+    using Launch = void (*)(const DeviceView&, int, size_t, cudaStream_t, int*);
+    // [lj][energy][ewald]
+    static const Launch table[4][2][2] = {
+        { { launch_k_force<false, false, 0>, launch_k_force<false, true, 0> },
+          { launch_k_force<true, false, 0>, launch_k_force<true, true, 0> } },
+        { { launch_k_force<false, false, 1>, launch_k_force<false, true, 1> },
+          { launch_k_force<true, false, 1>, launch_k_force<true, true, 1> } },
+        { { launch_k_force<false, false, 2>, launch_k_force<false, true, 2> },
+          { launch_k_force<true, false, 2>, launch_k_force<true, true, 2> } },
+        { { launch_k_force<false, false, 3>, launch_k_force<false, true, 3> },
+          { launch_k_force<true, false, 3>, launch_k_force<true, true, 3> } },
+    };
+    table[lj][energy ? 1 : 0][ewald ? 1 : 0](kv, blocks, smem, s, counter);
     if (ev1)
     {
         cudaEventRecord(ev1, s);
@@ -647,6 +662,8 @@ namespace
 {
 constexpr int kMaxDevices = 64;
 std::mutex    g_noalloc_mutex;
+// failure-detection test hook (nbx_noalloc_set_wait_test): bytes the stage barriers wait for in vain
+unsigned      g_noalloc_wait_test = 0u;
 void*         g_noalloc_addr[kMaxDevices] = { nullptr };
 
 // Device address of the scratch array on the current device (set-up on the
@@ -689,8 +706,9 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     {
         return NBX_ERR_INVALID_INPUT;
     }
+    // the grid holds every atom, in whole 64-slot cells
     if (a->num_atoms <= 0 || a->num_slots <= 0 || a->num_sci < 0 || a->num_types <= 0
-        || a->num_types + 1 > kMaxTypes1)
+        || a->num_types + 1 > kMaxTypes1 || a->num_atoms > a->num_slots || a->num_slots % kSc != 0)
     {
         return NBX_ERR_INVALID_INPUT;
     }
@@ -739,6 +757,7 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     v.fshift     = sums + 2;
     v.virial     = sums + 2 + kNShift * 3;
     v.hdr        = reinterpret_cast<ListHeader*>(base + kNoAllocFnbBytes + 256 + kNoAllocSumsBytes + 256);
+    v.wait_test_bytes = g_noalloc_wait_test;
     for (int d = 0; d < 3; d++)
     {
         v.g.box[d] = a->box[d];
@@ -785,9 +804,9 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
     k_noalloc_init<<<1, 1, 0, s>>>(v.hdr, a->num_sci, a->num_slots / kSc);
     cudaError_t e = cudaMemsetAsync(v.fnb, 0, sizeof(float4) * (size_t)a->num_slots, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(sums, 0, kNoAllocSumsBytes, s);
-    int num_sms = 152, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    int num_sms = 0, dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
     {
         const int    blocks = num_sms * kForceMinBlocks;
@@ -798,20 +817,20 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
             k_excl_energy<<<excl_blocks(v.n, num_sms), kExclThreads, 0, s>>>(v);
             if (v.coulomb == 0)
             {
-                k_force<true, true><<<blocks, kForceThreads, smem, s>>>(v, ctr);
+                launch_k_force<true, true, 0>(v, blocks, smem, s, ctr);
             }
             else
             {
-                k_force<true, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
+                launch_k_force<true, false, 0>(v, blocks, smem, s, ctr);
             }
         }
         else if (v.coulomb == 0)
         {
-            k_force<false, true><<<blocks, kForceThreads, smem, s>>>(v, ctr);
+            launch_k_force<false, true, 0>(v, blocks, smem, s, ctr);
         }
         else
         {
-            k_force<false, false><<<blocks, kForceThreads, smem, s>>>(v, ctr);
+            launch_k_force<false, false, 0>(v, blocks, smem, s, ctr);
         }
         k_reduce_f<<<(v.n + kReduceThreads * kReduceAtoms - 1) / (kReduceThreads * kReduceAtoms), kReduceThreads, 0, s>>>(
                 v, d_f, d_virial ? 1 : 0, nullptr, nullptr, 0);
@@ -819,7 +838,48 @@ extern "C" int nbx_compute_noalloc(const nbx_noalloc_args* a, float* d_f, double
         {
             k_finish<<<1, 32, 0, s>>>(v, d_energies, d_virial);
         }
+        k_noalloc_check<<<std::min(num_sms, (3 * v.n + 255) / 256), 256, 0, s>>>(v.hdr, d_f, 3 * v.n, d_energies,
+                                                                                 d_virial);
         e = cudaGetLastError();
     }
     return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
+extern "C" int nbx_noalloc_status(void* stream)
+{
+    using namespace nbx;
+    unsigned char* base = nullptr;
+    if (noalloc_scratch_address(&base) != cudaSuccess)
+    {
+        return NBX_ERR_CUDA;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the status word sits in the scratch array's header; a synchronous read into a host
+    // variable (pageable: no pinned buffer is allocated)
+    const ListHeader* hdr = reinterpret_cast<const ListHeader*>(base + kNoAllocFnbBytes + 256 + kNoAllocSumsBytes + 256);
+    unsigned          st  = 0u;
+    cudaError_t       e   = cudaStreamSynchronize(s);
+    if (e == cudaSuccess)
+    {
+        e = cudaMemcpy(&st, &hdr->status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess)
+    {
+        return NBX_ERR_CUDA;
+    }
+    if (st & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    {
+        return NBX_ERR_LIST_OVERFLOW;
+    }
+    if (st & kStatusTimeout)
+    {
+        return NBX_ERR_TIMEOUT;
+    }
+    return st ? NBX_ERR_INVALID_INPUT : NBX_OK;
+}
+
+extern "C" int nbx_noalloc_set_wait_test(int enable)
+{
+    nbx::g_noalloc_wait_test = enable ? 16u : 0u;
+    return NBX_OK;
 }

@@ -324,10 +324,24 @@ typedef struct
  * call before any stream capture.  All calls share the array: calls that
  * overlap on the GPU (different streams, or different threads) race and must
  * be serialised by the caller.  Returns NBX_ERR_LIST_OVERFLOW when num_slots
- * exceeds the maximum.  f: [3N] output in atom order; energies (double[2]) and
- * virial (double[9]) may be NULL.  Asynchronous on cuda_stream. */
+ * exceeds the maximum and NBX_ERR_INVALID_INPUT when num_atoms > num_slots or
+ * num_slots is not a multiple of 64; every cells[i] must be below num_slots.
+ * f: [3N] output in atom order; energies (double[2]) and virial (double[9]) may
+ * be NULL.  Asynchronous on cuda_stream: a failure on the device (a bounded
+ * wait that gave up) cannot be returned by this call, so it turns every output
+ * value of the call into NaN and leaves its code for nbx_noalloc_status. */
 int nbx_compute_noalloc(const nbx_noalloc_args* args, float* d_f, double* d_energies, double* d_virial,
                         void* cuda_stream);
+/* No counterpart in the reference: the device status of the last nbx_compute_noalloc on the
+ * current device, read after synchronising cuda_stream (allocates nothing): NBX_OK,
+ * NBX_ERR_TIMEOUT (a bounded device-side wait gave up; the outputs are NaN) or
+ * NBX_ERR_LIST_OVERFLOW.  The next nbx_compute_noalloc clears it. */
+int nbx_noalloc_status(void* cuda_stream);
+/* Failure-detection test hook (no counterpart in the reference), the allocation-free analogue
+ * of nbx_set_wait_test: with enable = 1 the stage barriers of later nbx_compute_noalloc calls
+ * wait for bytes that never arrive, so their bounded (1 s) waits give up.  Keep 0 outside
+ * that test. */
+int nbx_noalloc_set_wait_test(int enable);
 
 /* ---- smooth PME, reciprocal space (the long-range half of the Ewald sum) ---- */
 /* Rectangular boxes, pme_order 4, one GPU, charges only (no LJ-PME, no free-energy

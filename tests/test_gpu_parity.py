@@ -42,6 +42,9 @@ SYSTEMS = {
     "water_small_box": lambda: systems.spc_water(170, 1.72, seed=6),  # edge < 2 rlist: multiple images
     "water_tiny": lambda: systems.spc_water(20, 0.84, seed=7),        # <= 64 atoms: one cell, shp_x = 2
     "lj_liquid": lambda: systems.lj_liquid(n=1500, ntypes=8, seed=8),
+    # 47 types + the filler type, the most the kernels accept: the type table no longer fits the
+    # default 48 KB of shared memory
+    "lj_47_types": lambda: systems.lj_liquid(n=3000, ntypes=47, seed=9),
 }
 
 
