@@ -118,7 +118,9 @@ struct orc_ctx
     float rbb2;
     /* outputs */
     float* fnb;
-    float fshift[NSHIFT * 3];
+    /* shift forces summed in double (the reference's are `real`): the virial's shift part is a
+     * difference of large sums in small boxes, whose float rounding would dominate the check */
+    double fshift[NSHIFT * 3];
     double vc, vlj;
 };
 
@@ -1456,7 +1458,7 @@ void orc_force_entries(orc_ctx* c, int e0, int e1, int computeEnergy)
 
 /* Kernel body over entries [e_begin, e_end) into the given force / shift-force buffers
  * (cleared here) and energies; the single-threaded entry points pass the context's own. */
-static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int computeEnergy, float* fnb, float* fsh,
+static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int computeEnergy, float* fnb, double* fsh,
                              double* vc_out, double* vlj_out)
 {
     const int    npad   = c->ncells * SC;
@@ -1469,7 +1471,7 @@ static void force_range_into(const orc_ctx* c, int e_begin, int e_end, int compu
     const float* x      = c->xq;
     const int*   type   = c->tgrid;
     memset(fnb, 0, sizeof(float) * (size_t)npad * 3);
-    memset(fsh, 0, sizeof(float) * NSHIFT * 3);
+    memset(fsh, 0, sizeof(double) * NSHIFT * 3);
     double Vc = 0, Vvdw = 0;
     for (int e = e_begin; e < e_end; e++)
     {
@@ -1675,7 +1677,7 @@ typedef struct
     const orc_ctx* c;
     int            e0, e1, energy;
     float*         fnb;
-    float          fsh[NSHIFT * 3];
+    double         fsh[NSHIFT * 3];
     double         vc, vlj;
 } mt_task;
 
@@ -1782,7 +1784,7 @@ void orc_virial(const orc_ctx* c, const float* x, const float* f, double* vir9)
         {
             for (int b = 0; b < 3; b++)
             {
-                v[a * 3 + b] += (double)c->shiftvec[s * 3 + a] * (double)c->fshift[s * 3 + b];
+                v[a * 3 + b] += (double)c->shiftvec[s * 3 + a] * c->fshift[s * 3 + b];
             }
         }
     }
@@ -1798,7 +1800,13 @@ void orc_energies(const orc_ctx* c, double* e2)
     e2[1] = c->vc;
 }
 
-void orc_fshift(const orc_ctx* c, float* fshift135) { memcpy(fshift135, c->fshift, sizeof(c->fshift)); }
+void orc_fshift(const orc_ctx* c, float* fshift135)
+{
+    for (int k = 0; k < NSHIFT * 3; k++)
+    {
+        fshift135[k] = (float)c->fshift[k];
+    }
+}
 
 float orc_beta(const orc_ctx* c) { return c->beta; }
 float orc_table_scale(const orc_ctx* c) { return c->tab_scale; }
