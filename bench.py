@@ -809,9 +809,9 @@ def run_ours(args) -> None:
     total = args.warmup + args.steps
     # schedule steps: the timed window starts on a search step (step % nstlist == 0), so it holds
     # ceil(K / nstlist) searches, and the warm-up steps run the rolling prunes just before it
-    t0 = NSTLIST * -(-args.warmup // NSTLIST)
-    sched0 = t0 - args.warmup
-    searches, prunes = schedule_counts(t0, args.steps)
+    first_timed = NSTLIST * -(-args.warmup // NSTLIST)
+    sched0 = first_timed - args.warmup
+    searches, prunes = schedule_counts(first_timed, args.steps)
     # coordinate frames: a Gaussian random walk, resident in HBM before timing
     gen = torch.Generator(device=f"cuda:{dev}").manual_seed(1234 + rank)
     frames = torch.empty((total, n * 3), dtype=torch.float32, device=f"cuda:{dev}")
@@ -906,7 +906,7 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SPC water)",
-        "config": dict(workload_config(), timed_schedule_steps=[t0, t0 + args.steps - 1],
+        "config": dict(workload_config(), timed_schedule_steps=[first_timed, first_timed + args.steps - 1],
                        searches_in_timed_window=searches, rolling_prunes_in_timed_window=prunes),
         "force_evals_per_s": world * args.steps / (total_ms * 1e-3),
         "pairs_computed_per_eval": pairs_avg, "useful_pairs_per_eval": up,

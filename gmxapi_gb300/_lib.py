@@ -45,7 +45,7 @@ EXPORTED = [
     "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
     "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
     "nbx_batch_set_parameters_device", "nbx_batch_backward_device", "nbx_batch_force_match_device",
-    "nbx_set_wait_test",
+    "nbx_set_wait_test", "nbx_set_force_kernel", "nbx_get_force_kernel",
     "nbx_ewald_coefficient", "nbx_pme_grid_size", "nbx_pme_create", "nbx_pme_destroy", "nbx_pme_last_error",
     "nbx_pme_set_stream", "nbx_pme_synchronize", "nbx_pme_get_info", "nbx_pme_compute_device",
     "nbx_pme_splines_device", "nbx_pme_spread_device", "nbx_pme_solve_device", "nbx_pme_gather_device",
@@ -178,6 +178,8 @@ def load():
     L.nbx_get_phase_timings.argtypes = [vp, dp, llp, C.c_int]
     L.nbx_set_list_balance.argtypes = [vp, C.c_int]
     L.nbx_set_wait_test.argtypes = [vp, C.c_int]
+    L.nbx_set_force_kernel.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.nbx_get_force_kernel.argtypes = [vp, ip, ip, ip]
     L.nbx_batch_set_parameters_device.argtypes = [vp, vp, vp]
     L.nbx_batch_backward_device.argtypes = [vp] * 7
     L.nbx_batch_force_match_device.argtypes = [vp] * 10

@@ -25,6 +25,7 @@ UNITS = {
     "nbx_search.cu": ["--fmad=false"],
     "nbx_prune.cu": ["--fmad=false"],
     "nbx_force.cu": [],
+    "nbx_force_x2.cu": [],
     "nbx_batch.cu": [],
     "nbx_adjoint.cu": [],
     "nbx_balance.cu": [],

@@ -701,6 +701,9 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
         v.self_energy = -v.epsfac_d * 0.5 * (double)v.c_rf * qsq;
     }
     set_pair_constants(v);
+    v.pair_core    = 1;
+    v.stage_depth  = 2;
+    v.force_blocks = 2;
     // ---- shift vectors (pbc.cpp:1187-1202), rectangular box ----
     for (int s = 0, m = -1; m <= 1; m++)
     {
@@ -784,6 +787,7 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (e == cudaSuccess) e = dalloc(h, &v.cells, n);
     if (e == cudaSuccess) e = dalloc(h, &v.xq, npad);
     if (e == cudaSuccess) e = dalloc(h, &v.tgrid, npad);
+    if (e == cudaSuccess) e = dalloc(h, &v.xqp, 5 * npad);
     if (e == cudaSuccess) e = dalloc(h, &v.bb, (size_t)g.cells_capacity * kNcl * 2);
     if (e == cudaSuccess) e = dalloc(h, &v.bbcz, g.cells_capacity);
     if (e == cudaSuccess) e = dalloc(h, &v.nclusters, g.cells_capacity);
@@ -1182,6 +1186,30 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
     cudaError_t e = launch_set_parameters(h->v, d_q, d_nbfp, h->stream);
     h->launches += (d_q ? 1 : 0) + (d_nbfp ? 1 : 0);
     return cuda_check(h, e, "nbx_set_parameters_device");
+}
+
+int nbx_set_force_kernel(nbx_handle* h, int tile, int stage_depth, int blocks_per_sm)
+{
+    if (!h || tile < 0 || tile > 1 || stage_depth < 2 || stage_depth > 3 || blocks_per_sm < 2 || blocks_per_sm > 3)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    h->v.pair_core    = tile;
+    h->v.stage_depth  = stage_depth;
+    h->v.force_blocks = blocks_per_sm;
+    return NBX_OK;
+}
+
+int nbx_get_force_kernel(const nbx_handle* h, int* tile, int* stage_depth, int* blocks_per_sm)
+{
+    if (!h || !tile || !stage_depth || !blocks_per_sm)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    *tile          = h->v.pair_core;
+    *stage_depth   = h->v.stage_depth;
+    *blocks_per_sm = h->v.force_blocks;
+    return NBX_OK;
 }
 
 int nbx_set_wait_test(nbx_handle* h, int enable)
@@ -1712,6 +1740,7 @@ int batch_refresh(nbx_batch* b)
         BatchSys&         t = b->h_table[i];
         t.xq                = v.xq;
         t.tgrid             = v.tgrid;
+        t.xqp               = v.xqp;
         t.fnb               = v.fnb;
         t.sci               = v.sci;
         t.cj4               = v.cj4;

@@ -90,6 +90,7 @@ __global__ void k_batch_convert(const BatchSys* __restrict__ sys, const float* _
             c[d]        = (s == 0) ? xa[d] : xa[d] + (float)s * b.box[d];
         }
         const_cast<float4*>(b.xq)[k] = make_float4(c[0], c[1], c[2], old.w);
+        write_packed_slot(const_cast<float*>(b.xqp), k, c[0], c[1], c[2], old.w, b.tgrid[k]);
     }
 }
 

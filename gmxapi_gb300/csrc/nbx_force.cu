@@ -490,23 +490,10 @@ __global__ void k_fma_probe(float* out, int iters)
     }
 }
 
-// Dynamic shared memory beyond the 48 KB default needs a per-kernel opt-in (type tables of more
-// than 45 types with the per-warp stages and the static energy sums); the attribute is a property
-// of the kernel in the current device's context, so it is set whenever the launch needs it.
-template<class Kernel>
-cudaError_t force_smem_optin(Kernel kernel, size_t smem)
-{
-    if (smem + sizeof(double) * 2 * kForceThreads <= 48 * 1024)
-    {
-        return cudaSuccess;
-    }
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
 template<bool kEnergy, bool kEwald, int kLj>
 void launch_k_force(const DeviceView& v, int blocks, size_t smem, cudaStream_t s, int* counter)
 {
-    if (force_smem_optin(k_force<kEnergy, kEwald, kLj>, smem) != cudaSuccess)
+    if (smem_optin<k_force<kEnergy, kEwald, kLj>>(smem + sizeof(double) * 2 * kForceThreads, smem) != cudaSuccess)
     {
         return;  // the launch error is reported by cudaGetLastError
     }
@@ -577,6 +564,16 @@ cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int n
                    : (v.vdw_mod == NBX_VDW_POTSWITCH) ? 2
                    : (v.vdw_mod == NBX_VDW_LJPME)     ? 3
                                                        : 0;
+    if (lj == 0 && v.pair_core == 1)
+    {
+        // the packed core (potential shift or plain cut-off)
+        launch_force_x2(kv, energy, s, num_sms, counter);
+        if (ev1)
+        {
+            cudaEventRecord(ev1, s);
+        }
+        return cudaGetLastError();
+    }
     using Launch = void (*)(const DeviceView&, int, size_t, cudaStream_t, int*);
     // [lj][energy][ewald]
     static const Launch table[4][2][2] = {

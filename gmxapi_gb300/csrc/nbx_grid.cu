@@ -491,6 +491,21 @@ __global__ void k_convert_x(DeviceView v, const float* __restrict__ x, int clear
         c[d]        = (s == 0) ? x[3 * a + d] : x[3 * a + d] + (float)s * v.g.box[d];
     }
     v.xq[k] = make_float4(c[0], c[1], c[2], old.w);
+    // the cluster-packed copy (charges and types too: they may change between searches)
+    write_packed_slot(v.xqp, k, c[0], c[1], c[2], old.w, v.tgrid[k]);
+}
+
+// After a search: the cluster-packed copy of every grid slot, fillers included (the coordinate
+// conversion rewrites only the slots that hold atoms).
+__global__ void k_pack_slots(DeviceView v)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.hdr->num_cells * kSc)
+    {
+        return;
+    }
+    const float4 x = v.xq[k];
+    write_packed_slot(v.xqp, k, x.x, x.y, x.z, x.w, v.tgrid[k]);
 }
 
 } // namespace
@@ -508,6 +523,7 @@ cudaError_t launch_grid(const DeviceView& v, float* d_x, int write_back, cudaStr
     k_column_scan<<<1, 1024, 0, s>>>(v);
     k_scatter<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v);
     k_sort_fill<<<v.g.ncol, kSortThreads, 0, s>>>(v, reinterpret_cast<unsigned long long*>(v.fnb));
+    k_pack_slots<<<(v.g.cells_capacity * kSc + tb - 1) / tb, tb, 0, s>>>(v);
     return cudaGetLastError();
 }
 

@@ -151,6 +151,10 @@ struct DeviceView
     int*    cells;         // [N]
     float4* xq;            // [cap*64]
     int*    tgrid;         // [cap*64]
+    // the same atoms cluster-packed for the packed force kernel: per cluster of 8 atoms one
+    // 160-byte record x[8], y[8], z[8], q[8], type[8] (int bits) with atom a at position
+    // 2 (a & 3) + (a >> 2), so atoms a and a + 4 are adjacent
+    float*  xqp;           // [cap*64*5]
     float4* bb;            // [cap*8*2] lower, upper
     float2* bbcz;          // [cap]
     int*    nclusters;     // [cap]
@@ -206,7 +210,23 @@ struct DeviceView
     // > 0: the energy flavours of k_force also compute the excluded-pair and self energies, as
     // this many work items of kExclChunkAtoms atoms interleaved with the list entries
     int excl_chunks;
+    // force kernel tile: 1 = packed core (two pairs per lane, FP32x2 arithmetic; potential-shift
+    // or plain cut-off LJ), 0 = scalar core (one pair per lane); j-stage buffers per warp (2, 3)
+    int pair_core;
+    int stage_depth;
+    int force_blocks;  // resident blocks of 256 threads per SM for the packed kernel (2, 3)
 };
+
+// Writes slot k's coordinates, charge and type into the cluster-packed records (DeviceView::xqp).
+__device__ __forceinline__ void write_packed_slot(float* xqp, int k, float x, float y, float z, float q, int type)
+{
+    float* pc = xqp + (size_t)(k >> 3) * 40 + 2 * (k & 3) + ((k >> 2) & 1);
+    pc[0]     = x;
+    pc[8]     = y;
+    pc[16]    = z;
+    pc[24]    = q;
+    pc[32]    = __int_as_float(type);
+}
 
 // One system of a batch, as the batched kernels see it (device table).
 // LJ modifier constants for cut-off rc (interaction_const setup, forcerec.cpp:787-872).
@@ -261,6 +281,7 @@ struct BatchSys
 {
     const float4*     xq;
     const int*        tgrid;
+    const float*      xqp;        // cluster-packed records (DeviceView::xqp)
     float4*           fnb;
     const Sci*        sci;
     const Cj4*        cj4;
@@ -283,6 +304,36 @@ struct BatchSys
     float             box[3];
     float             shiftvec[kNShift * 3];
 };
+
+// Dynamic shared memory beyond the 48 KB default needs a per-kernel opt-in; the attribute is a
+// property of the kernel in the current device's context.  total_bytes (dynamic + static) decides
+// whether the opt-in is needed; the largest dynamic size set so far is remembered per kernel and
+// device (setting it again is harmless, so concurrent first calls need no lock).
+template<auto kKernel>
+cudaError_t smem_optin(size_t total_bytes, size_t dynamic_bytes)
+{
+    if (total_bytes <= 48 * 1024)
+    {
+        return cudaSuccess;
+    }
+    static int done[64] = { 0 };
+    int        dev      = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    {
+        return cudaFuncSetAttribute(kKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dynamic_bytes);
+    }
+    if (done[dev] >= (int)dynamic_bytes)
+    {
+        return cudaSuccess;
+    }
+    const cudaError_t e = cudaFuncSetAttribute(kKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)dynamic_bytes);
+    if (e == cudaSuccess)
+    {
+        done[dev] = (int)dynamic_bytes;
+    }
+    return e;
+}
 
 // ---- host set-up helpers (nbx_api.cu) ----
 double one_4pi_eps0();
@@ -319,6 +370,9 @@ cudaError_t launch_search(const DeviceView& v, cudaStream_t s);
 cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, cudaStream_t s);
 cudaError_t launch_force(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, cudaEvent_t ev0 = nullptr,
                          cudaEvent_t ev1 = nullptr);
+// the packed-core force kernel (v.pair_core 1; potential-shift or plain cut-off LJ), with the
+// v.stage_depth j-stage buffers and v.force_blocks blocks per SM
+cudaError_t launch_force_x2(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, int* counter);
 // forces to atom order (+ virial); with d_e / d_vir the last block also finishes the energies
 // and virial (the accumulators must have been cleared by launch_convert_x(clear))
 // (stage: write the forces through shared memory as contiguous floats, for f in host memory)

@@ -234,6 +234,17 @@ class ForceCalculator:
         """Device calls add the nonbonded forces to the force buffer instead of overwriting it."""
         check(_lib.load().nbx_set_force_accumulate(self.h, int(bool(enable))), self.h)
 
+    def set_force_kernel(self, tile: int = 1, stage_depth: int = 2, blocks_per_sm: int = 2):
+        """Force-kernel shape: tile 1 = two atom pairs per lane (packed FP32x2), 0 = one pair per
+        lane; stage_depth = j-cluster stage buffers per warp (2 or 3); blocks_per_sm = resident
+        256-thread blocks per SM (2 or 3)."""
+        check(_lib.load().nbx_set_force_kernel(self.h, int(tile), int(stage_depth), int(blocks_per_sm)), self.h)
+
+    def force_kernel(self) -> tuple[int, int, int]:
+        t, d, b = C.c_int(), C.c_int(), C.c_int()
+        check(_lib.load().nbx_get_force_kernel(self.h, C.byref(t), C.byref(d), C.byref(b)), self.h)
+        return t.value, d.value, b.value
+
     def set_list_balance(self, entries_per_sm: int):
         """Entries per SM below which long list entries are split (0: never); next search."""
         check(_lib.load().nbx_set_list_balance(self.h, int(entries_per_sm)), self.h)

@@ -165,6 +165,16 @@ int nbx_get_timings(nbx_handle* h, double* force_ms, long long* counts, int rese
  * [2] search count pass, [3] search write pass, [4] prune (fresh or rolling).  ms and counts
  * are double[5] / long long[5] (either may be NULL); reset = 1 clears them. */
 int nbx_get_phase_timings(nbx_handle* h, double* ms, long long* counts, int reset);
+/* Force-kernel shape (no counterpart in the reference; the autotuner's tile and staging
+ * axes).  tile 0: one atom pair per lane, a warp instruction covers 8 i-atoms x 4 j-atoms
+ * (scalar FP32); tile 1 (default): two pairs per lane, 8 x 8 atoms per warp instruction
+ * (packed FP32x2 arithmetic; potential-shift or plain cut-off LJ -- the switch modifiers and
+ * LJ-PME always run tile 0).  stage_depth: j-cluster stage buffers per warp of tile 1, 2
+ * (default) or 3 (two groups' copies in flight).  blocks_per_sm: resident 256-thread blocks per
+ * SM of tile 1, 2 (default; up to 128 registers a thread) or 3 (80 registers).  Results agree
+ * to rounding between shapes. */
+int nbx_set_force_kernel(nbx_handle* h, int tile, int stage_depth, int blocks_per_sm);
+int nbx_get_force_kernel(const nbx_handle* h, int* tile, int* stage_depth, int* blocks_per_sm);
 /* Failure-detection test hook (no counterpart in the reference): with enable = 1 the force
  * kernel's shared-memory stage barriers wait for bytes that never arrive, so their bounded
  * (1 s) waits give up and the next nbx_compute / nbx_synchronize returns NBX_ERR_TIMEOUT; the

@@ -18,9 +18,11 @@ from tests.helpers import rel_rms
 pytestmark = pytest.mark.gpu
 
 
-def test_stage_wait_times_out_and_the_handle_recovers():
+@pytest.mark.parametrize("shape", [(1, 2, 2), (1, 3, 3), (0, 2, 2)])
+def test_stage_wait_times_out_and_the_handle_recovers(shape):
     s = systems.spc_water(300, 2.08, seed=5)
     calc = nblib.ForceCalculator(s, nblib.NBKernelOptions(pairlist_cutoff=1.0, rcoulomb=0.9))
+    calc.set_force_kernel(*shape)
     L = _lib.load()
     assert L.nbx_set_wait_test(calc.h, 1) == _lib.NBX_OK
     t0 = time.time()

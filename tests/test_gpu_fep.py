@@ -102,7 +102,9 @@ def test_unchanged_state_equals_the_plain_path(coulomb):
                              alpha_coul=0.0)
         f = calc.compute(s.x).astype(np.float64)
         assert rel_rms(f, f0) <= 2e-6
-        np.testing.assert_allclose(calc.energies, e0, rtol=2e-6)
+        # reaction field sums q_i q_j (1/r - c_rf) with float 1/r out to rc: ~2e-6 noise on the
+        # total, so the two summation routes agree to the RF energy bar of the parity tests
+        np.testing.assert_allclose(calc.energies, e0, rtol=2e-6 if coulomb == "ewald" else 5e-6)
         np.testing.assert_allclose(calc.virial, v0, rtol=0, atol=2e-6 * np.abs(v0).max())
         t = calc.free_energy_terms()
         assert abs(t["dvdl_coul"]) <= 1e-5 * (abs(t["V_coul"]) + 1) and abs(t["dvdl_lj"]) <= 1e-5 * (abs(t["V_lj"]) + 1)

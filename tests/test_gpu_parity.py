@@ -164,6 +164,29 @@ def test_forces_energies_virial_vs_oracle(name, coulomb):
     assert err64 <= 1e-5
 
 
+@pytest.mark.parametrize("shape", [(0, 2, 2), (1, 3, 2), (1, 2, 3), (1, 3, 3)])
+@pytest.mark.parametrize("name", ["water3000", "water_small_box", "water_tiny", "lj_liquid"])
+@pytest.mark.parametrize("coulomb", [nblib.CoulombType.Pme, nblib.CoulombType.ReactionField])
+def test_force_kernel_shapes_vs_oracle(name, coulomb, shape):
+    """The other force-kernel shapes (one pair per lane; two pairs per lane with three stage buffers
+    and/or three blocks per SM) against the oracle, F only and F + E; the default shape (two pairs
+    per lane, two buffers, two blocks) is covered above."""
+    s = SYSTEMS[name]()
+    calc, o = _pair(s, coulomb=coulomb)
+    calc.set_force_kernel(*shape)
+    assert calc.force_kernel() == shape
+    o.force(True)
+    fo, eo = o.forces(), o.energies()
+    f = calc.compute(s.x).copy()
+    assert rel_rms(f, fo) <= FORCE_RTOL
+    etol = ENERGY_RTOL if coulomb == nblib.CoulombType.Pme else ENERGY_RTOL_RF
+    for k in range(2):
+        if abs(eo[k]) > 0:
+            assert abs(calc.energies[k] - eo[k]) <= etol * abs(eo[k]) + 1e-9, (k, calc.energies[k], eo[k])
+    f_only = calc.compute(s.x, energies=False)
+    assert rel_rms(f_only, fo) <= FORCE_RTOL
+
+
 @pytest.mark.parametrize("key", ["argon", "spc_methanol"])
 def test_nblib_golden_forces(key):
     """The reference's own nblib golden vectors (Cutoff Coulomb, rc = rlist = 1.0)."""
