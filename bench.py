@@ -209,7 +209,7 @@ def run_reference(args) -> None:
 
 def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
     """256 uneven SPC water boxes (500..20,000 atoms, log-uniform): the batched step
-    (autotuned launch shape and prune interval, CUDA graph) against the same step as
+    (autotuned tile, stage depth, launch shape and prune interval, CUDA graph) against the same step as
     256 sequential single-system steps.  Each step is F + E + virial for every system."""
     import torch
 
@@ -230,7 +230,8 @@ def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
     frames[0] = torch.from_numpy(np.concatenate([s.x.reshape(-1) for s in ens])).to(frames.device)
     for t in range(1, total):
         frames[t] = frames[t - 1] + SIGMA_STEP * torch.randn(3 * n, generator=gen, device=frames.device)
-    best, tune = b.autotune(frames[: min(total, 12)], variants=(0, 1, 2, 3), prune_intervals=(4, 10, 20))
+    space = {"tiles": ((0, 2), (1, 2), (1, 3)), "variants": (0, 1, 2, 3), "prune_intervals": (4, 10, 20)}
+    best, tune = b.autotune(frames[: min(total, 12)], **space)
     f = torch.empty(3 * n, dtype=torch.float32, device=frames.device)
     e = torch.empty(2 * len(ens), dtype=torch.float64, device=frames.device)
     v = torch.empty(9 * len(ens), dtype=torch.float64, device=frames.device)
@@ -254,8 +255,13 @@ def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
             "steps": steps, "batched_ms_per_step": bat_ms, "sequential_ms_per_step": seq_ms,
             "speedup": seq_ms / bat_ms, "force_evals_per_s_batched": len(ens) / (bat_ms * 1e-3),
             "force_evals_per_s_sequential": len(ens) / (seq_ms * 1e-3),
-            "autotuned": best, "note": "each step: F+E+virial of all systems; search every 100 steps, "
-                                        "rolling prune as autotuned"}
+            "autotuned": best,
+            "search_space": {"tile_stage_depth": space["tiles"], "launch_shape": "0: 256x2, 1: 128x4, 2: 512x1, "
+                             "3: 64x8 threads x blocks per SM", "prune_intervals": space["prune_intervals"],
+                             "tile": "0: one atom pair per lane (8x4 atoms per warp instruction), 1: two pairs per "
+                                     "lane (8x8, packed FP32x2)", "candidates": len(tune),
+                             "best_ms_per_step": min(tune.values()), "worst_ms_per_step": max(tune.values())},
+            "note": "each step: F+E+virial of all systems; search every 100 steps, rolling prune as autotuned"}
 
 
 def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:

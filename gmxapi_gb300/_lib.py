@@ -42,7 +42,7 @@ EXPORTED = [
     "nbx_batch_create", "nbx_batch_destroy", "nbx_batch_last_error", "nbx_batch_atoms", "nbx_batch_set_stream",
     "nbx_batch_search_device", "nbx_batch_prune_device", "nbx_batch_compute_device", "nbx_batch_md_step_device",
     "nbx_batch_sequential_md_step_device", "nbx_batch_set_graph", "nbx_batch_set_kernel_variant",
-    "nbx_batch_set_prune", "nbx_backward_device", "nbx_set_parameters_device",
+    "nbx_batch_set_prune", "nbx_batch_set_force_kernel", "nbx_backward_device", "nbx_set_parameters_device",
     "nbx_get_phase_timings", "nbx_set_list_balance", "nbx_get_list_balance",
     "nbx_batch_set_parameters_device", "nbx_batch_backward_device", "nbx_batch_force_match_device",
     "nbx_set_wait_test", "nbx_set_force_kernel", "nbx_get_force_kernel",
@@ -202,6 +202,7 @@ def load():
     L.nbx_batch_set_graph.argtypes = [vp, C.c_int]
     L.nbx_batch_set_kernel_variant.argtypes = [vp, C.c_int]
     L.nbx_batch_set_prune.argtypes = [vp, C.c_int, C.c_float]
+    L.nbx_batch_set_force_kernel.argtypes = [vp, C.c_int, C.c_int]
     L.nbx_backward_device.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.nbx_set_parameters_device.argtypes = [vp, vp, vp]
     L.nbx_ewald_coefficient.argtypes = [C.c_float, C.c_float]

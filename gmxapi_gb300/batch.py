@@ -3,8 +3,9 @@
 ``BatchForceCalculator`` wraps the nbx_batch_* C ABI: per-system grids and
 pair lists, one persistent force launch over all systems' list entries,
 per-system FP64 energies and virials, and a CUDA graph for the step.
-``autotune`` picks the force-kernel launch shape and the rolling-prune
-interval by timing candidate settings on the caller's own coordinate frames.
+``autotune`` picks the force-kernel tile (one or two atom pairs per lane), the
+j-stage depth, the launch shape and the rolling-prune interval by timing
+candidate settings on the caller's own coordinate frames.
 """
 from __future__ import annotations
 
@@ -112,19 +113,27 @@ class BatchForceCalculator:
     def set_kernel_variant(self, variant: int):
         self._check(_lib.load().nbx_batch_set_kernel_variant(self.h, int(variant)))
 
+    def set_force_kernel(self, tile: int = 1, stage_depth: int = 2):
+        """Force-kernel tile (1: two atom pairs per lane, packed FP32x2; 0: one pair per lane) and
+        j-stage buffers per warp (2 or 3)."""
+        self._check(_lib.load().nbx_batch_set_force_kernel(self.h, int(tile), int(stage_depth)))
+
     def set_prune(self, nstlist_prune: int, rlist_inner: float):
         self._check(_lib.load().nbx_batch_set_prune(self.h, int(nstlist_prune), float(rlist_inner)))
 
     # ---- autotuner ----
     def autotune(self, frames, variants=(0, 1, 2, 3), prune_intervals=(4, 10, 20), steps=None,
-                 buffer_at_10=0.05):
-        """Time every (launch shape, prune interval) on ``frames`` and keep the fastest.
+                 buffer_at_10=0.05, tiles=((0, 2), (1, 2), (1, 3))):
+        """Time every (tile, stage depth, launch shape, prune interval) on ``frames``; keep the fastest.
 
-        frames: torch tensor (nframes, 3 * total_atoms) on the device, a trajectory
-        segment of the workload.  For a prune interval n the inner radius is
-        rc + buffer_at_10 * sqrt(n / 10) (a diffusive drift over n steps).  Each
-        candidate runs the full schedule (search, rolling prune, compute with
-        energies) over the frames; returns (best settings, all timings in ms/step).
+        frames: torch tensor (nframes, 3 * total_atoms) on the device, a trajectory segment of the
+        workload.  tiles: (tile, stage depth) pairs of the force kernel (tile 1 = two atom pairs per
+        lane in packed FP32x2 arithmetic, tile 0 = one pair per lane; depth = j-stage buffers per
+        warp).  variants: launch shapes (0: 256x2, 1: 128x4, 2: 512x1, 3: 64x8 threads x blocks per
+        SM).  For a prune interval n the inner radius is rc + buffer_at_10 * sqrt(n / 10) (a
+        diffusive drift over n steps).  Each candidate runs the full schedule (search, rolling
+        prune, compute with energies) over the frames; returns (best settings, timings in ms/step
+        keyed by (tile, depth, variant, interval)).
         """
         import torch
 
@@ -139,21 +148,26 @@ class BatchForceCalculator:
         for n in prune_intervals:
             rin = min(self.options.pairlist_cutoff, rc + buffer_at_10 * math.sqrt(n / 10.0))
             self.set_prune(n, rin)
-            for var in variants:
-                self.set_kernel_variant(var)
-                # warm-up pass (search + graph capture), then the timed pass
-                for t in range(min(3, nfr)):
-                    self.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), e.data_ptr(), v.data_ptr())
-                torch.cuda.synchronize()
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record()
-                for t in range(nfr):
-                    self.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), e.data_ptr(), v.data_ptr())
-                b.record()
-                torch.cuda.synchronize()
-                results[(var, n)] = a.elapsed_time(b) / nfr
+            for tile, depth in tiles:
+                self.set_force_kernel(tile, depth)
+                for var in variants:
+                    self.set_kernel_variant(var)
+                    # warm-up pass (search + graph capture), then the timed pass
+                    for t in range(min(3, nfr)):
+                        self.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), e.data_ptr(), v.data_ptr())
+                    torch.cuda.synchronize()
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record()
+                    for t in range(nfr):
+                        self.md_step_device(t, frames[t].data_ptr(), f.data_ptr(), e.data_ptr(), v.data_ptr())
+                    b.record()
+                    torch.cuda.synchronize()
+                    results[(tile, depth, var, n)] = a.elapsed_time(b) / nfr
         best = min(results, key=results.get)
-        rin = min(self.options.pairlist_cutoff, rc + buffer_at_10 * math.sqrt(best[1] / 10.0))
-        self.set_prune(best[1], rin)
-        self.set_kernel_variant(best[0])
-        return {"kernel_variant": best[0], "nstlist_prune": best[1], "rlist_inner": rin}, results
+        tile, depth, var, n = best
+        rin = min(self.options.pairlist_cutoff, rc + buffer_at_10 * math.sqrt(n / 10.0))
+        self.set_prune(n, rin)
+        self.set_force_kernel(tile, depth)
+        self.set_kernel_variant(var)
+        return {"tile": tile, "stage_depth": depth, "kernel_variant": var, "nstlist_prune": n,
+                "rlist_inner": rin}, results

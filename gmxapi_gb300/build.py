@@ -27,6 +27,7 @@ UNITS = {
     "nbx_force.cu": [],
     "nbx_force_x2.cu": [],
     "nbx_batch.cu": [],
+    "nbx_batch_x2.cu": [],
     "nbx_adjoint.cu": [],
     "nbx_balance.cu": [],
     "nbx_api.cu": [],

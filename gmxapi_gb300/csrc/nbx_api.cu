@@ -1684,7 +1684,9 @@ struct nbx_batch
     int                      prune_part = 0;
     int                      nparts     = 1;
     bool                     use_prune  = false;
-    int                      variant    = 0;
+    int                      variant    = 0;  // launch shape of the batched force kernel (0..3)
+    int                      tile       = 1;  // 1: packed pair core, 0: one pair per lane
+    int                      depth      = 2;  // j-stage buffers per warp of the packed core
     bool                     use_graph  = true;
     cudaGraphExec_t          graph      = nullptr;
     cudaStream_t             capture_stream = nullptr;  // private: capture is not allowed on legacy streams
@@ -1702,6 +1704,13 @@ struct nbx_batch
 namespace
 {
 thread_local std::string g_batch_error;
+
+// The force-kernel choice passed to launch_batch_compute: launch shape in bits 0-1, the packed
+// core in bit 2, three stage buffers in bit 3.
+int batch_variant_code(const nbx_batch* b)
+{
+    return b->variant | (b->tile ? 4 : 0) | (b->tile && b->depth == 3 ? 8 : 0);
+}
 
 int batch_error(nbx_batch* b, int code, const std::string& msg)
 {
@@ -1801,7 +1810,7 @@ int batch_compute(nbx_batch* b, const float* d_x, float* d_f, double* d_e, doubl
     const int nsys = (int)b->sys.size();
     auto      run  = [&](cudaStream_t s) {
         return launch_batch_compute(b->cv, b->d_table, b->d_prefix, nsys, b->max_slots, b->max_atoms, d_x, d_f,
-                                    b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, b->variant, b->num_sms, s);
+                                    b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, batch_variant_code(b), b->num_sms, s);
     };
     if (!b->use_graph)
     {
@@ -1989,7 +1998,7 @@ int nbx_batch_force_match_device(nbx_batch* b, const float* d_x, const float* d_
         if (e == cudaSuccess) e = launch_batch_set_q(b->d_table, nsys, b->max_slots, d_q, s);
         if (e == cudaSuccess)
             e = launch_batch_compute(b->cv, b->d_table, b->d_prefix, nsys, b->max_slots, b->max_atoms, d_x,
-                                     b->d_fm_f, b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, b->variant,
+                                     b->d_fm_f, b->d_sums, b->sums_bytes, b->d_counter, d_e, d_vir, batch_variant_code(b),
                                      b->num_sms, s);
         if (e == cudaSuccess) e = launch_match_loss(b->d_fm_f, d_ftarget, n3, b->d_fm_g, d_loss, b->num_sms, s);
         if (e == cudaSuccess) e = batch_backward_launch(b, b->d_fm_g, nullptr, nullptr, d_gq, d_gnbfp, s);
@@ -2072,6 +2081,7 @@ int nbx_batch_create(int num_systems, const nbx_system_desc* systems, const nbx_
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
     optin_batch_force_smem();
+    optin_batch_force_x2_smem();
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
     b->own_stream = true;
@@ -2323,6 +2333,18 @@ int nbx_batch_set_kernel_variant(nbx_batch* b, int variant)
         return NBX_ERR_INVALID_INPUT;
     }
     b->variant = variant;
+    drop_graph(b);
+    return NBX_OK;
+}
+
+int nbx_batch_set_force_kernel(nbx_batch* b, int tile, int stage_depth)
+{
+    if (!b || tile < 0 || tile > 1 || stage_depth < 2 || stage_depth > 3)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    b->tile  = tile;
+    b->depth = stage_depth;
     drop_graph(b);
     return NBX_OK;
 }

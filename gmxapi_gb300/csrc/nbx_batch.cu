@@ -17,24 +17,6 @@ namespace nbx
 namespace
 {
 
-__device__ __forceinline__ int find_system(const int* prefix, int nsys, int e)
-{
-    int lo = 0, hi = nsys - 1;
-    while (lo < hi)
-    {
-        const int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= e)
-        {
-            lo = mid;
-        }
-        else
-        {
-            hi = mid - 1;
-        }
-    }
-    return lo;
-}
-
 // Entry prefix sums over the systems' lists (after every search), prefix[0..nsys], and the
 // prefix sums of their exclusion work items (kExclChunkAtoms atoms each),
 // prefix[nsys + 1 .. 2 nsys + 1]; systems whose list or grid overflowed contribute neither
@@ -375,7 +357,17 @@ cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, cons
         k_batch_excl_energy<<<num_sms * 8, 256, 0, s>>>(cv, sys, prefix, nsys, en);
     }
     const bool ewald = (cv.coulomb == 0);
-    if (energy)
+    if (variant & 4)
+    {
+        // the packed pair core: launch shape in bits 0-1, three stage buffers in bit 3
+        const cudaError_t ex = launch_batch_force_x2(cv, sys, prefix, nsys, counter, en, fs, variant & 3,
+                                                     (variant & 8) ? 3 : 2, energy, num_sms, s);
+        if (e == cudaSuccess)
+        {
+            e = ex;
+        }
+    }
+    else if (energy)
     {
         if (ewald)
             launch_batch_force_variant<true, true>(variant, cv, sys, prefix, nsys, counter, en, fs, num_sms, s);

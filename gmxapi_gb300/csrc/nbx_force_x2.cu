@@ -20,7 +20,7 @@ constexpr int kForceThreads = 256;
 
 // The same force / energy evaluation with the packed pair core (nbx_pair_x2.cuh): potential-shift
 // or plain cut-off LJ with Ewald or reaction-field Coulomb.  kDepth: j-stage buffers per warp.
-template<bool kEnergy, bool kEwald, int kDepth, int kBlocks>
+template<bool kEnergy, int kCoul, int kDepth, int kBlocks>
 __global__ void __launch_bounds__(kForceThreads, kBlocks) k_force_x2(DeviceView v, int* work_counter)
 {
     // {-6*C6, 12*C12, LJ energy shift of the pair, 0} per type pair
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kForceThreads, kBlocks) k_force_x2(DeviceView 
             }
             continue;
         }
-        if (!process_entry_x2<kEnergy, kEwald, kDepth>(k, p, v.sci[e], reinterpret_cast<const char*>(nbfp_s), js, w,
+        if (!process_entry_x2<kEnergy, kCoul, kDepth>(k, p, v.sci[e], reinterpret_cast<const char*>(nbfp_s), js, w,
                                                         nt1, lane, v.wait_test_bytes, e_lj_acc, e_el_acc))
         {
             stage_timeout_x2(js, &v.hdr->status, lane);
@@ -116,19 +116,30 @@ __global__ void __launch_bounds__(kForceThreads, kBlocks) k_force_x2(DeviceView 
     }
 }
 
-template<bool kEnergy, bool kEwald, int kDepth, int kBlocks>
+template<bool kEnergy, int kCoul, int kDepth, int kBlocks>
 cudaError_t launch_x2(const DeviceView& v, cudaStream_t s, int num_sms, int* counter)
 {
     const size_t smem = sizeof(float4) * ((size_t)v.ntypes1 * v.ntypes1
                                           + (size_t)(kForceThreads / 32) * warp_smem_f4_x2<kDepth>());
-    cudaError_t e = smem_optin<k_force_x2<kEnergy, kEwald, kDepth, kBlocks>>(
+    cudaError_t e = smem_optin<k_force_x2<kEnergy, kCoul, kDepth, kBlocks>>(
             smem + sizeof(double) * 2 * kForceThreads, smem);
     if (e != cudaSuccess)
     {
         return e;
     }
-    k_force_x2<kEnergy, kEwald, kDepth, kBlocks><<<num_sms * kBlocks, kForceThreads, smem, s>>>(v, counter);
+    k_force_x2<kEnergy, kCoul, kDepth, kBlocks><<<num_sms * kBlocks, kForceThreads, smem, s>>>(v, counter);
     return cudaGetLastError();
+}
+
+// Coulomb flavour of the packed core: 0 reaction field, 1 Ewald, 2 Ewald with the potential shift
+// (energies only; forces do not depend on the shift)
+int coulomb_flavour(const DeviceView& v, bool energy)
+{
+    if (v.coulomb != 0)
+    {
+        return 0;
+    }
+    return (energy && v.sh_ewald != 0.0f) ? 2 : 1;
 }
 
 } // namespace
@@ -136,18 +147,18 @@ cudaError_t launch_x2(const DeviceView& v, cudaStream_t s, int num_sms, int* cou
 cudaError_t launch_force_x2(const DeviceView& v, bool energy, cudaStream_t s, int num_sms, int* counter)
 {
     using Launch = cudaError_t (*)(const DeviceView&, cudaStream_t, int, int*);
-    // [blocks 2, 3][depth 2, 3][energy][ewald]
-    static const Launch table[2][2][2][2] = {
-        { { { launch_x2<false, false, 2, 2>, launch_x2<false, true, 2, 2> },
-            { launch_x2<true, false, 2, 2>, launch_x2<true, true, 2, 2> } },
-          { { launch_x2<false, false, 3, 2>, launch_x2<false, true, 3, 2> },
-            { launch_x2<true, false, 3, 2>, launch_x2<true, true, 3, 2> } } },
-        { { { launch_x2<false, false, 2, 3>, launch_x2<false, true, 2, 3> },
-            { launch_x2<true, false, 2, 3>, launch_x2<true, true, 2, 3> } },
-          { { launch_x2<false, false, 3, 3>, launch_x2<false, true, 3, 3> },
-            { launch_x2<true, false, 3, 3>, launch_x2<true, true, 3, 3> } } },
+    // [blocks 2, 3][depth 2, 3][energy][coulomb flavour]
+    static const Launch table[2][2][2][3] = {
+        { { { launch_x2<false, 0, 2, 2>, launch_x2<false, 1, 2, 2>, launch_x2<false, 1, 2, 2> },
+            { launch_x2<true, 0, 2, 2>, launch_x2<true, 1, 2, 2>, launch_x2<true, 2, 2, 2> } },
+          { { launch_x2<false, 0, 3, 2>, launch_x2<false, 1, 3, 2>, launch_x2<false, 1, 3, 2> },
+            { launch_x2<true, 0, 3, 2>, launch_x2<true, 1, 3, 2>, launch_x2<true, 2, 3, 2> } } },
+        { { { launch_x2<false, 0, 2, 3>, launch_x2<false, 1, 2, 3>, launch_x2<false, 1, 2, 3> },
+            { launch_x2<true, 0, 2, 3>, launch_x2<true, 1, 2, 3>, launch_x2<true, 2, 2, 3> } },
+          { { launch_x2<false, 0, 3, 3>, launch_x2<false, 1, 3, 3>, launch_x2<false, 1, 3, 3> },
+            { launch_x2<true, 0, 3, 3>, launch_x2<true, 1, 3, 3>, launch_x2<true, 2, 3, 3> } } },
     };
-    return table[v.force_blocks == 3 ? 1 : 0][v.stage_depth == 3 ? 1 : 0][energy ? 1 : 0][v.coulomb == 0 ? 1 : 0](
+    return table[v.force_blocks == 3 ? 1 : 0][v.stage_depth == 3 ? 1 : 0][energy ? 1 : 0][coulomb_flavour(v, energy)](
             v, s, num_sms, counter);
 }
 

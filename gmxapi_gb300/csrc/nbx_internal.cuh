@@ -217,6 +217,25 @@ struct DeviceView
     int force_blocks;  // resident blocks of 256 threads per SM for the packed kernel (2, 3)
 };
 
+// The system of batch entry e: the last system whose entry prefix sum is <= e.
+__device__ __forceinline__ int find_system(const int* prefix, int nsys, int e)
+{
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= e)
+        {
+            lo = mid;
+        }
+        else
+        {
+            hi = mid - 1;
+        }
+    }
+    return lo;
+}
+
 // Writes slot k's coordinates, charge and type into the cluster-packed records (DeviceView::xqp).
 __device__ __forceinline__ void write_packed_slot(float* xqp, int k, float x, float y, float z, float q, int type)
 {
@@ -398,6 +417,12 @@ cudaError_t launch_batch_set_q(const BatchSys* sys, int nsys, int max_slots, con
 cudaError_t launch_match_loss(const float* d_f, const float* d_ft, size_t n3, float* d_gF, double* d_loss,
                               int num_sms, cudaStream_t s);
 cudaError_t launch_batch_prefix(const BatchSys* sys, int nsys, int* prefix, unsigned* status, cudaStream_t s);
+// The batched force kernel with the packed pair core: launch shape 0..3 as the one-pair-per-lane
+// kernel's (256 x 2, 128 x 4, 512 x 1, 64 x 8 threads x blocks per SM), stage_depth 2 or 3.
+cudaError_t launch_batch_force_x2(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys, int* counter,
+                                  double* energies, double* fshift, int shape, int stage_depth, bool energy,
+                                  int num_sms, cudaStream_t s);
+cudaError_t optin_batch_force_x2_smem();
 cudaError_t launch_batch_compute(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
                                  int max_slots, int max_atoms, const float* d_x, float* d_f, double* sums,
                                  size_t sums_bytes, int* counter, double* d_e, double* d_vir, int variant,

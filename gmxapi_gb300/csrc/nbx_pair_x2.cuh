@@ -47,16 +47,21 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b)
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
     return *reinterpret_cast<float2*>(&rd);
 }
+// The erfc expansion polynomial of erfc_poly (nbx_internal.cuh), same coefficients, evaluated by
+// Estrin's scheme: (c0 + c1 t) + (c2 + c3 t) t^2 + ((c4 + c5 t) + (c6 + c7 t) t^2) t^4 -- a
+// dependency depth of 4 instead of Horner's 7, for two more multiplications (the pair loop is
+// bound by dependent-instruction latency).
 __device__ __forceinline__ float2 erfc_poly2(float2 t)
 {
-    float2 p = f2(1.128007565e-02f);
-    p        = fma2(p, t, f2(3.713922575e-02f));
-    p        = fma2(p, t, f2(-3.248904943e-01f));
-    p        = fma2(p, t, f2(5.147097111e-01f));
-    p        = fma2(p, t, f2(-7.699845731e-02f));
-    p        = fma2(p, t, f2(3.232774734e-01f));
-    p        = fma2(p, t, f2(2.490737736e-01f));
-    return fma2(p, t, f2(2.664087117e-01f));
+    const float2 t2 = mul2(t, t);
+    const float2 a  = fma2(f2(2.490737736e-01f), t, f2(2.664087117e-01f));
+    const float2 b  = fma2(f2(-7.699845731e-02f), t, f2(3.232774734e-01f));
+    const float2 c  = fma2(f2(-3.248904943e-01f), t, f2(5.147097111e-01f));
+    const float2 d  = fma2(f2(1.128007565e-02f), t, f2(3.713922575e-02f));
+    const float2 t4 = mul2(t2, t2);
+    const float2 lo = fma2(b, t2, a);
+    const float2 hi = fma2(d, t2, c);
+    return fma2(hi, t4, lo);
 }
 
 // Position of atom a (0..7) of a cluster in the packed layout: a and a + 4 adjacent.
@@ -197,7 +202,7 @@ struct PairConstsX2
 // One packed step: i-cluster c (data in shared memory) against the two j-atoms of the lane; the
 // lane's i-force partial for atom (c, ii) is read, updated and written back in shared memory.
 // kExcl: the pairs' exclusion bits (intA / intB) and the diagonal self pairs (in okA / okB).
-template<bool kEnergy, bool kEwald, bool kExcl>
+template<bool kEnergy, int kCoul, bool kExcl>
 __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* __restrict__ nbfp_b,
                                              float4* __restrict__ rec, int jj, const float2 xj, const float2 yj,
                                              const float2 zj, const float2 qje, const int2 tjb, bool okA, bool okB,
@@ -217,8 +222,10 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
     float2 rinv      = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
     if (kEnergy)
     {
-        // one Newton step: rsqrt.approx -> ~correctly rounded, unbiased for the energy sums
-        rinv = mul2(rinv, fma2(f2(-0.5f), mul2(mul2(r2, rinv), rinv), f2(1.5f)));
+        // one Newton step: rsqrt.approx -> ~correctly rounded, unbiased for the energy sums;
+        // y (1.5 - (r^2 / 2) y^2) with -r^2 / 2 formed beside the rsqrt
+        const float2 r2h = mul2(r2, f2(-0.5f));
+        rinv             = mul2(rinv, fma2(r2h, mul2(rinv, rinv), f2(1.5f)));
     }
     // pairs outside the cut-off (or of a pruned half, or the diagonal's lower triangle) get
     // 1/r = 0: every force term below carries 1/r^2 and vanishes
@@ -239,7 +246,7 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
     const float2 qq     = mul2(make_float2(i1.z, i1.w), qje);
     float2       fcr2;  // Coulomb F r^2 / (q_i q_j)
     float2       hel;   // Coulomb energy / (q_i q_j epsfac), before masking
-    if (kEwald)
+    if (kCoul >= 1)
     {
         // erfc(beta r) = t P(t) exp(-beta^2 r^2), t = 1/(1 + p beta r)
         const float2 r    = mul2(r2, rinv);
@@ -257,7 +264,10 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
         }
         if (kEnergy)
         {
-            hel = fma2(tpr, expm, f2(-k.sh_ewald));
+            // with the Ewald potential modifier the shift counts for pairs in range; without it the
+            // term vanishes outside the cut-off by itself (1/r = 0)
+            hel = (kCoul == 2) ? fma2(tpr, expm, make_float2(inA ? -k.sh_ewald : 0.0f, inB ? -k.sh_ewald : 0.0f))
+                               : mul2(tpr, expm);
         }
     }
     else
@@ -265,19 +275,27 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
         fcr2 = kExcl ? fma2(f2(k.nk_rf2), r2, mul2(rinv, make_float2(intA, intB))) : fma2(f2(k.nk_rf2), r2, rinv);
         if (kEnergy)
         {
+            // 1/r + k_rf r^2 - c_rf for pairs in range, 0 outside
             hel = fma2(f2(k.k_rf), r2, sub2(rinv, f2(k.c_rf)));
+            hel = make_float2(inA ? hel.x : 0.0f, inB ? hel.y : 0.0f);
         }
     }
     const float2 fscal = mul2(fma2(qq, fcr2, flj), rinv2);
     if (kEnergy)
     {
-        // pairs that count: inside the cut-off and not excluded
-        const float2 m = kExcl ? make_float2(inA ? intA : 0.0f, inB ? intB : 0.0f)
-                               : make_float2(inA ? 1.0f : 0.0f, inB ? 1.0f : 0.0f);
+        // Only pairs inside the cut-off that are not excluded count.  Outside the cut-off 1/r = 0
+        // already zeroes every r-dependent term, so only the constant shifts need the mask; an
+        // excluded pair inside the cut-off (int 0) has 1/r^6 = 0 (LJ) but its Ewald term must go.
+        const bool cA = kExcl ? (inA && intA != 0.0f) : inA;
+        const bool cB = kExcl ? (inB && intB != 0.0f) : inB;
         // LJ energy: vrep/12 - vdisp/6 + shift = (flj - vdisp)/12 + shift
-        const float2 vlj = fma2(add2(flj, nvdisp), f2(1.0f / 12.0f), make_float2(lA.z * m.x, lB.z * m.y));
+        const float2 vlj = fma2(add2(flj, nvdisp), f2(1.0f / 12.0f), make_float2(cA ? lA.z : 0.0f, cB ? lB.z : 0.0f));
         ejlj             = add2(ejlj, vlj);
-        ejel             = fma2(make_float2(i1.z, i1.w), mul2(hel, m), ejel);
+        if (kExcl)
+        {
+            hel = make_float2(cA ? hel.x : 0.0f, cB ? hel.y : 0.0f);
+        }
+        ejel = fma2(make_float2(i1.z, i1.w), hel, ejel);
     }
     float4 fi = rec[2 + jj];
     fi.x      = fmaf(fscal.y, dx.y, fmaf(fscal.x, dx.x, fi.x));
@@ -313,11 +331,53 @@ __device__ __forceinline__ void pair_bits_x2(int c, unsigned mA, unsigned mB, un
     }
 }
 
+// The set i-clusters `rem` of one j-cluster, visited two at a time so that two independent
+// pair computations share a basic block.  kSame: both halves' masks equal rem (no per-half test).
+template<bool kEnergy, int kCoul, bool kExcl, bool kSame>
+__device__ __forceinline__ void jcluster_x2(const PairConstsX2& k, const char* __restrict__ nbfp_b,
+                                            float4* __restrict__ lane_rec, unsigned rem, unsigned mA, unsigned mB,
+                                            unsigned xA, unsigned xB, bool central, int sci, int cj, int ii, int jj,
+                                            const float2 xj, const float2 yj, const float2 zj, const float2 qje,
+                                            const int2 tjb, float2& fjx, float2& fjy, float2& fjz, float2& ejel,
+                                            float2& ejlj)
+{
+#pragma unroll 1
+    while (rem)
+    {
+        const int ca = __ffs(rem) - 1;
+        rem &= rem - 1;
+        bool  okA = true, okB = true;
+        float intA = 1.0f, intB = 1.0f;
+        if (!kSame)
+        {
+            pair_bits_x2<kExcl>(ca, mA, mB, xA, xB, central, sci, cj, ii, jj, okA, okB, intA, intB);
+        }
+        if (rem)
+        {
+            const int cb = __ffs(rem) - 1;
+            rem &= rem - 1;
+            bool  okA2 = true, okB2 = true;
+            float intA2 = 1.0f, intB2 = 1.0f;
+            if (!kSame)
+            {
+                pair_bits_x2<kExcl>(cb, mA, mB, xA, xB, central, sci, cj, ii, jj, okA2, okB2, intA2, intB2);
+            }
+            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
+                                                okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
+            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + cb * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
+                                                okA2, okB2, intA2, intB2, fjx, fjy, fjz, ejel, ejlj);
+        }
+        else
+        {
+            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
+                                                okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
+        }
+    }
+}
+
 // All set cluster pairs of one cj4 group.  m0 / m1: the group's half masks; wA / wB: the
-// lane's exclusion words of the two halves (all ones without exclusions).  The set i-clusters
-// of each j-cluster are visited two at a time, so two independent pair computations share a
-// basic block.
-template<bool kEnergy, bool kEwald, bool kExcl>
+// lane's exclusion words of the two halves (all ones without exclusions).
+template<bool kEnergy, int kCoul, bool kExcl>
 __device__ __forceinline__ void group_x2(const PairConstsX2& k, const SysPtrsX2& p, const char* __restrict__ nbfp_b,
                                          const float* __restrict__ jx,
                                          float4* __restrict__ lane_rec, int cj_lane, unsigned m0, unsigned m1,
@@ -347,31 +407,16 @@ __device__ __forceinline__ void group_x2(const PairConstsX2& k, const SysPtrsX2&
         const unsigned xA = wA >> (jm * kNcl), xB = wB >> (jm * kNcl);
         float2 fjx = f2(0.0f), fjy = f2(0.0f), fjz = f2(0.0f);
         float2 ejel = f2(0.0f), ejlj = f2(0.0f);
-#pragma unroll 1
-        while (rem)
+        if (!kExcl && ((mA ^ mB) & 0xffu) == 0)
         {
-            const int ca = __ffs(rem) - 1;
-            rem &= rem - 1;
-            bool  okA, okB;
-            float intA, intB;
-            pair_bits_x2<kExcl>(ca, mA, mB, xA, xB, central, sci, cj, ii, jj, okA, okB, intA, intB);
-            if (rem)
-            {
-                const int cb = __ffs(rem) - 1;
-                rem &= rem - 1;
-                bool  okA2, okB2;
-                float intA2, intB2;
-                pair_bits_x2<kExcl>(cb, mA, mB, xA, xB, central, sci, cj, ii, jj, okA2, okB2, intA2, intB2);
-                pair_step_x2<kEnergy, kEwald, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje,
-                                                     tjb, okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
-                pair_step_x2<kEnergy, kEwald, kExcl>(k, nbfp_b, lane_rec + cb * (kCl * kIRecF4), jj, xj, yj, zj, qje,
-                                                     tjb, okA2, okB2, intA2, intB2, fjx, fjy, fjz, ejel, ejlj);
-            }
-            else
-            {
-                pair_step_x2<kEnergy, kEwald, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje,
-                                                     tjb, okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
-            }
+            // both halves set for every i-cluster of this j-cluster (the common case)
+            jcluster_x2<kEnergy, kCoul, false, true>(k, nbfp_b, lane_rec, rem, mA, mB, xA, xB, central, sci, cj, ii,
+                                                     jj, xj, yj, zj, qje, tjb, fjx, fjy, fjz, ejel, ejlj);
+        }
+        else
+        {
+            jcluster_x2<kEnergy, kCoul, kExcl, false>(k, nbfp_b, lane_rec, rem, mA, mB, xA, xB, central, sci, cj, ii,
+                                                      jj, xj, yj, zj, qje, tjb, fjx, fjy, fjz, ejel, ejlj);
         }
         if (kEnergy)
         {
@@ -412,7 +457,7 @@ __device__ __forceinline__ uint2 excl_words(const SysPtrsX2& p, const int4 ime, 
 }
 
 // One list entry with the packed core; energies added to e_lj_acc / e_el_acc (per lane, FP64).
-template<bool kEnergy, bool kEwald, int kDepth>
+template<bool kEnergy, int kCoul, int kDepth>
 __device__ __forceinline__ bool process_entry_x2(const PairConstsX2& k, const SysPtrsX2& p, const Sci& s,
                                                  const char* __restrict__ nbfp_b, JStageP<kDepth>& js,
                                                  const WarpSmemX2& w, int nt1, int lane, unsigned wait_test_bytes,
@@ -506,12 +551,12 @@ __device__ __forceinline__ bool process_entry_x2(const PairConstsX2& k, const Sy
         const float* jx = js.x + b * kJg * kPackWords;
         if ((ime.y | ime.w) == 0)
         {
-            group_x2<kEnergy, kEwald, false>(k, p, nbfp_b, jx, lane_rec, cj_lane, m0, m1, ~0u, ~0u, s.sci, central,
+            group_x2<kEnergy, kCoul, false>(k, p, nbfp_b, jx, lane_rec, cj_lane, m0, m1, ~0u, ~0u, s.sci, central,
                                              ii, jj, acc_el, cmp_el, acc_lj, cmp_lj);
         }
         else
         {
-            group_x2<kEnergy, kEwald, true>(k, p, nbfp_b, jx, lane_rec, cj_lane, m0, m1, wAB.x, wAB.y, s.sci,
+            group_x2<kEnergy, kCoul, true>(k, p, nbfp_b, jx, lane_rec, cj_lane, m0, m1, wAB.x, wAB.y, s.sci,
                                             central, ii, jj, acc_el, cmp_el, acc_lj, cmp_lj);
         }
     }

@@ -278,6 +278,12 @@ int nbx_batch_sequential_md_step_device(nbx_batch* b, long long step, const floa
  * interval with its inner radius (takes effect at the next search). */
 int nbx_batch_set_graph(nbx_batch* b, int enable);
 int nbx_batch_set_kernel_variant(nbx_batch* b, int variant);
+/* The batched force kernel's tile and j-stage depth (as nbx_set_force_kernel; no counterpart in
+ * the reference): tile 1 (default) two atom pairs per lane in packed FP32x2 arithmetic, tile 0
+ * one pair per lane; stage_depth 2 (default) or 3.  The launch shape stays the kernel variant's.
+ * The batched autotuner (gmxapi_gb300/batch.py) chooses among tile x depth x shape x prune
+ * interval. */
+int nbx_batch_set_force_kernel(nbx_batch* b, int tile, int stage_depth);
 int nbx_batch_set_prune(nbx_batch* b, int nstlist_prune, float rlist_inner);
 /* Batched adjoint (no counterpart in the reference).  d_q: all systems' charges, concatenated atom
  * order; d_nbfp: the shared {6 C6, 12 C12} table ([num_types^2 * 2]); either may be NULL.  Once

@@ -115,6 +115,28 @@ void orc_fp64_allpairs(int n, const float* x, const float* box, const float* q, 
 /* nblib's 1/(4 pi eps0) in kJ mol^-1 nm e^-2 (src/gromacs/math/units.h:79) */
 double orc_one_4pi_eps0(void);
 
+/* ---- CPU layout (nbnxm_cpu_oracle.c): 4-atom clusters, the simple 4x4 list, a 4-wide kernel ----
+ * Ewald real space with potential-shift LJ; x must stay valid for the lifetime of the context
+ * (in box), nbfp holds ntypes^2 {6C6, 12C12}. */
+typedef struct orc_cpu orc_cpu;
+orc_cpu* orc_cpu_create(int n, const float* x, const float* box, const float* q, const int* type, int ntypes,
+                        const float* nbfp, const int* excl_index, const int* excl_list, float rc, float rlist,
+                        float beta, float epsfac);
+void orc_cpu_destroy(orc_cpu* c);
+/* grid.cpp setDimensions / calcColumnIndices / setCellIndices / sortColumnsCpuGeometry */
+void orc_cpu_grid(orc_cpu* c);
+/* pairlist.cpp nbnxn_make_pairlist_part with makeClusterListSimple */
+void orc_cpu_search(orc_cpu* c);
+/* new coordinates (atom order, same box images) into the grid layout without re-gridding */
+void orc_cpu_set_x(orc_cpu* c, const float* x);
+/* the cluster-pair kernel over list entries [e0, e1) on nthreads POSIX threads; 0 on success */
+int  orc_cpu_force(orc_cpu* c, int e0, int e1, int energy, int nthreads);
+void orc_cpu_sizes(const orc_cpu* c, int* s4); /* clusters, list entries, j entries, geometric rule */
+void orc_cpu_list(const orc_cpu* c, int* ci4, int* cj2); /* {ci, shift, cj_start, cj_end}, {cj, excl} */
+void orc_cpu_grid_arrays(const orc_cpu* c, int* atom_indices, float* xs); /* 4 per cluster; 16 per cluster */
+void orc_cpu_forces(const orc_cpu* c, float* f_out); /* N*3, atom order */
+void orc_cpu_energies(const orc_cpu* c, double* e2); /* {Vlj, Vcoul} */
+
 #ifdef __cplusplus
 }
 #endif

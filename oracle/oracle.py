@@ -29,9 +29,8 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-            os.path.join(_HERE, "nbnxm_oracle.c")
-        ):
+        srcs = [os.path.join(_HERE, n) for n in ("nbnxm_oracle.c", "nbnxm_cpu_oracle.c", "nbnxm_oracle.h")]
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(p) for p in srcs):
             build()
         L = C.CDLL(_LIB_PATH)
         vp = C.c_void_p
@@ -81,6 +80,20 @@ def lib():
                                         C.c_double, C.c_int, ip, C.c_int, dp, dp, C.c_int, C.c_double,
                                         C.c_double]
         L.orc_one_4pi_eps0.restype = C.c_double
+        L.orc_cpu_create.restype = vp
+        L.orc_cpu_create.argtypes = [C.c_int, fp, fp, fp, ip, C.c_int, fp, ip, ip, C.c_float, C.c_float,
+                                     C.c_float, C.c_float]
+        for name in ("orc_cpu_destroy", "orc_cpu_grid", "orc_cpu_search"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = None
+        L.orc_cpu_set_x.argtypes = [vp, fp]
+        L.orc_cpu_force.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_cpu_force.restype = C.c_int
+        L.orc_cpu_sizes.argtypes = [vp, ip]
+        L.orc_cpu_list.argtypes = [vp, ip, ip]
+        L.orc_cpu_grid_arrays.argtypes = [vp, ip, fp]
+        L.orc_cpu_forces.argtypes = [vp, fp]
+        L.orc_cpu_energies.argtypes = [vp, dp]
         _lib = L
     return _lib
 
@@ -285,3 +298,73 @@ def fp64_allpairs(system, coulomb=COULOMB_EWALD, rc=0.9, beta=None, subset=None,
                         e.ctypes.data_as(C.POINTER(C.c_double)) if full else None, int(vdw_modifier),
                         float(np.float32(rvdw_switch)), float(beta_lj))
     return (f, e) if full else (f, None)
+
+
+class CpuOracle:
+    """The reference's CPU layout for one system (4-atom clusters, the simple 4x4 cluster pair list
+    of makeClusterListSimple) and a 4-wide cluster-pair kernel (Ewald, potential-shift LJ): the
+    list checker and the timed CPU baseline.  Coordinates are wrapped into the box."""
+
+    def __init__(self, system, rc=0.9, rlist=1.0, beta=None, ewald_rtol=1e-5):
+        L = lib()
+        self.system = system
+        box = np.asarray(system.box, np.float64)
+        x = np.ascontiguousarray(np.asarray(system.x, np.float64) % box, dtype=np.float32)
+        # values that round up to the box edge wrap to 0, as put_atoms_in_box does
+        x = np.where(x >= box.astype(np.float32), np.float32(0), x).astype(np.float32)
+        self._x, xp = _f(x)
+        self._box, bp = _f(system.box)
+        self._q, qp = _f(system.q)
+        self._t, tp = _i(system.type)
+        self._nb, nbp = _f(system.nbfp)
+        self._ei, eip = _i(system.excl_index)
+        self._el, elp = _i(system.excl_list if len(system.excl_list) else np.zeros(1, np.int32))
+        if beta is None:
+            beta = Oracle(system, rc=rc, rlist=rlist, ewald_rtol=ewald_rtol).beta
+        self.beta = float(beta)
+        epsfac = np.float32(L.orc_one_4pi_eps0())
+        self.c = L.orc_cpu_create(system.n, xp, bp, qp, tp, system.ntypes, nbp, eip, elp, rc, rlist,
+                                  self.beta, float(epsfac))
+
+    def __del__(self):
+        if getattr(self, "c", None):
+            lib().orc_cpu_destroy(self.c)
+            self.c = None
+
+    def grid(self):
+        lib().orc_cpu_grid(self.c)
+
+    def search(self):
+        lib().orc_cpu_search(self.c)
+
+    def sizes(self):
+        s = np.zeros(4, np.int32)
+        lib().orc_cpu_sizes(self.c, s.ctypes.data_as(C.POINTER(C.c_int)))
+        return {"clusters": int(s[0]), "entries": int(s[1]), "j_entries": int(s[2]), "geometric": bool(s[3])}
+
+    def force(self, energy=True, threads=1, e0=0, e1=None):
+        n = self.sizes()["entries"] if e1 is None else e1
+        if lib().orc_cpu_force(self.c, int(e0), int(n), int(energy), int(threads)) != 0:
+            raise RuntimeError("CPU kernel failed")
+
+    def forces(self):
+        f = np.empty((self.system.n, 3), np.float32)
+        lib().orc_cpu_forces(self.c, f.ctypes.data_as(C.POINTER(C.c_float)))
+        return f
+
+    def energies(self):
+        e = np.zeros(2, np.float64)
+        lib().orc_cpu_energies(self.c, e.ctypes.data_as(C.POINTER(C.c_double)))
+        return e
+
+    def pairlist(self):
+        sz = self.sizes()
+        ci = np.zeros(max(1, sz["entries"]) * 4, np.int32)
+        cj = np.zeros(max(1, sz["j_entries"]) * 2, np.int32)
+        lib().orc_cpu_list(self.c, ci.ctypes.data_as(C.POINTER(C.c_int)), cj.ctypes.data_as(C.POINTER(C.c_int)))
+        ai = np.zeros(sz["clusters"] * 4, np.int32)
+        xs = np.zeros(sz["clusters"] * 16, np.float32)
+        lib().orc_cpu_grid_arrays(self.c, ai.ctypes.data_as(C.POINTER(C.c_int)),
+                                  xs.ctypes.data_as(C.POINTER(C.c_float)))
+        return {"ci": ci[: 4 * sz["entries"]].reshape(-1, 4), "cj": cj[: 2 * sz["j_entries"]].reshape(-1, 2),
+                "atom_indices": ai, "xs": xs.reshape(-1, 4, 4)}

@@ -24,7 +24,8 @@ def _opts(prune=0, rlist_inner=None):
 
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
-def test_batch_matches_single_systems(graph, variant):
+@pytest.mark.parametrize("tile,depth", [(0, 2), (1, 2), (1, 3)])
+def test_batch_matches_single_systems(graph, variant, tile, depth):
     torch = pytest.importorskip("torch")
     ens = _ensemble()
     b = BatchForceCalculator(ens, _opts())
@@ -32,6 +33,7 @@ def test_batch_matches_single_systems(graph, variant):
         b.set_stream(0)  # the legacy default stream (graphs are captured on a private stream)
     b.set_graph(graph)
     b.set_kernel_variant(variant)
+    b.set_force_kernel(tile, depth)
     dev = torch.device("cuda:0")
     x = torch.from_numpy(np.concatenate([s.x.reshape(-1) for s in ens])).to(dev)
     f = torch.empty_like(x)
@@ -85,6 +87,7 @@ def test_autotune_picks_a_setting():
     dev = torch.device("cuda:0")
     x0 = torch.from_numpy(np.concatenate([s.x.reshape(-1) for s in ens])).to(dev)
     frames = x0[None, :] + 0.002 * torch.randn((12, x0.numel()), device=dev).cumsum(0)
-    best, timings = b.autotune(frames, variants=(0, 1), prune_intervals=(4, 10))
+    best, timings = b.autotune(frames, variants=(0, 1), prune_intervals=(4, 10), tiles=((0, 2), (1, 2), (1, 3)))
     assert best["kernel_variant"] in (0, 1) and best["nstlist_prune"] in (4, 10)
-    assert len(timings) == 4 and all(t > 0 for t in timings.values())
+    assert (best["tile"], best["stage_depth"]) in ((0, 2), (1, 2), (1, 3))
+    assert len(timings) == 12 and all(t > 0 for t in timings.values())
