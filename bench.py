@@ -378,6 +378,29 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
                     "forward + loss + backward; inputs fit in L2"}
 
 
+def min_pair_distances(ens) -> dict:
+    """The closest pair of each liquid of the ensemble (periodic), over all systems: the smallest
+    distance in nm and the smallest distance in units of the pair's sigma_ij (Lorentz-Berthelot)."""
+    from scipy.spatial import cKDTree
+
+    best_r, best_ratio = np.inf, np.inf
+    for s in ens:
+        box = float(s.box[0])
+        x = np.mod(np.asarray(s.x, np.float64), box)
+        pairs = cKDTree(x, boxsize=box).query_pairs(0.5 * float(np.max(s.sigma)), output_type="ndarray")
+        if len(pairs) == 0:
+            continue
+        d = x[pairs[:, 0]] - x[pairs[:, 1]]
+        d -= box * np.round(d / box)
+        r = np.sqrt((d ** 2).sum(1))
+        sij = 0.5 * (s.sigma[s.type[pairs[:, 0]]] + s.sigma[s.type[pairs[:, 1]]])
+        best_r = min(best_r, float(r.min()))
+        best_ratio = min(best_ratio, float((r / sij).min()))
+    return {"min_nm": best_r, "min_over_sigma_ij": best_ratio,
+            "construction": "pairs closer than 0.5 sigma_ij rejected and redrawn (0.8 sigma_ij at 100 atoms/nm^3 "
+                            "packs beyond random close packing)"}
+
+
 def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
     """Batched differentiable force matching: 64 random LJ + Coulomb liquids (8 types,
     2,000-50,000 atoms log-uniform, shared sigma / epsilon / per-type charge scales).
@@ -496,7 +519,12 @@ def measure_force_matching(dev: int, iters: int = 50, warmup: int = 3) -> dict:
             "loss_first": float(losses[0].detach()), "loss_last": float(losses[-1].detach()),
             "fd_gradient_step_ms": fd_ms, "fd_force_evals_per_s": 64 * 48 * 1e3 / fd_ms,
             "speedup_vs_fd": fd_ms / step_ms, "fd_vs_adjoint_rel_diff": fd_vs_adj,
-            "gradient_rel_err_vs_fp64": "<= 1e-4 (tests/test_gpu_batch_adjoint.py, 2-system instance)",
+            "gradient_vs_fp64": "the two smallest systems of this batch (2,007 + 2,095 atoms, same targets): "
+                                "loss and sigma / epsilon / charge-scale gradients within 2e-5 relative of FP64 "
+                                "autograd over all pairs (tests/test_gpu_batch_adjoint.py::"
+                                "test_benchmarked_force_matching_batch_subset_vs_fp64); the whole batch against "
+                                "central differences: fd_vs_adjoint_rel_diff",
+            "min_pair_distance": min_pair_distances(ens),
             "build_s": t_build,
             "note": "adjoint step = one graph launch (set parameters, forces+energies+virials, loss, adjoint) "
                     "+ Adam on 24 shared parameters; FD = 48 evaluations x 64 sequential per-system "

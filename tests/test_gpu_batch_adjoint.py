@@ -147,3 +147,47 @@ def test_force_matching_step_matches_fp64_autograd():
     assert rel_rms(e_p.grad.cpu(), ge) < 2e-5
     assert rel_rms(k_p.grad.cpu(), gk) < 2e-5
     m.close()
+
+
+def test_benchmarked_force_matching_batch_subset_vs_fp64():
+    """The force-matching benchmark's own batch (64 liquids, 2,000-50,000 atoms, seed 5), on the
+    subset its FP64 all-pairs reference can afford: the two smallest systems (2,007 and 2,095 atoms)
+    with the benchmark's target construction (forces at parameters perturbed by up to 5 %, seed 21)
+    and its list (static, at rc).  Loss and gradients against FP64 autograd."""
+    from gmxapi_gb300.adjoint import static_list_options
+
+    specs = sorted(systems.force_matching_specs(64), key=lambda k: k["n"])[:2]
+    ens = [systems.lj_liquid(**kw) for kw in specs]
+    assert [s.n for s in ens] == [2007, 2095]
+    sig, eps = ens[0].sigma, ens[0].epsilon
+    q0 = np.concatenate([s.q for s in ens]).astype(np.float64)
+    types = np.concatenate([s.type for s in ens]).astype(np.int64)
+    rng = np.random.default_rng(21)
+    pert = [rng.uniform(0.95, 1.05, 8) for _ in range(3)]
+    opts = static_list_options(0.9)
+    opts.compute_virial_and_energy = True
+    b = BatchForceCalculator(ens, opts)
+    b.set_stream(torch.cuda.current_stream().cuda_stream)
+    x = torch.cat([torch.tensor(s.x).reshape(-1) for s in ens]).to(DEV)
+    b.search_device(x.data_ptr())
+    q_t = torch.tensor(q0 * pert[2][types], dtype=torch.float32, device=DEV)
+    nb_t = lorentz_berthelot_nbfp(torch.tensor(sig * pert[0]), torch.tensor(eps * pert[1])).float().contiguous().to(DEV)
+    b.set_parameters_device(q_t.data_ptr(), nb_t.data_ptr())
+    f_target = torch.empty_like(x)
+    b.compute_device(x.data_ptr(), f_target.data_ptr())
+    torch.cuda.synchronize()
+    b.close()
+    m = BatchForceMatcher(ens, f_target, opts)
+    s_p = torch.tensor(sig, dtype=torch.float64, device=DEV, requires_grad=True)
+    e_p = torch.tensor(eps, dtype=torch.float64, device=DEV, requires_grad=True)
+    k_p = torch.ones(8, dtype=torch.float64, device=DEV, requires_grad=True)
+    charges = TypeScaledCharges(torch.tensor(q0, device=DEV), torch.tensor(types, device=DEV), 8)
+    loss = m(charges(k_p), lorentz_berthelot_nbfp(s_p, e_p))
+    loss.backward()
+    l64, gs, ge, gk = _fp64_loss_grads(ens, sig, eps, np.ones(8), q0, f_target.cpu().numpy())
+    errs = (abs(float(loss) - l64) / l64, rel_rms(s_p.grad.cpu(), gs), rel_rms(e_p.grad.cpu(), ge),
+            rel_rms(k_p.grad.cpu(), gk))
+    print("benchmarked batch, 2 smallest systems: loss rel err %.2e, grad rel RMS sigma %.2e epsilon %.2e "
+          "charge scale %.2e" % errs)
+    assert errs[0] <= 2e-5 and max(errs[1:]) < 2e-5
+    m.close()
