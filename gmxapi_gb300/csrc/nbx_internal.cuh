@@ -236,10 +236,15 @@ __device__ __forceinline__ int find_system(const int* prefix, int nsys, int e)
     return lo;
 }
 
+// Cluster-packed record of 8 atoms (kPackWords 32-bit words, 160 B): x[8], y[8], z[8], q[8],
+// type[8], atom a at position 2 (a & 3) + (a >> 2) of each, so that atoms a and a + 4 (the two
+// warp halves' j-atoms of one lane) are adjacent.
+constexpr int kPackWords = 40;
+
 // Writes slot k's coordinates, charge and type into the cluster-packed records (DeviceView::xqp).
 __device__ __forceinline__ void write_packed_slot(float* xqp, int k, float x, float y, float z, float q, int type)
 {
-    float* pc = xqp + (size_t)(k >> 3) * 40 + 2 * (k & 3) + ((k >> 2) & 1);
+    float* pc = xqp + (size_t)(k >> 3) * kPackWords + 2 * (k & 3) + ((k >> 2) & 1);
     pc[0]     = x;
     pc[8]     = y;
     pc[16]    = z;

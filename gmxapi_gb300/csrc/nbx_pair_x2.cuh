@@ -70,10 +70,6 @@ __host__ __device__ __forceinline__ int pack_pos(int a)
     return 2 * (a & 3) + (a >> 2);
 }
 
-// Cluster-packed record of 8 atoms (kPackWords 32-bit words, 160 B): x[8], y[8], z[8], q[8],
-// type[8], atom a at position pack_pos(a) of each.
-constexpr int kPackWords = 40;
-
 // A warp's j stage with kDepth buffers: each holds one cj4 group's four packed j-cluster records
 // (4 x 40 words).  uses counts the groups staged so far (buffer uses % kDepth, barrier parity
 // (uses / kDepth) & 1).

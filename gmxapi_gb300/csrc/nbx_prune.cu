@@ -16,6 +16,8 @@
 // restatement.
 #include "nbx_internal.cuh"
 
+#include <algorithm>
+
 namespace nbx
 {
 namespace
@@ -37,14 +39,122 @@ __device__ __forceinline__ float2 p_sub(float2 a, float2 b)
     return *reinterpret_cast<float2*>(&rd);
 }
 
-// Prunes one list entry (block-cooperative): the shifted i-atoms go to shared memory as duplicated
-// pairs {x, x, y, y}, {z, z, -, -}; each warp takes cj4 groups of the entry.  Lane (ii, jj) tests,
-// for every i-cluster with a bit to test in either half, the pairs (ii, jj) of half 0 and
-// (ii, jj + 4) of half 1 with packed arithmetic, collects the in-range results of all i-clusters of
-// a j-cluster as per-lane bit masks and ORs them over the warp with one reduction per mask.
+// Fresh prune of one list entry: each warp of the block takes cj4 groups warp, warp + W, ... on its
+// own (no block barrier).  Lane (ii, jj) holds the shifted i-atom ii of the entry's 8 i-clusters in
+// registers as duplicated pairs {x, x}, ...; for every i-cluster with a bit in either half it tests
+// the pairs (ii, jj) of half 0 and (ii, jj + 4) of half 1 in one packed operation against the
+// j-cluster's {x_jj, x_jj+4} pair read from the cluster-packed coordinate records, collects the
+// in-range results of all i-clusters of a j-cluster as per-lane bit masks and ORs them over the
+// warp with one reduction per mask.
 template<int kPruneWarps>
-__device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
-                            const float* shiftvec, float outer2, float inner2, int fresh, float4* xib)
+__device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
+                                  const float* xqp, const float* shiftvec, float outer2, float inner2)
+{
+    const int      lane = threadIdx.x & 31;
+    const int      warp = threadIdx.x >> 5;
+    const int      ii   = lane & 7;
+    const int      jj   = lane >> 3;
+    const unsigned full = 0xffffffffu;
+    if (s.cj4_start + warp >= s.cj4_end)
+    {
+        return;
+    }
+    // the next group's record is loaded while the current one is tested
+    Cj4 c4n = cj4[s.cj4_start + warp];
+    const float sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
+    float2 xi[kNcl], yi[kNcl], zi[kNcl];
+#pragma unroll
+    for (int c = 0; c < kNcl; c++)
+    {
+        const float4 x  = xq[s.sci * kSc + c * kCl + ii];
+        const float  xs = x.x + sx, ys = x.y + sy, zs = x.z + sz;
+        xi[c]           = make_float2(xs, xs);
+        yi[c]           = make_float2(ys, ys);
+        zi[c]           = make_float2(zs, zs);
+    }
+    for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
+    {
+        const Cj4 c4 = c4n;
+        if (j4 + kPruneWarps < s.cj4_end)
+        {
+            c4n = cj4[j4 + kPruneWarps];
+        }
+        // per half: the bits to test (all set bits), the outer mask kept so far, the inner mask
+        const unsigned check[kSplit]  = { c4.imei[0].imask, c4.imei[1].imask };
+        unsigned       full_m[kSplit] = { check[0], check[1] };
+        unsigned       nw[kSplit]     = { 0u, 0u };
+        const unsigned either         = check[0] | check[1];
+        if (!either)
+        {
+            continue;
+        }
+        // the {half 0, half 1} coordinate pairs of the group's j-clusters with bits to test, all
+        // loaded before any is tested (one memory latency per group instead of one per j-cluster)
+        float2 xj[kJg], yj[kJg], zj[kJg];
+#pragma unroll
+        for (int jm = 0; jm < kJg; jm++)
+        {
+            if ((either >> (jm * kNcl)) & 0xffu)
+            {
+                const float2* pj = reinterpret_cast<const float2*>(xqp + (size_t)c4.cj[jm] * kPackWords);
+                xj[jm]           = pj[jj];
+                yj[jm]           = pj[4 + jj];
+                zj[jm]           = pj[8 + jj];
+            }
+        }
+#pragma unroll
+        for (int jm = 0; jm < kJg; jm++)
+        {
+            const unsigned cu = (either >> (jm * kNcl)) & 0xffu;
+            if (!cu)
+            {
+                continue;
+            }
+            // per lane: bit c set when this lane's pair of half 0 / half 1 is in range
+            unsigned in0 = 0u, in1 = 0u, out0 = 0u, out1 = 0u;
+#pragma unroll
+            for (int i = 0; i < kNcl; i++)
+            {
+                if (!(cu & (1u << i)))
+                {
+                    continue;
+                }
+                const float2 dx = p_sub(xi[i], xj[jm]);
+                const float2 dy = p_sub(yi[i], yj[jm]);
+                const float2 dz = p_sub(zi[i], zj[jm]);
+                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+                in0 |= (r2.x < inner2) ? (1u << i) : 0u;
+                in1 |= (r2.y < inner2) ? (1u << i) : 0u;
+                out0 |= (r2.x < outer2) ? (1u << i) : 0u;
+                out1 |= (r2.y < outer2) ? (1u << i) : 0u;
+            }
+            // any pair of the (i-cluster, half) within range: OR over the lanes
+            const unsigned sh = jm * kNcl;
+            in0               = __reduce_or_sync(full, in0) << sh;
+            in1               = __reduce_or_sync(full, in1) << sh;
+            out0              = __reduce_or_sync(full, out0) << sh;
+            out1              = __reduce_or_sync(full, out1) << sh;
+            const unsigned t0 = check[0] & (0xffu << sh), t1 = check[1] & (0xffu << sh);
+            nw[0] |= in0 & t0;
+            nw[1] |= in1 & t1;
+            full_m[0] &= ~(t0 & ~out0);
+            full_m[1] &= ~(t1 & ~out1);
+        }
+        if (lane < kSplit)
+        {
+            imask_outer[2 * j4 + lane]                 = lane == 0 ? full_m[0] : full_m[1];
+            const_cast<Cj4*>(cj4)[j4].imei[lane].imask = lane == 0 ? nw[0] : nw[1];
+        }
+    }
+}
+
+// The rolling prune of one list entry (block-cooperative): only bits in (outer XOR inner) are
+// tested (few per group), per bit with warp votes.  The 64 shifted i-atoms are staged in shared
+// memory once per entry; the j-atoms of the bits' halves and j-clusters are loaded up front per
+// group.
+template<int kPruneWarps>
+__device__ void prune_entry_rolling(const Sci& s, const Cj4* cj4, const unsigned* imask_outer, const float4* xq,
+                                    const float* shiftvec, float inner2, float4* xib)
 {
     const int      lane = threadIdx.x & 31;
     const int      warp = threadIdx.x >> 5;
@@ -56,18 +166,15 @@ __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer,
     for (int k = threadIdx.x; k < kSc; k += blockDim.x)
     {
         const float4 x = xq[s.sci * kSc + k];
-        const float  xs = x.x + sx, ys = x.y + sy, zs = x.z + sz;
-        xib[2 * k]     = make_float4(xs, xs, ys, ys);
-        xib[2 * k + 1] = make_float4(zs, zs, 0.0f, 0.0f);
+        xib[k]         = make_float4(x.x + sx, x.y + sy, x.z + sz, 0.0f);
     }
     __syncthreads();
-    // the next group's record and outer masks are loaded while the current one is tested
     Cj4   c4n{};
     uint2 outn{};
     if (s.cj4_start + warp < s.cj4_end)
     {
         c4n  = cj4[s.cj4_start + warp];
-        outn = fresh ? uint2{} : reinterpret_cast<const uint2*>(imask_outer)[s.cj4_start + warp];
+        outn = reinterpret_cast<const uint2*>(imask_outer)[s.cj4_start + warp];
     }
     for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
     {
@@ -76,96 +183,84 @@ __device__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer,
         if (j4 + kPruneWarps < s.cj4_end)
         {
             c4n  = cj4[j4 + kPruneWarps];
-            outn = fresh ? uint2{} : reinterpret_cast<const uint2*>(imask_outer)[j4 + kPruneWarps];
+            outn = reinterpret_cast<const uint2*>(imask_outer)[j4 + kPruneWarps];
         }
-        // per half: the bits to test, the outer mask kept so far, the inner mask so far
-        unsigned full_m[kSplit], check[kSplit], nw[kSplit];
-#pragma unroll
-        for (int w = 0; w < kSplit; w++)
-        {
-            if (fresh)
-            {
-                full_m[w] = c4.imei[w].imask;
-                check[w]  = full_m[w];
-                nw[w]     = 0u;
-            }
-            else
-            {
-                full_m[w] = w == 0 ? out.x : out.y;
-                nw[w]     = c4.imei[w].imask;
-                check[w]  = nw[w] ^ full_m[w];
-            }
-        }
-        const unsigned either = check[0] | check[1];
-        if (!either)
+        unsigned nw[kSplit], check[kSplit];
+        nw[0]    = c4.imei[0].imask;
+        nw[1]    = c4.imei[1].imask;
+        check[0] = nw[0] ^ out.x;
+        check[1] = nw[1] ^ out.y;
+        if (!(check[0] | check[1]))
         {
             continue;
         }
-#pragma unroll 1
-        for (int jm = 0; jm < kJg; jm++)
-        {
-            const unsigned cu = (either >> (jm * kNcl)) & 0xffu;
-            if (!cu)
-            {
-                continue;
-            }
-            const float4 xa = xq[c4.cj[jm] * kCl + jj];
-            const float4 xb = xq[c4.cj[jm] * kCl + jj + 4];
-            const float2 xj = make_float2(xa.x, xb.x), yj = make_float2(xa.y, xb.y), zj = make_float2(xa.z, xb.z);
-            // per lane: bit c set when this lane's pair of half 0 / half 1 is in range
-            unsigned in0 = 0u, in1 = 0u, out0 = 0u, out1 = 0u;
+        float4 xj[kSplit][kJg];
 #pragma unroll
-            for (int i = 0; i < kNcl; i++)
+        for (int w = 0; w < kSplit; w++)
+        {
+#pragma unroll
+            for (int jm = 0; jm < kJg; jm++)
             {
-                if (!(cu & (1u << i)))
+                if ((check[w] >> (jm * kNcl)) & 0xffu)
+                {
+                    xj[w][jm] = xq[c4.cj[jm] * kCl + w * (kCl / kSplit) + jj];
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < kSplit; w++)
+        {
+#pragma unroll
+            for (int jm = 0; jm < kJg; jm++)
+            {
+                if (!((check[w] >> (jm * kNcl)) & 0xffu))
                 {
                     continue;
                 }
-                const float4 p0 = xib[2 * (i * kCl + ii)];
-                const float4 p1 = xib[2 * (i * kCl + ii) + 1];
-                const float2 dx = p_sub(make_float2(p0.x, p0.y), xj);
-                const float2 dy = p_sub(make_float2(p0.z, p0.w), yj);
-                const float2 dz = p_sub(make_float2(p1.x, p1.y), zj);
-                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                in0 |= (r2.x < inner2) ? (1u << i) : 0u;
-                in1 |= (r2.y < inner2) ? (1u << i) : 0u;
-                if (fresh)
+#pragma unroll
+                for (int i = 0; i < kNcl; i++)
                 {
-                    out0 |= (r2.x < outer2) ? (1u << i) : 0u;
-                    out1 |= (r2.y < outer2) ? (1u << i) : 0u;
+                    const unsigned bit = 1u << (jm * kNcl + i);
+                    if (check[w] & bit)
+                    {
+                        const float4 xi = xib[i * kCl + ii];
+                        const float  dx = xi.x - xj[w][jm].x, dy = xi.y - xj[w][jm].y, dz = xi.z - xj[w][jm].z;
+                        const float  r2 = dx * dx + dy * dy + dz * dz;
+                        if (__any_sync(full, r2 < inner2))
+                        {
+                            nw[w] |= bit;
+                        }
+                    }
                 }
-            }
-            // any pair of the (i-cluster, half) within range: OR over the lanes
-            const unsigned sh = jm * kNcl;
-            in0               = __reduce_or_sync(full, in0) << sh;
-            in1               = __reduce_or_sync(full, in1) << sh;
-            const unsigned t0 = check[0] & (0xffu << sh), t1 = check[1] & (0xffu << sh);
-            nw[0] |= in0 & t0;
-            nw[1] |= in1 & t1;
-            if (fresh)
-            {
-                out0 = __reduce_or_sync(full, out0) << sh;
-                out1 = __reduce_or_sync(full, out1) << sh;
-                full_m[0] &= ~(t0 & ~out0);
-                full_m[1] &= ~(t1 & ~out1);
             }
         }
         if (lane < kSplit)
         {
-            const int w = lane;
-            if (fresh)
-            {
-                imask_outer[2 * j4 + w] = full_m[w];
-            }
-            const_cast<Cj4*>(cj4)[j4].imei[w].imask = nw[w];
+            const_cast<Cj4*>(cj4)[j4].imei[lane].imask = lane == 0 ? nw[0] : nw[1];
         }
     }
 }
 
-template<int kPruneWarps>
-__global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fresh, int part, int nparts)
+// Fresh or rolling prune of one list entry (each kernel instantiates one of the two).
+template<int kPruneWarps, bool kFresh>
+__device__ __forceinline__ void prune_entry(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
+                                            const float* xqp, const float* shiftvec, float outer2, float inner2,
+                                            float4* xib)
 {
-    __shared__ float4 xib[2 * kSc];
+    if constexpr (kFresh)
+    {
+        prune_entry_fresh<kPruneWarps>(s, cj4, imask_outer, xq, xqp, shiftvec, outer2, inner2);
+    }
+    else
+    {
+        prune_entry_rolling<kPruneWarps>(s, cj4, imask_outer, xq, shiftvec, inner2, xib);
+    }
+}
+
+template<int kPruneWarps, bool kFresh>
+__global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int part, int nparts)
+{
+    __shared__ float4 xib[kFresh ? 1 : kSc];  // the rolling pass's shifted i-atoms
     const int         numSci = v.hdr->num_sci;
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow))
     {
@@ -174,20 +269,20 @@ __global__ void __launch_bounds__(32 * kPruneWarps) k_prune(DeviceView v, int fr
     // entries part, part + nparts, ... (all entries for a fresh list)
     for (int e = part + blockIdx.x * nparts; e < numSci; e += gridDim.x * nparts)
     {
-        prune_entry<kPruneWarps>(v.sci[e], v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2, v.rlist_inner2, fresh,
-                                 xib);
+        prune_entry<kPruneWarps, kFresh>(v.sci[e], v.cj4, v.imask_outer, v.xq, v.xqp, v.shiftvec, v.rlist2,
+                                         v.rlist_inner2, xib);
     }
 }
 
 // The same prune over a batch of systems: global entry index -> system by a
 // search of the entry prefix sums; entries whose index within their system is
 // part (mod nparts) are pruned.
-template<int kPruneWarps>
+template<int kPruneWarps, bool kFresh>
 __global__ void __launch_bounds__(32 * kPruneWarps)
-        k_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2, int fresh,
-                      int part, int nparts)
+        k_batch_prune(const BatchSys* sys, const int* entry_prefix, int nsys, float outer2, float inner2, int part,
+                      int nparts)
 {
-    __shared__ float4 xib[2 * kSc];
+    __shared__ float4 xib[kFresh ? 1 : kSc];  // the rolling pass's shifted i-atoms
     const int         total = entry_prefix[nsys];
     for (int e = blockIdx.x; e < total; e += gridDim.x)
     {
@@ -205,13 +300,32 @@ __global__ void __launch_bounds__(32 * kPruneWarps)
             }
         }
         const int local = e - entry_prefix[lo];
-        if (!fresh && (local % nparts) != part)
+        if (!kFresh && (local % nparts) != part)
         {
             continue;
         }
         const BatchSys& b = sys[lo];
-        prune_entry<kPruneWarps>(b.sci[local], b.cj4, b.imask_outer, b.xq, b.shiftvec, outer2, inner2, fresh, xib);
+        prune_entry<kPruneWarps, kFresh>(b.sci[local], b.cj4, b.imask_outer, b.xq, b.xqp, b.shiftvec, outer2,
+                                         inner2, xib);
     }
+}
+
+// One wave of resident blocks of a prune kernel (SM count x blocks per SM at its register and
+// shared-memory use), computed once: entries are spread over the blocks by the grid-stride loops,
+// so a second partial wave would only add a tail.
+template<auto kKernel, int kThreads>
+int resident_grid()
+{
+    static int blocks = 0;
+    if (blocks == 0)
+    {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kKernel, kThreads, 0);
+        blocks = std::max(sms, 1) * std::max(per_sm, 1);
+    }
+    return blocks;
 }
 
 } // namespace
@@ -221,13 +335,15 @@ cudaError_t launch_batch_prune(const BatchSys* sys, const int* entry_prefix, int
 {
     if (fresh)
     {
-        k_batch_prune<kPruneWarpsFresh><<<152 * 8, 32 * kPruneWarpsFresh, 0, s>>>(sys, entry_prefix, nsys, outer2,
-                                                                                 inner2, fresh, part, 1);
+        constexpr auto kKernel = k_batch_prune<kPruneWarpsFresh, true>;
+        kKernel<<<resident_grid<kKernel, 32 * kPruneWarpsFresh>(), 32 * kPruneWarpsFresh, 0, s>>>(
+                sys, entry_prefix, nsys, outer2, inner2, part, 1);
     }
     else
     {
-        k_batch_prune<kPruneWarpsRolling><<<152 * 8, 32 * kPruneWarpsRolling, 0, s>>>(sys, entry_prefix, nsys, outer2,
-                                                                                     inner2, fresh, part, nparts);
+        constexpr auto kKernel = k_batch_prune<kPruneWarpsRolling, false>;
+        kKernel<<<resident_grid<kKernel, 32 * kPruneWarpsRolling>(), 32 * kPruneWarpsRolling, 0, s>>>(
+                sys, entry_prefix, nsys, outer2, inner2, part, nparts);
     }
     return cudaGetLastError();
 }
@@ -236,17 +352,14 @@ cudaError_t launch_prune(const DeviceView& v, int fresh, int part, int nparts, c
 {
     if (fresh)
     {
-        part   = 0;
-        nparts = 1;
-    }
-    // enough blocks for ~8 per SM; entries beyond are picked up by the grid-stride loop
-    if (fresh)
-    {
-        k_prune<kPruneWarpsFresh><<<152 * 8, 32 * kPruneWarpsFresh, 0, s>>>(v, fresh, part, nparts);
+        constexpr auto kKernel = k_prune<kPruneWarpsFresh, true>;
+        kKernel<<<resident_grid<kKernel, 32 * kPruneWarpsFresh>(), 32 * kPruneWarpsFresh, 0, s>>>(v, 0, 1);
     }
     else
     {
-        k_prune<kPruneWarpsRolling><<<152 * 8, 32 * kPruneWarpsRolling, 0, s>>>(v, fresh, part, nparts);
+        constexpr auto kKernel = k_prune<kPruneWarpsRolling, false>;
+        kKernel<<<resident_grid<kKernel, 32 * kPruneWarpsRolling>(), 32 * kPruneWarpsRolling, 0, s>>>(v, part,
+                                                                                                      nparts);
     }
     return cudaGetLastError();
 }

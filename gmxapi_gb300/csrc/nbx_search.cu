@@ -225,25 +225,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                 }
                 __syncwarp();
                 int nj = 0;  // j-clusters in this entry
-                for (int cx = cxf; cx <= cxl; cx++)
+                // The candidate j-columns (cx major, cy minor, the reference's visiting order), 32
+                // at a time: each lane finds the z-range of cells of one column, a warp scan turns
+                // the cell counts into offsets of one flat, increasing sequence of j-cells.
+                const int ny   = cyl - cyf + 1;
+                const int ncol = (cxl - cxf + 1) * ny;
+                for (int c0 = 0; c0 < ncol; c0 += 32)
                 {
-                    const float cx_real = (float)cx;
-                    float       d2zx    = d2z;
-                    if (0.0f + cx_real * v.g.cs[0] > bx1)
+                    int       first = 0, count = 0;
+                    const int c     = c0 + lane;
+                    if (c < ncol)
                     {
-                        d2zx = d2zx + sq(0.0f + cx_real * v.g.cs[0] - bx1);
-                    }
-                    else if (0.0f + (cx_real + 1.0f) * v.g.cs[0] < bx0)
-                    {
-                        d2zx = d2zx + sq(0.0f + (cx_real + 1.0f) * v.g.cs[0] - bx0);
-                    }
-                    const int cyf_x = (cx == 0 && shift == kCentral && cyf < ci_y) ? ci_y : cyf;
-                    for (int cy = cyf_x; cy <= cyl; cy++)
-                    {
-                        const int   columnStart = v.cxy_ind[cx * v.g.ncy + cy];
-                        const int   columnEnd   = v.cxy_ind[cx * v.g.ncy + cy + 1];
-                        const float cy_real     = (float)cy;
-                        float       d2zxy       = d2zx;
+                        const int   cx      = cxf + c / ny;
+                        const int   cy      = cyf + c % ny;
+                        const float cx_real = (float)cx;
+                        float       d2zx    = d2z;
+                        if (0.0f + cx_real * v.g.cs[0] > bx1)
+                        {
+                            d2zx = d2zx + sq(0.0f + cx_real * v.g.cs[0] - bx1);
+                        }
+                        else if (0.0f + (cx_real + 1.0f) * v.g.cs[0] < bx0)
+                        {
+                            d2zx = d2zx + sq(0.0f + (cx_real + 1.0f) * v.g.cs[0] - bx0);
+                        }
+                        const int cyf_x = (cx == 0 && shift == kCentral && cyf < ci_y) ? ci_y : cyf;
+                        const int columnStart = v.cxy_ind[cx * v.g.ncy + cy];
+                        const int columnEnd   = v.cxy_ind[cx * v.g.ncy + cy + 1];
+                        const float cy_real   = (float)cy;
+                        float       d2zxy     = d2zx;
                         if (0.0f + cy_real * v.g.cs[1] > by1)
                         {
                             d2zxy = d2zxy + sq(0.0f + cy_real * v.g.cs[1] - by1);
@@ -252,128 +261,145 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                         {
                             d2zxy = d2zxy + sq(0.0f + (cy_real + 1.0f) * v.g.cs[1] - by0);
                         }
-                        if (!(columnStart < columnEnd && d2zxy < listRangeBBToJCell2))
+                        if (cy >= cyf_x && columnStart < columnEnd && d2zxy < listRangeBBToJCell2)
                         {
-                            continue;
-                        }
-                        int midCell = columnStart + (int)(bz1_frac * (float)(columnEnd - columnStart));
-                        if (midCell >= columnEnd)
-                        {
-                            midCell = columnEnd - 1;
-                        }
-                        const float d2xy = d2zxy - d2z;
-                        int         down = midCell;
-                        while (down >= columnStart)
-                        {
-                            const float u = v.bbcz[down].y;
-                            if (!(u >= bz0 || d2xy + sq(u - bz0) < rlist2))
+                            int midCell = columnStart + (int)(bz1_frac * (float)(columnEnd - columnStart));
+                            if (midCell >= columnEnd)
                             {
-                                break;
+                                midCell = columnEnd - 1;
                             }
-                            down--;
-                        }
-                        int firstCell = down + 1;
-                        int up        = midCell + 1;
-                        while (up < columnEnd)
-                        {
-                            const float l = v.bbcz[up].x;
-                            if (!(l <= bz1 || d2xy + sq(l - bz1) < rlist2))
+                            const float d2xy = d2zxy - d2z;
+                            int         down = midCell;
+                            while (down >= columnStart)
                             {
-                                break;
+                                const float u = v.bbcz[down].y;
+                                if (!(u >= bz0 || d2xy + sq(u - bz0) < rlist2))
+                                {
+                                    break;
+                                }
+                                down--;
                             }
-                            up++;
-                        }
-                        const int lastCell = up - 1;
-                        if (shift == kCentral && firstCell < ci)
-                        {
-                            firstCell = ci;
-                        }
-                        for (int scj = firstCell; scj <= lastCell; scj++)
-                        {
-                            // make_cluster_list_supersub for (ci, scj): lane = i-half*32? no:
-                            // lane l handles j-cluster jc = l & 7 against i-clusters l>>3 and (l>>3)+4
-                            const int  ncl_j = v.nclusters[scj];
-                            const int  jc    = lane & 7;
-                            const int  ia    = lane >> 3;
-                            const int  ib    = ia + 4;
-                            const bool diag  = excludeSubDiagonal && (scj == ci);
-                            const int  ci1   = diag ? jc + 1 : ncl_i;
-                            const bool va    = (jc < ncl_j) && (ia < ci1);
-                            const bool vb    = (jc < ncl_j) && (ib < ci1);
-                            float      d2a = 0.0f, d2b = 0.0f;
-                            if (jc < ncl_j)
+                            int firstCell = down + 1;
+                            int up        = midCell + 1;
+                            while (up < columnEnd)
                             {
-                                const float4 jlo = v.bb[2 * (scj * kNcl + jc)];
-                                const float4 jhi = v.bb[2 * (scj * kNcl + jc) + 1];
-                                d2a = bb_dist2(sm.bbi_lo[ia], sm.bbi_hi[ia], jlo, jhi);
-                                d2b = bb_dist2(sm.bbi_lo[ib], sm.bbi_hi[ib], jlo, jhi);
+                                const float l = v.bbcz[up].x;
+                                if (!(l <= bz1 || d2xy + sq(l - bz1) < rlist2))
+                                {
+                                    break;
+                                }
+                                up++;
                             }
-                            const unsigned Ba = __ballot_sync(full, va && d2a < rlist2);
-                            const unsigned Bb = __ballot_sync(full, vb && d2b < rlist2);
-                            // 8-bit i-cluster mask of j-cluster jc (valid on every lane)
-                            unsigned im8 = 0;
+                            const int lastCell = up - 1;
+                            if (shift == kCentral && firstCell < ci)
+                            {
+                                firstCell = ci;
+                            }
+                            if (lastCell >= firstCell)
+                            {
+                                first = firstCell;
+                                count = lastCell - firstCell + 1;
+                            }
+                        }
+                    }
+                    int incl = count;
 #pragma unroll
-                            for (int i = 0; i < 4; i++)
-                            {
-                                im8 |= ((Ba >> (i * 8 + jc)) & 1u) << i;
-                                im8 |= ((Bb >> (i * 8 + jc)) & 1u) << (i + 4);
-                            }
-                            // a single cluster pair in range: check atom pairs (PRUNE_LIST_CPU_ONE)
-                            for (int j = 0; j < kNcl; j++)
-                            {
-                                const unsigned imj = __shfl_sync(full, im8, j);
-                                if (__popc(imj) != 1)
-                                {
-                                    continue;
-                                }
-                                const int   cl    = __ffs(imj) - 1;
-                                const int   srcl  = (cl & 3) * 8 + j;
-                                const float d2a_s = __shfl_sync(full, d2a, srcl);
-                                const float d2b_s = __shfl_sync(full, d2b, srcl);
-                                const float d2l   = (cl < 4) ? d2a_s : d2b_s;
-                                if (!(d2l >= rbb2))
-                                {
-                                    continue;
-                                }
-                                // clusterpair_in_range (pairlist.cpp:479-606): i atoms shifted
-                                const float4 xi  = v.xq[ci * kSc + cl * kCl + (lane & 7)];
-                                const float  ix  = xi.x + shx, iy = xi.y + shy, iz = xi.z + shz;
-                                const int    csj = scj * kNcl + j;
-                                bool         in  = false;
-#pragma unroll
-                                for (int h = 0; h < 2; h++)
-                                {
-                                    const float4 xj = v.xq[csj * kCl + (lane >> 3) + 4 * h];
-                                    const float  dx = ix - xj.x, dy = iy - xj.y, dz = iz - xj.z;
-                                    const float  r2 = dx * dx + dy * dy + dz * dz;
-                                    in              = in || (r2 < rlist2);
-                                }
-                                if (!__any_sync(full, in) && jc == j)
-                                {
-                                    im8 = 0u;
-                                }
-                            }
-                            const unsigned nz = __ballot_sync(full, lane < kNcl && im8 != 0u);
-                            if (kWrite && lane < kNcl && im8 != 0u)
-                            {
-                                const int pos = nj + __popc(nz & ((1u << lane) - 1u));
-                                if (pos < kMaxCj4PerEntry * kJg)
-                                {
-                                    const int j4  = cj4_out + pos / kJg;
-                                    const int off = pos % kJg;
-                                    v.cj4[j4].cj[off] = scj * kNcl + lane;
-                                    const unsigned bits = im8 << (off * kNcl);
-                                    atomicOr(&v.cj4[j4].imei[0].imask, bits);
-                                    atomicOr(&v.cj4[j4].imei[1].imask, bits);
-                                    if (diag)
-                                    {
-                                        sm.diag_pos[lane] = pos;
-                                        atomicOr(&sm.need[(2 * (pos / kJg)) / 32], 3u << ((2 * (pos / kJg)) % 32));
-                                    }
-                                }
-                            }
-                            nj += __popc(nz);
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const int t = __shfl_up_sync(full, incl, o);
+                        if (lane >= o)
+                        {
+                            incl += t;
                         }
+                    }
+                    const int total = __shfl_sync(full, incl, 31);
+                    // four j-cells per step: lane (kk, jc) tests j-cluster jc of j-cell k0 + kk
+                    // against the 8 i-clusters (make_cluster_list_supersub for (ci, scj))
+                    const int kk = lane >> 3;
+                    const int jc = lane & 7;
+                    for (int k0 = 0; k0 < total; k0 += 4)
+                    {
+                        int col = 0;
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                        {
+                            // columns that end at or before flat index k0 + q
+                            const int before = __popc(__ballot_sync(full, incl <= k0 + q));
+                            col              = (kk == q) ? before : col;
+                        }
+                        col                 = min(col, 31);
+                        const int colFirst  = __shfl_sync(full, first, col);
+                        const int colIncl   = __shfl_sync(full, incl, col);
+                        const int colCount  = __shfl_sync(full, count, col);
+                        const int k         = k0 + kk;
+                        const int scj       = colFirst + (k - (colIncl - colCount));
+                        const bool has_cell = k < total;
+                        const int  ncl_j    = has_cell ? v.nclusters[scj] : 0;
+                        const bool diag     = has_cell && excludeSubDiagonal && (scj == ci);
+                        const int  ci1      = diag ? jc + 1 : ncl_i;
+                        unsigned   im8      = 0u;
+                        float      d2one    = 0.0f;
+                        if (jc < ncl_j)
+                        {
+                            const float4 jlo = v.bb[2 * (scj * kNcl + jc)];
+                            const float4 jhi = v.bb[2 * (scj * kNcl + jc) + 1];
+#pragma unroll
+                            for (int i = 0; i < kNcl; i++)
+                            {
+                                const float d2 = bb_dist2(sm.bbi_lo[i], sm.bbi_hi[i], jlo, jhi);
+                                if (i < ci1 && d2 < rlist2)
+                                {
+                                    im8 |= 1u << i;
+                                    d2one = d2;
+                                }
+                            }
+                        }
+                        // a single cluster pair in range beyond the bounding-box-only distance:
+                        // check its atom pairs (PRUNE_LIST_CPU_ONE), one flagged j-cluster at a time
+                        unsigned flagged = __ballot_sync(full, __popc(im8) == 1 && d2one >= rbb2);
+                        while (flagged)
+                        {
+                            const int src = __ffs(flagged) - 1;
+                            flagged &= flagged - 1;
+                            const int    s_scj = __shfl_sync(full, scj, src);
+                            const int    s_cl  = __ffs(__shfl_sync(full, im8, src)) - 1;
+                            const float4 xi    = v.xq[ci * kSc + s_cl * kCl + (lane & 7)];
+                            const float  ix = xi.x + shx, iy = xi.y + shy, iz = xi.z + shz;
+                            const int    csj = s_scj * kNcl + (src & 7);
+                            bool         in  = false;
+#pragma unroll
+                            for (int h = 0; h < 2; h++)
+                            {
+                                const float4 xj = v.xq[csj * kCl + (lane >> 3) + 4 * h];
+                                const float  dx = ix - xj.x, dy = iy - xj.y, dz = iz - xj.z;
+                                const float  r2 = dx * dx + dy * dy + dz * dz;
+                                in              = in || (r2 < rlist2);
+                            }
+                            if (!__any_sync(full, in) && lane == src)
+                            {
+                                im8 = 0u;
+                            }
+                        }
+                        const unsigned nz = __ballot_sync(full, im8 != 0u);
+                        if (kWrite && im8 != 0u)
+                        {
+                            const int pos = nj + __popc(nz & ((1u << lane) - 1u));
+                            if (pos < kMaxCj4PerEntry * kJg)
+                            {
+                                const int j4  = cj4_out + pos / kJg;
+                                const int off = pos % kJg;
+                                v.cj4[j4].cj[off] = scj * kNcl + jc;
+                                const unsigned bits = im8 << (off * kNcl);
+                                atomicOr(&v.cj4[j4].imei[0].imask, bits);
+                                atomicOr(&v.cj4[j4].imei[1].imask, bits);
+                                if (diag)
+                                {
+                                    sm.diag_pos[jc] = pos;
+                                    atomicOr(&sm.need[(2 * (pos / kJg)) / 32], 3u << ((2 * (pos / kJg)) % 32));
+                                }
+                            }
+                        }
+                        nj += __popc(nz);
                     }
                 }
                 if (nj == 0)
