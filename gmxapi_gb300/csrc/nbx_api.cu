@@ -194,7 +194,8 @@ int status_to_error(nbx_handle* h, unsigned st)
     {
         return set_error(h, NBX_ERR_INVALID_INPUT, "a coordinate is more than 127 box lengths outside the box");
     }
-    if (st & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
+    if (st & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow | kStatusEntryOverflow
+              | kStatusRecordOverflow))
     {
         return set_error(h, NBX_ERR_LIST_OVERFLOW, "pair list or grid capacity exceeded");
     }
@@ -232,12 +233,14 @@ int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
     dfree(h, v.cj4);
     dfree(h, v.excl);
     dfree(h, v.imask_outer);
+    dfree(h, v.grp_pairs);
     v.sci = nullptr;
     v.sci_tmp = nullptr;
     v.sci_pieces = nullptr;
     v.cj4 = nullptr;
     v.excl = nullptr;
     v.imask_outer = nullptr;
+    v.grp_pairs   = nullptr;
     v.sci_cap  = need_sci;
     v.cj4_cap  = need_cj4;
     v.excl_cap = 2 * need_cj4 + 1;  // at most one mask per cj4 half
@@ -247,6 +250,7 @@ int ensure_list_capacity(nbx_handle* h, int num_sci, int num_cj4)
     if (e == cudaSuccess) e = dalloc(h, &v.cj4, v.cj4_cap);
     if (e == cudaSuccess) e = dalloc(h, &v.excl, v.excl_cap);
     if (e == cudaSuccess) e = dalloc(h, &v.imask_outer, 2 * (size_t)v.cj4_cap);
+    if (e == cudaSuccess) e = dalloc(h, &v.grp_pairs, (size_t)v.cj4_cap);
     if (e != cudaSuccess)
     {
         return cuda_check(h, e, "list allocation");
@@ -311,6 +315,26 @@ struct PhaseTimer
     ~PhaseTimer() { stop(); }
 };
 
+// Search records per cell allocated up front (a water cell at rlist 1 nm finds about 150 j-clusters);
+// a cell that finds more makes the host grow them and count again.
+constexpr int kInitialRecordsPerCell = 512;
+
+// (Re)allocates the per-cell search records (j-cluster index and i-cluster mask) for per_cell
+// records in every cell of the grid.
+cudaError_t alloc_search_records(nbx_handle* h, int per_cell)
+{
+    DeviceView& v = h->v;
+    dfree(h, v.rec_cj);
+    dfree(h, v.rec_m);
+    v.rec_cj  = nullptr;
+    v.rec_m   = nullptr;
+    v.rec_cap = per_cell;
+    const size_t n = (size_t)v.g.cells_capacity * per_cell;
+    cudaError_t  e = dalloc(h, &v.rec_cj, n);
+    if (e == cudaSuccess) e = dalloc(h, &v.rec_m, n);
+    return e;
+}
+
 // Grid + count, size the list, write, prune: the synchronous search.
 int search_sync(nbx_handle* h, float* d_x, int write_back)
 {
@@ -324,7 +348,7 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
         PhaseTimer t(h, 2);
         if (e == cudaSuccess) e = launch_search_count(v, h->stream);
     }
-    h->launches += 6;
+    h->launches += 7;  // 5 grid kernels, count, scan
     int rc = cuda_check(h, e, "grid/search count");
     if (rc != NBX_OK)
     {
@@ -334,10 +358,28 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
     {
         return rc;
     }
-    unsigned st = h->h_hdr->status & ~(unsigned)kStatusListOverflow;
+    unsigned st = h->h_hdr->status & ~(unsigned)(kStatusListOverflow | kStatusRecordOverflow);
     if ((rc = status_to_error(h, st)) != NBX_OK)
     {
         return rc;
+    }
+    if (h->h_hdr->status & kStatusRecordOverflow)
+    {
+        // a cell found more j-clusters than its records hold: grow them and count again
+        const int need = h->h_hdr->rec_need;
+        e = alloc_search_records(h, need + need / 4 + 64);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
+        if (e == cudaSuccess) e = launch_search_count(v, h->stream);
+        h->launches += 2;
+        if ((rc = cuda_check(h, e, "search count")) != NBX_OK || (rc = read_header(h)) != NBX_OK)
+        {
+            return rc;
+        }
+        st = h->h_hdr->status & ~(unsigned)kStatusListOverflow;
+        if ((rc = status_to_error(h, st)) != NBX_OK)
+        {
+            return rc;
+        }
     }
     if ((rc = ensure_list_capacity(h, h->h_hdr->num_sci, h->h_hdr->num_cj4)) != NBX_OK)
     {
@@ -356,7 +398,7 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
         PhaseTimer t(h, 4);
         e = launch_prune(v, 1, 0, 1, h->stream);
     }
-    h->launches += 6 + (h->use_prune ? 1 : 0);
+    h->launches += 5 + (h->use_prune ? 1 : 0);  // emit, 4 balancing kernels, prune
     if ((rc = cuda_check(h, e, "search write")) != NBX_OK)
     {
         return rc;
@@ -795,6 +837,8 @@ int nbx_create(const nbx_system_desc* sys, const nbx_options* opts_in, int devic
     if (e == cudaSuccess) e = dalloc(h, &v.cj4_count, g.cells_capacity + 1);
     if (e == cudaSuccess) e = dalloc(h, &v.sci_offset, g.cells_capacity + 1);
     if (e == cudaSuccess) e = dalloc(h, &v.cj4_offset, g.cells_capacity + 1);
+    if (e == cudaSuccess) e = dalloc(h, &v.rec_ent, (size_t)g.cells_capacity * kMaxEntriesPerCell);
+    if (e == cudaSuccess) e = alloc_search_records(h, kInitialRecordsPerCell);
     if (e == cudaSuccess) e = dalloc(h, &v.fnb, npad);
     if (e == cudaSuccess) e = dalloc(h, &v.energy, 2);
     if (e == cudaSuccess) e = dalloc(h, &v.fshift, kNShift * 3);

@@ -43,10 +43,10 @@ __device__ __forceinline__ int balance_target(const ListHeader* hdr, int min_ci_
     return t > kMinTarget ? (int)t : kMinTarget;
 }
 
-// Walks entry e's cj4 groups and returns its number of pieces; with kWrite the
-// pieces are stored from out[0].
+// Walks entry e's cj4 groups (their cluster-pair counts, the bits of imei[0].imask, written by
+// the search) and returns its number of pieces; with kWrite the pieces are stored from out[0].
 template<bool kWrite>
-__device__ int split_entry(const Cj4* __restrict__ cj4, Sci e, int nsp_max, Sci* out)
+__device__ int split_entry(const unsigned char* __restrict__ grp_pairs, Sci e, int nsp_max, Sci* out)
 {
     const int j4len = e.cj4_end - e.cj4_start;
     if (!(nsp_max > 0 && j4len > 1 && j4len * kNcl * kJg > nsp_max))
@@ -64,7 +64,7 @@ __device__ int split_entry(const Cj4* __restrict__ cj4, Sci e, int nsp_max, Sci*
     for (int j = e.cj4_start; j < e.cj4_end; j++)
     {
         const int nsp_cj4_p = nsp_cj4;
-        nsp_cj4             = __popc(cj4[j].imei[0].imask);
+        nsp_cj4             = grp_pairs[j];
         if (nsp > 0 && nsp_max - nsp < nsp + nsp_cj4 - nsp_max)
         {
             if (kWrite)
@@ -118,7 +118,7 @@ __global__ void k_balance_count(DeviceView v, int min_ci_balanced)
     }
     if (e < nsci)
     {
-        v.sci_pieces[e] = split_entry<false>(v.cj4, v.sci[e], nsp_max, nullptr);
+        v.sci_pieces[e] = split_entry<false>(v.grp_pairs, v.sci[e], nsp_max, nullptr);
     }
 }
 
@@ -201,7 +201,7 @@ __global__ void k_balance_write(DeviceView v)
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e < hdr->num_sci_unsplit)
     {
-        split_entry<true>(v.cj4, v.sci[e], hdr->nsp_max, v.sci_tmp + v.sci_pieces[e]);
+        split_entry<true>(v.grp_pairs, v.sci[e], hdr->nsp_max, v.sci_tmp + v.sci_pieces[e]);
     }
 }
 

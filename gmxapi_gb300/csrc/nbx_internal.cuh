@@ -75,7 +75,16 @@ enum StatusBits : unsigned
     kStatusWrapLimit      = 1u << 3,
     kStatusTimeout        = 1u << 4,
     kStatusExclOverflow   = 1u << 5,
+    // a cell found more j-clusters than its search-record capacity (the host grows the records and
+    // counts again; never an error)
+    kStatusRecordOverflow = 1u << 6,
+    // an entry with more than the per-entry cj4 limit of the search (an error)
+    kStatusEntryOverflow  = 1u << 7,
 };
+
+// Entries one i-cell can have: one per shift of the half shell, at most 23 (5 x 3 x 3 shifts when the
+// box is shorter than rlist along x, of which 22 backward and the central one).
+constexpr int kMaxEntriesPerCell = 24;
 
 struct Sci
 {
@@ -117,6 +126,7 @@ struct ListHeader
     int nsp_max;         // split target of the last balancing (0: no split)
     int num_sci_unsplit; // entries before splitting
     int num_sci_split;   // entries after splitting (scan result)
+    int rec_need;        // largest number of j-cluster records one cell produced in the count pass
 };
 
 // Grid dimensions, fixed for a handle (box and atom count do not change).
@@ -170,6 +180,14 @@ struct DeviceView
     int*      cj4_count;    // [cap] cj4 per cell
     int*      sci_offset;   // [cap+1]
     int*      cj4_offset;   // [cap+1]
+    // search records, written by the count pass and turned into the list by the emit pass: per cell
+    // up to rec_cap j-clusters (index, 8-bit i-cluster mask) in list order and up to
+    // kMaxEntriesPerCell entry codes (shift | j-clusters << 8)
+    int*           rec_cj;     // [cap * rec_cap]
+    unsigned char* rec_m;      // [cap * rec_cap]
+    int*           rec_ent;    // [cap * kMaxEntriesPerCell]
+    int            rec_cap;
+    unsigned char* grp_pairs;  // [cj4_cap] cluster pairs (bits of imei[0].imask) per cj4 group
     // outputs
     float4*  fnb;           // [cap*64] grid-order forces
     double*  energy;        // [2] {LJ, Coulomb}

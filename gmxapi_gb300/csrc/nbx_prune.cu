@@ -61,8 +61,9 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
     }
     // the next group's record is loaded while the current one is tested
     Cj4 c4n = cj4[s.cj4_start + warp];
-    const float sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
-    float2 xi[kNcl], yi[kNcl], zi[kNcl];
+    const float  sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
+    const float2 neg_inner2 = make_float2(-inner2, -inner2), neg_outer2 = make_float2(-outer2, -outer2);
+    float2       xi[kNcl], yi[kNcl], zi[kNcl];
 #pragma unroll
     for (int c = 0; c < kNcl; c++)
     {
@@ -105,28 +106,28 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
 #pragma unroll
         for (int jm = 0; jm < kJg; jm++)
         {
-            const unsigned cu = (either >> (jm * kNcl)) & 0xffu;
-            if (!cu)
+            if (!((either >> (jm * kNcl)) & 0xffu))
             {
                 continue;
             }
-            // per lane: bit c set when this lane's pair of half 0 / half 1 is in range
+            // per lane: bit i set when this lane's pair of half 0 / half 1 with i-cluster i is in
+            // range.  All 8 i-clusters are tested (no per-cluster branch); the in-range flag is the
+            // sign bit of r^2 - cutoff^2 (exactly the sign of the difference: r^2 < cutoff^2), shifted
+            // into the masks from the top i-cluster down, one funnel shift per flag.
             unsigned in0 = 0u, in1 = 0u, out0 = 0u, out1 = 0u;
 #pragma unroll
-            for (int i = 0; i < kNcl; i++)
+            for (int i = kNcl - 1; i >= 0; i--)
             {
-                if (!(cu & (1u << i)))
-                {
-                    continue;
-                }
                 const float2 dx = p_sub(xi[i], xj[jm]);
                 const float2 dy = p_sub(yi[i], yj[jm]);
                 const float2 dz = p_sub(zi[i], zj[jm]);
                 const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                in0 |= (r2.x < inner2) ? (1u << i) : 0u;
-                in1 |= (r2.y < inner2) ? (1u << i) : 0u;
-                out0 |= (r2.x < outer2) ? (1u << i) : 0u;
-                out1 |= (r2.y < outer2) ? (1u << i) : 0u;
+                const float2 di = __fadd2_rn(r2, neg_inner2);
+                const float2 dd = __fadd2_rn(r2, neg_outer2);
+                in0             = __funnelshift_l(__float_as_uint(di.x), in0, 1);
+                in1             = __funnelshift_l(__float_as_uint(di.y), in1, 1);
+                out0            = __funnelshift_l(__float_as_uint(dd.x), out0, 1);
+                out1            = __funnelshift_l(__float_as_uint(dd.y), out1, 1);
             }
             // any pair of the (i-cluster, half) within range: OR over the lanes
             const unsigned sh = jm * kNcl;

@@ -6,14 +6,20 @@
 // boundingbox_only_distance2 (:2841-2878), setSelfAndNewtonExclusionsGpu
 // (:880-904) and setExclusionsForIEntry for GPU lists (:1874-1972).
 //
-// One warp per i-cell (super-cluster).  The warp walks the shifts and the
-// candidate j-columns/cells in exactly the reference's order with the same
-// single-precision arithmetic (this file is compiled with --fmad=false), and
-// evaluates the 8x8 i/j cluster bounding-box distances of a j-cell in one
-// step (2 per lane).  A count pass sizes every cell's entries; after a prefix
-// sum, a write pass emits sci / cj4 entries at fixed offsets and then sets
-// the diagonal and topology exclusion masks.
+// Count pass: one warp per i-cell (super-cluster) walks the shifts in the
+// reference's order with the same single-precision arithmetic (this file is
+// compiled with --fmad=false).  For each shift the lanes find the z-ranges of
+// cells of up to 32 candidate j-columns at once; the warp then takes the flat,
+// increasing sequence of j-cells four at a time, lane (cell, j-cluster)
+// testing its j-cluster's bounding box against the 8 i-clusters.  The j-clusters
+// found are stored as per-cell records (index, 8-bit i-cluster mask) with one
+// code per entry, and the cell's entry / cj4 counts are written.  After a
+// prefix sum of the counts, the emit pass (one warp per cell) turns the records
+// into sci / cj4 entries at fixed offsets, with the outer masks and per-group
+// pair counts, and sets the diagonal and topology exclusion masks.
 #include "nbx_internal.cuh"
+
+#include <cstddef>
 
 namespace nbx
 {
@@ -79,21 +85,20 @@ __device__ __forceinline__ float bb_dist2(const float4 ilo, const float4 ihi, co
     return d2;
 }
 
-struct WarpSmem
+constexpr int kEmitStage = 512;  // j-lists up to this length are staged in shared memory for the
+                                 // exclusion lookups
+
+struct CountSmem
 {
-    float4   bbi_lo[kNcl], bbi_hi[kNcl];  // shifted i-cluster bounding boxes
-    unsigned need[2 * kMaxCj4PerEntry / 32];  // per (cj4, half): exclusion mask needed
-    int      diag_pos[kNcl];               // list positions of the diagonal j-clusters
-    int      excl_base;
+    float4 bbi_lo[kNcl], bbi_hi[kNcl];  // shifted i-cluster bounding boxes
 };
 
-template<bool kWrite>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_count(DeviceView v)
 {
-    __shared__ WarpSmem wsm[kWarpsPerBlock];
+    __shared__ CountSmem wsm[kWarpsPerBlock];
     const int           lane = threadIdx.x & 31;
     const int           wib  = threadIdx.x >> 5;
-    WarpSmem&           sm   = wsm[wib];
+    CountSmem&          sm   = wsm[wib];
     const int           ci   = blockIdx.x * kWarpsPerBlock + wib;
     const int           numCells = v.hdr->num_cells;
     if (ci >= numCells)
@@ -125,17 +130,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
     const int    ncl_i  = v.nclusters[ci];
     int          shp_x  = (box[0] < rlist) ? 2 : 1;
 
-    int sci_out = 0, cj4_out = 0;
-    if (kWrite)
-    {
-        sci_out = v.sci_offset[ci];
-        cj4_out = v.cj4_offset[ci];
-        if (v.hdr->status & kStatusListOverflow)
-        {
-            return;
-        }
-    }
-    int num_entries = 0, num_cj4 = 0;
+    int            num_entries = 0, num_cj4 = 0;
+    int            rec_n = 0;   // records of this cell so far
+    unsigned       pairs = 0u;  // cluster pairs found by this lane
+    int* const           rec_cj = v.rec_cj + (size_t)ci * v.rec_cap;
+    unsigned char* const rec_m  = v.rec_m + (size_t)ci * v.rec_cap;
 
     const float d2cx = 0.0f;
     for (int tz = -1; tz <= 1; tz++)
@@ -208,20 +207,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                     cxf = ci_x;
                 }
                 // shifted i-cluster bounding boxes (set_icell_bb, pairlist.cpp:2260-2303)
+                __syncwarp();
                 if (lane < kNcl)
                 {
                     const float4 l = v.bb[2 * (ci * kNcl + lane)];
                     const float4 h = v.bb[2 * (ci * kNcl + lane) + 1];
                     sm.bbi_lo[lane] = make_float4(l.x + shx, l.y + shy, l.z + shz, 0.0f);
                     sm.bbi_hi[lane] = make_float4(h.x + shx, h.y + shy, h.z + shz, 0.0f);
-                    sm.diag_pos[lane] = -1;
-                }
-                if (kWrite)
-                {
-                    for (int k = lane; k < 2 * kMaxCj4PerEntry / 32; k += 32)
-                    {
-                        sm.need[k] = 0u;
-                    }
                 }
                 __syncwarp();
                 int nj = 0;  // j-clusters in this entry
@@ -334,15 +326,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                         const int k         = k0 + kk;
                         const int scj       = colFirst + (k - (colIncl - colCount));
                         const bool has_cell = k < total;
-                        const int  ncl_j    = has_cell ? v.nclusters[scj] : 0;
-                        const bool diag     = has_cell && excludeSubDiagonal && (scj == ci);
-                        const int  ci1      = diag ? jc + 1 : ncl_i;
-                        unsigned   im8      = 0u;
-                        float      d2one    = 0.0f;
+                        // the j-cluster's bounding box is read with the cell's cluster count (empty
+                        // cluster slots hold far-away boxes, their results are discarded)
+                        int    ncl_j = 0;
+                        float4 jlo{}, jhi{};
+                        if (has_cell)
+                        {
+                            ncl_j = v.nclusters[scj];
+                            jlo   = v.bb[2 * (scj * kNcl + jc)];
+                            jhi   = v.bb[2 * (scj * kNcl + jc) + 1];
+                        }
+                        const bool diag  = has_cell && excludeSubDiagonal && (scj == ci);
+                        const int  ci1   = diag ? jc + 1 : ncl_i;
+                        unsigned   im8   = 0u;
+                        float      d2one = 0.0f;
                         if (jc < ncl_j)
                         {
-                            const float4 jlo = v.bb[2 * (scj * kNcl + jc)];
-                            const float4 jhi = v.bb[2 * (scj * kNcl + jc) + 1];
 #pragma unroll
                             for (int i = 0; i < kNcl; i++)
                             {
@@ -381,23 +380,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                             }
                         }
                         const unsigned nz = __ballot_sync(full, im8 != 0u);
-                        if (kWrite && im8 != 0u)
+                        if (im8 != 0u)
                         {
-                            const int pos = nj + __popc(nz & ((1u << lane) - 1u));
-                            if (pos < kMaxCj4PerEntry * kJg)
+                            const int r = rec_n + nj + __popc(nz & ((1u << lane) - 1u));
+                            if (r < v.rec_cap)
                             {
-                                const int j4  = cj4_out + pos / kJg;
-                                const int off = pos % kJg;
-                                v.cj4[j4].cj[off] = scj * kNcl + jc;
-                                const unsigned bits = im8 << (off * kNcl);
-                                atomicOr(&v.cj4[j4].imei[0].imask, bits);
-                                atomicOr(&v.cj4[j4].imei[1].imask, bits);
-                                if (diag)
-                                {
-                                    sm.diag_pos[jc] = pos;
-                                    atomicOr(&sm.need[(2 * (pos / kJg)) / 32], 3u << ((2 * (pos / kJg)) % 32));
-                                }
+                                rec_cj[r] = scj * kNcl + jc;
+                                rec_m[r]  = (unsigned char)im8;
                             }
+                            pairs += __popc(im8);
                         }
                         nj += __popc(nz);
                     }
@@ -407,187 +398,281 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search(DeviceView v)
                     continue;  // closeIEntry drops empty entries
                 }
                 const int ncj4 = (nj + kJg - 1) / kJg;
-                if (ncj4 > kMaxCj4PerEntry)
+                if (ncj4 > kMaxCj4PerEntry && lane == 0)
                 {
-                    if (lane == 0)
-                    {
-                        set_status(v.hdr, kStatusListOverflow);
-                    }
-                    return;
+                    set_status(v.hdr, kStatusEntryOverflow);
                 }
-                if (kWrite)
+                if (lane == 0)
                 {
-                    __syncwarp();
-                    __threadfence_block();
-                    if (lane == 0)
-                    {
-                        Sci e;
-                        e.sci       = ci;
-                        e.shift     = shift;
-                        e.cj4_start = cj4_out;
-                        e.cj4_end   = cj4_out + ncj4;
-                        v.sci[sci_out] = e;
-                    }
-                    // --- topology exclusions (setExclusionsForIEntry, GPU list) ---
-                    const int    cjFirst      = v.cj4[cj4_out].cj[0];
-                    const int    cjLast       = v.cj4[cj4_out + (nj - 1) / kJg].cj[(nj - 1) % kJg];
-                    const bool   diagRemoved  = excludeSubDiagonal;
-                    // pass A: flag (cj4, half) pairs that need an exclusion mask
-                    for (int rep = 0; rep < 2; rep++)
-                    {
-                        for (int i = lane; i < kSc; i += 32)
-                        {
-                            const int iIndex = ci * kSc + i;
-                            const int iAtom  = v.atom_indices[iIndex];
-                            if (iAtom < 0)
-                            {
-                                continue;
-                            }
-                            const int iCluster = i / kCl;
-                            for (int k = v.excl_index[iAtom]; k < v.excl_index[iAtom + 1]; k++)
-                            {
-                                const int jAtom = v.excl_list[k];
-                                if (jAtom == iAtom)
-                                {
-                                    continue;
-                                }
-                                const int jIndex = v.cells[jAtom];
-                                if (diagRemoved && jIndex <= ci * kSc + i)
-                                {
-                                    continue;
-                                }
-                                const int jCluster = jIndex / kCl;
-                                if (jCluster < cjFirst || jCluster > cjLast)
-                                {
-                                    continue;
-                                }
-                                // the j-list of an entry is sorted on cluster index
-                                int a = 0, b = nj - 1, index = -1;
-                                while (a <= b)
-                                {
-                                    const int m  = (a + b) >> 1;
-                                    const int cm = v.cj4[cj4_out + m / kJg].cj[m % kJg];
-                                    if (cm == jCluster)
-                                    {
-                                        index = m;
-                                        break;
-                                    }
-                                    if (cm < jCluster)
-                                    {
-                                        a = m + 1;
-                                    }
-                                    else
-                                    {
-                                        b = m - 1;
-                                    }
-                                }
-                                if (index < 0)
-                                {
-                                    continue;
-                                }
-                                const int      j4       = cj4_out + index / kJg;
-                                const unsigned pairMask = 1u << ((index % kJg) * kNcl + iCluster);
-                                if (!(v.cj4[j4].imei[0].imask & pairMask))
-                                {
-                                    continue;
-                                }
-                                const int innerI = i & (kCl - 1);
-                                const int innerJ = jIndex & (kCl - 1);
-                                const int jHalf  = innerJ / (kCl / kSplit);
-                                const int slot   = 2 * (index / kJg) + jHalf;
-                                if (rep == 0)
-                                {
-                                    atomicOr(&sm.need[slot / 32], 1u << (slot % 32));
-                                }
-                                else
-                                {
-                                    const int ei = v.cj4[j4].imei[jHalf].excl_ind;
-                                    atomicAnd(&v.excl[ei].pair[(innerJ & (kCl / kSplit - 1)) * kCl + innerI], ~pairMask);
-                                }
-                            }
-                        }
-                        if (rep == 0)
-                        {
-                            // pass B: allocate the flagged masks, all interacting
-                            __syncwarp();
-                            int nneed = 0;
-                            for (int k = 0; k < (2 * ncj4 + 31) / 32; k++)
-                            {
-                                nneed += __popc(sm.need[k]);
-                            }
-                            int basei = 0;
-                            if (lane == 0)
-                            {
-                                basei = atomicAdd(&v.hdr->num_excl, nneed);
-                            }
-                            basei = __shfl_sync(full, basei, 0);
-                            if (basei + nneed > v.hdr->excl_capacity)
-                            {
-                                if (lane == 0)
-                                {
-                                    set_status(v.hdr, kStatusExclOverflow);
-                                }
-                                return;
-                            }
-                            int run = basei;
-                            for (int k = 0; k < (2 * ncj4 + 31) / 32; k++)
-                            {
-                                unsigned w = sm.need[k];
-                                while (w)
-                                {
-                                    const int b    = __ffs(w) - 1;
-                                    w &= w - 1;
-                                    const int slot = k * 32 + b;
-                                    v.excl[run].pair[lane] = 0xffffffffu;
-                                    if (lane == 0)
-                                    {
-                                        v.cj4[cj4_out + slot / 2].imei[slot % 2].excl_ind = run;
-                                    }
-                                    run++;
-                                }
-                            }
-                            __syncwarp();
-                            __threadfence_block();
-                            // self and Newton exclusions of the diagonal cluster pairs
-                            // (setSelfAndNewtonExclusionsGpu): clear j <= i
-                            for (int dj = 0; dj < kNcl; dj++)
-                            {
-                                const int pos = sm.diag_pos[dj];
-                                if (pos < 0)
-                                {
-                                    continue;
-                                }
-                                const int j4  = cj4_out + pos / kJg;
-                                const int off = pos % kJg;
-                                // lane = (jIndexInPart, i): word jIndexInPart*8 + i
-                                const int jip = lane >> 3, ii = lane & 7;
-                                for (int part = 0; part < kSplit; part++)
-                                {
-                                    const int jOffset = part * (kCl / kSplit);
-                                    if (ii >= jOffset + jip)
-                                    {
-                                        const int ei = v.cj4[j4].imei[part].excl_ind;
-                                        atomicAnd(&v.excl[ei].pair[jip * kCl + ii], ~(1u << (off * kNcl + dj)));
-                                    }
-                                }
-                            }
-                            __syncwarp();
-                        }
-                    }
-                    __syncwarp();
+                    v.rec_ent[ci * kMaxEntriesPerCell + num_entries] = shift | (nj << 8);
                 }
                 num_entries++;
                 num_cj4 += ncj4;
-                sci_out++;
-                cj4_out += ncj4;
-                __syncwarp();
+                rec_n += nj;
             }
         }
     }
-    if (!kWrite && lane == 0)
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        pairs += __shfl_xor_sync(full, pairs, o);
+    }
+    if (lane == 0)
     {
         v.sci_count[ci] = num_entries;
         v.cj4_count[ci] = num_cj4;
+        // cluster pairs of the list, the count that list balancing splits by
+        if (pairs > 0u)
+        {
+            atomicAdd(&v.hdr->num_subpairs, (int)pairs);
+        }
+        if (rec_n > v.rec_cap)
+        {
+            atomicMax(&v.hdr->rec_need, rec_n);
+            set_status(v.hdr, kStatusRecordOverflow);
+        }
+    }
+}
+
+struct EmitSmem
+{
+    unsigned need[2 * kMaxCj4PerEntry / 32];  // per (cj4, half): exclusion mask needed
+    int      diag_pos[kNcl];                   // list positions of the diagonal j-clusters
+    int      jl[kEmitStage];                   // the entry's j-clusters (short entries)
+};
+
+// Emit pass: one warp per i-cell turns its search records into list entries at the offsets of the
+// prefix sum.  Per entry: the cj4 groups (one per lane: four j-clusters, the i-cluster masks of both
+// warp halves, exclusion index 0 = all interacting), the outer masks (the fresh list's masks until
+// a prune refines them) and the group's cluster-pair count for balancing; then the exclusions:
+// flag the (cj4, half) pairs that need a mask (self/Newton pairs of the diagonal j-clusters and
+// topology exclusions), allocate the flagged masks all interacting, clear j <= i on the diagonal
+// (setSelfAndNewtonExclusionsGpu) and the excluded atom pairs (setExclusionsForIEntry).
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView v)
+{
+    __shared__ EmitSmem wsm[kWarpsPerBlock];
+    const int           lane = threadIdx.x & 31;
+    const int           wib  = threadIdx.x >> 5;
+    EmitSmem&           sm   = wsm[wib];
+    const int           ci   = blockIdx.x * kWarpsPerBlock + wib;
+    const unsigned      full = 0xffffffffu;
+    if (ci >= v.hdr->num_cells
+        || (v.hdr->status & (kStatusListOverflow | kStatusRecordOverflow | kStatusEntryOverflow)))
+    {
+        return;
+    }
+    const int nent    = v.sci_count[ci];
+    int       sci_out = v.sci_offset[ci];
+    int       cj4_out = v.cj4_offset[ci];
+    const int*           rec_cj = v.rec_cj + (size_t)ci * v.rec_cap;
+    const unsigned char* rec_m  = v.rec_m + (size_t)ci * v.rec_cap;
+    for (int k = 0; k < nent; k++)
+    {
+        const int  code  = v.rec_ent[ci * kMaxEntriesPerCell + k];
+        const int  shift = code & 0xff;
+        const int  nj    = code >> 8;
+        const int  ncj4  = (nj + kJg - 1) / kJg;
+        const bool excludeSubDiagonal = (shift == kCentral);
+        if (lane < kNcl)
+        {
+            sm.diag_pos[lane] = -1;
+        }
+        for (int w = lane; w < 2 * kMaxCj4PerEntry / 32; w += 32)
+        {
+            sm.need[w] = 0u;
+        }
+        __syncwarp();
+        for (int g = lane; g < ncj4; g += 32)
+        {
+            Cj4      c;
+            unsigned im = 0u;
+#pragma unroll
+            for (int off = 0; off < kJg; off++)
+            {
+                const int p = g * kJg + off;
+                c.cj[off]   = p < nj ? rec_cj[p] : 0;
+                im |= p < nj ? (unsigned)rec_m[p] << (off * kNcl) : 0u;
+            }
+            c.imei[0].imask    = im;
+            c.imei[0].excl_ind = 0;
+            c.imei[1]          = c.imei[0];
+            v.cj4[cj4_out + g] = c;
+            reinterpret_cast<uint2*>(v.imask_outer)[cj4_out + g] = make_uint2(im, im);
+            v.grp_pairs[cj4_out + g] = (unsigned char)__popc(im);
+        }
+        // the j-list is sorted on cluster index; short lists go to shared memory for the lookups
+        const bool staged = nj <= kEmitStage;
+        for (int p = lane; p < nj; p += 32)
+        {
+            const int cj = rec_cj[p];
+            if (staged)
+            {
+                sm.jl[p] = cj;
+            }
+            // the diagonal j-clusters (the i-cell's own clusters, central shift)
+            if (excludeSubDiagonal && (cj >> 3) == ci)
+            {
+                sm.diag_pos[cj & (kNcl - 1)] = p;
+                atomicOr(&sm.need[(2 * (p / kJg)) / 32], 3u << ((2 * (p / kJg)) % 32));
+            }
+        }
+        const int* jlist = staged ? sm.jl : rec_cj;
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0)
+        {
+            Sci e;
+            e.sci          = ci;
+            e.shift        = shift;
+            e.cj4_start    = cj4_out;
+            e.cj4_end      = cj4_out + ncj4;
+            v.sci[sci_out] = e;
+        }
+        // --- topology exclusions (setExclusionsForIEntry, GPU list) ---
+        const int  cjFirst     = jlist[0];
+        const int  cjLast      = jlist[nj - 1];
+        const bool diagRemoved = excludeSubDiagonal;
+        // pass A: flag (cj4, half) pairs that need an exclusion mask; pass B (rep 1): clear the bits
+        for (int rep = 0; rep < 2; rep++)
+        {
+            for (int i = lane; i < kSc; i += 32)
+            {
+                const int iIndex = ci * kSc + i;
+                const int iAtom  = v.atom_indices[iIndex];
+                if (iAtom < 0)
+                {
+                    continue;
+                }
+                const int iCluster = i / kCl;
+                for (int x = v.excl_index[iAtom]; x < v.excl_index[iAtom + 1]; x++)
+                {
+                    const int jAtom = v.excl_list[x];
+                    if (jAtom == iAtom)
+                    {
+                        continue;
+                    }
+                    const int jIndex = v.cells[jAtom];
+                    if (diagRemoved && jIndex <= ci * kSc + i)
+                    {
+                        continue;
+                    }
+                    const int jCluster = jIndex / kCl;
+                    if (jCluster < cjFirst || jCluster > cjLast)
+                    {
+                        continue;
+                    }
+                    int a = 0, b = nj - 1, index = -1;
+                    while (a <= b)
+                    {
+                        const int m  = (a + b) >> 1;
+                        const int cm = jlist[m];
+                        if (cm == jCluster)
+                        {
+                            index = m;
+                            break;
+                        }
+                        if (cm < jCluster)
+                        {
+                            a = m + 1;
+                        }
+                        else
+                        {
+                            b = m - 1;
+                        }
+                    }
+                    if (index < 0 || !((rec_m[index] >> iCluster) & 1u))
+                    {
+                        continue;
+                    }
+                    const int      j4       = cj4_out + index / kJg;
+                    const unsigned pairMask = 1u << ((index % kJg) * kNcl + iCluster);
+                    const int      innerI   = i & (kCl - 1);
+                    const int      innerJ   = jIndex & (kCl - 1);
+                    const int      jHalf    = innerJ / (kCl / kSplit);
+                    const int      slot     = 2 * (index / kJg) + jHalf;
+                    if (rep == 0)
+                    {
+                        atomicOr(&sm.need[slot / 32], 1u << (slot % 32));
+                    }
+                    else
+                    {
+                        const int ei = v.cj4[j4].imei[jHalf].excl_ind;
+                        atomicAnd(&v.excl[ei].pair[(innerJ & (kCl / kSplit - 1)) * kCl + innerI], ~pairMask);
+                    }
+                }
+            }
+            if (rep == 0)
+            {
+                // allocate the flagged masks, all interacting
+                __syncwarp();
+                int nneed = 0;
+                for (int w = 0; w < (2 * ncj4 + 31) / 32; w++)
+                {
+                    nneed += __popc(sm.need[w]);
+                }
+                int basei = 0;
+                if (lane == 0 && nneed > 0)
+                {
+                    basei = atomicAdd(&v.hdr->num_excl, nneed);
+                }
+                basei = __shfl_sync(full, basei, 0);
+                if (basei + nneed > v.hdr->excl_capacity)
+                {
+                    if (lane == 0)
+                    {
+                        set_status(v.hdr, kStatusExclOverflow);
+                    }
+                    return;
+                }
+                int run = basei;
+                for (int w = 0; w < (2 * ncj4 + 31) / 32; w++)
+                {
+                    unsigned bits = sm.need[w];
+                    while (bits)
+                    {
+                        const int b = __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        const int slot = w * 32 + b;
+                        v.excl[run].pair[lane] = 0xffffffffu;
+                        if (lane == 0)
+                        {
+                            v.cj4[cj4_out + slot / 2].imei[slot % 2].excl_ind = run;
+                        }
+                        run++;
+                    }
+                }
+                __syncwarp();
+                __threadfence_block();
+                // self and Newton exclusions of the diagonal cluster pairs
+                // (setSelfAndNewtonExclusionsGpu): clear j <= i
+                for (int dj = 0; dj < kNcl; dj++)
+                {
+                    const int pos = sm.diag_pos[dj];
+                    if (pos < 0)
+                    {
+                        continue;
+                    }
+                    const int j4  = cj4_out + pos / kJg;
+                    const int off = pos % kJg;
+                    // lane = (jIndexInPart, i): word jIndexInPart*8 + i
+                    const int jip = lane >> 3, ii = lane & 7;
+                    for (int part = 0; part < kSplit; part++)
+                    {
+                        const int jOffset = part * (kCl / kSplit);
+                        if (ii >= jOffset + jip)
+                        {
+                            const int ei = v.cj4[j4].imei[part].excl_ind;
+                            atomicAnd(&v.excl[ei].pair[jip * kCl + ii], ~(1u << (off * kNcl + dj)));
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        __syncwarp();
+        rec_cj += nj;
+        rec_m += nj;
+        sci_out++;
+        cj4_out += ncj4;
     }
 }
 
@@ -665,41 +750,18 @@ __global__ void k_scan_counts(DeviceView v)
     }
 }
 
-// The fresh list's masks are also the outer masks until a prune refines them.
-__global__ void k_copy_outer(DeviceView v)
-{
-    const int  j  = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ok = j < v.hdr->num_cj4 && !(v.hdr->status & kStatusListOverflow);
-    int        n  = 0;
-    if (ok)
-    {
-        const unsigned m0        = v.cj4[j].imei[0].imask;
-        v.imask_outer[2 * j]     = m0;
-        v.imask_outer[2 * j + 1] = v.cj4[j].imei[1].imask;
-        n                        = __popc(m0);
-    }
-    // cluster pairs of the list, the count that list balancing splits by
-    // (whole warps reach this point: the grid is a multiple of 32 threads)
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        n += __shfl_xor_sync(0xffffffffu, n, o);
-    }
-    if ((threadIdx.x & 31) == 0 && n > 0)
-    {
-        atomicAdd(&v.hdr->num_subpairs, n);
-    }
-}
-
 } // namespace
 
-// count -> prefix sum | memset -> write (+ outer-mask copy).  All sizes stay
-// on the device; the host reads them between the two halves only when the
-// list capacity has to be checked.
+// count (+ records) -> prefix sum | emit.  All sizes stay on the device; the host reads them
+// between the two halves to check the list and record capacities.
 cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s)
 {
     const int cap    = v.g.cells_capacity;
     const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    k_search<false><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
+    // num_subpairs .. rec_need: accumulated by the count pass or set by balancing
+    cudaMemsetAsync(&v.hdr->num_subpairs, 0,
+                    offsetof(ListHeader, rec_need) + sizeof(int) - offsetof(ListHeader, num_subpairs), s);
+    k_search_count<<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
     k_scan_counts<<<1, 1024, 0, s>>>(v);
     return cudaGetLastError();
 }
@@ -708,18 +770,8 @@ cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s)
 {
     const int cap    = v.g.cells_capacity;
     const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    // cj4 entries are filled with atomicOr: start from zero (no bits, excl_ind 0)
-    cudaMemsetAsync(v.cj4, 0, sizeof(Cj4) * (size_t)v.cj4_cap, s);
-    cudaMemsetAsync(&v.hdr->num_subpairs, 0, sizeof(int), s);
-    k_search<true><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
-    k_copy_outer<<<(v.cj4_cap + 255) / 256, 256, 0, s>>>(v);
+    k_search_emit<<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
     return cudaGetLastError();
-}
-
-cudaError_t launch_search(const DeviceView& v, cudaStream_t s)
-{
-    cudaError_t e = launch_search_count(v, s);
-    return e == cudaSuccess ? launch_search_write(v, s) : e;
 }
 
 } // namespace nbx
