@@ -58,24 +58,23 @@ class _NonbondedFunction(torch.autograd.Function):
         # the kernels read float32 parameters; the table gradient comes back in the
         # table's own dtype (FP64 sums when the table is float64)
         nbfp32 = nbfp.to(torch.float32).contiguous()
-        calc.set_parameters_device(q.data_ptr(), nbfp32.data_ptr())
+        engine._upload(q, nbfp32)
         f = torch.empty_like(x)
         e = torch.zeros(2, dtype=torch.float64, device=x.device)
         calc.compute_device(x.data_ptr(), f.data_ptr(), e.data_ptr(), None)
         ctx.engine = engine
-        ctx.save_for_backward(x, q, nbfp)
+        ctx.save_for_backward(x, q, nbfp, nbfp32)
         return f, e
 
     @staticmethod
     @once_differentiable
     def backward(ctx, g_f, g_e):
-        x, q, nbfp = ctx.saved_tensors
+        x, q, nbfp, nbfp32 = ctx.saved_tensors
         calc = ctx.engine.calc
         dev = x.device
         calc.set_stream(torch.cuda.current_stream(dev).cuda_stream)
-        # the handle may have seen other parameters since the forward pass
-        nbfp32 = nbfp.to(torch.float32).contiguous()
-        calc.set_parameters_device(q.data_ptr(), nbfp32.data_ptr())
+        # the handle may have seen other parameters since the forward pass (uploaded again then)
+        ctx.engine._upload(q, nbfp32)
         g_f = torch.zeros_like(x) if g_f is None else g_f.to(torch.float32).contiguous()
         g_e = None if g_e is None else g_e.to(torch.float64).contiguous()
         need_x, need_q, need_p = ctx.needs_input_grad[:3]
@@ -109,6 +108,16 @@ class DifferentiableNonbonded:
         self.ntypes = int(system.ntypes)
         self.device = torch.device("cuda", device)
         self.calc = ForceCalculator(system, opts, device)
+        self._uploaded = None
+
+    def _upload(self, q: torch.Tensor, nbfp32: torch.Tensor):
+        """Charges and float32 type table to the handle, unless the same storage, unmodified, was
+        the last one uploaded.  The uploaded tensors are kept referenced, so their memory cannot be
+        reused by another tensor while their addresses serve as the key."""
+        key = (q.data_ptr(), q._version, nbfp32.data_ptr(), nbfp32._version)
+        if self._uploaded is None or key != self._uploaded[0]:
+            self.calc.set_parameters_device(q.data_ptr(), nbfp32.data_ptr())
+            self._uploaded = (key, q, nbfp32)
 
     def search(self, x: torch.Tensor):
         self.calc.set_stream(torch.cuda.current_stream(x.device).cuda_stream)

@@ -33,6 +33,22 @@ namespace
 constexpr int kAdjThreads    = 256;
 constexpr int kAdjWarps      = kAdjThreads / 32;
 constexpr int kAdjMaxTypes1  = 16;
+// Up to this many types (+ the dummy type) every warp keeps one type-pair gradient table per
+// i-atom lane index (8 replicas): the lanes that add into one table in the same instruction then
+// share their i-atom, so two of them hit the same entry only when their j-atoms have the same type.
+constexpr int kAdjRepTypes1  = 10;
+constexpr int kAdjReplicas   = kCl;
+
+// Type-pair gradient tables of one warp: replicas x (nt1^2 + 1) float2 (the +1 staggers the
+// replicas over the shared-memory banks).
+__host__ __device__ __forceinline__ int adj_table_replicas(int nt1)
+{
+    return nt1 <= kAdjRepTypes1 ? kAdjReplicas : 1;
+}
+__host__ __device__ __forceinline__ int adj_table_stride(int nt1)
+{
+    return nt1 * nt1 + 1;
+}
 
 struct AdjConsts
 {
@@ -204,6 +220,9 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
     const int      nt1     = v.ntypes1;
     const float    sx = p.shiftvec[3 * s.shift], sy = p.shiftvec[3 * s.shift + 1], sz = p.shiftvec[3 * s.shift + 2];
     const bool     central = (s.shift == kCentral);
+    const int      reps    = adj_table_replicas(nt1);
+    const int      tstride = adj_table_stride(nt1);
+    float2* const  ttab_lane = ttab + (reps > 1 ? ii : 0) * tstride;
     __syncwarp();
     for (int m = lane; m < kSc; m += 32)
     {
@@ -266,13 +285,13 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
             }
             if (exi == 0)
             {
-                adj_half<kEwald, false>(v, jx, jg, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h, s.sci,
+                adj_half<kEwald, false>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h, s.sci,
                                         central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
             }
             else
             {
                 const unsigned wexcl = p.excl[exi].pair[lane];
-                adj_half<kEwald, true>(v, jx, jg, nbfp_s, ttab, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl, h,
+                adj_half<kEwald, true>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl, h,
                                        s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
             }
         }
@@ -299,33 +318,37 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
     __syncwarp();
     for (int m = lane; m < nt1 * nt1; m += 32)
     {
-        const float2 t = ttab[m];
-        if (t.x != 0.0f || t.y != 0.0f)
+        double tx = 0.0, ty = 0.0;
+        for (int r = 0; r < reps; r++)
         {
-            atomicAdd(&gnbfp[2 * m], (double)t.x);
-            atomicAdd(&gnbfp[2 * m + 1], (double)t.y);
-            ttab[m] = make_float2(0.0f, 0.0f);
+            const float2 t = ttab[r * tstride + m];
+            tx += (double)t.x;
+            ty += (double)t.y;
+            ttab[r * tstride + m] = make_float2(0.0f, 0.0f);
+        }
+        if (tx != 0.0 || ty != 0.0)
+        {
+            atomicAdd(&gnbfp[2 * m], tx);
+            atomicAdd(&gnbfp[2 * m + 1], ty);
         }
     }
     __syncwarp();
 }
 
 // Shared set-up of the adjoint kernels: the type table and zeroed per-warp tables.
-__device__ __forceinline__ void adj_setup(const DeviceView& v, float2* nbfp_s, float2 (*ttab_s)[kAdjMaxTypes1 * kAdjMaxTypes1],
-                                          double* gsum_s)
+__device__ __forceinline__ void adj_setup(const DeviceView& v, float2* nbfp_s, float2* ttab_all, double* gsum_s)
 {
-    const int nt1  = v.ntypes1;
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
+    const int nt1 = v.ntypes1;
     for (int m = threadIdx.x; m < nt1 * nt1; m += blockDim.x)
     {
         nbfp_s[m]         = v.nbfp[m];
         gsum_s[2 * m]     = 0.0;
         gsum_s[2 * m + 1] = 0.0;
     }
-    for (int m = lane; m < nt1 * nt1; m += 32)
+    const int ntab = kAdjWarps * adj_table_replicas(nt1) * adj_table_stride(nt1);
+    for (int m = threadIdx.x; m < ntab; m += blockDim.x)
     {
-        ttab_s[warp][m] = make_float2(0.0f, 0.0f);
+        ttab_all[m] = make_float2(0.0f, 0.0f);
     }
     __syncthreads();
 }
@@ -357,12 +380,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
     }
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
-    __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
+    extern __shared__ float2 ttab_s[];  // kAdjWarps x replicas x stride type-pair gradient tables
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
     __shared__ float4 jg_s[kAdjWarps][32];
     adj_setup(v, nbfp_s, ttab_s, gsum_s);
+    float2* const ttab_w = ttab_s + (threadIdx.x >> 5) * adj_table_replicas(v.ntypes1) * adj_table_stride(v.ntypes1);
     if (v.hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
         return;
@@ -384,7 +408,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         {
             break;
         }
-        adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp], jx_s[warp], jg_s[warp],
+        adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_w, xis_s[warp], gis_s[warp], jx_s[warp], jg_s[warp],
                           lane, k, v.pbeta,
                           v.beta2l2, v.c2b, b2c2b, gsum_s);
     }
@@ -418,12 +442,14 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
 {
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
-    __shared__ float2 ttab_s[kAdjWarps][kAdjMaxTypes1 * kAdjMaxTypes1];
+    extern __shared__ float2 ttab_s[];  // kAdjWarps x replicas x stride type-pair gradient tables
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
     __shared__ float4 jg_s[kAdjWarps][32];
     adj_setup(cv, nbfp_s, ttab_s, gsum_s);
+    float2* const ttab_w =
+            ttab_s + (threadIdx.x >> 5) * adj_table_replicas(cv.ntypes1) * adj_table_stride(cv.ntypes1);
     const int   warp  = threadIdx.x >> 5;
     const int   lane  = threadIdx.x & 31;
     const int   total = prefix[nsys];
@@ -449,7 +475,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
             k.gE_c  = (float)gE[2 * sidx + 1];
         }
         const AdjPtrs p = { b.xq, b.tgrid, b.cj4, b.excl, b.shiftvec, b.gnb, b.dnb };
-        adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_s[warp], xis_s[warp], gis_s[warp],
+        adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_w, xis_s[warp], gis_s[warp],
                           jx_s[warp], jg_s[warp], lane, k,
                           cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gsum_s);
     }
@@ -626,6 +652,29 @@ int adjoint_max_types1()
     return kAdjMaxTypes1;
 }
 
+namespace
+{
+
+size_t adj_table_bytes(int nt1)
+{
+    return sizeof(float2) * (size_t)kAdjWarps * adj_table_replicas(nt1) * adj_table_stride(nt1);
+}
+
+// Opts an adjoint kernel in to its static + dynamic shared memory beyond 48 KB.
+template<auto kKernel>
+cudaError_t adj_optin(size_t dynamic_bytes)
+{
+    cudaFuncAttributes a{};
+    cudaError_t        e = cudaFuncGetAttributes(&a, kKernel);
+    if (e != cudaSuccess)
+    {
+        return e;
+    }
+    return smem_optin<kKernel>(a.sharedSizeBytes + dynamic_bytes, dynamic_bytes);
+}
+
+} // namespace
+
 cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* d_gF, const double* d_gE,
                             float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
                             int num_sms, cudaStream_t s)
@@ -634,13 +683,21 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* 
     const int slots = v.g.cells_capacity * kSc;
     k_adj_prepare<<<(slots + tb - 1) / tb, tb, 0, s>>>(v, d_x, d_gF, gnb, dnb, counter, d_gnbfp,
                                                        2 * v.ntypes1 * v.ntypes1);
+    const size_t dyn = adj_table_bytes(v.ntypes1);
+    cudaError_t  e   = cudaSuccess;
     if (v.coulomb == 0)
     {
-        k_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+        e = adj_optin<k_backward<true>>(dyn);
+        k_backward<true><<<num_sms * 2, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
     }
     else
     {
-        k_backward<false><<<num_sms * 2, kAdjThreads, 0, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+        e = adj_optin<k_backward<false>>(dyn);
+        k_backward<false><<<num_sms * 2, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+    }
+    if (e != cudaSuccess)
+    {
+        return e;
     }
     k_adj_finish<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, dnb, d_gE, d_gx, d_gq);
     return cudaGetLastError();
@@ -653,13 +710,21 @@ cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, con
     const int tb = 256;
     k_batch_adj_prepare<<<dim3((max_slots + tb - 1) / tb, nsys), tb, 0, s>>>(sys, d_gF, counter, d_gnbfp,
                                                                              2 * cv.ntypes1 * cv.ntypes1);
+    const size_t dyn = adj_table_bytes(cv.ntypes1);
+    cudaError_t  e   = cudaSuccess;
     if (cv.coulomb == 0)
     {
-        k_batch_backward<true><<<num_sms * 2, kAdjThreads, 0, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+        e = adj_optin<k_batch_backward<true>>(dyn);
+        k_batch_backward<true><<<num_sms * 2, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
     }
     else
     {
-        k_batch_backward<false><<<num_sms * 2, kAdjThreads, 0, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+        e = adj_optin<k_batch_backward<false>>(dyn);
+        k_batch_backward<false><<<num_sms * 2, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+    }
+    if (e != cudaSuccess)
+    {
+        return e;
     }
     k_batch_adj_finish<<<dim3((max_atoms + tb - 1) / tb, nsys), tb, 0, s>>>(cv, sys, d_gE, d_gx, d_gq);
     return cudaGetLastError();

@@ -930,8 +930,19 @@ int nbx_set_stream(nbx_handle* h, void* s)
         return NBX_OK;
     }
     cudaSetDevice(h->device);
-    // work queued on the previous stream finishes before the new one is used
-    cudaStreamSynchronize(h->stream);
+    // work queued on the previous stream finishes before the new one is used -- unless the new
+    // stream is being captured into a CUDA graph, where a host synchronisation is not allowed and
+    // the capturing code orders the streams itself (a capture starts after the work before it)
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(s), &capture) != cudaSuccess)
+    {
+        cudaGetLastError();
+        capture = cudaStreamCaptureStatusNone;
+    }
+    if (capture == cudaStreamCaptureStatusNone)
+    {
+        cudaStreamSynchronize(h->stream);
+    }
     if (h->own_stream)
     {
         cudaStreamDestroy(h->stream);
@@ -2253,9 +2264,19 @@ int nbx_batch_set_stream(nbx_batch* b, void* s)
         return NBX_OK;
     }
     cudaSetDevice(b->device);
-    // work queued on the previous stream finishes before the new one is used; the
-    // graphs were captured on a private stream and are launched on whichever is current
-    cudaStreamSynchronize(b->stream);
+    // work queued on the previous stream finishes before the new one is used (not while the new
+    // stream is capturing a CUDA graph); the batch's own graphs were captured on a private stream
+    // and are launched on whichever is current
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(s), &capture) != cudaSuccess)
+    {
+        cudaGetLastError();
+        capture = cudaStreamCaptureStatusNone;
+    }
+    if (capture == cudaStreamCaptureStatusNone)
+    {
+        cudaStreamSynchronize(b->stream);
+    }
     if (b->own_stream)
     {
         cudaStreamDestroy(b->stream);

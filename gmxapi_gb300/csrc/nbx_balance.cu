@@ -122,11 +122,11 @@ __global__ void k_balance_count(DeviceView v, int min_ci_balanced)
     }
 }
 
-// Exclusive scan of the piece counts in place; the total goes to num_sci_split.
+// Exclusive scan of the piece counts in place (one block, each thread a contiguous run); the
+// total goes to num_sci_split.
 __global__ void __launch_bounds__(1024) k_balance_scan(DeviceView v)
 {
-    __shared__ int warp_sums[32];
-    __shared__ int carry;
+    __shared__ int    warp_sums[32];
     const ListHeader* hdr = v.hdr;
     if (hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
@@ -134,60 +134,54 @@ __global__ void __launch_bounds__(1024) k_balance_scan(DeviceView v)
     }
     const int n    = hdr->num_sci_unsplit;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0)
+    const int per  = (n + blockDim.x - 1) / blockDim.x;
+    const int i0   = min(n, (int)threadIdx.x * per);
+    const int i1   = min(n, i0 + per);
+    int       own  = 0;
+    for (int i = i0; i < i1; i++)
     {
-        carry = 0;
+        own += v.sci_pieces[i];
+    }
+    int inc = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o)
+        {
+            inc += t;
+        }
+    }
+    if (lane == 31)
+    {
+        warp_sums[warp] = inc;
     }
     __syncthreads();
-    for (int base = 0; base < n; base += blockDim.x)
+    if (warp == 0)
     {
-        const int i   = base + threadIdx.x;
-        const int val = (i < n) ? v.sci_pieces[i] : 0;
-        int       inc = val;
+        int w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
-            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            const int t = __shfl_up_sync(0xffffffffu, w, o);
             if (lane >= o)
             {
-                inc += t;
+                w += t;
             }
         }
-        if (lane == 31)
-        {
-            warp_sums[warp] = inc;
-        }
-        __syncthreads();
-        if (warp == 0)
-        {
-            int w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-            {
-                const int t = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o)
-                {
-                    w += t;
-                }
-            }
-            warp_sums[lane] = w;  // inclusive over warps
-        }
-        __syncthreads();
-        const int before = carry + (warp > 0 ? warp_sums[warp - 1] : 0) + inc - val;
-        if (i < n)
-        {
-            v.sci_pieces[i] = before;
-        }
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1)
-        {
-            carry = before + val;
-        }
-        __syncthreads();
+        warp_sums[lane] = w;  // inclusive over warps
     }
-    if (threadIdx.x == 0)
+    __syncthreads();
+    int run = (warp > 0 ? warp_sums[warp - 1] : 0) + inc - own;
+    for (int i = i0; i < i1; i++)
     {
-        v.hdr->num_sci_split = carry;
+        const int val   = v.sci_pieces[i];
+        v.sci_pieces[i] = run;
+        run += val;
+    }
+    if (threadIdx.x == blockDim.x - 1)
+    {
+        v.hdr->num_sci_split = run;
     }
 }
 
@@ -205,15 +199,14 @@ __global__ void k_balance_write(DeviceView v)
     }
 }
 
-// Stable counting sort of sci_tmp into sci, size classes descending (one block).
-// Within each 1024-entry chunk an entry's rank among equal classes comes from
-// __match_any_sync inside its warp plus the counts of the warps before it.
+// Stable counting sort of sci_tmp into sci, size classes descending (one block).  Warp w owns the
+// w-th contiguous chunk of the entries: a per-warp class histogram, then per class the offsets of
+// the warps' runs (warps in order, classes descending), then each warp places its chunk in order,
+// the rank among equal classes of a batch of 32 from __match_any_sync.
 __global__ void __launch_bounds__(kSortThreads) k_sort_entries(DeviceView v)
 {
-    __shared__ int hist[kMaxSizeClass + 1];
-    __shared__ int running[kMaxSizeClass + 1];
-    __shared__ unsigned short wcount[kSortWarps][kMaxSizeClass + 1];
-    ListHeader* hdr = v.hdr;
+    __shared__ int hist[kSortWarps][kMaxSizeClass + 1];  // counts, then each warp's first position
+    ListHeader*    hdr = v.hdr;
     if (hdr->status & (kStatusListOverflow | kStatusExclOverflow | kStatusGridOverflow))
     {
         return;
@@ -231,69 +224,82 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_entries(DeviceView v)
     }
     int m = (ncj4 > n) ? (int)((2LL * ncj4) / n) : 0;  // m = 0: one class, order kept
     m     = m > kMaxSizeClass ? kMaxSizeClass : m;
-    for (int k = threadIdx.x; k <= kMaxSizeClass; k += blockDim.x)
-    {
-        hist[k]    = 0;
-        running[k] = 0;
-    }
     for (int k = threadIdx.x; k < kSortWarps * (kMaxSizeClass + 1); k += blockDim.x)
     {
-        (&wcount[0][0])[k] = 0;
+        (&hist[0][0])[k] = 0;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < n; e += blockDim.x)
+    const int chunk = (n + kSortWarps - 1) / kSortWarps;
+    const int e0    = min(n, warp * chunk);
+    const int e1    = min(n, e0 + chunk);
+    for (int e = e0 + lane; e < e1; e += 32)
     {
         const int len = v.sci_tmp[e].cj4_end - v.sci_tmp[e].cj4_start;
-        atomicAdd(&hist[len < m ? len : m], 1);
+        atomicAdd(&hist[warp][len < m ? len : m], 1);
     }
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (warp == 0)
     {
-        // class m first, then decreasing sizes (exclusive offsets in place)
-        int off = 0;
-        for (int c = m; c >= 0; c--)
+        // per class: the warps' runs in warp order; classes from m down to 0
+        int base = 0;
+        for (int c0 = m; c0 >= 0; c0 -= 32)
         {
-            const int k = hist[c];
-            hist[c]     = off;
-            off += k;
+            const int c     = c0 - lane;
+            int       total = 0;
+            if (c >= 0)
+            {
+                for (int w = 0; w < kSortWarps; w++)
+                {
+                    const int h = hist[w][c];
+                    hist[w][c]  = total;
+                    total += h;
+                }
+            }
+            int incl = total;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                {
+                    incl += t;
+                }
+            }
+            const int start = base + incl - total;
+            if (c >= 0)
+            {
+                for (int w = 0; w < kSortWarps; w++)
+                {
+                    hist[w][c] += start;
+                }
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
     __syncthreads();
-    for (int base = 0; base < n; base += blockDim.x)
+    for (int b = e0; b < e1; b += 32)
     {
-        const int e   = base + threadIdx.x;
+        const int e   = b + lane;
         Sci       s{};
         int       cls = -1;
-        if (e < n)
+        if (e < e1)
         {
-            s         = v.sci_tmp[e];
+            s             = v.sci_tmp[e];
             const int len = s.cj4_end - s.cj4_start;
-            cls       = len < m ? len : m;
+            cls           = len < m ? len : m;
         }
-        const unsigned peers  = __match_any_sync(0xffffffffu, cls);
-        const int      rank   = __popc(peers & ((1u << lane) - 1u));
-        const bool     leader = (peers & ((1u << lane) - 1u)) == 0u;
-        if (cls >= 0 && leader)
-        {
-            wcount[warp][cls] = (unsigned short)__popc(peers);
-        }
-        __syncthreads();
+        const unsigned peers = __match_any_sync(0xffffffffu, cls);
+        const unsigned lower = peers & ((1u << lane) - 1u);
         if (cls >= 0)
         {
-            int before = 0;
-            for (int w = 0; w < warp; w++)
-            {
-                before += wcount[w][cls];
-            }
-            v.sci[hist[cls] + running[cls] + before + rank] = s;
+            v.sci[hist[warp][cls] + __popc(lower)] = s;
         }
-        __syncthreads();
-        if (cls >= 0 && leader)
+        __syncwarp();
+        if (cls >= 0 && lower == 0u)
         {
-            atomicAdd(&running[cls], __popc(peers));
-            wcount[warp][cls] = 0;
+            hist[warp][cls] += __popc(peers);
         }
-        __syncthreads();
+        __syncwarp();
     }
     if (threadIdx.x == 0)
     {

@@ -8,12 +8,15 @@
 //    any pair is within rlistInner;
 //  - rolling pass: only bits in (outer XOR inner) are re-tested and may be
 //    added to the inner mask.
-// One block per list entry, one warp per cj4 (lane = j-atom-in-half * 8 +
-// i-atom, both halves at once in packed FP32x2 arithmetic), the 64 shifted
-// i-atoms staged in shared memory, the any-pair tests of a j-cluster's
-// i-clusters combined into per-lane bit masks and one warp OR reduction per
-// mask.  Compiled with --fmad=false: r^2 rounds exactly like the CPU
-// restatement.
+// One block per list entry, its warps taking the entry's cj4 groups in turn.
+// Fresh pass: lane (ii, jj) holds the shifted i-atom ii of the 8 i-clusters in
+// registers and tests its pairs with j-atoms jj and jj + 4 (both warp halves)
+// in packed FP32x2 arithmetic; the in-range flags of a j-cluster's 8 i-clusters
+// become per-lane bit masks, ORed over the warp with one reduction per mask.
+// Rolling pass: the few bits to re-test are visited one at a time with warp
+// votes, the shifted i-atoms staged in shared memory.  Compiled with
+// --fmad=false; r^2 = fma(dz, dz, fma(dy, dy, dx dx)) is written out with
+// explicit multiply-adds, so it rounds exactly like the CPU restatement.
 #include "nbx_internal.cuh"
 
 #include <algorithm>
@@ -62,7 +65,9 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
     // the next group's record is loaded while the current one is tested
     Cj4 c4n = cj4[s.cj4_start + warp];
     const float  sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
-    const float2 neg_inner2 = make_float2(-inner2, -inner2), neg_outer2 = make_float2(-outer2, -outer2);
+    // r^2 and the squared cut-offs are non-negative floats: r^2 < c^2 exactly when the difference
+    // of their bit patterns is negative
+    const unsigned inner_bits = __float_as_uint(inner2), outer_bits = __float_as_uint(outer2);
     float2       xi[kNcl], yi[kNcl], zi[kNcl];
 #pragma unroll
     for (int c = 0; c < kNcl; c++)
@@ -112,8 +117,9 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
             }
             // per lane: bit i set when this lane's pair of half 0 / half 1 with i-cluster i is in
             // range.  All 8 i-clusters are tested (no per-cluster branch); the in-range flag is the
-            // sign bit of r^2 - cutoff^2 (exactly the sign of the difference: r^2 < cutoff^2), shifted
-            // into the masks from the top i-cluster down, one funnel shift per flag.
+            // sign of the bit-pattern difference r^2 - cutoff^2, shifted into the masks from the top
+            // i-cluster down, one funnel shift per flag.  r^2 = fma(dz, dz, fma(dy, dy, dx dx)), the
+            // contraction of the reference's norm2 in its prune kernel.
             unsigned in0 = 0u, in1 = 0u, out0 = 0u, out1 = 0u;
 #pragma unroll
             for (int i = kNcl - 1; i >= 0; i--)
@@ -121,13 +127,11 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
                 const float2 dx = p_sub(xi[i], xj[jm]);
                 const float2 dy = p_sub(yi[i], yj[jm]);
                 const float2 dz = p_sub(zi[i], zj[jm]);
-                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                const float2 di = __fadd2_rn(r2, neg_inner2);
-                const float2 dd = __fadd2_rn(r2, neg_outer2);
-                in0             = __funnelshift_l(__float_as_uint(di.x), in0, 1);
-                in1             = __funnelshift_l(__float_as_uint(di.y), in1, 1);
-                out0            = __funnelshift_l(__float_as_uint(dd.x), out0, 1);
-                out1            = __funnelshift_l(__float_as_uint(dd.y), out1, 1);
+                const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+                in0             = __funnelshift_l(__float_as_uint(r2.x) - inner_bits, in0, 1);
+                in1             = __funnelshift_l(__float_as_uint(r2.y) - inner_bits, in1, 1);
+                out0            = __funnelshift_l(__float_as_uint(r2.x) - outer_bits, out0, 1);
+                out1            = __funnelshift_l(__float_as_uint(r2.y) - outer_bits, out1, 1);
             }
             // any pair of the (i-cluster, half) within range: OR over the lanes
             const unsigned sh = jm * kNcl;
@@ -226,7 +230,7 @@ __device__ void prune_entry_rolling(const Sci& s, const Cj4* cj4, const unsigned
                     {
                         const float4 xi = xib[i * kCl + ii];
                         const float  dx = xi.x - xj[w][jm].x, dy = xi.y - xj[w][jm].y, dz = xi.z - xj[w][jm].z;
-                        const float  r2 = dx * dx + dy * dy + dz * dz;
+                        const float  r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                         if (__any_sync(full, r2 < inner2))
                         {
                             nw[w] |= bit;

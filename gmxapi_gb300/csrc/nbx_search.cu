@@ -433,11 +433,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_count(DeviceView
     }
 }
 
+constexpr int kExclStage = 256;  // topology exclusions of a cell's i-atoms staged in shared memory
+
 struct EmitSmem
 {
-    unsigned need[2 * kMaxCj4PerEntry / 32];  // per (cj4, half): exclusion mask needed
-    int      diag_pos[kNcl];                   // list positions of the diagonal j-clusters
-    int      jl[kEmitStage];                   // the entry's j-clusters (short entries)
+    unsigned      need[2 * kMaxCj4PerEntry / 32];  // per (cj4, half): exclusion mask needed
+    int           diag_pos[kNcl];                   // list positions of the diagonal j-clusters
+    int           jl[kEmitStage];                   // the entry's j-clusters (short entries)
+    unsigned char jm[kEmitStage];                   // and their i-cluster masks
+    int           ex_j[kExclStage];                 // excluded partner's grid slot (-1: itself)
+    unsigned char ex_i[kExclStage];                 // the i-atom's slot within the cell
 };
 
 // Emit pass: one warp per i-cell turns its search records into list entries at the offsets of the
@@ -465,6 +470,45 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
     int       cj4_out = v.cj4_offset[ci];
     const int*           rec_cj = v.rec_cj + (size_t)ci * v.rec_cap;
     const unsigned char* rec_m  = v.rec_m + (size_t)ci * v.rec_cap;
+    // the topology exclusions of the cell's i-atoms as (i-slot, partner grid slot) pairs, looked up
+    // once for all entries of the cell (when they fit; else each entry walks the exclusion lists)
+    int nex = 0;
+    for (int base = 0; base < kSc && nent > 0; base += 32)
+    {
+        const int i     = base + lane;
+        const int iAtom = v.atom_indices[ci * kSc + i];
+        int       x0 = 0, x1 = 0;
+        if (iAtom >= 0)
+        {
+            x0 = v.excl_index[iAtom];
+            x1 = v.excl_index[iAtom + 1];
+        }
+        const int cnt  = x1 - x0;
+        int       incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int t = __shfl_up_sync(full, incl, o);
+            if (lane >= o)
+            {
+                incl += t;
+            }
+        }
+        const int tot = __shfl_sync(full, incl, 31);
+        if (nex + tot <= kExclStage)
+        {
+            const int off = nex + incl - cnt;
+            for (int x = x0; x < x1; x++)
+            {
+                const int jAtom          = v.excl_list[x];
+                sm.ex_j[off + (x - x0)] = (jAtom == iAtom) ? -1 : v.cells[jAtom];
+                sm.ex_i[off + (x - x0)] = (unsigned char)i;
+            }
+        }
+        nex += tot;
+    }
+    const bool ex_staged = nex <= kExclStage;
+    __syncwarp();
     for (int k = 0; k < nent; k++)
     {
         const int  code  = v.rec_ent[ci * kMaxEntriesPerCell + k];
@@ -507,6 +551,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
             if (staged)
             {
                 sm.jl[p] = cj;
+                sm.jm[p] = rec_m[p];
             }
             // the diagonal j-clusters (the i-cell's own clusters, central shift)
             if (excludeSubDiagonal && (cj >> 3) == ci)
@@ -515,7 +560,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
                 atomicOr(&sm.need[(2 * (p / kJg)) / 32], 3u << ((2 * (p / kJg)) % 32));
             }
         }
-        const int* jlist = staged ? sm.jl : rec_cj;
+        const int*           jlist = staged ? sm.jl : rec_cj;
+        const unsigned char* mlist = staged ? sm.jm : rec_m;
+        int                  basei = 0;  // first exclusion mask of this entry
+        // the mask of a flagged (cj4, half) slot: masks are allocated to the flagged slots in order
+        auto excl_of_slot = [&](int slot) {
+            int e = basei;
+            for (int w = 0; w < slot / 32; w++)
+            {
+                e += __popc(sm.need[w]);
+            }
+            return e + __popc(sm.need[slot / 32] & ((1u << (slot % 32)) - 1u));
+        };
         __syncwarp();
         __threadfence_block();
         if (lane == 0)
@@ -534,69 +590,82 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
         // pass A: flag (cj4, half) pairs that need an exclusion mask; pass B (rep 1): clear the bits
         for (int rep = 0; rep < 2; rep++)
         {
-            for (int i = lane; i < kSc; i += 32)
-            {
-                const int iIndex = ci * kSc + i;
-                const int iAtom  = v.atom_indices[iIndex];
-                if (iAtom < 0)
+            // one excluded atom pair (i-slot i of the cell, partner at grid slot jIndex)
+            auto exclude = [&](int i, int jIndex) {
+                if (diagRemoved && jIndex <= ci * kSc + i)
                 {
-                    continue;
+                    return;
                 }
-                const int iCluster = i / kCl;
-                for (int x = v.excl_index[iAtom]; x < v.excl_index[iAtom + 1]; x++)
+                const int jCluster = jIndex / kCl;
+                if (jCluster < cjFirst || jCluster > cjLast)
                 {
-                    const int jAtom = v.excl_list[x];
-                    if (jAtom == iAtom)
+                    return;
+                }
+                int a = 0, b = nj - 1, index = -1;
+                while (a <= b)
+                {
+                    const int m  = (a + b) >> 1;
+                    const int cm = jlist[m];
+                    if (cm == jCluster)
                     {
-                        continue;
+                        index = m;
+                        break;
                     }
-                    const int jIndex = v.cells[jAtom];
-                    if (diagRemoved && jIndex <= ci * kSc + i)
+                    if (cm < jCluster)
                     {
-                        continue;
-                    }
-                    const int jCluster = jIndex / kCl;
-                    if (jCluster < cjFirst || jCluster > cjLast)
-                    {
-                        continue;
-                    }
-                    int a = 0, b = nj - 1, index = -1;
-                    while (a <= b)
-                    {
-                        const int m  = (a + b) >> 1;
-                        const int cm = jlist[m];
-                        if (cm == jCluster)
-                        {
-                            index = m;
-                            break;
-                        }
-                        if (cm < jCluster)
-                        {
-                            a = m + 1;
-                        }
-                        else
-                        {
-                            b = m - 1;
-                        }
-                    }
-                    if (index < 0 || !((rec_m[index] >> iCluster) & 1u))
-                    {
-                        continue;
-                    }
-                    const int      j4       = cj4_out + index / kJg;
-                    const unsigned pairMask = 1u << ((index % kJg) * kNcl + iCluster);
-                    const int      innerI   = i & (kCl - 1);
-                    const int      innerJ   = jIndex & (kCl - 1);
-                    const int      jHalf    = innerJ / (kCl / kSplit);
-                    const int      slot     = 2 * (index / kJg) + jHalf;
-                    if (rep == 0)
-                    {
-                        atomicOr(&sm.need[slot / 32], 1u << (slot % 32));
+                        a = m + 1;
                     }
                     else
                     {
-                        const int ei = v.cj4[j4].imei[jHalf].excl_ind;
-                        atomicAnd(&v.excl[ei].pair[(innerJ & (kCl / kSplit - 1)) * kCl + innerI], ~pairMask);
+                        b = m - 1;
+                    }
+                }
+                const int iCluster = i / kCl;
+                if (index < 0 || !((mlist[index] >> iCluster) & 1u))
+                {
+                    return;
+                }
+                const unsigned pairMask = 1u << ((index % kJg) * kNcl + iCluster);
+                const int      innerI   = i & (kCl - 1);
+                const int      innerJ   = jIndex & (kCl - 1);
+                const int      jHalf    = innerJ / (kCl / kSplit);
+                const int      slot     = 2 * (index / kJg) + jHalf;
+                if (rep == 0)
+                {
+                    atomicOr(&sm.need[slot / 32], 1u << (slot % 32));
+                }
+                else
+                {
+                    const int ei = excl_of_slot(slot);
+                    atomicAnd(&v.excl[ei].pair[(innerJ & (kCl / kSplit - 1)) * kCl + innerI], ~pairMask);
+                }
+            };
+            if (ex_staged)
+            {
+                for (int t = lane; t < nex; t += 32)
+                {
+                    if (sm.ex_j[t] >= 0)
+                    {
+                        exclude(sm.ex_i[t], sm.ex_j[t]);
+                    }
+                }
+            }
+            else
+            {
+                for (int i = lane; i < kSc; i += 32)
+                {
+                    const int iAtom = v.atom_indices[ci * kSc + i];
+                    if (iAtom < 0)
+                    {
+                        continue;
+                    }
+                    for (int x = v.excl_index[iAtom]; x < v.excl_index[iAtom + 1]; x++)
+                    {
+                        const int jAtom = v.excl_list[x];
+                        if (jAtom != iAtom)
+                        {
+                            exclude(i, v.cells[jAtom]);
+                        }
                     }
                 }
             }
@@ -609,7 +678,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
                 {
                     nneed += __popc(sm.need[w]);
                 }
-                int basei = 0;
                 if (lane == 0 && nneed > 0)
                 {
                     basei = atomicAdd(&v.hdr->num_excl, nneed);
@@ -651,7 +719,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
                     {
                         continue;
                     }
-                    const int j4  = cj4_out + pos / kJg;
                     const int off = pos % kJg;
                     // lane = (jIndexInPart, i): word jIndexInPart*8 + i
                     const int jip = lane >> 3, ii = lane & 7;
@@ -660,7 +727,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
                         const int jOffset = part * (kCl / kSplit);
                         if (ii >= jOffset + jip)
                         {
-                            const int ei = v.cj4[j4].imei[part].excl_ind;
+                            const int ei = excl_of_slot(2 * (pos / kJg) + part);
                             atomicAnd(&v.excl[ei].pair[jip * kCl + ii], ~(1u << (off * kNcl + dj)));
                         }
                     }

@@ -118,6 +118,8 @@ int nbx_update_pairlist(nbx_handle* h, const float* x);
 int nbx_compute(nbx_handle* h, const float* x, float* f, double* energies, double* virial);
 
 /* ---- device-resident interface (pointers into device memory, asynchronous on the handle's stream) ---- */
+/* Work queued on the previous stream is waited for, except when the new stream is capturing a CUDA
+ * graph (then the capturing code orders the streams). */
 int nbx_set_stream(nbx_handle* h, void* cuda_stream);
 void* nbx_get_stream(nbx_handle* h);
 /* nbnxn_put_on_grid + constructPairlist (src/gromacs/nbnxm/nbnxm.cpp:58-74, pairlist.cpp:4247-4262),

@@ -1337,12 +1337,16 @@ int orc_balance(orc_ctx* c, int min_ci_balanced)
 
 /* ------------------------------------------------------------------ prune */
 
+/* r^2 of the prune kernel.  The reference's prune-only kernel computes norm2(rv)
+ * (nbnxm_cuda_kernel_pruneonly.cuh:245) in a unit built with nvcc's default
+ * multiply-add contraction; the restatement fixes one contraction order,
+ * fma(dz, dz, fma(dy, dy, dx * dx)), which the GPU prune uses explicitly. */
 static float pair_r2(const float* xi, const float* xj)
 {
     float dx = xi[0] - xj[0];
     float dy = xi[1] - xj[1];
     float dz = xi[2] - xj[2];
-    return dx * dx + dy * dy + dz * dz;
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
 }
 
 /* cuda/nbnxm_cuda_kernel_pruneonly.cuh:104-279, one "warp" = (8 i-atoms) x

@@ -166,3 +166,44 @@ def test_adjoint_rejects_too_many_types():
     with pytest.raises(Exception, match="15"):
         f.sum().backward()
     eng.close()
+
+
+def test_gradient_step_captured_in_a_cuda_graph_matches_eager():
+    """The whole force-matching step (Lorentz-Berthelot table, forward, loss, backward) captured in
+    one CUDA graph and replayed gives the eager gradients (the engine's stream switch must not
+    synchronise while the graph is being captured)."""
+    s = CASES["liquid2000"]()
+    eng = DifferentiableNonbonded(s)
+    x = torch.tensor(s.x, device=DEV, requires_grad=True)
+    q = torch.tensor(s.q, device=DEV, requires_grad=True)
+    sig = torch.tensor(s.sigma, dtype=torch.float64, device=DEV, requires_grad=True)
+    eps = torch.tensor(s.epsilon, dtype=torch.float64, device=DEV, requires_grad=True)
+    with torch.no_grad():
+        f_t, _ = eng(x, q * 1.02, lorentz_berthelot_nbfp(sig * 0.98, eps * 1.03))
+    eng.search(x)
+
+    def step():
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        ((f - f_t) ** 2).sum().backward()
+
+    step()
+    eager = [t.grad.clone() for t in (x, q, sig, eps)]
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            for t in (x, q, sig, eps):
+                t.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    for t in (x, q, sig, eps):
+        t.grad = None
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, t in zip(eager, (x, q, sig, eps)):
+        assert rel_rms(t.grad.cpu(), a.cpu()) < 1e-5  # atomics sum in another order
+    eng.close()
