@@ -52,7 +52,8 @@ EXPORTED = [
     "nbx_get_options", "nbx_set_force_accumulate", "nbx_get_force_accumulate", "nbx_leapfrog_create", "nbx_leapfrog_destroy",
     "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
     "nbx_md_run_device", "nbx_fep_enable", "nbx_fep_set_lambda", "nbx_fep_get_energies", "nbx_fep_energies_device",
-    "nbx_fep_disable", "nbx_pme_create_lj", "nbx_ewald_coefficient_lj",
+    "nbx_fep_disable", "nbx_pme_create_lj", "nbx_ewald_coefficient_lj", "nbx_lb_table_device",
+    "nbx_lb_table_backward_device",
 ]
 
 
@@ -205,6 +206,8 @@ def load():
     L.nbx_batch_set_force_kernel.argtypes = [vp, C.c_int, C.c_int]
     L.nbx_backward_device.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.nbx_set_parameters_device.argtypes = [vp, vp, vp]
+    L.nbx_lb_table_device.argtypes = [vp, vp, C.c_int, vp, vp]
+    L.nbx_lb_table_backward_device.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp]
     L.nbx_ewald_coefficient.argtypes = [C.c_float, C.c_float]
     L.nbx_ewald_coefficient.restype = C.c_float
     L.nbx_pme_grid_size.argtypes = [fp, C.c_float, ip]

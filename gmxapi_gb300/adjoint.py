@@ -24,19 +24,60 @@ from torch.autograd.function import once_differentiable
 from .nblib import CoulombType, ForceCalculator, NBKernelOptions
 
 
+class _LorentzBerthelot(torch.autograd.Function):
+    """The combination rule on the GPU: one kernel forward, one kernel backward (float64)."""
+
+    @staticmethod
+    def forward(ctx, sigma, epsilon):
+        from . import _lib
+
+        nt = sigma.numel()
+        table = torch.empty(nt, nt, 2, dtype=torch.float64, device=sigma.device)
+        stream = torch.cuda.current_stream(sigma.device).cuda_stream
+        code = _lib.load().nbx_lb_table_device(sigma.data_ptr(), epsilon.data_ptr(), nt, table.data_ptr(), stream)
+        if code != 0:
+            raise RuntimeError(f"nbx_lb_table_device failed ({code})")
+        ctx.save_for_backward(sigma, epsilon)
+        return table
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, g):
+        from . import _lib
+
+        sigma, epsilon = ctx.saved_tensors
+        nt = sigma.numel()
+        g = g.to(torch.float64).contiguous()
+        gs = torch.empty_like(sigma)
+        ge = torch.empty_like(epsilon)
+        stream = torch.cuda.current_stream(sigma.device).cuda_stream
+        code = _lib.load().nbx_lb_table_backward_device(sigma.data_ptr(), epsilon.data_ptr(), nt, g.data_ptr(),
+                                                        gs.data_ptr(), ge.data_ptr(), stream)
+        if code != 0:
+            raise RuntimeError(f"nbx_lb_table_backward_device failed ({code})")
+        return gs, ge
+
+
 def lorentz_berthelot_nbfp(sigma: torch.Tensor, epsilon: torch.Tensor) -> torch.Tensor:
     """(ntypes, ntypes, 2) table {6*C6, 12*C12} from per-type sigma and epsilon.
 
     sigma_ij = (sigma_i + sigma_j) / 2, epsilon_ij = sqrt(epsilon_i epsilon_j),
     C6 = 4 eps s^6, C12 = 4 eps s^12 (the combination nblib applies in
-    api/nblib/particletype.cpp and gmxsetup.cpp:143-166).
+    api/nblib/particletype.cpp and gmxsetup.cpp:143-166).  float64 CUDA vectors go through one
+    kernel each way; other tensors (the FP64 reference on the CPU) through torch operations.  The
+    table is symmetric by construction and is marked so (the engine then skips symmetrising it).
     """
-    sig = 0.5 * (sigma[:, None] + sigma[None, :])
-    eps = torch.sqrt(epsilon[:, None] * epsilon[None, :])
-    s6 = sig**6
-    c6 = 4.0 * eps * s6
-    c12 = c6 * s6
-    return torch.stack((6.0 * c6, 12.0 * c12), dim=-1)
+    if sigma.is_cuda and sigma.dtype == torch.float64 and epsilon.dtype == torch.float64:
+        table = _LorentzBerthelot.apply(sigma.contiguous(), epsilon.contiguous())
+    else:
+        sig = 0.5 * (sigma[:, None] + sigma[None, :])
+        eps = torch.sqrt(epsilon[:, None] * epsilon[None, :])
+        s6 = sig**6
+        c6 = 4.0 * eps * s6
+        c12 = c6 * s6
+        table = torch.stack((6.0 * c6, 12.0 * c12), dim=-1)
+    table._symmetric_types = True
+    return table
 
 
 def static_list_options(rc: float = 0.9) -> NBKernelOptions:
@@ -131,7 +172,8 @@ class DifferentiableNonbonded:
             raise ValueError("x must be (N, 3), q (N,) and nbfp (ntypes, ntypes, 2)")
         x = x.to(torch.float32).contiguous()
         q = q.to(torch.float32).contiguous()
-        nbfp = (0.5 * (nbfp + nbfp.transpose(0, 1))).contiguous()
+        if not getattr(nbfp, "_symmetric_types", False):
+            nbfp = (0.5 * (nbfp + nbfp.transpose(0, 1))).contiguous()
         if search:
             self.search(x)
         return _NonbondedFunction.apply(x, q, nbfp, self)

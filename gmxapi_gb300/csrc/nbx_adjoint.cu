@@ -31,6 +31,7 @@ namespace
 {
 
 constexpr int kAdjThreads    = 256;
+constexpr int kAdjBlocksPerSm = 2;  // 16 warps per SM (128 registers a thread, no spills)
 constexpr int kAdjWarps      = kAdjThreads / 32;
 constexpr int kAdjMaxTypes1  = 16;
 // Up to this many types (+ the dummy type) every warp keeps one type-pair gradient table per
@@ -67,127 +68,159 @@ struct AdjPtrs
     float4*       dnb;
 };
 
+// One atom pair (i-atom ii of i-cluster c, the lane's j-atom): recomputes the pair terms, adds
+// the i-side gradients to the lane's accumulator slot acc[(c * 8 + ii) * 4 + jj] (shared memory,
+// one slot per lane and i-atom: no conflicts), the j-side ones to dj*, and the type-pair gradient
+// to the lane's table.
+template<bool kEwald, bool kExcl>
+__device__ __forceinline__ void adj_pair(const DeviceView& v, const float2* __restrict__ nbfp_s, float2* ttab,
+                                         const float4* __restrict__ xis, const float4* __restrict__ gis, float4* acc,
+                                         int c, const float4 xj, const float4 gj, int tj, unsigned wj, bool diag_cj,
+                                         int h, int ii, int jj, const AdjConsts& k, float pbeta, float beta2l2,
+                                         float c2b, float b2c2b, float& djx, float& djy, float& djz, float& djq)
+{
+    const int    nt1 = v.ntypes1;
+    const float4 xi  = xis[c * kCl + ii];
+    const float4 gi  = gis[c * kCl + ii];
+    const int    ti  = __float_as_int(gi.w);
+    const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    float        r2 = dx * dx + dy * dy + dz * dz;
+    bool         in_range;
+    float        int_bit;
+    if (kExcl)
+    {
+        // the diagonal cluster pair counts j > i only
+        const bool self_lower = diag_cj && (c == (int)(wj >> 24)) && (h * (kCl / kSplit) + jj <= ii);
+        in_range              = (r2 < v.rc2) && !self_lower;
+        int_bit               = (wj & (1u << c)) ? 1.0f : 0.0f;
+    }
+    else
+    {
+        in_range = r2 < v.rc2;
+        int_bit  = 1.0f;
+    }
+    r2                   = fmaxf(r2, kMinDist2);
+    float       rinv     = rsqrtf(r2);
+    rinv                 = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
+    const float  rinv2   = rinv * rinv;
+    const float2 lj      = nbfp_s[ti * nt1 + tj];
+    float        rinv6   = rinv2 * rinv2 * rinv2;
+    if (kExcl)
+    {
+        rinv6 *= int_bit;
+    }
+    const float vrep    = lj.y * rinv6 * rinv6;
+    const float vdisp   = lj.x * rinv6;
+    const float phi_lj  = (vrep - vdisp) * rinv2;
+    const float dphi_lj = (4.0f * vdisp - 7.0f * vrep) * rinv2 * rinv2;
+    float       psi, dpsi, hq;  // Coulomb phi / qq, its s-derivative, energy / qq
+    if (kEwald)
+    {
+        const float r    = r2 * rinv;
+        const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
+        const float poly = erfc_poly(t);
+        const float expm = fast_ex2(-beta2l2 * r2);
+        const float tp   = t * poly;
+        psi              = expm * fmaf(tp, rinv, c2b) * rinv2;
+        hq               = tp * expm * rinv - int_bit * v.sh_ewald;
+        if (kExcl)
+        {
+            psi -= (1.0f - int_bit) * rinv * rinv2;
+            hq -= (1.0f - int_bit) * rinv;
+        }
+        dpsi = -(1.5f * psi + b2c2b * expm) * rinv2;
+    }
+    else
+    {
+        const float r3 = rinv * rinv2;
+        psi            = int_bit * r3 - 2.0f * v.k_rf;
+        dpsi           = -1.5f * int_bit * r3 * rinv2;
+        hq             = int_bit * rinv + v.k_rf * r2 - v.c_rf;
+    }
+    const float qq   = v.epsfac * xi.w * xj.w;
+    const float phi  = fmaf(qq, psi, phi_lj);
+    const float dphi = fmaf(qq, dpsi, dphi_lj);
+    const float gx = gi.x - gj.x, gy = gi.y - gj.y, gz = gi.z - gj.z;
+    const float gr   = gx * dx + gy * dy + gz * dz;
+    const float coef = 2.0f * dphi * gr - fmaf(k.gE_c * qq, psi, k.gE_lj * phi_lj);
+    float       ux   = fmaf(phi, gx, coef * dx);
+    float       uy   = fmaf(phi, gy, coef * dy);
+    float       uz   = fmaf(phi, gz, coef * dz);
+    float       wq   = v.epsfac * fmaf(psi, gr, k.gE_c * hq);
+    ux               = in_range ? ux : 0.0f;
+    uy               = in_range ? uy : 0.0f;
+    uz               = in_range ? uz : 0.0f;
+    wq               = in_range ? wq : 0.0f;
+    float4* const ai = &acc[(c * kCl + ii) * 4 + jj];
+    float4        av = *ai;
+    av.x += ux;
+    av.y += uy;
+    av.z += uz;
+    av.w = fmaf(wq, xj.w, av.w);
+    *ai  = av;
+    djx -= ux;
+    djy -= uy;
+    djz -= uz;
+    djq = fmaf(wq, xi.w, djq);
+    // dL/d(6C6), dL/d(12C12) of this type pair
+    if (in_range && int_bit != 0.0f)
+    {
+        const float dc12 = fmaf(gr * rinv6, rinv6 * rinv2, k.gE_lj * (rinv6 * rinv6 + v.cpot12) * (1.0f / 12.0f));
+        const float dc6  = -fmaf(gr * rinv6, rinv2, k.gE_lj * (rinv6 + v.cpot6) * (1.0f / 6.0f));
+        float2*     slot = &ttab[ti * nt1 + tj];
+        atomicAdd(&slot->x, dc6);
+        atomicAdd(&slot->y, dc12);
+    }
+}
+
+// One warp half's j-clusters of a cj4 group: per j-cluster with set bits, the set i-clusters are
+// visited two at a time (two independent pair computations in one basic block), the j-side sums
+// reduced over the 8 i-lanes and added with one vector red per j-atom.
 template<bool kEwald, bool kExcl>
 __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __restrict__ jx,
                                          const float4* __restrict__ jg, const float2* __restrict__ nbfp_s,
                                          float2* ttab, const float4* __restrict__ xis, const float4* __restrict__ gis,
-                                         const float4* __restrict__ gnb, float4* dnb, const int cj_lane,
-                                         unsigned im, unsigned wexcl, int h, int sci, bool central, int ii, int jj,
-                                         float dxa[kNcl], float dya[kNcl], float dza[kNcl], float dqa[kNcl],
-                                         const AdjConsts& k, float pbeta, float beta2l2, float c2b, float b2c2b)
+                                         float4* acc, float4* dnb, const int cj_lane, unsigned im, unsigned wexcl,
+                                         int h, int sci, bool central, int ii, int jj, const AdjConsts& k,
+                                         float pbeta, float beta2l2, float c2b, float b2c2b)
 {
     const unsigned full = 0xffffffffu;
-    const int      nt1  = v.ntypes1;
 #pragma unroll 1
     for (int jm = 0; jm < kJg; jm++)
     {
-        const unsigned imj = (im >> (jm * kNcl)) & 0xffu;
-        const int      cj  = __shfl_sync(full, cj_lane, jm);
-        if (!imj)
+        unsigned   rem = (im >> (jm * kNcl)) & 0xffu;
+        const int  cj  = __shfl_sync(full, cj_lane, jm);
+        if (!rem)
         {
             continue;
         }
-        const int      aj = cj * kCl + h * (kCl / kSplit) + jj;
+        const int    aj = cj * kCl + h * (kCl / kSplit) + jj;
         // the cj4 group's 32 j-atoms are staged in shared memory (slot jm * 8 + atom)
-        const int      sj = jm * kCl + h * (kCl / kSplit) + jj;
-        const float4   xj = jx[sj];
-        const float4   gj = jg[sj];
-        const int      tj = __float_as_int(gj.w);
-        const unsigned wj = wexcl >> (jm * kNcl);
+        const int    sj = jm * kCl + h * (kCl / kSplit) + jj;
+        const float4 xj = jx[sj];
+        const float4 gj = jg[sj];
+        const int    tj = __float_as_int(gj.w);
+        // exclusion bits of this j-cluster's i-clusters; bits 24.. carry the diagonal i-cluster
+        const bool     diag_cj = kExcl && central && (cj >= sci * kNcl) && (cj < sci * kNcl + kNcl);
+        const unsigned wj      = kExcl ? (((wexcl >> (jm * kNcl)) & 0xffu) | ((unsigned)(cj - sci * kNcl) << 24)) : 0u;
         float          djx = 0.0f, djy = 0.0f, djz = 0.0f, djq = 0.0f;
-#pragma unroll
-        for (int c = 0; c < kNcl; c++)
+        while (rem)
         {
-            if (!(imj & (1u << c)))
+            const int ca = __ffs(rem) - 1;
+            rem &= rem - 1;
+            if (rem)
             {
-                continue;
-            }
-            const float4 xi = xis[c * kCl + ii];
-            const float4 gi = gis[c * kCl + ii];
-            const int    ti = __float_as_int(gi.w);
-            const float  dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-            float        r2 = dx * dx + dy * dy + dz * dz;
-            bool         in_range;
-            float        int_bit;
-            if (kExcl)
-            {
-                const bool self_lower = central && (sci * kNcl + c == cj) && (h * (kCl / kSplit) + jj <= ii);
-                in_range              = (r2 < v.rc2) && !self_lower;
-                int_bit               = (wj & (1u << c)) ? 1.0f : 0.0f;
+                const int cb = __ffs(rem) - 1;
+                rem &= rem - 1;
+                adj_pair<kEwald, kExcl>(v, nbfp_s, ttab, xis, gis, acc, ca, xj, gj, tj, wj, diag_cj, h, ii, jj, k,
+                                        pbeta, beta2l2, c2b, b2c2b, djx, djy, djz, djq);
+                adj_pair<kEwald, kExcl>(v, nbfp_s, ttab, xis, gis, acc, cb, xj, gj, tj, wj, diag_cj, h, ii, jj, k,
+                                        pbeta, beta2l2, c2b, b2c2b, djx, djy, djz, djq);
             }
             else
             {
-                in_range = r2 < v.rc2;
-                int_bit  = 1.0f;
-            }
-            r2                  = fmaxf(r2, kMinDist2);
-            float       rinv    = rsqrtf(r2);
-            rinv                = rinv * (1.5f - 0.5f * r2 * rinv * rinv);
-            const float rinv2   = rinv * rinv;
-            const float2 lj     = nbfp_s[ti * nt1 + tj];
-            float        rinv6  = rinv2 * rinv2 * rinv2;
-            if (kExcl)
-            {
-                rinv6 *= int_bit;
-            }
-            const float vrep    = lj.y * rinv6 * rinv6;
-            const float vdisp   = lj.x * rinv6;
-            const float phi_lj  = (vrep - vdisp) * rinv2;
-            const float dphi_lj = (4.0f * vdisp - 7.0f * vrep) * rinv2 * rinv2;
-            float       psi, dpsi, hq;  // Coulomb phi / qq, its s-derivative, energy / qq
-            if (kEwald)
-            {
-                const float r    = r2 * rinv;
-                const float t    = fast_rcp(fmaf(pbeta, r, 1.0f));
-                const float poly = erfc_poly(t);
-                const float expm = fast_ex2(-beta2l2 * r2);
-                const float tp   = t * poly;
-                psi              = expm * fmaf(tp, rinv, c2b) * rinv2;
-                hq               = tp * expm * rinv - int_bit * v.sh_ewald;
-                if (kExcl)
-                {
-                    psi -= (1.0f - int_bit) * rinv * rinv2;
-                    hq -= (1.0f - int_bit) * rinv;
-                }
-                dpsi = -(1.5f * psi + b2c2b * expm) * rinv2;
-            }
-            else
-            {
-                const float r3 = rinv * rinv2;
-                psi            = int_bit * r3 - 2.0f * v.k_rf;
-                dpsi           = -1.5f * int_bit * r3 * rinv2;
-                hq             = int_bit * rinv + v.k_rf * r2 - v.c_rf;
-            }
-            const float qq   = v.epsfac * xi.w * xj.w;
-            const float phi  = fmaf(qq, psi, phi_lj);
-            const float dphi = fmaf(qq, dpsi, dphi_lj);
-            const float gx = gi.x - gj.x, gy = gi.y - gj.y, gz = gi.z - gj.z;
-            const float gr   = gx * dx + gy * dy + gz * dz;
-            const float coef = 2.0f * dphi * gr - fmaf(k.gE_c * qq, psi, k.gE_lj * phi_lj);
-            float       ux   = fmaf(phi, gx, coef * dx);
-            float       uy   = fmaf(phi, gy, coef * dy);
-            float       uz   = fmaf(phi, gz, coef * dz);
-            float       wq   = v.epsfac * fmaf(psi, gr, k.gE_c * hq);
-            ux               = in_range ? ux : 0.0f;
-            uy               = in_range ? uy : 0.0f;
-            uz               = in_range ? uz : 0.0f;
-            wq               = in_range ? wq : 0.0f;
-            dxa[c] += ux;
-            dya[c] += uy;
-            dza[c] += uz;
-            dqa[c] = fmaf(wq, xj.w, dqa[c]);
-            djx -= ux;
-            djy -= uy;
-            djz -= uz;
-            djq = fmaf(wq, xi.w, djq);
-            // dL/d(6C6), dL/d(12C12) of this type pair
-            if (in_range && int_bit != 0.0f)
-            {
-                const float dc12 = fmaf(gr * rinv6, rinv6 * rinv2, k.gE_lj * (rinv6 * rinv6 + v.cpot12) * (1.0f / 12.0f));
-                const float dc6  = -fmaf(gr * rinv6, rinv2, k.gE_lj * (rinv6 + v.cpot6) * (1.0f / 6.0f));
-                float2*     slot = &ttab[ti * nt1 + tj];
-                atomicAdd(&slot->x, dc6);
-                atomicAdd(&slot->y, dc12);
+                adj_pair<kEwald, kExcl>(v, nbfp_s, ttab, xis, gis, acc, ca, xj, gj, tj, wj, diag_cj, h, ii, jj, k,
+                                        pbeta, beta2l2, c2b, b2c2b, djx, djy, djz, djq);
             }
         }
 #pragma unroll
@@ -211,8 +244,8 @@ __device__ __forceinline__ void adj_half(const DeviceView& v, const float4* __re
 template<bool kEwald>
 __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p, const Sci& s,
                                           const float2* __restrict__ nbfp_s, float2* ttab, float4* xis, float4* gis,
-                                          float4* jx, float4* jg, int lane, const AdjConsts& k, float pbeta,
-                                          float beta2l2, float c2b, float b2c2b, double* gnbfp)
+                                          float4* jx, float4* jg, float4* acc, int lane, const AdjConsts& k,
+                                          float pbeta, float beta2l2, float c2b, float b2c2b, double* gnbfp)
 {
     const unsigned full    = 0xffffffffu;
     const int      ii      = lane & 7;
@@ -232,13 +265,11 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
         xis[m]         = make_float4(x.x + sx, x.y + sy, x.z + sz, x.w);
         gis[m]         = make_float4(g.x, g.y, g.z, __int_as_float(p.tgrid[a]));
     }
-    __syncwarp();
-    float dxa[kNcl], dya[kNcl], dza[kNcl], dqa[kNcl];
-#pragma unroll
-    for (int c = 0; c < kNcl; c++)
+    for (int m = lane; m < kSc * 4; m += 32)
     {
-        dxa[c] = dya[c] = dza[c] = dqa[c] = 0.0f;
+        acc[m] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
+    __syncwarp();
     // software pipeline over the cj4 groups, as in the force kernel: the next group's
     // record is loaded when a group starts, its 32 j-atoms after the group's first half
     int4   rec_ime{};
@@ -285,33 +316,24 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
             }
             if (exi == 0)
             {
-                adj_half<kEwald, false>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, p.gnb, p.dnb, cj_lane, im, 0u, h, s.sci,
-                                        central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                adj_half<kEwald, false>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, acc, p.dnb, cj_lane, im, 0u, h, s.sci,
+                                        central, ii, jj, k, pbeta, beta2l2, c2b, b2c2b);
             }
             else
             {
                 const unsigned wexcl = p.excl[exi].pair[lane];
-                adj_half<kEwald, true>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, p.gnb, p.dnb, cj_lane, im, wexcl, h,
-                                       s.sci, central, ii, jj, dxa, dya, dza, dqa, k, pbeta, beta2l2, c2b, b2c2b);
+                adj_half<kEwald, true>(v, jx, jg, nbfp_s, ttab_lane, xis, gis, acc, p.dnb, cj_lane, im, wexcl, h,
+                                       s.sci, central, ii, jj, k, pbeta, beta2l2, c2b, b2c2b);
             }
         }
     }
-#pragma unroll
-    for (int c = 0; c < kNcl; c++)
+    // the i-side sums: the 4 lane slots of every i-atom, one vector red per atom
+    __syncwarp();
+    for (int m = lane; m < kSc; m += 32)
     {
-        float ax = dxa[c], ay = dya[c], az = dza[c], aq = dqa[c];
-        for (int o = 8; o < 32; o <<= 1)
-        {
-            ax += __shfl_xor_sync(full, ax, o);
-            ay += __shfl_xor_sync(full, ay, o);
-            az += __shfl_xor_sync(full, az, o);
-            aq += __shfl_xor_sync(full, aq, o);
-        }
-        if (jj == 0)
-        {
-            float4* dst = &p.dnb[(s.sci * kNcl + c) * kCl + ii];
-            red_add_v4(dst, ax, ay, az, aq);
-        }
+        const float4 a0 = acc[m * 4], a1 = acc[m * 4 + 1], a2 = acc[m * 4 + 2], a3 = acc[m * 4 + 3];
+        red_add_v4(&p.dnb[s.sci * kSc + m], (a0.x + a1.x) + (a2.x + a3.x), (a0.y + a1.y) + (a2.y + a3.y),
+                   (a0.z + a1.z) + (a2.z + a3.z), (a0.w + a1.w) + (a2.w + a3.w));
     }
     // flush the type-pair gradients of this entry into the block's FP64 sums (shared memory;
     // added to the global sums once per block at the end)
@@ -368,7 +390,7 @@ __device__ __forceinline__ void adj_flush(const double* gsum_s, double* gnbfp, i
 }
 
 template<bool kEwald>
-__global__ void __launch_bounds__(kAdjThreads, 2)
+__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm)
         k_backward(DeviceView v, const float4* __restrict__ gnb, float4* dnb, double* gnbfp, int* work_counter,
                    const double* __restrict__ gE)
 {
@@ -380,7 +402,11 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
     }
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
-    extern __shared__ float2 ttab_s[];  // kAdjWarps x replicas x stride type-pair gradient tables
+    // dynamic: per warp the i-side accumulators (64 i-atoms x 4 lane slots), then the type-pair
+    // gradient tables (kAdjWarps x replicas x stride)
+    extern __shared__ float4 adj_dyn[];
+    float4* const acc_w  = adj_dyn + (threadIdx.x >> 5) * (kSc * 4);
+    float2* const ttab_s = reinterpret_cast<float2*>(adj_dyn + kAdjWarps * kSc * 4);
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
@@ -409,7 +435,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
             break;
         }
         adj_entry<kEwald>(v, p, v.sci[e], nbfp_s, ttab_w, xis_s[warp], gis_s[warp], jx_s[warp], jg_s[warp],
-                          lane, k, v.pbeta,
+                          acc_w, lane, k, v.pbeta,
                           v.beta2l2, v.c2b, b2c2b, gsum_s);
     }
     adj_flush(gsum_s, gnbfp, 2 * v.ntypes1 * v.ntypes1);
@@ -436,13 +462,17 @@ __device__ __forceinline__ int adj_find_system(const int* prefix, int nsys, int 
 // The adjoint over all systems of a batch (shared type table and type-pair
 // gradient sums; per-system upstream energy gradients gE[2 s], gE[2 s + 1]).
 template<bool kEwald>
-__global__ void __launch_bounds__(kAdjThreads, 2)
+__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm)
         k_batch_backward(DeviceView cv, const BatchSys* __restrict__ sys, const int* __restrict__ prefix, int nsys,
                          double* gnbfp, int* work_counter, const double* __restrict__ gE)
 {
     __shared__ float2 nbfp_s[kAdjMaxTypes1 * kAdjMaxTypes1];
     __shared__ double gsum_s[2 * kAdjMaxTypes1 * kAdjMaxTypes1];
-    extern __shared__ float2 ttab_s[];  // kAdjWarps x replicas x stride type-pair gradient tables
+    // dynamic: per warp the i-side accumulators (64 i-atoms x 4 lane slots), then the type-pair
+    // gradient tables (kAdjWarps x replicas x stride)
+    extern __shared__ float4 adj_dyn[];
+    float4* const acc_w  = adj_dyn + (threadIdx.x >> 5) * (kSc * 4);
+    float2* const ttab_s = reinterpret_cast<float2*>(adj_dyn + kAdjWarps * kSc * 4);
     __shared__ float4 xis_s[kAdjWarps][kSc];
     __shared__ float4 gis_s[kAdjWarps][kSc];
     __shared__ float4 jx_s[kAdjWarps][32];
@@ -476,7 +506,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2)
         }
         const AdjPtrs p = { b.xq, b.tgrid, b.cj4, b.excl, b.shiftvec, b.gnb, b.dnb };
         adj_entry<kEwald>(cv, p, b.sci[e - prefix[sidx]], nbfp_s, ttab_w, xis_s[warp], gis_s[warp],
-                          jx_s[warp], jg_s[warp], lane, k,
+                          jx_s[warp], jg_s[warp], acc_w, lane, k,
                           cv.pbeta, cv.beta2l2, cv.c2b, b2c2b, gsum_s);
     }
     adj_flush(gsum_s, gnbfp, 2 * cv.ntypes1 * cv.ntypes1);
@@ -645,6 +675,62 @@ __global__ void k_adj_finish(DeviceView v, const float4* __restrict__ dnb, const
     }
 }
 
+// Lorentz-Berthelot type table {6 C6, 12 C12} from per-type sigma and epsilon (one block):
+// sigma_ij = (sigma_i + sigma_j) / 2, epsilon_ij = sqrt(epsilon_i epsilon_j), C6 = 4 eps s^6,
+// C12 = 4 eps s^12 (the combination nblib applies, api/nblib/gmxsetup.cpp:143-166).
+__global__ void k_lb_table(const double* __restrict__ sig, const double* __restrict__ eps, int nt, double* table)
+{
+    for (int m = threadIdx.x; m < nt * nt; m += blockDim.x)
+    {
+        const int    i = m / nt, j = m - (m / nt) * nt;
+        const double s  = 0.5 * (sig[i] + sig[j]);
+        const double e  = sqrt(eps[i] * eps[j]);
+        const double s2 = s * s;
+        const double s6 = s2 * s2 * s2;
+        const double c6 = 4.0 * e * s6;
+        table[2 * m]     = 6.0 * c6;
+        table[2 * m + 1] = 12.0 * (c6 * s6);
+    }
+}
+
+// Its adjoint: d L / d sigma_k and d L / d epsilon_k from d L / d table (one block; every type's
+// sums run over its row and column in a fixed order).  d epsilon_ij / d epsilon_i is written
+// epsilon_j / (2 epsilon_ij), as the derivative of the square root of the product.
+__global__ void k_lb_table_backward(const double* __restrict__ sig, const double* __restrict__ eps, int nt,
+                                    const double* __restrict__ gt, double* gsig, double* geps)
+{
+    extern __shared__ double lbs[];  // [2][nt * nt]: d L / d sigma_ij, d L / d epsilon_ij
+    double* gs = lbs;
+    double* ge = lbs + nt * nt;
+    for (int m = threadIdx.x; m < nt * nt; m += blockDim.x)
+    {
+        const int    i = m / nt, j = m - (m / nt) * nt;
+        const double s  = 0.5 * (sig[i] + sig[j]);
+        const double e  = sqrt(eps[i] * eps[j]);
+        const double s2 = s * s;
+        const double s5 = s2 * s2 * s;
+        const double s6 = s5 * s;
+        const double g6 = gt[2 * m], g12 = gt[2 * m + 1];
+        // 6 C6 = 24 e s^6, 12 C12 = 48 e s^12
+        gs[m] = g6 * 144.0 * e * s5 + g12 * 576.0 * e * s5 * s6;
+        ge[m] = g6 * 24.0 * s6 + g12 * 48.0 * s6 * s6;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nt; k += blockDim.x)
+    {
+        double as = 0.0, ae = 0.0;
+        for (int j = 0; j < nt; j++)
+        {
+            const double eij = sqrt(eps[k] * eps[j]);
+            // row k (sigma_k, epsilon_k as the first index) and column k (as the second)
+            as += 0.5 * gs[k * nt + j] + 0.5 * gs[j * nt + k];
+            ae += (ge[k * nt + j] + ge[j * nt + k]) * (eps[j] / (2.0 * eij));
+        }
+        gsig[k] = as;
+        geps[k] = ae;
+    }
+}
+
 } // namespace
 
 int adjoint_max_types1()
@@ -652,12 +738,27 @@ int adjoint_max_types1()
     return kAdjMaxTypes1;
 }
 
+cudaError_t launch_lb_table(const double* sig, const double* eps, int nt, double* table, cudaStream_t s)
+{
+    k_lb_table<<<1, 256, 0, s>>>(sig, eps, nt, table);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lb_table_backward(const double* sig, const double* eps, int nt, const double* gtable,
+                                     double* gsig, double* geps, cudaStream_t s)
+{
+    k_lb_table_backward<<<1, 256, 2 * sizeof(double) * nt * nt, s>>>(sig, eps, nt, gtable, gsig, geps);
+    return cudaGetLastError();
+}
+
 namespace
 {
 
+// Dynamic shared memory of the adjoint kernels: the warps' i-side accumulators and type-pair tables.
 size_t adj_table_bytes(int nt1)
 {
-    return sizeof(float2) * (size_t)kAdjWarps * adj_table_replicas(nt1) * adj_table_stride(nt1);
+    return sizeof(float4) * (size_t)kAdjWarps * kSc * 4
+           + sizeof(float2) * (size_t)kAdjWarps * adj_table_replicas(nt1) * adj_table_stride(nt1);
 }
 
 // Opts an adjoint kernel in to its static + dynamic shared memory beyond 48 KB.
@@ -688,12 +789,12 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* 
     if (v.coulomb == 0)
     {
         e = adj_optin<k_backward<true>>(dyn);
-        k_backward<true><<<num_sms * 2, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+        k_backward<true><<<num_sms * kAdjBlocksPerSm, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
     }
     else
     {
         e = adj_optin<k_backward<false>>(dyn);
-        k_backward<false><<<num_sms * 2, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
+        k_backward<false><<<num_sms * kAdjBlocksPerSm, kAdjThreads, dyn, s>>>(v, gnb, dnb, d_gnbfp, counter, d_gE);
     }
     if (e != cudaSuccess)
     {
@@ -715,12 +816,12 @@ cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, con
     if (cv.coulomb == 0)
     {
         e = adj_optin<k_batch_backward<true>>(dyn);
-        k_batch_backward<true><<<num_sms * 2, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+        k_batch_backward<true><<<num_sms * kAdjBlocksPerSm, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
     }
     else
     {
         e = adj_optin<k_batch_backward<false>>(dyn);
-        k_batch_backward<false><<<num_sms * 2, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
+        k_batch_backward<false><<<num_sms * kAdjBlocksPerSm, kAdjThreads, dyn, s>>>(cv, sys, prefix, nsys, d_gnbfp, counter, d_gE);
     }
     if (e != cudaSuccess)
     {

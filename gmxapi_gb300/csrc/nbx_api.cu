@@ -1243,6 +1243,28 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
     return cuda_check(h, e, "nbx_set_parameters_device");
 }
 
+int nbx_lb_table_device(const double* d_sigma, const double* d_epsilon, int ntypes, double* d_table, void* stream)
+{
+    if (!d_sigma || !d_epsilon || !d_table || ntypes < 1 || ntypes > 64)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    const cudaError_t e = launch_lb_table(d_sigma, d_epsilon, ntypes, d_table, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
+int nbx_lb_table_backward_device(const double* d_sigma, const double* d_epsilon, int ntypes, const double* d_gtable,
+                                 double* d_gsigma, double* d_gepsilon, void* stream)
+{
+    if (!d_sigma || !d_epsilon || !d_gtable || !d_gsigma || !d_gepsilon || ntypes < 1 || ntypes > 64)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    const cudaError_t e = launch_lb_table_backward(d_sigma, d_epsilon, ntypes, d_gtable, d_gsigma, d_gepsilon,
+                                                   static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
 int nbx_set_force_kernel(nbx_handle* h, int tile, int stage_depth, int blocks_per_sm)
 {
     if (!h || tile < 0 || tile > 1 || stage_depth < 2 || stage_depth > 3 || blocks_per_sm < 2 || blocks_per_sm > 3)

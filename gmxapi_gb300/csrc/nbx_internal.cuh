@@ -431,6 +431,9 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* 
                             float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
                             int num_sms, cudaStream_t s);
 cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);
+cudaError_t launch_lb_table(const double* sig, const double* eps, int nt, double* table, cudaStream_t s);
+cudaError_t launch_lb_table_backward(const double* sig, const double* eps, int nt, const double* gtable,
+                                     double* gsig, double* geps, cudaStream_t s);
 cudaError_t launch_compact_gnbfp(const double* padded, double* out, int nt, cudaStream_t s);
 cudaError_t launch_batch_backward(const DeviceView& cv, const BatchSys* sys, const int* prefix, int nsys,
                                   int max_slots, int max_atoms, const float* d_gF, const double* d_gE,

@@ -214,6 +214,14 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
 /* Replaces the charges ([N], atom order) and/or the nbfp matrix ([num_types^2 * 2]), both in device
  * memory (either may be NULL); the list is kept.  The self energy then follows the new charges. */
 int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nbfp);
+/* The Lorentz-Berthelot type table and its adjoint, one kernel each on `stream` (device memory, no
+ * handle): table[(i * ntypes + j) * 2 + {0, 1}] = {6 C6, 12 C12} with sigma_ij = (sigma_i +
+ * sigma_j) / 2, epsilon_ij = sqrt(epsilon_i epsilon_j), C6 = 4 epsilon_ij sigma_ij^6, C12 = C6
+ * sigma_ij^6 (nblib's combination, api/nblib/gmxsetup.cpp:143-166), all double; the backward pass
+ * turns d L / d table into d L / d sigma and d L / d epsilon.  1 <= ntypes <= 64. */
+int nbx_lb_table_device(const double* d_sigma, const double* d_epsilon, int ntypes, double* d_table, void* stream);
+int nbx_lb_table_backward_device(const double* d_sigma, const double* d_epsilon, int ntypes, const double* d_gtable,
+                                 double* d_gsigma, double* d_gepsilon, void* stream);
 
 /* ---- free-energy perturbation of some atoms (the perturbed-pair kernel) ---- */
 /* Replaces the free-energy path of the nonbonded step: nb_free_energy_kernel

@@ -207,3 +207,20 @@ def test_gradient_step_captured_in_a_cuda_graph_matches_eager():
     for a, t in zip(eager, (x, q, sig, eps)):
         assert rel_rms(t.grad.cpu(), a.cpu()) < 1e-5  # atomics sum in another order
     eng.close()
+
+
+@pytest.mark.parametrize("nt", [1, 8, 15])
+def test_lorentz_berthelot_kernels_match_torch(nt):
+    """The one-kernel combination rule and its adjoint against the torch formula (FP64)."""
+    rng = np.random.default_rng(nt)
+    sig = torch.tensor(rng.uniform(0.25, 0.45, nt), dtype=torch.float64, device=DEV, requires_grad=True)
+    eps = torch.tensor(rng.uniform(0.05, 1.2, nt), dtype=torch.float64, device=DEV, requires_grad=True)
+    g = torch.tensor(rng.normal(size=(nt, nt, 2)), dtype=torch.float64, device=DEV)
+    t = lorentz_berthelot_nbfp(sig, eps)
+    (t * g).sum().backward()
+    s_c, e_c = sig.detach().cpu().requires_grad_(), eps.detach().cpu().requires_grad_()
+    t_c = lorentz_berthelot_nbfp(s_c, e_c)
+    (t_c * g.cpu()).sum().backward()
+    np.testing.assert_allclose(t.detach().cpu().numpy(), t_c.detach().numpy(), rtol=1e-13)
+    np.testing.assert_allclose(sig.grad.cpu().numpy(), s_c.grad.numpy(), rtol=1e-11, atol=1e-12)
+    np.testing.assert_allclose(eps.grad.cpu().numpy(), e_c.grad.numpy(), rtol=1e-11, atol=1e-12)
