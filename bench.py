@@ -931,6 +931,13 @@ def run_ours(args) -> None:
     pairs1 = calc.pair_count()
     up = useful_pairs(n, s.box)
     total_ms, value = replica_throughput(total_ms, up, args.steps, world, frames.device)
+    if args.core_only:
+        # profiling runs: the device-timed schedule alone (no e2e, memory passes or baselines)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "pairs/s", "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                              "force_ms_per_launch": force_ms / max(1, force_launches), "core_only": True}))
+        return
 
     # e2e: the same schedule through the C ABI with host arrays (pinned), H2D x and D2H f/E/virial per step
     hx = frames.cpu().pin_memory()
@@ -1029,6 +1036,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-ensemble, adjoint and force-matching measurements")
+    ap.add_argument("--core-only", action="store_true",
+                    help="time the force schedule only and print a reduced line (profiling)")
     ap.add_argument("--only", choices=["ensemble", "adjoint", "force_matching", "pme", "md", "fep"],
                     help="run one of the extra measurements alone and print its JSON (profiling)")
     args = ap.parse_args()
