@@ -229,17 +229,20 @@ __global__ void k_batch_reduce(const BatchSys* __restrict__ sys, float* __restri
     }
     __shared__ double ws[9][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the warp's sum in float (FP64 runs at a small fraction of the FP32 rate here), the warps'
+    // partials in FP64
 #pragma unroll
     for (int k = 0; k < 9; k++)
     {
-        double t = (double)w[k];
+        float t = w[k];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1)
         {
             t += __shfl_xor_sync(0xffffffffu, t, o);
         }
         if (lane == 0)
         {
-            ws[k][warp] = t;
+            ws[k][warp] = (double)t;
         }
     }
     __syncthreads();

@@ -354,17 +354,21 @@ __global__ void __launch_bounds__(kReduceThreads)
     {
         __shared__ double ws[9][32];
         const int         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        // the warp's 128 atoms summed in float (FP64 arithmetic runs at a small fraction of the
+        // FP32 rate on this GPU: 9 x 5 FP64 shuffle levels per warp cost several microseconds),
+        // the warps' partials in FP64
 #pragma unroll
         for (int k = 0; k < 9; k++)
         {
-            double t = (double)w[k];
+            float t = w[k];
+#pragma unroll
             for (int o = 16; o > 0; o >>= 1)
             {
                 t += __shfl_xor_sync(0xffffffffu, t, o);
             }
             if (lane == 0)
             {
-                ws[k][warp] = t;
+                ws[k][warp] = (double)t;
             }
         }
         __syncthreads();

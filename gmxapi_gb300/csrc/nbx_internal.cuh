@@ -255,8 +255,9 @@ __device__ __forceinline__ int find_system(const int* prefix, int nsys, int e)
 }
 
 // Cluster-packed record of 8 atoms (kPackWords 32-bit words, 160 B): x[8], y[8], z[8], q[8],
-// type[8], atom a at position 2 (a & 3) + (a >> 2) of each, so that atoms a and a + 4 (the two
-// warp halves' j-atoms of one lane) are adjacent.
+// and the type as a byte offset into a row of 16-byte type-pair entries (type * 16), atom a at
+// position 2 (a & 3) + (a >> 2) of each, so that atoms a and a + 4 (the two warp halves' j-atoms
+// of one lane) are adjacent.
 constexpr int kPackWords = 40;
 
 // Writes slot k's coordinates, charge and type into the cluster-packed records (DeviceView::xqp).
@@ -267,7 +268,7 @@ __device__ __forceinline__ void write_packed_slot(float* xqp, int k, float x, fl
     pc[8]     = y;
     pc[16]    = z;
     pc[24]    = q;
-    pc[32]    = __int_as_float(type);
+    pc[32]    = __int_as_float(type * 16);
 }
 
 // One system of a batch, as the batched kernels see it (device table).

@@ -195,27 +195,50 @@ struct PairConstsX2
     float rc2, pbeta, nbeta2l2, c2b, k_rf2, nk_rf2, sh_ewald, k_rf, c_rf, epsfac;
 };
 
-// One packed step: i-cluster c (data in shared memory) against the two j-atoms of the lane; the
-// lane's i-force partial for atom (c, ii) is read, updated and written back in shared memory.
-// kExcl: the pairs' exclusion bits (intA / intB) and the diagonal self pairs (in okA / okB).
-template<bool kEnergy, int kCoul, bool kExcl>
-__device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* __restrict__ nbfp_b,
-                                             float4* __restrict__ rec, int jj, const float2 xj, const float2 yj,
-                                             const float2 zj, const float2 qje, const int2 tjb, bool okA, bool okB,
-                                             float intA, float intB, float2& fjx, float2& fjy, float2& fjz,
-                                             float2& ejel, float2& ejlj)
+// The geometry of one packed step: i-cluster c's atom ii (record rec in shared memory) against
+// the lane's two j-atoms.  in: the pair is inside the cut-off and its half's mask bit is set (and,
+// on the diagonal, j > i); kExcl: int = the pair's exclusion bit as 0 / 1.
+struct GeomX2
+{
+    float4* rec;
+    float2  qi;               // {q_i, q_i}
+    float2  dx, dy, dz, r2;
+    bool    inA, inB;
+    float   intA, intB;
+};
+
+__device__ __forceinline__ void pair_geom_x2(const PairConstsX2& k, float4* __restrict__ rec, const float2 xj,
+                                             const float2 yj, const float2 zj, bool okA, bool okB, float intA,
+                                             float intB, GeomX2& g)
 {
     const float4 i0 = rec[0];  // {x, x, y, y}
     const float4 i1 = rec[1];  // {z, z, q, q}
-    const int    ti = __float_as_int(rec[6].x);  // type-table row, bytes
-    const float2 dx = sub2(make_float2(i0.x, i0.y), xj);
-    const float2 dy = sub2(make_float2(i0.z, i0.w), yj);
-    const float2 dz = sub2(make_float2(i1.x, i1.y), zj);
-    float2       r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-    const bool   inA = okA && (r2.x < k.rc2);
-    const bool   inB = okB && (r2.y < k.rc2);
-    r2               = make_float2(fmaxf(r2.x, kMinDist2), fmaxf(r2.y, kMinDist2));
-    float2 rinv      = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    g.rec           = rec;
+    g.qi            = make_float2(i1.z, i1.w);
+    g.dx            = sub2(make_float2(i0.x, i0.y), xj);
+    g.dy            = sub2(make_float2(i0.z, i0.w), yj);
+    g.dz            = sub2(make_float2(i1.x, i1.y), zj);
+    g.r2            = fma2(g.dz, g.dz, fma2(g.dy, g.dy, mul2(g.dx, g.dx)));
+    g.inA           = okA && (g.r2.x < k.rc2);
+    g.inB           = okB && (g.r2.y < k.rc2);
+    g.intA          = intA;
+    g.intB          = intB;
+}
+
+// The forces and energies of one packed step whose geometry is g; the lane's i-force partial for
+// atom (c, ii) is read, updated and written back in shared memory.
+template<bool kEnergy, int kCoul, bool kExcl>
+__device__ __forceinline__ void pair_phys_x2(const PairConstsX2& k, const char* __restrict__ nbfp_b, const GeomX2& g,
+                                             int jj, const float2 qje, const int2 tjb, float2& fjx, float2& fjy,
+                                             float2& fjz, float2& ejel, float2& ejlj)
+{
+    float4* const rec  = g.rec;
+    const int     ti   = __float_as_int(rec[6].x);  // type-table row, bytes
+    const float2  dx = g.dx, dy = g.dy, dz = g.dz;
+    const bool    inA = g.inA, inB = g.inB;
+    const float   intA = g.intA, intB = g.intB;
+    float2        r2   = make_float2(fmaxf(g.r2.x, kMinDist2), fmaxf(g.r2.y, kMinDist2));
+    float2        rinv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
     if (kEnergy)
     {
         // one Newton step: rsqrt.approx -> ~correctly rounded, unbiased for the energy sums;
@@ -239,7 +262,7 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
     const float2 nvdisp = make_float2(lA.x * rinv6.x, lB.x * rinv6.y);
     const float2 flj    = make_float2(fmaf(lA.y * rinv6.x, rinv6.x, nvdisp.x),
                                       fmaf(lB.y * rinv6.y, rinv6.y, nvdisp.y));  // F r^2: vrep - vdisp
-    const float2 qq     = mul2(make_float2(i1.z, i1.w), qje);
+    const float2 qq     = mul2(g.qi, qje);
     float2       fcr2;  // Coulomb F r^2 / (q_i q_j)
     float2       hel;   // Coulomb energy / (q_i q_j epsfac), before masking
     if (kCoul >= 1)
@@ -291,7 +314,7 @@ __device__ __forceinline__ void pair_step_x2(const PairConstsX2& k, const char* 
         {
             hel = make_float2(cA ? hel.x : 0.0f, cB ? hel.y : 0.0f);
         }
-        ejel = fma2(make_float2(i1.z, i1.w), hel, ejel);
+        ejel = fma2(g.qi, hel, ejel);
     }
     float4 fi = rec[2 + jj];
     fi.x      = fmaf(fscal.y, dx.y, fmaf(fscal.x, dx.x, fi.x));
@@ -327,8 +350,38 @@ __device__ __forceinline__ void pair_bits_x2(int c, unsigned mA, unsigned mB, un
     }
 }
 
-// The set i-clusters `rem` of one j-cluster, visited two at a time so that two independent
-// pair computations share a basic block.  kSame: both halves' masks equal rem (no per-half test).
+// Takes set i-clusters off `rem` until one has a pair inside the cut-off (any lane) and returns its
+// geometry; false when `rem` runs out.  Steps with every pair beyond the cut-off (about one in
+// eight on a list pruned to rlist_inner 0.95 nm at rc 0.9 nm) contribute exact zeros, so they are
+// left out after the cheap geometry part.  kSame: both halves' masks equal rem.
+template<bool kExcl, bool kSame>
+__device__ __forceinline__ bool next_step_x2(const PairConstsX2& k, float4* __restrict__ lane_rec, unsigned& rem,
+                                             unsigned mA, unsigned mB, unsigned xA, unsigned xB, bool central,
+                                             int sci, int cj, int ii, int jj, const float2 xj, const float2 yj,
+                                             const float2 zj, GeomX2& g)
+{
+#pragma unroll 1
+    while (rem)
+    {
+        const int c = __ffs(rem) - 1;
+        rem &= rem - 1;
+        bool  okA = true, okB = true;
+        float intA = 1.0f, intB = 1.0f;
+        if (!kSame)
+        {
+            pair_bits_x2<kExcl>(c, mA, mB, xA, xB, central, sci, cj, ii, jj, okA, okB, intA, intB);
+        }
+        pair_geom_x2(k, lane_rec + c * (kCl * kIRecF4), xj, yj, zj, okA, okB, intA, intB, g);
+        if (__any_sync(0xffffffffu, g.inA || g.inB))
+        {
+            return true;
+        }
+    }
+    return false;
+}
+
+// The set i-clusters `rem` of one j-cluster, the ones with pairs inside the cut-off visited two at
+// a time so that two independent pair computations share a basic block.
 template<bool kEnergy, int kCoul, bool kExcl, bool kSame>
 __device__ __forceinline__ void jcluster_x2(const PairConstsX2& k, const char* __restrict__ nbfp_b,
                                             float4* __restrict__ lane_rec, unsigned rem, unsigned mA, unsigned mB,
@@ -338,36 +391,21 @@ __device__ __forceinline__ void jcluster_x2(const PairConstsX2& k, const char* _
                                             float2& ejlj)
 {
 #pragma unroll 1
-    while (rem)
+    for (;;)
     {
-        const int ca = __ffs(rem) - 1;
-        rem &= rem - 1;
-        bool  okA = true, okB = true;
-        float intA = 1.0f, intB = 1.0f;
-        if (!kSame)
+        GeomX2 ga;
+        if (!next_step_x2<kExcl, kSame>(k, lane_rec, rem, mA, mB, xA, xB, central, sci, cj, ii, jj, xj, yj, zj, ga))
         {
-            pair_bits_x2<kExcl>(ca, mA, mB, xA, xB, central, sci, cj, ii, jj, okA, okB, intA, intB);
+            break;
         }
-        if (rem)
+        GeomX2 gb;
+        if (!next_step_x2<kExcl, kSame>(k, lane_rec, rem, mA, mB, xA, xB, central, sci, cj, ii, jj, xj, yj, zj, gb))
         {
-            const int cb = __ffs(rem) - 1;
-            rem &= rem - 1;
-            bool  okA2 = true, okB2 = true;
-            float intA2 = 1.0f, intB2 = 1.0f;
-            if (!kSame)
-            {
-                pair_bits_x2<kExcl>(cb, mA, mB, xA, xB, central, sci, cj, ii, jj, okA2, okB2, intA2, intB2);
-            }
-            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
-                                                okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
-            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + cb * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
-                                                okA2, okB2, intA2, intB2, fjx, fjy, fjz, ejel, ejlj);
+            pair_phys_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, ga, jj, qje, tjb, fjx, fjy, fjz, ejel, ejlj);
+            break;
         }
-        else
-        {
-            pair_step_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, lane_rec + ca * (kCl * kIRecF4), jj, xj, yj, zj, qje, tjb,
-                                                okA, okB, intA, intB, fjx, fjy, fjz, ejel, ejlj);
-        }
+        pair_phys_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, ga, jj, qje, tjb, fjx, fjy, fjz, ejel, ejlj);
+        pair_phys_x2<kEnergy, kCoul, kExcl>(k, nbfp_b, gb, jj, qje, tjb, fjx, fjy, fjz, ejel, ejlj);
     }
 }
 
@@ -396,8 +434,7 @@ __device__ __forceinline__ void group_x2(const PairConstsX2& k, const SysPtrsX2&
         const float2 yj   = *reinterpret_cast<const float2*>(xs + 8);
         const float2 zj   = *reinterpret_cast<const float2*>(xs + 16);
         const float2 qj   = *reinterpret_cast<const float2*>(xs + 24);
-        const int2   tj   = *reinterpret_cast<const int2*>(xs + 32);
-        const int2   tjb  = make_int2(tj.x * (int)sizeof(float4), tj.y * (int)sizeof(float4));
+        const int2   tjb  = *reinterpret_cast<const int2*>(xs + 32);  // type-pair row offsets, bytes
         const float2 qje  = mul2(qj, f2(k.epsfac));
         const unsigned mA = m0 >> (jm * kNcl), mB = m1 >> (jm * kNcl);
         const unsigned xA = wA >> (jm * kNcl), xB = wB >> (jm * kNcl);

@@ -19,9 +19,11 @@ FP64 numpy, vectorised over pairs.  Restates nb_free_energy_kernel
   analytic.  The reference keeps an excluded pair's correction while the pair is in its list
   (r < rlist); here while r < rc, as the cluster kernel does.
 
-Pinned by its end states: at lambda = 0 (1) with state B (A) equal to A (B) it reduces to the
-pinned cluster-pair oracle for the same pairs (``tests/test_fep_oracle.py``), and dV/dlambda
-equals the central difference of V(lambda).
+Parity unpinned: the reference holds no test data for this kernel and its compiled code is not
+run here, so no reference output checks the soft-core branches at intermediate lambda.  What is
+checked: at lambda = 0 (1) with state B (A) equal to A (B) it reduces to the pinned cluster-pair
+oracle for the same pairs (``tests/test_fep_oracle.py``), and dV/dlambda equals the central
+difference of V(lambda).
 """
 from __future__ import annotations
 
