@@ -275,7 +275,8 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
     import torch
 
     from gmxapi_gb300 import nblib, systems
-    from gmxapi_gb300.adjoint import DifferentiableNonbonded, lorentz_berthelot_nbfp, static_list_options
+    from gmxapi_gb300.adjoint import (DifferentiableNonbonded, force_matching_loss, lorentz_berthelot_nbfp,
+                                      static_list_options)
 
     s = systems.lj_liquid(n=24000, ntypes=8, seed=4)
     eng = DifferentiableNonbonded(s, static_list_options(RC), device=dev)  # fixed coordinates: list at rc
@@ -297,6 +298,14 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
             eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
 
     def grad_step():
+        for t in (x, q, sig, eps):
+            t.grad = None
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        force_matching_loss(f, f_target).backward()
+
+    def grad_step_torch_loss():
+        # the same step with the loss written as a torch expression (three element-wise kernels
+        # each way instead of the fused loss kernel)
         for t in (x, q, sig, eps):
             t.grad = None
         f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
@@ -395,9 +404,10 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
     try:
         fwd_graph_ms = graph_replay_ms(forward, ())
         step_graph_ms = graph_replay_ms(grad_step, (x, q, sig, eps))
+        step_torch_graph_ms = graph_replay_ms(grad_step_torch_loss, (x, q, sig, eps))
         graph_note = "replayed from a CUDA graph"
     except Exception as exc:  # capture unavailable: report the eager ratio only
-        fwd_graph_ms = step_graph_ms = None
+        fwd_graph_ms = step_graph_ms = step_torch_graph_ms = None
         graph_note = f"eager (capture failed: {type(exc).__name__}: {exc})"
     eng.close()
     return {"workload": "random LJ+Coulomb liquid, 24000 atoms, 8 types, Lorentz-Berthelot, "
@@ -405,6 +415,8 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
             "forward_graph_ms": fwd_graph_ms, "gradient_step_graph_ms": step_graph_ms,
             "gradient_step_vs_forward": (step_graph_ms / fwd_graph_ms) if step_graph_ms else step_ms / fwd_ms,
             "gradient_step_vs_forward_timing": graph_note,
+            "gradient_step_torch_loss_graph_ms": step_torch_graph_ms,
+            "gradient_step_torch_loss_vs_forward": (step_torch_graph_ms / fwd_graph_ms) if step_torch_graph_ms else None,
             "gradient_steps_per_s": 1e3 / (step_graph_ms or step_ms),
             "forward_eager_ms": fwd_ms, "gradient_step_eager_ms": step_ms,
             "gradient_step_vs_forward_eager": step_ms / fwd_ms,
@@ -413,8 +425,9 @@ def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
             "entry_timing": entry_timing, "forward_entry_call_ms": fwd_call_ms,
             "backward_entry_call_ms": bwd_call_ms,
             "note": "forward = the autograd forward (Lorentz-Berthelot table, parameter upload, F+E); "
-                    "gradient step = autograd forward + loss + backward (adjoint kernel and the table's "
-                    "chain rule); the graph figures replay the same Python step captured once in a CUDA "
+                    "gradient step = autograd forward + loss (gmxapi_gb300.adjoint.force_matching_loss: one "
+                    "kernel each way; the torch_loss figures write it as ((f - f_t) ** 2).sum()) + backward "
+                    "(adjoint kernel and the table's chain rule); the graph figures replay the same Python step captured once in a CUDA "
                     "graph, the eager ones call it from Python every step (host-bound at 24,000 atoms); "
                     "forward entry = C-ABI F+E (convert, force, reduce, energies); backward entry = C-ABI "
                     "adjoint (convert, gradient prepare, adjoint kernel, finish, FP64 table gradients); "

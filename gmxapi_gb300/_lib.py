@@ -53,7 +53,7 @@ EXPORTED = [
     "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
     "nbx_md_run_device", "nbx_fep_enable", "nbx_fep_set_lambda", "nbx_fep_get_energies", "nbx_fep_energies_device",
     "nbx_fep_disable", "nbx_pme_create_lj", "nbx_ewald_coefficient_lj", "nbx_lb_table_device",
-    "nbx_lb_table_backward_device",
+    "nbx_lb_table_backward_device", "nbx_match_loss_device",
 ]
 
 
@@ -208,6 +208,7 @@ def load():
     L.nbx_set_parameters_device.argtypes = [vp, vp, vp]
     L.nbx_lb_table_device.argtypes = [vp, vp, C.c_int, vp, vp]
     L.nbx_lb_table_backward_device.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp]
+    L.nbx_match_loss_device.argtypes = [vp, vp, C.c_longlong, vp, vp, vp]
     L.nbx_ewald_coefficient.argtypes = [C.c_float, C.c_float]
     L.nbx_ewald_coefficient.restype = C.c_float
     L.nbx_pme_grid_size.argtypes = [fp, C.c_float, ip]

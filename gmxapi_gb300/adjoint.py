@@ -80,6 +80,44 @@ def lorentz_berthelot_nbfp(sigma: torch.Tensor, epsilon: torch.Tensor) -> torch.
     return table
 
 
+class _ForceMatchingLoss(torch.autograd.Function):
+    """sum_k (F_k - F_target_k)^2 as a float64 scalar; the same pass writes 2 (F - F_target)."""
+
+    @staticmethod
+    def forward(ctx, f, f_target):
+        from . import _lib
+
+        g = torch.empty_like(f)
+        loss = torch.empty((), dtype=torch.float64, device=f.device)
+        stream = torch.cuda.current_stream(f.device).cuda_stream
+        code = _lib.load().nbx_match_loss_device(f.data_ptr(), f_target.data_ptr(), f.numel(), g.data_ptr(),
+                                                 loss.data_ptr(), stream)
+        if code != 0:
+            raise RuntimeError(f"nbx_match_loss_device failed ({code})")
+        ctx.save_for_backward(g)
+        return loss
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, g_loss):
+        (g,) = ctx.saved_tensors
+        return g * g_loss, None
+
+
+def force_matching_loss(f: torch.Tensor, f_target: torch.Tensor) -> torch.Tensor:
+    """The force-matching loss sum |F - F_target|^2 (float64 scalar) of float32 CUDA forces.
+
+    One kernel forward (the loss in FP64 and its gradient 2 (F - F_target) in the same pass) and
+    one scaling kernel backward, in place of the three element-wise kernels each way that the torch
+    expression ``((f - f_target) ** 2).sum()`` launches.  f_target is a constant (no gradient).
+    """
+    if not (f.is_cuda and f.dtype == torch.float32 and f_target.is_cuda and f_target.dtype == torch.float32):
+        raise TypeError("force_matching_loss takes float32 CUDA tensors")
+    if f.shape != f_target.shape:
+        raise ValueError(f"shape mismatch: {tuple(f.shape)} vs {tuple(f_target.shape)}")
+    return _ForceMatchingLoss.apply(f.contiguous(), f_target.detach().contiguous())
+
+
 def static_list_options(rc: float = 0.9) -> NBKernelOptions:
     """Options for coordinates that do not move between searches (force matching on fixed
     frames, or a search on every call): the list radius equals the cut-off and the fresh

@@ -25,6 +25,8 @@
 #include "nbx_internal.cuh"
 #include "nbx_pair_core.cuh"
 
+#include <algorithm>
+
 namespace nbx
 {
 namespace
@@ -336,22 +338,24 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
                    (a0.z + a1.z) + (a2.z + a3.z), (a0.w + a1.w) + (a2.w + a3.w));
     }
     // flush the type-pair gradients of this entry into the block's FP64 sums (shared memory;
-    // added to the global sums once per block at the end)
+    // added to the global sums once per block at the end).  The replicas are summed in float
+    // first: one conversion and one FP64 add per element, where FP64 runs at a small fraction of
+    // the FP32 rate (a conversion and an add per replica kept the FP64 pipe 37 % busy).
     __syncwarp();
     for (int m = lane; m < nt1 * nt1; m += 32)
     {
-        double tx = 0.0, ty = 0.0;
+        float tx = 0.0f, ty = 0.0f;
         for (int r = 0; r < reps; r++)
         {
             const float2 t = ttab[r * tstride + m];
-            tx += (double)t.x;
-            ty += (double)t.y;
+            tx += t.x;
+            ty += t.y;
             ttab[r * tstride + m] = make_float2(0.0f, 0.0f);
         }
-        if (tx != 0.0 || ty != 0.0)
+        if (tx != 0.0f || ty != 0.0f)
         {
-            atomicAdd(&gnbfp[2 * m], tx);
-            atomicAdd(&gnbfp[2 * m + 1], ty);
+            atomicAdd(&gnbfp[2 * m], (double)tx);
+            atomicAdd(&gnbfp[2 * m + 1], (double)ty);
         }
     }
     __syncwarp();
@@ -648,10 +652,22 @@ __global__ void k_adj_prepare(DeviceView v, const float* __restrict__ x, const f
     dnb[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-// Atom-order outputs; dL/dq also gets the self-energy term.
+// Atom-order outputs; dL/dq also gets the self-energy term.  Block 0 also copies the type-pair
+// gradients out of the padded (nt+1)^2 table into the caller's nt^2 one when gout is given (the
+// adjoint kernel has finished: no separate launch).
 __global__ void k_adj_finish(DeviceView v, const float4* __restrict__ dnb, const double* __restrict__ gE, float* gx,
-                             float* gq)
+                             float* gq, const double* __restrict__ gpad, double* gout)
 {
+    if (gout && blockIdx.x == 0)
+    {
+        const int nt = v.ntypes1 - 1;
+        for (int m = threadIdx.x; m < nt * nt; m += blockDim.x)
+        {
+            const int i = m / nt, j = m % nt;
+            gout[2 * m]     = gpad[2 * (i * (nt + 1) + j)];
+            gout[2 * m + 1] = gpad[2 * (i * (nt + 1) + j) + 1];
+        }
+    }
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= v.n)
     {
@@ -778,7 +794,7 @@ cudaError_t adj_optin(size_t dynamic_bytes)
 
 cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* d_gF, const double* d_gE,
                             float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
-                            int num_sms, cudaStream_t s)
+                            double* d_gnbfp_out, int num_sms, cudaStream_t s)
 {
     const int tb    = 256;
     const int slots = v.g.cells_capacity * kSc;
@@ -800,7 +816,7 @@ cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* 
     {
         return e;
     }
-    k_adj_finish<<<(v.n + tb - 1) / tb, tb, 0, s>>>(v, dnb, d_gE, d_gx, d_gq);
+    k_adj_finish<<<std::max(1, (v.n + tb - 1) / tb), tb, 0, s>>>(v, dnb, d_gE, d_gx, d_gq, d_gnbfp, d_gnbfp_out);
     return cudaGetLastError();
 }
 

@@ -1211,13 +1211,10 @@ int nbx_backward_device(nbx_handle* h, const float* d_x, const float* d_gF, cons
         }
     }
     // the coordinate conversion is part of the preparation kernel
-    e = launch_backward(v, d_x, d_gF, d_gE, h->d_gnb, h->d_dnb, h->d_gnbfp, h->d_adj_counter, d_gx, d_gq,
+    // (the type-pair gradients are copied out by the finishing kernel)
+    e = launch_backward(v, d_x, d_gF, d_gE, h->d_gnb, h->d_dnb, h->d_gnbfp, h->d_adj_counter, d_gx, d_gq, d_gnbfp,
                         h->num_sms, h->stream);
-    if (e == cudaSuccess && d_gnbfp)
-    {
-        e = launch_compact_gnbfp(h->d_gnbfp, d_gnbfp, v.ntypes1 - 1, h->stream);
-    }
-    h->launches += 3 + (d_gnbfp ? 1 : 0);
+    h->launches += 3;
     return cuda_check(h, e, "nbx_backward_device");
 }
 
@@ -1262,6 +1259,22 @@ int nbx_lb_table_backward_device(const double* d_sigma, const double* d_epsilon,
     }
     const cudaError_t e = launch_lb_table_backward(d_sigma, d_epsilon, ntypes, d_gtable, d_gsigma, d_gepsilon,
                                                    static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
+}
+
+int nbx_match_loss_device(const float* d_f, const float* d_ftarget, long long n3, float* d_gF, double* d_loss,
+                          void* stream)
+{
+    if (!d_f || !d_ftarget || !d_gF || !d_loss || n3 < 0)
+    {
+        return NBX_ERR_INVALID_INPUT;
+    }
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    {
+        return NBX_ERR_CUDA;
+    }
+    const cudaError_t e = launch_match_loss(d_f, d_ftarget, (size_t)n3, d_gF, d_loss, sms, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? NBX_OK : NBX_ERR_CUDA;
 }
 

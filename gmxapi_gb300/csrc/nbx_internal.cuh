@@ -430,7 +430,7 @@ cudaError_t optin_batch_force_smem();
 // d_x: coordinates converted into xq by the preparation kernel (nullptr: xq is current)
 cudaError_t launch_backward(const DeviceView& v, const float* d_x, const float* d_gF, const double* d_gE,
                             float4* gnb, float4* dnb, double* d_gnbfp, int* counter, float* d_gx, float* d_gq,
-                            int num_sms, cudaStream_t s);
+                            double* d_gnbfp_out, int num_sms, cudaStream_t s);
 cudaError_t launch_set_parameters(const DeviceView& v, const float* d_q, const float* d_nbfp, cudaStream_t s);
 cudaError_t launch_lb_table(const double* sig, const double* eps, int nt, double* table, cudaStream_t s);
 cudaError_t launch_lb_table_backward(const double* sig, const double* eps, int nt, const double* gtable,

@@ -222,6 +222,12 @@ int nbx_set_parameters_device(nbx_handle* h, const float* d_q, const float* d_nb
 int nbx_lb_table_device(const double* d_sigma, const double* d_epsilon, int ntypes, double* d_table, void* stream);
 int nbx_lb_table_backward_device(const double* d_sigma, const double* d_epsilon, int ntypes, const double* d_gtable,
                                  double* d_gsigma, double* d_gepsilon, void* stream);
+/* The force-matching loss sum_k (F_k - F_target_k)^2 over n3 float components, summed in FP64 into
+ * d_loss (overwritten), and its gradient 2 (F - F_target) into d_gF, in one pass on `stream` (device
+ * memory, no handle).  No counterpart in the reference (it computes forces, not fits); the batched
+ * force matcher runs the same kernel inside its step. */
+int nbx_match_loss_device(const float* d_f, const float* d_ftarget, long long n3, float* d_gF, double* d_loss,
+                          void* stream);
 
 /* ---- free-energy perturbation of some atoms (the perturbed-pair kernel) ---- */
 /* Replaces the free-energy path of the nonbonded step: nb_free_energy_kernel

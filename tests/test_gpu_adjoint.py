@@ -224,3 +224,61 @@ def test_lorentz_berthelot_kernels_match_torch(nt):
     np.testing.assert_allclose(t.detach().cpu().numpy(), t_c.detach().numpy(), rtol=1e-13)
     np.testing.assert_allclose(sig.grad.cpu().numpy(), s_c.grad.numpy(), rtol=1e-11, atol=1e-12)
     np.testing.assert_allclose(eps.grad.cpu().numpy(), e_c.grad.numpy(), rtol=1e-11, atol=1e-12)
+
+
+def test_fused_force_matching_loss_matches_the_torch_expression():
+    """force_matching_loss (one kernel each way) against ((f - f_t) ** 2).sum(): the loss in FP64,
+    the gradients of a full force-matching step, and the step captured in a CUDA graph."""
+    from gmxapi_gb300.adjoint import force_matching_loss
+
+    s = CASES["liquid2000"]()
+    eng = DifferentiableNonbonded(s)
+    x = torch.tensor(s.x, device=DEV, requires_grad=True)
+    q = torch.tensor(s.q, device=DEV, requires_grad=True)
+    sig = torch.tensor(s.sigma, dtype=torch.float64, device=DEV, requires_grad=True)
+    eps = torch.tensor(s.epsilon, dtype=torch.float64, device=DEV, requires_grad=True)
+    with torch.no_grad():
+        f_t, _ = eng(x, q * 1.02, lorentz_berthelot_nbfp(sig * 0.98, eps * 1.03))
+    eng.search(x)
+    params = (x, q, sig, eps)
+
+    def step(fused):
+        for t in params:
+            t.grad = None
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        loss = force_matching_loss(f, f_t) if fused else ((f.double() - f_t.double()) ** 2).sum()
+        loss.backward()
+        return loss.detach().clone(), [t.grad.clone() for t in params]
+
+    l_ref, g_ref = step(False)
+    l_fused, g_fused = step(True)
+    # the two steps' forces differ by the order of their atomic sums; the losses of one force array:
+    with torch.no_grad():
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        a = float(force_matching_loss(f, f_t))
+        b = float(((f.double() - f_t.double()) ** 2).sum())
+    assert abs(a - b) <= 1e-12 * abs(b)
+    assert abs(float(l_fused) - float(l_ref)) <= 1e-6 * abs(float(l_ref))
+    for a, b in zip(g_fused, g_ref):
+        assert rel_rms(a.cpu(), b.cpu()) < 1e-5
+    # inside a CUDA graph: the same gradients after replays
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            step(True)
+    torch.cuda.current_stream().wait_stream(side)
+    for t in params:
+        t.grad = None
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        f, _e = eng(x, q, lorentz_berthelot_nbfp(sig, eps), search=False)
+        force_matching_loss(f, f_t).backward()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, t in zip(g_ref, params):
+        assert rel_rms(t.grad.cpu(), a.cpu()) < 1e-5
+    with pytest.raises(TypeError):
+        force_matching_loss(f_t.double(), f_t.double())
+    eng.close()
