@@ -49,6 +49,7 @@ EXPORTED = [
     "nbx_ewald_coefficient", "nbx_pme_grid_size", "nbx_pme_create", "nbx_pme_destroy", "nbx_pme_last_error",
     "nbx_pme_set_stream", "nbx_pme_synchronize", "nbx_pme_get_info", "nbx_pme_compute_device",
     "nbx_pme_splines_device", "nbx_pme_spread_device", "nbx_pme_solve_device", "nbx_pme_gather_device",
+    "nbx_pme_fft_device", "nbx_fft3d_create", "nbx_fft3d_destroy", "nbx_fft3d_execute_device",
     "nbx_get_options", "nbx_set_force_accumulate", "nbx_get_force_accumulate", "nbx_leapfrog_create", "nbx_leapfrog_destroy",
     "nbx_leapfrog_last_error", "nbx_leapfrog_set_stream", "nbx_leapfrog_integrate", "nbx_leapfrog_integrate_device",
     "nbx_md_run_device", "nbx_fep_enable", "nbx_fep_set_lambda", "nbx_fep_get_energies", "nbx_fep_energies_device",
@@ -227,6 +228,10 @@ def load():
     L.nbx_pme_spread_device.argtypes = [vp, C.c_int, vp, vp, vp]
     L.nbx_pme_solve_device.argtypes = [vp, vp, vp, vp]
     L.nbx_pme_gather_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.nbx_pme_fft_device.argtypes = [vp, C.c_int, vp, vp]
+    L.nbx_fft3d_create.argtypes = [C.POINTER(C.c_int), C.c_int, C.POINTER(vp)]
+    L.nbx_fft3d_destroy.argtypes = [vp]
+    L.nbx_fft3d_execute_device.argtypes = [vp, C.c_int, vp, vp, vp]
     L.nbx_get_options.argtypes = [vp, C.POINTER(nbx_options)]
     L.nbx_set_force_accumulate.argtypes = [vp, C.c_int]
     L.nbx_get_force_accumulate.argtypes = [vp, C.POINTER(C.c_int)]

@@ -34,6 +34,7 @@ UNITS = {
     "nbx_pme.cu": [],
     "nbx_md.cu": [],
     "nbx_fep.cu": [],
+    "nbx_fft.cu": [],
 }
 
 
@@ -74,10 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
-        # cuFFT (the PME transforms) from the toolkit that compiles the library
-        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
-        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static",
-             "-L", cudalib, "-lcufft", "-Xlinker", "-rpath," + cudalib])
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static"])
     return LIB
 
 

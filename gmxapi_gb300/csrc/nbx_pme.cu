@@ -16,18 +16,18 @@
 //    src/gromacs/ewald/pme_solve.cpp:332-587);
 //  - the force gather (gather_f_bsplines / do_fspline,
 //    src/gromacs/ewald/pme_gather.cpp:78-360).
-// The 3-D real<->complex transforms are cuFFT's (unnormalised both ways, like the
-// reference's).  Spreading accumulates with float atomics (16-byte vector reductions
+// The 3-D real<->complex transforms are hand-written (nbx_fft.cu: one warp per line, Stockham
+// stages; unnormalised both ways, like the reference's).  Spreading accumulates with float atomics (16-byte vector reductions
 // when nz is a multiple of 4); the energy and the virial terms are summed per warp in
 // float and across the grid in FP64.
 //
 // Layouts in device memory: real grid [nx][ny][nz] (z fastest); half-complex grid
-// [nx][ny][nz/2+1] of float2 (the r2c output of cuFFT), so the complex index
+// [nx][ny][nz/2+1] of float2 (the usual real-to-complex layout), so the complex index
 // (kx, ky, kz) is the reference's (x, y, z) complex-grid cell with z halved.
 #include "../../include/nbnxm_gb300.h"
 #include "nbx_internal.cuh"
 
-#include <cufft.h>
+#include "nbx_fft.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -576,8 +576,8 @@ struct nbx_pme
     double*      sums      = nullptr;  // solve partials [kSolveMaxBlocks][8]: energy + 6 virial terms
     unsigned*    done      = nullptr;  // blocks of the running solve that have written their partials
     int          num_sms   = 1;
-    cufftHandle  r2c = 0, c2r = 0;
-    bool         plan_r2c = false, plan_c2r = false;
+    nbx::FftPlan3 fft{};  // the hand-written 3D real <-> half-complex transform (nbx_fft.cu)
+    bool          plan = false;
     std::string  err;
 };
 
@@ -758,15 +758,16 @@ int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float 
         nbx_pme_destroy(p);
         return pme_error(nullptr, NBX_ERR_OUT_OF_MEMORY, "PME allocation: " + msg);
     }
-    p->plan_r2c = cufftPlan3d(&p->r2c, grid[0], grid[1], grid[2], CUFFT_R2C) == CUFFT_SUCCESS;
-    p->plan_c2r = p->plan_r2c && cufftPlan3d(&p->c2r, grid[0], grid[1], grid[2], CUFFT_C2R) == CUFFT_SUCCESS;
-    if (!p->plan_c2r)
+    const cudaError_t fe = nbx::fft_plan_create(&p->fft, grid);
+    p->plan              = (fe == cudaSuccess);
+    if (!p->plan)
     {
         nbx_pme_destroy(p);
-        return pme_error(nullptr, NBX_ERR_CUDA, "cuFFT plan creation failed");
+        return pme_error(nullptr, fe == cudaErrorInvalidValue ? NBX_ERR_INVALID_INPUT : NBX_ERR_CUDA,
+                         fe == cudaErrorInvalidValue
+                                 ? "FFT grid size: every dimension must be at most 1024 with prime factors of at most 255"
+                                 : std::string("FFT plan: ") + cudaGetErrorString(fe));
     }
-    cufftSetStream(p->r2c, p->stream);
-    cufftSetStream(p->c2r, p->stream);
     *out = p;
     return NBX_OK;
 }
@@ -828,13 +829,9 @@ int nbx_pme_destroy(nbx_pme* p)
     {
         cudaStreamSynchronize(p->stream);
     }
-    if (p->plan_r2c)
+    if (p->plan)
     {
-        cufftDestroy(p->r2c);
-    }
-    if (p->plan_c2r)
-    {
-        cufftDestroy(p->c2r);
+        nbx::fft_plan_destroy(&p->fft);
     }
     cudaFree(p->grid);
     cudaFree(p->cgrid);
@@ -867,8 +864,6 @@ int nbx_pme_set_stream(nbx_pme* p, void* s)
     }
     p->stream     = static_cast<cudaStream_t>(s);
     p->own_stream = false;
-    cufftSetStream(p->r2c, p->stream);
-    cufftSetStream(p->c2r, p->stream);
     return NBX_OK;
 }
 
@@ -934,6 +929,75 @@ int nbx_pme_gather_device(nbx_pme* p, int natoms, const float* d_x, const float*
     return cuda_status(p, launch_gather(p, natoms, d_x, d_q, d_grid, d_f));
 }
 
+struct nbx_fft3d
+{
+    int           device = 0;
+    nbx::FftPlan3 plan{};
+};
+
+int nbx_fft3d_create(const int* grid, int device, nbx_fft3d** out)
+{
+    if (!grid || !out)
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null argument");
+    }
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess)
+    {
+        return pme_error(nullptr, NBX_ERR_NO_DEVICE, "no CUDA device " + std::to_string(device));
+    }
+    auto*             f = new nbx_fft3d;
+    f->device           = device;
+    const cudaError_t e = nbx::fft_plan_create(&f->plan, grid);
+    if (e != cudaSuccess)
+    {
+        nbx::fft_plan_destroy(&f->plan);
+        delete f;
+        return pme_error(nullptr, e == cudaErrorInvalidValue ? NBX_ERR_INVALID_INPUT : NBX_ERR_CUDA,
+                         e == cudaErrorInvalidValue
+                                 ? "FFT grid size: every dimension must be at most 1024 with prime factors of at most 255"
+                                 : std::string("FFT plan: ") + cudaGetErrorString(e));
+    }
+    *out = f;
+    return NBX_OK;
+}
+
+int nbx_fft3d_destroy(nbx_fft3d* f)
+{
+    if (f)
+    {
+        cudaSetDevice(f->device);
+        nbx::fft_plan_destroy(&f->plan);
+        delete f;
+    }
+    return NBX_OK;
+}
+
+int nbx_fft3d_execute_device(nbx_fft3d* f, int direction, float* d_real, void* d_cgrid, void* stream)
+{
+    if (!f || !d_real || !d_cgrid || (direction != 1 && direction != -1))
+    {
+        return pme_error(nullptr, NBX_ERR_INVALID_INPUT, "null argument or direction other than +1 / -1");
+    }
+    cudaSetDevice(f->device);
+    const auto        s = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = direction > 0 ? nbx::fft_r2c(f->plan, d_real, static_cast<float2*>(d_cgrid), s)
+                                        : nbx::fft_c2r(f->plan, static_cast<float2*>(d_cgrid), d_real, s);
+    return e == cudaSuccess ? NBX_OK : pme_error(nullptr, NBX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int nbx_pme_fft_device(nbx_pme* p, int direction, float* d_real, void* d_cgrid)
+{
+    if (!p || !d_real || !d_cgrid || (direction != 1 && direction != -1))
+    {
+        return pme_error(p, NBX_ERR_INVALID_INPUT, "null argument or direction other than +1 / -1");
+    }
+    cudaSetDevice(p->device);
+    const cudaError_t e = direction > 0 ? nbx::fft_r2c(p->fft, d_real, static_cast<float2*>(d_cgrid), p->stream)
+                                        : nbx::fft_c2r(p->fft, static_cast<float2*>(d_cgrid), d_real, p->stream);
+    return cuda_status(p, e);
+}
+
 int nbx_pme_compute_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_f, double* d_energy,
                            double* d_virial)
 {
@@ -947,18 +1011,20 @@ int nbx_pme_compute_device(nbx_pme* p, int natoms, const float* d_x, const float
     {
         return cuda_status(p, e);
     }
-    if (cufftExecR2C(p->r2c, p->grid, reinterpret_cast<cufftComplex*>(p->cgrid)) != CUFFT_SUCCESS)
+    e = nbx::fft_r2c(p->fft, p->grid, p->cgrid, p->stream);
+    if (e != cudaSuccess)
     {
-        return pme_error(p, NBX_ERR_CUDA, "cuFFT real-to-complex transform failed");
+        return cuda_status(p, e);
     }
     e = launch_solve(p, p->cgrid, d_energy, d_virial);
     if (e != cudaSuccess)
     {
         return cuda_status(p, e);
     }
-    if (cufftExecC2R(p->c2r, reinterpret_cast<cufftComplex*>(p->cgrid), p->grid) != CUFFT_SUCCESS)
+    e = nbx::fft_c2r(p->fft, p->cgrid, p->grid, p->stream);
+    if (e != cudaSuccess)
     {
-        return pme_error(p, NBX_ERR_CUDA, "cuFFT complex-to-real transform failed");
+        return cuda_status(p, e);
     }
     return cuda_status(p, launch_gather(p, natoms, d_x, d_q, p->grid, d_f));
 }

@@ -48,6 +48,34 @@ def grid_size(box, spacing: float = 0.12) -> tuple[int, int, int]:
     return int(n[0]), int(n[1]), int(n[2])
 
 
+class Fft3d:
+    """The 3D real <-> half-complex transform of a grid [nx][ny][nz] on one GPU (hand-written,
+    unnormalised; gmx_parallel_3dfft_init / _execute of src/gromacs/fft/parallel_3dfft.h on one
+    rank).  ``execute_device(+1, real, cgrid)``: real -> half-complex [nx][ny][nz/2+1] float2;
+    ``execute_device(-1, real, cgrid)``: back (cgrid overwritten)."""
+
+    def __init__(self, grid, device: int = 0):
+        self.grid = tuple(int(v) for v in grid)
+        n = (C.c_int * 3)(*self.grid)
+        h = C.c_void_p()
+        _check(_lib.load().nbx_fft3d_create(n, int(device), C.byref(h)))
+        self.h = h
+
+    def execute_device(self, direction: int, real_ptr: int, cgrid_ptr: int, stream_ptr: int = 0):
+        _check(_lib.load().nbx_fft3d_execute_device(self.h, int(direction), real_ptr, cgrid_ptr, stream_ptr))
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().nbx_fft3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Pme:
     """One PME grid of a rectangular box (pme_order 4) on one GPU: Coulomb (charges), or with
     ``lj=True`` the LJ-PME dispersion grid (geometric rule; coefficients sqrt(C6_ii), the
@@ -107,6 +135,11 @@ class Pme:
 
     def gather_device(self, natoms: int, x_ptr: int, q_ptr: int, grid_ptr: int, f_ptr: int):
         _check(_lib.load().nbx_pme_gather_device(self.h, natoms, x_ptr, q_ptr, grid_ptr, f_ptr), self.h)
+
+    def fft_device(self, direction: int, real_ptr: int, cgrid_ptr: int):
+        """The grid's 3D transform: +1 real -> half-complex, -1 back (unnormalised; the complex
+        grid is overwritten by the backward transform)."""
+        _check(_lib.load().nbx_pme_fft_device(self.h, int(direction), real_ptr, cgrid_ptr), self.h)
 
     def set_stream(self, stream_ptr: int):
         _check(_lib.load().nbx_pme_set_stream(self.h, stream_ptr), self.h)

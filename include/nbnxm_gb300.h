@@ -428,6 +428,22 @@ int nbx_pme_splines_device(nbx_pme* p, int natoms, const float* d_x, int* d_idx,
 int nbx_pme_spread_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, float* d_grid);
 int nbx_pme_solve_device(nbx_pme* p, void* d_cgrid, double* d_energy, double* d_virial);
 int nbx_pme_gather_device(nbx_pme* p, int natoms, const float* d_x, const float* d_q, const float* d_grid, float* d_f);
+/* The 3D transform of the handle's grid between the stages (see nbx_fft3d_execute_device). */
+int nbx_pme_fft_device(nbx_pme* p, int direction, float* d_real, void* d_cgrid);
+
+/* ---- the 3D real <-> half-complex FFT on its own (hand-written, no FFT library) ---- */
+typedef struct nbx_fft3d nbx_fft3d;
+/* Replaces gmx_parallel_3dfft_init (src/gromacs/fft/parallel_3dfft.h) on one rank for real data:
+ * grid[3] = {nx, ny, nz}, each in [1, 1024] with prime factors of at most 255 (NBX_ERR_INVALID_INPUT
+ * otherwise; PME grids from nbx_pme_grid_size always qualify). */
+int nbx_fft3d_create(const int* grid, int device, nbx_fft3d** out);
+int nbx_fft3d_destroy(nbx_fft3d* f);
+/* Replaces gmx_parallel_3dfft_execute: direction +1 real d_real[nx][ny][nz] -> half-complex
+ * d_cgrid[nx][ny][nz/2+1] (float2, exp(-2 pi i ...)); -1 d_cgrid -> d_real (exp(+2 pi i ...),
+ * d_cgrid overwritten; the imaginary parts of the kz = 0 and, for even nz, kz = nz/2 planes are
+ * taken as a Hermitian spectrum's, i.e. dropped).  Unnormalised both ways, as the reference's.  On
+ * `stream`; device memory. */
+int nbx_fft3d_execute_device(nbx_fft3d* f, int direction, float* d_real, void* d_cgrid, void* stream);
 
 /* ---- GPU-resident MD steps: leap-frog and the step loop ---- */
 typedef struct nbx_leapfrog nbx_leapfrog;

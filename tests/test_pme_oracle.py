@@ -204,3 +204,24 @@ def test_lj_pme_reproduces_the_fcc_lattice_energy():
     expect = 0.5 * s.n * (c12 * 12.13188 / a ** 12 - c6 * 14.45392 / a ** 6) - 0.5 * s.n * n_rc * c12 / rc ** 12
     assert e_real[0] + e_rec == pytest.approx(expect, rel=2e-5)
     assert np.abs(f_real + f_rec).max() < 1e-2  # lattice sites are force-free
+
+
+def test_fft_golden_vector_is_numpy_rfftn():
+    """The reference's 3D FFT test vector (tests/golden/fft_golden.json, from FFFTest3D.Real5_6_9)
+    is numpy's unnormalised rfftn forward and N * irfftn backward in the engine's layout."""
+    import json
+    import os
+
+    import numpy as np
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fft_golden.json")) as fh:
+        g = json.load(fh)
+    grid = g["grid"]
+    nzc = grid[2] // 2 + 1
+    x = np.array(g["forward_input"]).reshape(grid)
+    want = np.array(g["forward_output"]).reshape(grid[0], grid[1], nzc, 2)
+    np.testing.assert_allclose(np.fft.rfftn(x), want[..., 0] + 1j * want[..., 1], rtol=1e-12, atol=1e-10)
+    c = np.array(g["backward_input"]).reshape(grid[0], grid[1], nzc, 2)
+    back = np.fft.irfftn(c[..., 0] + 1j * c[..., 1], s=grid, axes=(0, 1, 2)) * np.prod(grid)
+    np.testing.assert_allclose(back, np.array(g["backward_output"]).reshape(grid), rtol=1e-12, atol=1e-10)
+    assert g["reference_complex_axis_order"] == ["y", "kz", "x"]
