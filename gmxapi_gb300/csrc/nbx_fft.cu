@@ -21,7 +21,7 @@ size_t z_smem(int n)
 
 size_t strided_smem(int n)
 {
-    return sizeof(float2) * ((size_t)n + (size_t)n * (kFftTile + 1) + (size_t)kFftTile * n);
+    return fft_tiled_smem(n);
 }
 
 __device__ __forceinline__ void load_roots(float2* W, const FftAxis& ax)
@@ -218,7 +218,25 @@ bool factorize(int n, FftAxis& ax)
             m /= p;
         }
     }
-    return m == 1;
+    if (m != 1)
+    {
+        return false;
+    }
+    for (auto& wd : ax.stw)
+    {
+        wd = 0;
+    }
+    int Ns = 1;
+    for (int st = 0; st < ax.nfac; st++)
+    {
+        const int R  = (int)((ax.facs >> (8 * st)) & 255u);
+        const int mm = n / R;
+        const int ts = mm / Ns;
+        const unsigned long long word = (unsigned)R | ((unsigned)mm << 8) | ((unsigned)ts << 20);
+        ax.stw[st / 2] |= word << (32 * (st & 1));
+        Ns *= R;
+    }
+    return true;
 }
 
 } // namespace
@@ -289,7 +307,7 @@ void fft_plan_destroy(FftPlan3* p)
     p->roots = nullptr;
 }
 
-cudaError_t fft_r2c(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s)
+cudaError_t fft_r2c_zy(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s)
 {
     const int nlines = p.n[0] * p.n[1];
     k_fft_z_r2c<<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], real, cplx, nlines);
@@ -298,6 +316,12 @@ cudaError_t fft_r2c(const FftPlan3& p, const float* real, float2* cplx, cudaStre
     {
         e = strided_pass<false>(p, 1, cplx, s);
     }
+    return e;
+}
+
+cudaError_t fft_r2c(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s)
+{
+    cudaError_t e = fft_r2c_zy(p, real, cplx, s);
     if (e == cudaSuccess && p.n[0] > 1)
     {
         e = strided_pass<false>(p, 0, cplx, s);
@@ -305,14 +329,10 @@ cudaError_t fft_r2c(const FftPlan3& p, const float* real, float2* cplx, cudaStre
     return e;
 }
 
-cudaError_t fft_c2r(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s)
+cudaError_t fft_c2r_yz(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s)
 {
     cudaError_t e = cudaSuccess;
-    if (p.n[0] > 1)
-    {
-        e = strided_pass<true>(p, 0, cplx, s);
-    }
-    if (e == cudaSuccess && p.n[1] > 1)
+    if (p.n[1] > 1)
     {
         e = strided_pass<true>(p, 1, cplx, s);
     }
@@ -323,6 +343,16 @@ cudaError_t fft_c2r(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s
     const int nlines = p.n[0] * p.n[1];
     k_fft_z_c2r<<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], cplx, real, nlines);
     return cudaGetLastError();
+}
+
+cudaError_t fft_c2r(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s)
+{
+    cudaError_t e = cudaSuccess;
+    if (p.n[0] > 1)
+    {
+        e = strided_pass<true>(p, 0, cplx, s);
+    }
+    return e == cudaSuccess ? fft_c2r_yz(p, cplx, real, s) : e;
 }
 
 } // namespace nbx

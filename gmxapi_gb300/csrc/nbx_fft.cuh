@@ -30,6 +30,9 @@ struct FftAxis
     int                n;
     int                nfac;
     unsigned long long facs;
+    // stage words, two per element (stage s in bits 32 (s & 1) of stw[s / 2]): radix R (bits 0-7),
+    // butterflies m = n / R (bits 8-19), root step ts = n / (Ns R) (bits 20-31)
+    unsigned long long stw[kFftMaxFactors / 2];
     const float2*      roots;  // exp(-2 pi i k / n), k = 0 .. n-1 (device)
 };
 
@@ -190,27 +193,37 @@ __device__ bool fft_line(float2* a, int sa, float2* b, int sb, const float2* W, 
     bool      inb = false;
     for (int s = 0; s < ax.nfac; s++)
     {
-        FftStage st;
-        st.R              = (int)((ax.facs >> (8 * s)) & 255u);
+        // the stage's constants from the plan (no integer division on the device)
+        const unsigned long long q = (s < 2) ? ax.stw[0] : (s < 4) ? ax.stw[1] : (s < 6) ? ax.stw[2] : ax.stw[3];
+        const unsigned           w = (unsigned)(q >> (32 * (s & 1)));
+        FftStage                 st;
+        st.R              = (int)(w & 255u);
+        st.m              = (int)((w >> 8) & 4095u);
+        st.ts             = (int)(w >> 20);
         st.Ns             = Ns;
-        st.m              = n / st.R;
-        st.ts             = st.m / Ns;
-        st.inv_ns         = 1.0f / (float)Ns;
+        st.inv_ns         = __frcp_rn((float)Ns);
         const int     R   = st.R;
         const int     m   = st.m;
         const float2* src = inb ? b : a;
         float2*       dst = inb ? a : b;
         const int     ss = inb ? sb : sa, ds = inb ? sa : sb;
-        for (int j = lane; j < m; j += 32)
+        switch (R)
         {
-            switch (R)
-            {
-                case 2: fft_butterfly<2, kInv>(src, ss, dst, ds, W, n, st, j); break;
-                case 3: fft_butterfly<3, kInv>(src, ss, dst, ds, W, n, st, j); break;
-                case 4: fft_butterfly<4, kInv>(src, ss, dst, ds, W, n, st, j); break;
-                case 5: fft_butterfly<5, kInv>(src, ss, dst, ds, W, n, st, j); break;
-                default: fft_butterfly_any<kInv>(src, ss, dst, ds, W, st, j); break;
-            }
+            case 2:
+                for (int j = lane; j < m; j += 32) fft_butterfly<2, kInv>(src, ss, dst, ds, W, n, st, j);
+                break;
+            case 3:
+                for (int j = lane; j < m; j += 32) fft_butterfly<3, kInv>(src, ss, dst, ds, W, n, st, j);
+                break;
+            case 4:
+                for (int j = lane; j < m; j += 32) fft_butterfly<4, kInv>(src, ss, dst, ds, W, n, st, j);
+                break;
+            case 5:
+                for (int j = lane; j < m; j += 32) fft_butterfly<5, kInv>(src, ss, dst, ds, W, n, st, j);
+                break;
+            default:
+                for (int j = lane; j < m; j += 32) fft_butterfly_any<kInv>(src, ss, dst, ds, W, st, j);
+                break;
         }
         __syncwarp();
         Ns *= R;
@@ -236,5 +249,13 @@ void        fft_plan_destroy(FftPlan3* p);
 cudaError_t fft_r2c(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s);
 // half-complex -> real (unnormalised, exp(+2 pi i ...)); cplx is overwritten.
 cudaError_t fft_c2r(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s);
+// The same without the x transforms (a caller that fuses its own x pass between them).
+cudaError_t fft_r2c_zy(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s);
+cudaError_t fft_c2r_yz(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s);
+// Dynamic shared memory of a tiled pass over lines of length n (roots, tile, per-warp scratch).
+inline size_t fft_tiled_smem(int n)
+{
+    return sizeof(float2) * ((size_t)n + (size_t)n * (kFftTile + 1) + (size_t)kFftTile * n);
+}
 
 } // namespace nbx

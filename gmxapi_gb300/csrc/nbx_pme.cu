@@ -298,6 +298,122 @@ __device__ void solve_finish(const float acc[7], double* partials, unsigned int*
     }
 }
 
+// One point (kx, ky, kz) != 0 of solve_pme_yzx (pme_solve.cpp:332-587): scales c by eterm and, with
+// energies, adds its energy and virial terms to acc.
+__device__ __forceinline__ void solve_point(const PmeDims& d, const float* __restrict__ bsp, float elfac, float factor,
+                                            float pivol, int kx, int ky, int kz, bool energy, float2& c, float acc[7])
+{
+    const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
+    const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
+    const float mhx   = (float)mx * d.rec[0];
+    const float mhy   = (float)my * d.rec[1];
+    const float mhz   = (float)kz * d.rec[2];
+    const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
+    const float by    = pivol * bsp[d.n[0] + ky];
+    const float den   = m2 * bsp[d.n[0] + d.n[1] + kz] * by * bsp[kx];
+    const float eterm = elfac / den * expf(-factor * m2);
+    if (energy)
+    {
+        const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
+        const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
+        const float ets2    = corner * eterm * struct2;
+        const float ets2vf  = ets2 * ((factor * m2 + 1.0f) * 2.0f / m2);
+        acc[0] += ets2;
+        acc[1] += ets2vf * mhx * mhx - ets2;
+        acc[2] += ets2vf * mhx * mhy;
+        acc[3] += ets2vf * mhx * mhz;
+        acc[4] += ets2vf * mhy * mhy - ets2;
+        acc[5] += ets2vf * mhy * mhz;
+        acc[6] += ets2vf * mhz * mhz - ets2;
+    }
+    c.x *= eterm;
+    c.y *= eterm;
+}
+
+// The x transform of the forward FFT, the solve and the x transform of the backward FFT in one
+// pass over the half-complex grid (the x lines are the last forward and the first backward
+// transform): block (ky, z-tile) loads the tile [nx][T] of x lines, warp c transforms column c,
+// solves its points (kx, ky, kz = tile * T + c) and transforms it back; energy and virial sums as
+// k_pme_solve's.
+template<bool kEnergy>
+__global__ void __launch_bounds__(kSolveThreads) k_pme_fft_x_solve(nbx::FftAxis ax, PmeDims d, float2* cgrid,
+                                                                   const float* __restrict__ bsp, float elfac,
+                                                                   float factor, float pivol, int ntiles, double* partials,
+                                                                   unsigned int* done, double* energy_out,
+                                                                   double* virial_out)
+{
+    constexpr int T    = nbx::kFftTile;
+    extern __shared__ float2 xsm[];
+    const int     n    = ax.n;  // nx
+    const int     nzc  = d.n[2] / 2 + 1;
+    float2*       W    = xsm;
+    float2*       tile = xsm + n;                  // [n][T + 1]
+    float2*       scr  = tile + (size_t)n * (T + 1);  // [T][n]
+    const int     ky   = blockIdx.x / ntiles;
+    const int     t    = blockIdx.x - ky * ntiles;
+    const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t  base = (size_t)ky * nzc + (size_t)t * T;
+    const size_t  es   = (size_t)d.n[1] * nzc;
+    const int     cols = min(T, nzc - t * T);
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+    {
+        W[k] = ax.roots[k];
+    }
+    for (int idx = threadIdx.x; idx < n * T; idx += blockDim.x)
+    {
+        const int i = idx / T, c = idx - i * T;
+        tile[i * (T + 1) + c] = c < cols ? cgrid[base + (size_t)i * es + c] : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    float acc[7] = { 0, 0, 0, 0, 0, 0, 0 };
+    if (warp < cols)
+    {
+        float2*   col = tile + warp;
+        float2*   s   = scr + (size_t)warp * n;
+        const int kz  = t * T + warp;
+        // forward along x, then the solve on the column wherever the transform left it
+        const bool in_s = nbx::fft_line<false>(col, T + 1, s, 1, W, ax, lane);
+        float2*    v    = in_s ? s : col;
+        const int  vs   = in_s ? 1 : T + 1;
+        for (int kx = lane; kx < n; kx += 32)
+        {
+            if (kx != 0 || ky != 0 || kz != 0)
+            {
+                float2 c = v[kx * vs];
+                solve_point(d, bsp, elfac, factor, pivol, kx, ky, kz, kEnergy, c, acc);
+                v[kx * vs] = c;
+            }
+        }
+        __syncwarp();
+        // backward along x
+        float2*    other = in_s ? col : s;
+        const int  os    = in_s ? T + 1 : 1;
+        const bool moved = nbx::fft_line<true>(v, vs, other, os, W, ax, lane);
+        // the result is in `other` when moved; bring it to the tile column
+        if (moved != in_s)
+        {
+            // result in s
+            for (int i = lane; i < n; i += 32)
+            {
+                col[i * (T + 1)] = s[i];
+            }
+        }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * T; idx += blockDim.x)
+    {
+        const int i = idx / T, c = idx - i * T;
+        if (c < cols)
+        {
+            cgrid[base + (size_t)i * es + c] = tile[i * (T + 1) + c];
+        }
+    }
+    if (kEnergy)
+    {
+        solve_finish(acc, partials, done, energy_out, virial_out);
+    }
+}
+
 // solve_pme_yzx over the half-complex grid: scales each element by eterm and sums the
 // energy and virial terms (energy = 0.5 sum, virial = 0.25 sum).  Per-point terms and
 // per-thread / per-warp sums are float (the reference sums them in `real`); each block
@@ -321,32 +437,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_pme_solve(PmeDims d, float2* 
     {
         if (kx != 0 || ky != 0 || kz != 0)
         {
-            const int   mx    = kx < (d.n[0] + 1) / 2 ? kx : kx - d.n[0];
-            const int   my    = ky < (d.n[1] + 1) / 2 ? ky : ky - d.n[1];
-            const float mhx   = (float)mx * d.rec[0];
-            const float mhy   = (float)my * d.rec[1];
-            const float mhz   = (float)kz * d.rec[2];
-            const float m2    = mhx * mhx + mhy * mhy + mhz * mhz;
-            const float by    = pivol * bsp[d.n[0] + ky];
-            const float den   = m2 * bsp[d.n[0] + d.n[1] + kz] * by * bsp[kx];
-            const float eterm = elfac / den * expf(-factor * m2);
-            float2      c     = cgrid[t];
-            if (energy)
-            {
-                const float corner  = (kz == 0 || kz == (d.n[2] + 1) / 2) ? 0.5f : 1.0f;
-                const float struct2 = 2.0f * (c.x * c.x + c.y * c.y);
-                const float ets2    = corner * eterm * struct2;
-                const float ets2vf  = ets2 * ((factor * m2 + 1.0f) * 2.0f / m2);
-                acc[0] += ets2;
-                acc[1] += ets2vf * mhx * mhx - ets2;
-                acc[2] += ets2vf * mhx * mhy;
-                acc[3] += ets2vf * mhx * mhz;
-                acc[4] += ets2vf * mhy * mhy - ets2;
-                acc[5] += ets2vf * mhy * mhz;
-                acc[6] += ets2vf * mhz * mhz - ets2;
-            }
-            c.x *= eterm;
-            c.y *= eterm;
+            float2 c = cgrid[t];
+            solve_point(d, bsp, elfac, factor, pivol, kx, ky, kz, energy, c, acc);
             cgrid[t] = c;
         }
         kz += sz;
@@ -578,6 +670,7 @@ struct nbx_pme
     int          num_sms   = 1;
     nbx::FftPlan3 fft{};  // the hand-written 3D real <-> half-complex transform (nbx_fft.cu)
     bool          plan = false;
+    bool          fused_smem_ok = false;  // the fused x pass + solve has its shared memory
     std::string  err;
 };
 
@@ -646,6 +739,43 @@ cudaError_t launch_solve(nbx_pme* p, float2* cgrid, double* d_energy, double* d_
     const float pivol = (float)M_PI * (float)vol;
     k_pme_solve<<<nblocks, kSolveThreads, 0, p->stream>>>(p->d, cgrid, p->bsp, elfac, factor, pivol, p->sums,
                                                           p->done, d_energy, d_virial);
+    return cudaGetLastError();
+}
+
+// The fused x pass + Coulomb solve: one block per (ky, z-tile), the solve's partials sized for
+// kSolveMaxBlocks blocks.
+int x_solve_blocks(const nbx_pme* p)
+{
+    const int nzc = p->d.n[2] / 2 + 1;
+    return p->d.n[1] * ((nzc + nbx::kFftTile - 1) / nbx::kFftTile);
+}
+
+bool fused_x_solve(const nbx_pme* p)
+{
+    return !p->lj && p->d.n[0] > 1 && x_solve_blocks(p) <= kSolveMaxBlocks && p->fused_smem_ok;
+}
+
+cudaError_t launch_x_solve(nbx_pme* p, double* d_energy, double* d_virial)
+{
+    const double vol    = (double)p->box[0] * p->box[1] * p->box[2];
+    const float  factor = (float)(M_PI * M_PI) / (p->beta * p->beta);
+    const float  elfac  = (float)nbx::one_4pi_eps0() / p->epsilon_r;
+    const float  pivol  = (float)M_PI * (float)vol;
+    const int    nzc    = p->d.n[2] / 2 + 1;
+    const int    ntiles = (nzc + nbx::kFftTile - 1) / nbx::kFftTile;
+    const size_t smem   = nbx::fft_tiled_smem(p->d.n[0]);
+    if (d_energy || d_virial)
+    {
+        k_pme_fft_x_solve<true><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
+                p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, d_energy,
+                d_virial);
+    }
+    else
+    {
+        k_pme_fft_x_solve<false><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
+                p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, nullptr,
+                nullptr);
+    }
     return cudaGetLastError();
 }
 
@@ -760,6 +890,15 @@ int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float 
     }
     const cudaError_t fe = nbx::fft_plan_create(&p->fft, grid);
     p->plan              = (fe == cudaSuccess);
+    if (p->plan)
+    {
+        const size_t xs  = nbx::fft_tiled_smem(grid[0]);
+        p->fused_smem_ok = xs <= 48 * 1024
+                           || (cudaFuncSetAttribute(k_pme_fft_x_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)xs) == cudaSuccess
+                               && cudaFuncSetAttribute(k_pme_fft_x_solve<false>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs) == cudaSuccess);
+    }
     if (!p->plan)
     {
         nbx_pme_destroy(p);
@@ -1010,6 +1149,24 @@ int nbx_pme_compute_device(nbx_pme* p, int natoms, const float* d_x, const float
     if (e != cudaSuccess)
     {
         return cuda_status(p, e);
+    }
+    if (fused_x_solve(p))
+    {
+        // z and y forward, then x forward + solve + x backward in one pass, then y and z backward
+        e = nbx::fft_r2c_zy(p->fft, p->grid, p->cgrid, p->stream);
+        if (e == cudaSuccess)
+        {
+            e = launch_x_solve(p, d_energy, d_virial);
+        }
+        if (e == cudaSuccess)
+        {
+            e = nbx::fft_c2r_yz(p->fft, p->cgrid, p->grid, p->stream);
+        }
+        if (e != cudaSuccess)
+        {
+            return cuda_status(p, e);
+        }
+        return cuda_status(p, launch_gather(p, natoms, d_x, d_q, p->grid, d_f));
     }
     e = nbx::fft_r2c(p->fft, p->grid, p->cgrid, p->stream);
     if (e != cudaSuccess)
