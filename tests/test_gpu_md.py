@@ -166,3 +166,34 @@ def test_md_nve_energy_drift(md):
     assert np.all(np.isfinite(etot))
     assert drift <= 2e-3 * ekin.mean()  # measured ~3e-5
     run.close()
+
+
+def test_leapfrog_kernel_reproduces_the_reference_leapfrog_test(md):
+    """The reference's own LeapFrogTest.SimpleIntegration data (10 cases without coupling) through
+    the GPU update; the kernel puts atoms in the box, so positions are compared modulo the box
+    (edges 25, 10, 10 nm), within the reference test's tolerance (absolute, steps x 5e-6) plus the
+    rounding of the wrap."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "leapfrog_golden.json")) as fh:
+        cases = json.load(fh)["cases"]
+    box = np.array([25.0, 10.0, 10.0])
+    for case in cases:
+        n = case["num_atoms"]
+        i = np.arange(n)
+        x = np.stack([(i % 21) * 1.0, 6.5 - (i % 13) * 1.0, np.zeros(n)], -1).astype(np.float32)
+        v = np.tile(np.array(case["v0"], np.float32), (n, 1))
+        f = np.tile(np.array(case["f0"], np.float32), (n, 1))
+        im = (1.0 / (1.0 + (i % 100))).astype(np.float32)
+        lf = md.LeapFrog(im, tuple(box))
+        for _ in range(case["num_steps"]):
+            lf.integrate(case["dt"], x, v, f)
+        lf.close()
+        want = np.array(case["final_x"])
+        want = want - np.floor(want / box) * box
+        d = np.abs(x - want)
+        d = np.minimum(d, box - d)  # a coordinate on the box edge may wrap to either side
+        tol = case["tolerance"] + 2e-6
+        assert d.max() <= tol, (case["index"], d.max())
+        np.testing.assert_allclose(v, case["final_v"], rtol=0, atol=case["tolerance"])

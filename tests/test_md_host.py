@@ -80,3 +80,39 @@ def test_leapfrog_without_gpu_reports_no_device(md_mod):
     with pytest.raises(_lib.NbxError) as ei:
         md_mod.LeapFrog(np.ones(4, np.float32), (2.0, 2.0, 2.0))
     assert ei.value.code == _lib.NBX_ERR_NO_DEVICE
+
+
+def _leapfrog_golden():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "leapfrog_golden.json")) as fh:
+        return json.load(fh)["cases"]
+
+
+def _leapfrog_start(case):
+    import numpy as np
+
+    n = case["num_atoms"]
+    i = np.arange(n)
+    x = np.stack([(i % 21) * 1.0, 6.5 - (i % 13) * 1.0, np.zeros(n)], -1).astype(np.float32)
+    v = np.tile(np.array(case["v0"], np.float32), (n, 1))
+    f = np.tile(np.array(case["f0"], np.float32), (n, 1))
+    im = (1.0 / (1.0 + (i % 100))).astype(np.float32)
+    return x, v, f, im
+
+
+def test_leapfrog_oracle_reproduces_the_reference_leapfrog_test():
+    """The reference's own LeapFrogTest.SimpleIntegration data (src/gromacs/mdlib/tests/leapfrog.cpp,
+    the 10 cases without coupling; tests/golden/leapfrog_golden.json) within that test's tolerance
+    (absolute, steps x 5e-6), with the positions left unwrapped as the reference test does."""
+    import numpy as np
+
+    from oracle import md_oracle as M
+
+    for case in _leapfrog_golden():
+        x, v, f, im = _leapfrog_start(case)
+        for _ in range(case["num_steps"]):
+            x, v, _ = M.leapfrog(x, v, f, im, case["dt"], (1e3, 1e3, 1e3), wrap=False)
+        np.testing.assert_allclose(x, case["final_x"], rtol=0, atol=case["tolerance"])
+        np.testing.assert_allclose(v, case["final_v"], rtol=0, atol=case["tolerance"])

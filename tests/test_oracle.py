@@ -237,3 +237,23 @@ def test_erf_series_coefficients_and_accuracy():
         exact = erf(x) / x * math.sqrt(math.pi) / 2
         worst = max(worst, abs(s - exact) / exact)
     assert worst <= 1.5e-8, worst
+
+
+def test_shift_numbering_is_the_references():
+    """The shift index the pair-list entries carry (xyz2is: 5 (3 (z + 1) + y + 1) + x + 2, central
+    22, as in the oracle and the search kernels) against the reference's calc_shifts output for its
+    test box (PbcTest.CalcShiftsWorks, tests/golden/shift_golden.json), whose 45 vectors are all
+    distinct: vector n = x a + y b + z c for the decomposition of n."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shift_golden.json")) as fh:
+        g = json.load(fh)
+    a, b, c = (np.array(r) for r in g["box"])
+    got = []
+    for n in range(45):
+        x, y, z = n % 5 - 2, (n // 5) % 3 - 1, n // 15 - 1
+        assert 5 * (3 * (z + 1) + y + 1) + x + 2 == n
+        got.append(x * a + y * b + z * c)
+    np.testing.assert_allclose(np.array(got), np.array(g["shift_vectors"]), rtol=0, atol=1e-9)
+    assert 5 * (3 * 1 + 1) + 2 == 22  # the central shift (no image), CENTRAL / kCentral
