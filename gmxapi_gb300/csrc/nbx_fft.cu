@@ -24,6 +24,11 @@ size_t strided_smem(int n)
     return fft_tiled_smem(n);
 }
 
+int z_blocks(int nlines)
+{
+    return std::max(1, ((nlines + 1) / 2 + kZWarps - 1) / kZWarps);
+}
+
 __device__ __forceinline__ void load_roots(float2* W, const FftAxis& ax)
 {
     for (int k = threadIdx.x; k < ax.n; k += blockDim.x)
@@ -35,12 +40,13 @@ __device__ __forceinline__ void load_roots(float2* W, const FftAxis& ax)
 
 // z forward: lines 2p and 2p + 1 of the real grid as one complex line a + i b, transformed, then
 // A_k = (Z_k + conj Z_{n-k}) / 2 and B_k = (Z_k - conj Z_{n-k}) / 2i for k = 0 .. n/2.
+template<int kN>
 __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_r2c(FftAxis ax, const float* __restrict__ real,
                                                             float2* __restrict__ cplx, int nlines)
 {
     extern __shared__ float2 fsm[];
     float2*   W    = fsm;
-    const int n    = ax.n;
+    const int n    = kN > 0 ? kN : ax.n;
     const int nzc  = n / 2 + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2*   a    = fsm + n + warp * 2 * n;
@@ -56,7 +62,7 @@ __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_r2c(FftAxis ax, const fl
             a[i] = make_float2(real[(size_t)la * n + i], hb ? real[(size_t)lb * n + i] : 0.0f);
         }
         __syncwarp();
-        const float2* z = fft_line<false>(a, 1, b, 1, W, ax, lane) ? b : a;
+        const float2* z = fft_line_any<kN, false>(a, 1, b, 1, W, ax, lane) ? b : a;
         for (int k = lane; k < nzc; k += 32)
         {
             const float2 zk = z[k];
@@ -75,12 +81,13 @@ __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_r2c(FftAxis ax, const fl
 // imaginary parts are lines 2p and 2p + 1 of the real grid.  The imaginary parts of A_0 and B_0
 // (and of A_{n/2}, B_{n/2} for even n) are dropped, as a complex-to-real transform that assumes a
 // Hermitian line does.
+template<int kN>
 __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_c2r(FftAxis ax, const float2* __restrict__ cplx,
                                                             float* __restrict__ real, int nlines)
 {
     extern __shared__ float2 fsm[];
     float2*   W    = fsm;
-    const int n    = ax.n;
+    const int n    = kN > 0 ? kN : ax.n;
     const int nzc  = n / 2 + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2*   a    = fsm + n + warp * 2 * n;
@@ -111,7 +118,7 @@ __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_c2r(FftAxis ax, const fl
             a[k] = make_float2(A.x - B.y, A.y + B.x);
         }
         __syncwarp();
-        const float2* z = fft_line<true>(a, 1, b, 1, W, ax, lane) ? b : a;
+        const float2* z = fft_line_any<kN, true>(a, 1, b, 1, W, ax, lane) ? b : a;
         for (int i = lane; i < n; i += 32)
         {
             const float2 v             = z[i];
@@ -128,13 +135,13 @@ __global__ void __launch_bounds__(kZWarps * 32) k_fft_z_c2r(FftAxis ax, const fl
 // Lines along y or x of the half-complex grid: block (outer index o, tile t) loads the kFftTile
 // z-frequencies t*T .. t*T + T-1 of all n points of the line (rows of T consecutive elements:
 // coalesced), warp c transforms column c, the tile is written back.
-template<bool kInv>
+template<bool kInv, int kN>
 __global__ void __launch_bounds__(kFftTile * 32) k_fft_strided(FftAxis ax, float2* __restrict__ data, int elem_stride,
                                                                int outer_stride, int ntiles, int nzc)
 {
     extern __shared__ float2 fsm[];
     float2*   W    = fsm;
-    const int n    = ax.n;
+    const int n    = kN > 0 ? kN : ax.n;
     float2*   tile = fsm + n;                        // [n][T + 1]
     float2*   scr  = tile + (size_t)n * (kFftTile + 1);  // [T][n]
     const int o    = blockIdx.x / ntiles;
@@ -142,7 +149,7 @@ __global__ void __launch_bounds__(kFftTile * 32) k_fft_strided(FftAxis ax, float
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t base = (size_t)o * outer_stride + (size_t)t * kFftTile;
     const int    cols = min(kFftTile, nzc - t * kFftTile);
-    for (int k = threadIdx.x; k < ax.n; k += blockDim.x)
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
     {
         W[k] = ax.roots[k];
     }
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(kFftTile * 32) k_fft_strided(FftAxis ax, float
     {
         float2* col = tile + warp;
         float2* s   = scr + (size_t)warp * n;
-        if (fft_line<kInv>(col, kFftTile + 1, s, 1, W, ax, lane))
+        if (fft_line_any<kN, kInv>(col, kFftTile + 1, s, 1, W, ax, lane))
         {
             for (int i = lane; i < n; i += 32)
             {
@@ -175,14 +182,10 @@ __global__ void __launch_bounds__(kFftTile * 32) k_fft_strided(FftAxis ax, float
     }
 }
 
-int z_blocks(int nlines)
-{
-    return std::max(1, ((nlines + 1) / 2 + kZWarps - 1) / kZWarps);
-}
 
 // strided pass over axis 0 (x) or 1 (y)
-template<bool kInv>
-cudaError_t strided_pass(const FftPlan3& p, int axis, float2* cplx, cudaStream_t s)
+template<bool kInv, int kN>
+void strided_launch(const FftPlan3& p, int axis, float2* cplx, cudaStream_t s)
 {
     const int nzc    = p.n[2] / 2 + 1;
     const int ntiles = (nzc + kFftTile - 1) / kFftTile;
@@ -190,8 +193,48 @@ cudaError_t strided_pass(const FftPlan3& p, int axis, float2* cplx, cudaStream_t
     const int outer  = axis == 1 ? p.n[1] * nzc : nzc;
     const int nouter = axis == 1 ? p.n[0] : p.n[1];
     const FftAxis& ax = p.ax[axis];
-    k_fft_strided<kInv><<<nouter * ntiles, kFftTile * 32, strided_smem(ax.n), s>>>(ax, cplx, elem, outer, ntiles,
-                                                                                   nzc);
+    k_fft_strided<kInv, kN><<<nouter * ntiles, kFftTile * 32, strided_smem(ax.n), s>>>(ax, cplx, elem, outer, ntiles,
+                                                                                       nzc);
+}
+
+template<bool kInv>
+cudaError_t strided_pass(const FftPlan3& p, int axis, float2* cplx, cudaStream_t s)
+{
+    switch (p.n[axis])
+    {
+#define NBX_FFT_CASE(L)                                                                                                \
+    case L: strided_launch<kInv, L>(p, axis, cplx, s); break;
+        NBX_FFT_FIXED_LENGTHS(NBX_FFT_CASE)
+#undef NBX_FFT_CASE
+        default: strided_launch<kInv, 0>(p, axis, cplx, s); break;
+    }
+    return cudaGetLastError();
+}
+
+template<int kN>
+void z_launch(bool inv, const FftPlan3& p, const float* real_in, float* real_out, float2* cplx, cudaStream_t s)
+{
+    const int nlines = p.n[0] * p.n[1];
+    if (!inv)
+    {
+        k_fft_z_r2c<kN><<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], real_in, cplx, nlines);
+    }
+    else
+    {
+        k_fft_z_c2r<kN><<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], cplx, real_out, nlines);
+    }
+}
+
+cudaError_t z_pass(bool inv, const FftPlan3& p, const float* real_in, float* real_out, float2* cplx, cudaStream_t s)
+{
+    switch (p.n[2])
+    {
+#define NBX_FFT_CASE(L)                                                                                                \
+    case L: z_launch<L>(inv, p, real_in, real_out, cplx, s); break;
+        NBX_FFT_FIXED_LENGTHS(NBX_FFT_CASE)
+#undef NBX_FFT_CASE
+        default: z_launch<0>(inv, p, real_in, real_out, cplx, s); break;
+    }
     return cudaGetLastError();
 }
 
@@ -284,18 +327,18 @@ cudaError_t fft_plan_create(FftPlan3* p, const int n[3])
     const size_t smax = std::max(strided_smem(n[0]), strided_smem(n[1]));
     if (e == cudaSuccess && zmax > 48 * 1024)
     {
-        e = cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zmax);
+        e = cudaFuncSetAttribute(k_fft_z_r2c<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zmax);
         if (e == cudaSuccess)
         {
-            e = cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zmax);
+            e = cudaFuncSetAttribute(k_fft_z_c2r<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zmax);
         }
     }
     if (e == cudaSuccess && smax > 48 * 1024)
     {
-        e = cudaFuncSetAttribute(k_fft_strided<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+        e = cudaFuncSetAttribute(k_fft_strided<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
         if (e == cudaSuccess)
         {
-            e = cudaFuncSetAttribute(k_fft_strided<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+            e = cudaFuncSetAttribute(k_fft_strided<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
         }
     }
     return e;
@@ -309,9 +352,7 @@ void fft_plan_destroy(FftPlan3* p)
 
 cudaError_t fft_r2c_zy(const FftPlan3& p, const float* real, float2* cplx, cudaStream_t s)
 {
-    const int nlines = p.n[0] * p.n[1];
-    k_fft_z_r2c<<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], real, cplx, nlines);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = z_pass(false, p, real, nullptr, cplx, s);
     if (e == cudaSuccess && p.n[1] > 1)
     {
         e = strided_pass<false>(p, 1, cplx, s);
@@ -340,9 +381,7 @@ cudaError_t fft_c2r_yz(const FftPlan3& p, float2* cplx, float* real, cudaStream_
     {
         return e;
     }
-    const int nlines = p.n[0] * p.n[1];
-    k_fft_z_c2r<<<z_blocks(nlines), kZWarps * 32, z_smem(p.n[2]), s>>>(p.ax[2], cplx, real, nlines);
-    return cudaGetLastError();
+    return z_pass(true, p, nullptr, real, cplx, s);
 }
 
 cudaError_t fft_c2r(const FftPlan3& p, float2* cplx, float* real, cudaStream_t s)

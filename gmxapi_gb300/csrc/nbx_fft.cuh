@@ -232,6 +232,107 @@ __device__ bool fft_line(float2* a, int sa, float2* b, int sb, const float2* W, 
     return inb;
 }
 
+// ---- lines of a length known at compile time (the common PME grid lengths) ----
+// The same Stockham stages with every stage constant (radix, span, butterfly count, root step)
+// folded at compile time: the butterflies' index arithmetic reduces to shifts and multiplications by
+// constants, and no stage table or radix switch is read.  Lengths whose factors are 2, 3, 4, 5 only.
+
+// Radix of stage s of n in the plan's order (4s, then 2, 3, 5), 0 past the last stage.
+__host__ __device__ constexpr int fft_factor_c(int n, int s)
+{
+    int m = n, k = 0;
+    while (m % 4 == 0)
+    {
+        if (k == s)
+        {
+            return 4;
+        }
+        m /= 4;
+        k++;
+    }
+    for (int p = 2; p <= 5; p++)
+    {
+        while (m % p == 0)
+        {
+            if (k == s)
+            {
+                return p;
+            }
+            m /= p;
+            k++;
+        }
+    }
+    return 0;
+}
+
+template<int R, bool kInv, int N, int Ns>
+__device__ __forceinline__ void fft_butterfly_c(const float2* src, int ss, float2* dst, int ds, const float2* W, int j)
+{
+    constexpr int m  = N / R;
+    constexpr int ts = m / Ns;
+    const int     jq = j / Ns;  // constant divisor
+    const int     jn = j - jq * Ns;
+    float2        v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+    {
+        v[r] = src[(j + r * m) * ss];
+    }
+#pragma unroll
+    for (int r = 1; r < R; r++)
+    {
+        v[r] = cmul(v[r], fft_root<kInv>(W, r * jn * ts));
+    }
+    fft_small<R, kInv>(v, W, N);
+    const int d0 = jq * (Ns * R) + jn;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+    {
+        dst[(d0 + r * Ns) * ds] = v[r];
+    }
+}
+
+// Stages S, S+1, ... of a length-N line (data in a, scratch b); true when the result is in b.
+template<int N, bool kInv, int S = 0, int Ns = 1>
+__device__ __forceinline__ bool fft_line_c(float2* a, int sa, float2* b, int sb, const float2* W, int lane)
+{
+    constexpr int R = fft_factor_c(N, S);
+    if constexpr (R == 0)
+    {
+        return false;
+    }
+    else
+    {
+        static_assert(R == 2 || R == 3 || R == 4 || R == 5, "compile-time lengths take radices 2, 3, 4, 5");
+        constexpr int m = N / R;
+        for (int j = lane; j < m; j += 32)
+        {
+            fft_butterfly_c<R, kInv, N, Ns>(a, sa, b, sb, W, j);
+        }
+        __syncwarp();
+        return !fft_line_c<N, kInv, S + 1, Ns * R>(b, sb, a, sa, W, lane);
+    }
+}
+
+// A line of length kN when kN > 0, else of the runtime length ax.n.
+template<int kN, bool kInv>
+__device__ __forceinline__ bool fft_line_any(float2* a, int sa, float2* b, int sb, const float2* W, const FftAxis& ax,
+                                             int lane)
+{
+    if constexpr (kN > 0)
+    {
+        return fft_line_c<kN, kInv>(a, sa, b, sb, W, lane);
+    }
+    else
+    {
+        return fft_line<kInv>(a, sa, b, sb, W, ax, lane);
+    }
+}
+
+// The lengths with a compile-time path (kernels are instantiated for each; others run the
+// runtime-length path): the 288k-atom box's 120 and the MD benchmark's 192, and their neighbours.
+#define NBX_FFT_FIXED_LENGTHS(X) X(96) X(120) X(128) X(144) X(160) X(192)
+
 // The 3D plan: one axis per dimension (device root tables owned by the plan).
 struct FftPlan3
 {

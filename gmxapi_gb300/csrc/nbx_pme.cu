@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace
@@ -335,8 +336,8 @@ __device__ __forceinline__ void solve_point(const PmeDims& d, const float* __res
 // transform): block (ky, z-tile) loads the tile [nx][T] of x lines, warp c transforms column c,
 // solves its points (kx, ky, kz = tile * T + c) and transforms it back; energy and virial sums as
 // k_pme_solve's.
-template<bool kEnergy>
-__global__ void __launch_bounds__(kSolveThreads) k_pme_fft_x_solve(nbx::FftAxis ax, PmeDims d, float2* cgrid,
+template<bool kEnergy, int kN>
+__global__ void __launch_bounds__(kSolveThreads, 6) k_pme_fft_x_solve(nbx::FftAxis ax, PmeDims d, float2* cgrid,
                                                                    const float* __restrict__ bsp, float elfac,
                                                                    float factor, float pivol, int ntiles, double* partials,
                                                                    unsigned int* done, double* energy_out,
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_pme_fft_x_solve(nbx::FftAxis 
 {
     constexpr int T    = nbx::kFftTile;
     extern __shared__ float2 xsm[];
-    const int     n    = ax.n;  // nx
+    const int     n    = kN > 0 ? kN : ax.n;  // nx
     const int     nzc  = d.n[2] / 2 + 1;
     float2*       W    = xsm;
     float2*       tile = xsm + n;                  // [n][T + 1]
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_pme_fft_x_solve(nbx::FftAxis 
         float2*   s   = scr + (size_t)warp * n;
         const int kz  = t * T + warp;
         // forward along x, then the solve on the column wherever the transform left it
-        const bool in_s = nbx::fft_line<false>(col, T + 1, s, 1, W, ax, lane);
+        const bool in_s = nbx::fft_line_any<kN, false>(col, T + 1, s, 1, W, ax, lane);
         float2*    v    = in_s ? s : col;
         const int  vs   = in_s ? 1 : T + 1;
         for (int kx = lane; kx < n; kx += 32)
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_pme_fft_x_solve(nbx::FftAxis 
         // backward along x
         float2*    other = in_s ? col : s;
         const int  os    = in_s ? T + 1 : 1;
-        const bool moved = nbx::fft_line<true>(v, vs, other, os, W, ax, lane);
+        const bool moved = nbx::fft_line_any<kN, true>(v, vs, other, os, W, ax, lane);
         // the result is in `other` when moved; bring it to the tile column
         if (moved != in_s)
         {
@@ -764,17 +765,29 @@ cudaError_t launch_x_solve(nbx_pme* p, double* d_energy, double* d_virial)
     const int    nzc    = p->d.n[2] / 2 + 1;
     const int    ntiles = (nzc + nbx::kFftTile - 1) / nbx::kFftTile;
     const size_t smem   = nbx::fft_tiled_smem(p->d.n[0]);
-    if (d_energy || d_virial)
+    const bool   energy = d_energy || d_virial;
+    auto         go     = [&](auto kn) {
+        constexpr int kN = decltype(kn)::value;
+        if (energy)
+        {
+            k_pme_fft_x_solve<true, kN><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
+                    p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, d_energy,
+                    d_virial);
+        }
+        else
+        {
+            k_pme_fft_x_solve<false, kN><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
+                    p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, nullptr,
+                    nullptr);
+        }
+    };
+    switch (p->d.n[0])
     {
-        k_pme_fft_x_solve<true><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
-                p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, d_energy,
-                d_virial);
-    }
-    else
-    {
-        k_pme_fft_x_solve<false><<<x_solve_blocks(p), kSolveThreads, smem, p->stream>>>(
-                p->fft.ax[0], p->d, p->cgrid, p->bsp, elfac, factor, pivol, ntiles, p->sums, p->done, nullptr,
-                nullptr);
+#define NBX_FFT_CASE(L)                                                                                                \
+    case L: go(std::integral_constant<int, L>{}); break;
+        NBX_FFT_FIXED_LENGTHS(NBX_FFT_CASE)
+#undef NBX_FFT_CASE
+        default: go(std::integral_constant<int, 0>{}); break;
     }
     return cudaGetLastError();
 }
@@ -894,9 +907,9 @@ int nbx_pme_create(const float* box, const int* grid, float ewaldcoeff_q, float 
     {
         const size_t xs  = nbx::fft_tiled_smem(grid[0]);
         p->fused_smem_ok = xs <= 48 * 1024
-                           || (cudaFuncSetAttribute(k_pme_fft_x_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           || (cudaFuncSetAttribute(k_pme_fft_x_solve<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)xs) == cudaSuccess
-                               && cudaFuncSetAttribute(k_pme_fft_x_solve<false>,
+                               && cudaFuncSetAttribute(k_pme_fft_x_solve<false, 0>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs) == cudaSuccess);
     }
     if (!p->plan)

@@ -67,8 +67,9 @@ def test_reference_3d_fft_test_vector():
     p.close()
 
 
+# the last four cover every compile-time length (96, 120, 128, 144, 160, 192) on every axis
 GRIDS = [(16, 16, 16), (20, 16, 24), (32, 36, 25), (7, 11, 13), (1, 8, 5), (44, 52, 70), (45, 9, 81), (19, 17, 23),
-         (120, 120, 120), (192, 192, 192)]
+         (120, 120, 120), (192, 192, 192), (96, 144, 160), (160, 128, 96), (128, 96, 144), (144, 160, 128)]
 
 
 @pytest.mark.parametrize("grid", GRIDS)
