@@ -42,8 +42,9 @@ constexpr int kAdjMaxTypes1  = 16;
 constexpr int kAdjRepTypes1  = 10;
 constexpr int kAdjReplicas   = kCl;
 
-// Type-pair gradient tables of one warp: replicas x (nt1^2 + 1) float2 (the +1 staggers the
-// replicas over the shared-memory banks).
+// Type-pair gradient tables of one warp: replicas x (nt1^2 + 1) float2, each replica planar (its
+// nt1^2 + 1 dc6 sums, then its nt1^2 + 1 dc12 sums; the +1 staggers the replicas over the
+// shared-memory banks).
 __host__ __device__ __forceinline__ int adj_table_replicas(int nt1)
 {
     return nt1 <= kAdjRepTypes1 ? kAdjReplicas : 1;
@@ -169,9 +170,11 @@ __device__ __forceinline__ void adj_pair(const DeviceView& v, const float2* __re
     {
         const float dc12 = fmaf(gr * rinv6, rinv6 * rinv2, k.gE_lj * (rinv6 * rinv6 + v.cpot12) * (1.0f / 12.0f));
         const float dc6  = -fmaf(gr * rinv6, rinv2, k.gE_lj * (rinv6 + v.cpot6) * (1.0f / 6.0f));
-        float2*     slot = &ttab[ti * nt1 + tj];
-        atomicAdd(&slot->x, dc6);
-        atomicAdd(&slot->y, dc12);
+        // planar replica: the dc6 sums, then (one table stride on) the dc12 sums, so that a warp's
+        // 32 atomics spread over all banks instead of the even ones of interleaved pairs
+        float* const slot = reinterpret_cast<float*>(ttab) + ti * nt1 + tj;
+        atomicAdd(slot, dc6);
+        atomicAdd(slot + adj_table_stride(nt1), dc12);
     }
 }
 
@@ -347,10 +350,12 @@ __device__ __forceinline__ void adj_entry(const DeviceView& v, const AdjPtrs& p,
         float tx = 0.0f, ty = 0.0f;
         for (int r = 0; r < reps; r++)
         {
-            const float2 t = ttab[r * tstride + m];
-            tx += t.x;
-            ty += t.y;
-            ttab[r * tstride + m] = make_float2(0.0f, 0.0f);
+            // replica r: dc6 sums at 2 r stride + m, dc12 sums one stride on (planar)
+            float* const t = reinterpret_cast<float*>(ttab) + 2 * r * tstride + m;
+            tx += t[0];
+            ty += t[tstride];
+            t[0]       = 0.0f;
+            t[tstride] = 0.0f;
         }
         if (tx != 0.0f || ty != 0.0f)
         {
