@@ -9,6 +9,12 @@
 //   RF      qq*(1/r + k_rf r^2 - c_rf),
 // and the forces on j are the negated forces on i (half list).
 //
+// This file holds the one-pair-per-lane kernel (k_force: the switch modifiers, LJ-PME and the
+// autotuner's tile 0), the force reduction, the allocation-free entry and the launch dispatch; the
+// default kernel for potential-shift and plain cut-off LJ is the packed two-pairs-per-lane core of
+// nbx_force_x2.cu / nbx_pair_x2.cuh, which shares the work queue, the exclusion work items and the
+// reduction below.
+//
 // GB300 design (not the reference's 8x8-thread blocks):
 //  - persistent warps take list entries from an atomic work queue;
 //  - one warp owns one entry: lane = (j-atom of the half, 0..3) * 8 + i-atom;
@@ -29,8 +35,8 @@
 //    out) by work items of 128 atoms interleaved with the list entries in the
 //    same queue (k_excl_energy, a separate kernel, only for LJ-PME);
 //  - a force evaluation is three launches: k_convert_x (clears the
-//    accumulators), k_force, k_reduce_f (its last block writes the energies
-//    and the virial);
+//    accumulators), k_force or k_force_x2, k_reduce_f (its last block writes
+//    the energies and the virial);
 //  - j forces are reduced over the 8 i-lanes with shuffles and added with one
 //    vector red.global.add.v4.f32 per j-atom; i forces stay in registers
 //    until the entry ends; shift forces and energies are reduced in FP64.
