@@ -93,7 +93,7 @@ struct CountSmem
     float4 bbi_lo[kNcl], bbi_hi[kNcl];  // shifted i-cluster bounding boxes
 };
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_count(DeviceView v)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceView v)
 {
     __shared__ CountSmem wsm[kWarpsPerBlock];
     const int           lane = threadIdx.x & 31;
@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_count(DeviceView
                     // against the 8 i-clusters (make_cluster_list_supersub for (ci, scj))
                     const int kk = lane >> 3;
                     const int jc = lane & 7;
-                    for (int k0 = 0; k0 < total; k0 += 4)
-                    {
+                    // j-cell of this lane at flat index k0 + kk
+                    auto locate = [&](int k0) {
                         int col = 0;
 #pragma unroll
                         for (int q = 0; q < 4; q++)
@@ -319,22 +319,43 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_count(DeviceView
                             const int before = __popc(__ballot_sync(full, incl <= k0 + q));
                             col              = (kk == q) ? before : col;
                         }
-                        col                 = min(col, 31);
-                        const int colFirst  = __shfl_sync(full, first, col);
-                        const int colIncl   = __shfl_sync(full, incl, col);
-                        const int colCount  = __shfl_sync(full, count, col);
-                        const int k         = k0 + kk;
-                        const int scj       = colFirst + (k - (colIncl - colCount));
-                        const bool has_cell = k < total;
-                        // the j-cluster's bounding box is read with the cell's cluster count (empty
-                        // cluster slots hold far-away boxes, their results are discarded)
-                        int    ncl_j = 0;
-                        float4 jlo{}, jhi{};
-                        if (has_cell)
+                        col                = min(col, 31);
+                        const int colFirst = __shfl_sync(full, first, col);
+                        const int colIncl  = __shfl_sync(full, incl, col);
+                        const int colCount = __shfl_sync(full, count, col);
+                        return colFirst + (k0 + kk - (colIncl - colCount));
+                    };
+                    // the j-cluster's bounding box is read with the cell's cluster count (empty
+                    // cluster slots hold far-away boxes, their results are discarded); the next
+                    // four j-cells' boxes are loaded while the current ones are tested
+                    int    scj_n  = locate(0);
+                    int    ncl_n  = 0;
+                    float4 jlo_n{}, jhi_n{};
+                    if (kk < total)
+                    {
+                        ncl_n = v.nclusters[scj_n];
+                        jlo_n = v.bb[2 * (scj_n * kNcl + jc)];
+                        jhi_n = v.bb[2 * (scj_n * kNcl + jc) + 1];
+                    }
+                    for (int k0 = 0; k0 < total; k0 += 4)
+                    {
+                        const int    scj      = scj_n;
+                        const bool   has_cell = k0 + kk < total;
+                        const int    ncl_j    = ncl_n;
+                        const float4 jlo = jlo_n, jhi = jhi_n;
+                        if (k0 + 4 < total)
                         {
-                            ncl_j = v.nclusters[scj];
-                            jlo   = v.bb[2 * (scj * kNcl + jc)];
-                            jhi   = v.bb[2 * (scj * kNcl + jc) + 1];
+                            scj_n = locate(k0 + 4);
+                            if (k0 + 4 + kk < total)
+                            {
+                                ncl_n = v.nclusters[scj_n];
+                                jlo_n = v.bb[2 * (scj_n * kNcl + jc)];
+                                jhi_n = v.bb[2 * (scj_n * kNcl + jc) + 1];
+                            }
+                            else
+                            {
+                                ncl_n = 0;
+                            }
                         }
                         const bool diag  = has_cell && excludeSubDiagonal && (scj == ci);
                         const int  ci1   = diag ? jc + 1 : ncl_i;
