@@ -21,7 +21,7 @@
 namespace nbx
 {
 cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s);
-cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s);
+cudaError_t launch_search_write(const DeviceView& v, int num_entries, cudaStream_t s);
 cudaError_t launch_balance(const DeviceView& v, int min_ci_balanced, cudaStream_t s);
 } // namespace nbx
 
@@ -389,7 +389,7 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
     e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
     {
         PhaseTimer t(h, 3);
-        if (e == cudaSuccess) e = launch_search_write(v, h->stream);
+        if (e == cudaSuccess) e = launch_search_write(v, h->h_hdr->num_sci, h->stream);
         // split long entries and order them large-first (the GPU list's load balancing)
         if (e == cudaSuccess) e = launch_balance(v, h->min_ci_balanced, h->stream);
     }

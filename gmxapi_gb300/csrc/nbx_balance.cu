@@ -30,6 +30,8 @@ constexpr int kMinTarget    = 36;   // nsubpair_target_min, pairlist.cpp:2495
 constexpr int kMaxSizeClass = 255;
 constexpr int kSortThreads  = 1024;
 constexpr int kSortWarps    = kSortThreads / 32;
+constexpr int kSortBatch    = 8;  // entries per lane loaded at a time by the sort
+constexpr int kScanBatch    = 8;  // piece counts per thread loaded at a time by the scan
 
 __device__ __forceinline__ int balance_target(const ListHeader* hdr, int min_ci_balanced)
 {
@@ -138,9 +140,19 @@ __global__ void __launch_bounds__(1024) k_balance_scan(DeviceView v)
     const int i0   = min(n, (int)threadIdx.x * per);
     const int i1   = min(n, i0 + per);
     int       own  = 0;
-    for (int i = i0; i < i1; i++)
+    for (int b = i0; b < i1; b += kScanBatch)
     {
-        own += v.sci_pieces[i];
+        int val[kScanBatch];
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            val[u] = b + u < i1 ? v.sci_pieces[b + u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            own += val[u];
+        }
     }
     int inc = own;
 #pragma unroll
@@ -173,11 +185,23 @@ __global__ void __launch_bounds__(1024) k_balance_scan(DeviceView v)
     }
     __syncthreads();
     int run = (warp > 0 ? warp_sums[warp - 1] : 0) + inc - own;
-    for (int i = i0; i < i1; i++)
+    for (int b = i0; b < i1; b += kScanBatch)
     {
-        const int val   = v.sci_pieces[i];
-        v.sci_pieces[i] = run;
-        run += val;
+        int val[kScanBatch];
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            val[u] = b + u < i1 ? v.sci_pieces[b + u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            if (b + u < i1)
+            {
+                v.sci_pieces[b + u] = run;
+                run += val[u];
+            }
+        }
     }
     if (threadIdx.x == blockDim.x - 1)
     {
@@ -232,10 +256,24 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_entries(DeviceView v)
     const int chunk = (n + kSortWarps - 1) / kSortWarps;
     const int e0    = min(n, warp * chunk);
     const int e1    = min(n, e0 + chunk);
-    for (int e = e0 + lane; e < e1; e += 32)
+    // kSortBatch entries per lane loaded before any is counted or placed
+    for (int b = e0; b < e1; b += 32 * kSortBatch)
     {
-        const int len = v.sci_tmp[e].cj4_end - v.sci_tmp[e].cj4_start;
-        atomicAdd(&hist[warp][len < m ? len : m], 1);
+        int len[kSortBatch];
+#pragma unroll
+        for (int u = 0; u < kSortBatch; u++)
+        {
+            const int e = b + u * 32 + lane;
+            len[u]      = e < e1 ? v.sci_tmp[e].cj4_end - v.sci_tmp[e].cj4_start : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < kSortBatch; u++)
+        {
+            if (len[u] >= 0)
+            {
+                atomicAdd(&hist[warp][len[u] < m ? len[u] : m], 1);
+            }
+        }
     }
     __syncthreads();
     if (warp == 0)
@@ -277,29 +315,33 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_entries(DeviceView v)
         }
     }
     __syncthreads();
-    for (int b = e0; b < e1; b += 32)
+    for (int b = e0; b < e1; b += 32 * kSortBatch)
     {
-        const int e   = b + lane;
-        Sci       s{};
-        int       cls = -1;
-        if (e < e1)
+        Sci sv[kSortBatch];
+#pragma unroll
+        for (int u = 0; u < kSortBatch; u++)
         {
-            s             = v.sci_tmp[e];
-            const int len = s.cj4_end - s.cj4_start;
-            cls           = len < m ? len : m;
+            const int e = b + u * 32 + lane;
+            sv[u]       = e < e1 ? v.sci_tmp[e] : Sci{ 0, 0, 0, -1 };
         }
-        const unsigned peers = __match_any_sync(0xffffffffu, cls);
-        const unsigned lower = peers & ((1u << lane) - 1u);
-        if (cls >= 0)
+#pragma unroll
+        for (int u = 0; u < kSortBatch; u++)
         {
-            v.sci[hist[warp][cls] + __popc(lower)] = s;
+            const int      len   = sv[u].cj4_end - sv[u].cj4_start;
+            const int      cls   = len < 0 ? -1 : (len < m ? len : m);
+            const unsigned peers = __match_any_sync(0xffffffffu, cls);
+            const unsigned lower = peers & ((1u << lane) - 1u);
+            if (cls >= 0)
+            {
+                v.sci[hist[warp][cls] + __popc(lower)] = sv[u];
+            }
+            __syncwarp();
+            if (cls >= 0 && lower == 0u)
+            {
+                hist[warp][cls] += __popc(peers);
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        if (cls >= 0 && lower == 0u)
-        {
-            hist[warp][cls] += __popc(peers);
-        }
-        __syncwarp();
     }
     if (threadIdx.x == 0)
     {

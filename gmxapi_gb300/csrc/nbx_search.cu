@@ -14,9 +14,9 @@
 // testing its j-cluster's bounding box against the 8 i-clusters.  The j-clusters
 // found are stored as per-cell records (index, 8-bit i-cluster mask) with one
 // code per entry, and the cell's entry / cj4 counts are written.  After a
-// prefix sum of the counts, the emit pass (one warp per cell) turns the records
-// into sci / cj4 entries at fixed offsets, with the outer masks and per-group
-// pair counts, and sets the diagonal and topology exclusion masks.
+// prefix sum of the counts, the emit pass (one warp per list entry) turns the
+// records into sci / cj4 entries at fixed offsets, with the outer masks and
+// per-group pair counts, and sets the diagonal and topology exclusion masks.
 #include "nbx_internal.cuh"
 
 #include <cstddef>
@@ -454,6 +454,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceV
     }
 }
 
+constexpr int kScanBatch = 8;    // cell counts per thread loaded at a time by the prefix sum
 constexpr int kExclStage = 256;  // topology exclusions of a cell's i-atoms staged in shared memory
 
 struct EmitSmem
@@ -466,73 +467,123 @@ struct EmitSmem
     unsigned char ex_i[kExclStage];                 // the i-atom's slot within the cell
 };
 
-// Emit pass: one warp per i-cell turns its search records into list entries at the offsets of the
-// prefix sum.  Per entry: the cj4 groups (one per lane: four j-clusters, the i-cluster masks of both
-// warp halves, exclusion index 0 = all interacting), the outer masks (the fresh list's masks until
-// a prune refines them) and the group's cluster-pair count for balancing; then the exclusions:
-// flag the (cj4, half) pairs that need a mask (self/Newton pairs of the diagonal j-clusters and
-// topology exclusions), allocate the flagged masks all interacting, clear j <= i on the diagonal
-// (setSelfAndNewtonExclusionsGpu) and the excluded atom pairs (setExclusionsForIEntry).
+// Emit pass: one warp per list entry (the entries numbered by the prefix sum of the per-cell
+// counts) turns its search records into the entry's sci record and cj4 groups.  The warp finds its
+// cell by a 32-way search of the entry offsets and the entry's first record and group from the
+// codes of the cell's earlier entries, then writes the cj4 groups (one per lane: four j-clusters,
+// the i-cluster masks of both warp halves, exclusion index 0 = all interacting), the outer masks
+// (the fresh list's masks until a prune refines them) and the group's cluster-pair count for
+// balancing; then the exclusions: flag the (cj4, half) pairs that need a mask (self/Newton pairs of
+// the diagonal j-clusters and topology exclusions), allocate the flagged masks all interacting,
+// clear j <= i on the diagonal (setSelfAndNewtonExclusionsGpu) and the excluded atom pairs
+// (setExclusionsForIEntry).
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView v)
 {
     __shared__ EmitSmem wsm[kWarpsPerBlock];
     const int           lane = threadIdx.x & 31;
     const int           wib  = threadIdx.x >> 5;
     EmitSmem&           sm   = wsm[wib];
-    const int           ci   = blockIdx.x * kWarpsPerBlock + wib;
+    const int           e    = blockIdx.x * kWarpsPerBlock + wib;
     const unsigned      full = 0xffffffffu;
-    if (ci >= v.hdr->num_cells
+    if (e >= v.hdr->num_sci
         || (v.hdr->status & (kStatusListOverflow | kStatusRecordOverflow | kStatusEntryOverflow)))
     {
         return;
     }
-    const int nent    = v.sci_count[ci];
-    int       sci_out = v.sci_offset[ci];
-    int       cj4_out = v.cj4_offset[ci];
-    const int*           rec_cj = v.rec_cj + (size_t)ci * v.rec_cap;
-    const unsigned char* rec_m  = v.rec_m + (size_t)ci * v.rec_cap;
-    // the topology exclusions of the cell's i-atoms as (i-slot, partner grid slot) pairs, looked up
-    // once for all entries of the cell (when they fit; else each entry walks the exclusion lists)
-    int nex = 0;
-    for (int base = 0; base < kSc && nent > 0; base += 32)
+    // the cell of entry e: the last cell whose first entry is at most e (cells without entries
+    // share their successor's offset); the search window shrinks 32-fold per step
+    int ci = 0;
     {
-        const int i     = base + lane;
-        const int iAtom = v.atom_indices[ci * kSc + i];
-        int       x0 = 0, x1 = 0;
-        if (iAtom >= 0)
+        int len = v.hdr->num_cells;
+        while (len > 1)
         {
-            x0 = v.excl_index[iAtom];
-            x1 = v.excl_index[iAtom + 1];
+            const int  step = (len + 31) / 32;
+            const int  c    = ci + lane * step;
+            const bool le   = c < ci + len && v.sci_offset[c] <= e;
+            const int  cnt  = __popc(__ballot_sync(full, le));
+            const int  lo   = ci + (cnt - 1) * step;
+            len             = min(step, ci + len - lo);
+            ci              = lo;
         }
-        const int cnt  = x1 - x0;
-        int       incl = cnt;
+    }
+    const int kent = e - v.sci_offset[ci];
+    // this entry's code; the records and groups of the cell's earlier entries
+    const int cl   = lane <= kent ? v.rec_ent[ci * kMaxEntriesPerCell + lane] : 0;
+    int       rec0 = lane < kent ? cl >> 8 : 0;
+    int       grp0 = (rec0 + kJg - 1) / kJg;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        rec0 += __shfl_xor_sync(full, rec0, o);
+        grp0 += __shfl_xor_sync(full, grp0, o);
+    }
+    const int            code    = __shfl_sync(full, cl, kent);
+    const int            sci_out = e;
+    const int            cj4_out = v.cj4_offset[ci] + grp0;
+    const int*           rec_cj  = v.rec_cj + (size_t)ci * v.rec_cap + rec0;
+    const unsigned char* rec_m   = v.rec_m + (size_t)ci * v.rec_cap + rec0;
+    // the topology exclusions of the cell's i-atoms as (i-slot, partner grid slot) pairs (when they
+    // fit; else the entry walks the exclusion lists); both halves of the 64 i-atoms load together
+    int nex = 0;
+    {
+        int iAtom[2], x0[2] = { 0, 0 }, x1[2] = { 0, 0 };
+#pragma unroll
+        for (int h = 0; h < 2; h++)
         {
-            const int t = __shfl_up_sync(full, incl, o);
-            if (lane >= o)
+            iAtom[h] = v.atom_indices[ci * kSc + h * 32 + lane];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+        {
+            if (iAtom[h] >= 0)
             {
-                incl += t;
+                x0[h] = v.excl_index[iAtom[h]];
+                x1[h] = v.excl_index[iAtom[h] + 1];
             }
         }
-        const int tot = __shfl_sync(full, incl, 31);
-        if (nex + tot <= kExclStage)
+#pragma unroll
+        for (int h = 0; h < 2; h++)
         {
-            const int off = nex + incl - cnt;
-            for (int x = x0; x < x1; x++)
+            const int cnt  = x1[h] - x0[h];
+            int       incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
             {
-                const int jAtom          = v.excl_list[x];
-                sm.ex_j[off + (x - x0)] = (jAtom == iAtom) ? -1 : v.cells[jAtom];
-                sm.ex_i[off + (x - x0)] = (unsigned char)i;
+                const int t = __shfl_up_sync(full, incl, o);
+                if (lane >= o)
+                {
+                    incl += t;
+                }
             }
+            const int tot = __shfl_sync(full, incl, 31);
+            if (nex + tot <= kExclStage)
+            {
+                const int off = nex + incl - cnt;
+                // the partners four at a time: their list entries, then their grid slots
+                for (int x = x0[h]; x < x1[h]; x += 4)
+                {
+                    int jAtom[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                    {
+                        jAtom[u] = x + u < x1[h] ? v.excl_list[x + u] : -1;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                    {
+                        if (x + u < x1[h])
+                        {
+                            sm.ex_j[off + (x + u - x0[h])] = (jAtom[u] == iAtom[h]) ? -1 : v.cells[jAtom[u]];
+                            sm.ex_i[off + (x + u - x0[h])] = (unsigned char)(h * 32 + lane);
+                        }
+                    }
+                }
+            }
+            nex += tot;
         }
-        nex += tot;
     }
     const bool ex_staged = nex <= kExclStage;
-    __syncwarp();
-    for (int k = 0; k < nent; k++)
     {
-        const int  code  = v.rec_ent[ci * kMaxEntriesPerCell + k];
         const int  shift = code & 0xff;
         const int  nj    = code >> 8;
         const int  ncj4  = (nj + kJg - 1) / kJg;
@@ -545,7 +596,37 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
         {
             sm.need[w] = 0u;
         }
+        // the j-list is sorted on cluster index; short lists go to shared memory (four records per
+        // lane loaded at a time) for the group writes and the exclusion lookups
+        const bool staged = nj <= kEmitStage;
+        if (staged)
+        {
+            for (int p0 = 0; p0 < nj; p0 += 128)
+            {
+                int           c[4];
+                unsigned char m[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                {
+                    const int p = p0 + u * 32 + lane;
+                    c[u]        = p < nj ? rec_cj[p] : 0;
+                    m[u]        = p < nj ? rec_m[p] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                {
+                    const int p = p0 + u * 32 + lane;
+                    if (p < nj)
+                    {
+                        sm.jl[p] = c[u];
+                        sm.jm[p] = m[u];
+                    }
+                }
+            }
+        }
         __syncwarp();
+        const int*           jlist = staged ? sm.jl : rec_cj;
+        const unsigned char* mlist = staged ? sm.jm : rec_m;
         for (int g = lane; g < ncj4; g += 32)
         {
             Cj4      c;
@@ -554,8 +635,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
             for (int off = 0; off < kJg; off++)
             {
                 const int p = g * kJg + off;
-                c.cj[off]   = p < nj ? rec_cj[p] : 0;
-                im |= p < nj ? (unsigned)rec_m[p] << (off * kNcl) : 0u;
+                c.cj[off]   = p < nj ? jlist[p] : 0;
+                im |= p < nj ? (unsigned)mlist[p] << (off * kNcl) : 0u;
             }
             c.imei[0].imask    = im;
             c.imei[0].excl_ind = 0;
@@ -564,34 +645,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
             reinterpret_cast<uint2*>(v.imask_outer)[cj4_out + g] = make_uint2(im, im);
             v.grp_pairs[cj4_out + g] = (unsigned char)__popc(im);
         }
-        // the j-list is sorted on cluster index; short lists go to shared memory for the lookups
-        const bool staged = nj <= kEmitStage;
-        for (int p = lane; p < nj; p += 32)
+        // the diagonal j-clusters (the i-cell's own clusters, central shift)
+        if (excludeSubDiagonal)
         {
-            const int cj = rec_cj[p];
-            if (staged)
+            for (int p = lane; p < nj; p += 32)
             {
-                sm.jl[p] = cj;
-                sm.jm[p] = rec_m[p];
-            }
-            // the diagonal j-clusters (the i-cell's own clusters, central shift)
-            if (excludeSubDiagonal && (cj >> 3) == ci)
-            {
-                sm.diag_pos[cj & (kNcl - 1)] = p;
-                atomicOr(&sm.need[(2 * (p / kJg)) / 32], 3u << ((2 * (p / kJg)) % 32));
+                const int cj = jlist[p];
+                if ((cj >> 3) == ci)
+                {
+                    sm.diag_pos[cj & (kNcl - 1)] = p;
+                    atomicOr(&sm.need[(2 * (p / kJg)) / 32], 3u << ((2 * (p / kJg)) % 32));
+                }
             }
         }
-        const int*           jlist = staged ? sm.jl : rec_cj;
-        const unsigned char* mlist = staged ? sm.jm : rec_m;
-        int                  basei = 0;  // first exclusion mask of this entry
+        int basei = 0;  // first exclusion mask of this entry
         // the mask of a flagged (cj4, half) slot: masks are allocated to the flagged slots in order
         auto excl_of_slot = [&](int slot) {
-            int e = basei;
+            int x = basei;
             for (int w = 0; w < slot / 32; w++)
             {
-                e += __popc(sm.need[w]);
+                x += __popc(sm.need[w]);
             }
-            return e + __popc(sm.need[slot / 32] & ((1u << (slot % 32)) - 1u));
+            return x + __popc(sm.need[slot / 32] & ((1u << (slot % 32)) - 1u));
         };
         __syncwarp();
         __threadfence_block();
@@ -756,11 +831,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_search_emit(DeviceView 
                 __syncwarp();
             }
         }
-        __syncwarp();
-        rec_cj += nj;
-        rec_m += nj;
-        sci_out++;
-        cj4_out += ncj4;
     }
 }
 
@@ -774,10 +844,22 @@ __global__ void k_scan_counts(DeviceView v)
     const int      c0       = threadIdx.x * per;
     const int      c1       = min(n, c0 + per);
     int            ls = 0, lc = 0;
-    for (int c = c0; c < c1; c++)
+    // kScanBatch cells per thread loaded at a time
+    for (int b = c0; b < c1; b += kScanBatch)
     {
-        ls += v.sci_count[c];
-        lc += v.cj4_count[c];
+        int cs[kScanBatch], cc[kScanBatch];
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            cs[u] = b + u < c1 ? v.sci_count[b + u] : 0;
+            cc[u] = b + u < c1 ? v.cj4_count[b + u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            ls += cs[u];
+            lc += cc[u];
+        }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int       is = ls, ic = lc;
@@ -817,12 +899,26 @@ __global__ void k_scan_counts(DeviceView v)
     __syncthreads();
     int rs = is - ls + (warp > 0 ? ws[0][warp - 1] : 0);
     int rc = ic - lc + (warp > 0 ? ws[1][warp - 1] : 0);
-    for (int c = c0; c < c1; c++)
+    for (int b = c0; b < c1; b += kScanBatch)
     {
-        v.sci_offset[c] = rs;
-        v.cj4_offset[c] = rc;
-        rs += v.sci_count[c];
-        rc += v.cj4_count[c];
+        int cs[kScanBatch], cc[kScanBatch];
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            cs[u] = b + u < c1 ? v.sci_count[b + u] : 0;
+            cc[u] = b + u < c1 ? v.cj4_count[b + u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kScanBatch; u++)
+        {
+            if (b + u < c1)
+            {
+                v.sci_offset[b + u] = rs;
+                v.cj4_offset[b + u] = rc;
+                rs += cs[u];
+                rc += cc[u];
+            }
+        }
     }
     if (threadIdx.x == nthreads - 1)
     {
@@ -854,11 +950,13 @@ cudaError_t launch_search_count(const DeviceView& v, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_search_write(const DeviceView& v, cudaStream_t s)
+cudaError_t launch_search_write(const DeviceView& v, int num_entries, cudaStream_t s)
 {
-    const int cap    = v.g.cells_capacity;
-    const int blocks = (cap + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    k_search_emit<<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
+    if (num_entries > 0)
+    {
+        const int blocks = (num_entries + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        k_search_emit<<<blocks, 32 * kWarpsPerBlock, 0, s>>>(v);
+    }
     return cudaGetLastError();
 }
 
