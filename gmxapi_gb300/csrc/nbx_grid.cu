@@ -259,6 +259,67 @@ __device__ void bitonic_sort(unsigned long long* keys, int P)
     }
 }
 
+// Block-wide bitonic sort of keys[0..P) in shared memory, P a power of two from 64 on: the stages
+// whose partners are at most 32 apart run in registers, each warp holding 64-key segments two keys
+// per lane (partners 2..32 apart by shuffles, 1 apart within the lane); the wider stages run in
+// shared memory, one compare-exchange pair per thread, with a block barrier each.  Same network and
+// result as bitonic_sort.
+__device__ void bitonic_sort_smem(unsigned long long* keys, int P)
+{
+    const unsigned full   = 0xffffffffu;
+    const int      lane   = threadIdx.x & 31;
+    const int      warp   = threadIdx.x >> 5;
+    const int      nwarps = blockDim.x >> 5;
+    // the stages of merge sizes kfirst .. klast with partners at most 32 apart, per segment
+    auto reg_phase = [&](int kfirst, int klast) {
+        for (int seg = warp; seg < P / 64; seg += nwarps)
+        {
+            const int          p0 = seg * 64 + 2 * lane;
+            unsigned long long e0 = keys[p0], e1 = keys[p0 + 1];
+            for (int k = kfirst; k <= klast; k <<= 1)
+            {
+                // ascending where bit k of the position is clear (the same for p0 and p0 + 1)
+                const bool up = (p0 & k) == 0;
+                for (int j = min(k >> 1, 32); j >= 2; j >>= 1)
+                {
+                    const unsigned long long y0      = __shfl_xor_sync(full, e0, j >> 1);
+                    const unsigned long long y1      = __shfl_xor_sync(full, e1, j >> 1);
+                    const bool               takeMin = ((p0 & j) == 0) == up;
+                    e0                               = takeMin ? min(e0, y0) : max(e0, y0);
+                    e1                               = takeMin ? min(e1, y1) : max(e1, y1);
+                }
+                const unsigned long long lo = min(e0, e1), hi = max(e0, e1);
+                e0                          = up ? lo : hi;
+                e1                          = up ? hi : lo;
+            }
+            keys[p0]     = e0;
+            keys[p0 + 1] = e1;
+        }
+    };
+    reg_phase(2, min(P, 64));
+    __syncthreads();
+    for (int k = 128; k <= P; k <<= 1)
+    {
+        for (int j = k >> 1; j >= 64; j >>= 1)
+        {
+            for (int q = threadIdx.x; q < P / 2; q += blockDim.x)
+            {
+                const int                i = ((q & ~(j - 1)) << 1) | (q & (j - 1));  // lower key of pair q
+                const int                l = i | j;
+                const unsigned long long a = keys[i], b = keys[l];
+                if ((a > b) == ((i & k) == 0))
+                {
+                    keys[i] = b;
+                    keys[l] = a;
+                }
+            }
+            __syncthreads();
+        }
+        reg_phase(k, k);
+        __syncthreads();
+    }
+}
+
 // Rank of this lane's (coordinate, atom) among the first `cnt` lanes of its
 // group of `gsize` lanes (ascending, or descending when `backwards`).
 __device__ __forceinline__ int group_rank(float c, int a, int cnt, int gsize, bool backwards)
@@ -301,7 +362,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsign
     {
         return;
     }
-    int P = 1;
+    int P = 64;  // at least one 64-key segment of the shared-memory sort
     while (P < n)
     {
         P <<= 1;
@@ -320,7 +381,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_fill(DeviceView v, unsign
         }
     }
     __syncthreads();
-    bitonic_sort(keys, P);
+    if (P <= kSmemSortItems)
+    {
+        bitonic_sort_smem(keys, P);
+    }
+    else
+    {
+        bitonic_sort(keys, P);
+    }
     for (int t = threadIdx.x; t < ncells * kSc; t += blockDim.x)
     {
         v.atom_indices[base + t] = (t < n) ? (int)(unsigned)(keys[t] & 0xffffffffu) : -1;
