@@ -11,7 +11,7 @@
 // Fresh pass: one block per list entry, its warps taking the entry's cj4 groups
 // in turn; lane (ip, jj) holds the shifted i-atoms ip and ip + 4 of the 8
 // i-clusters in registers and tests both against j-atom jj in packed FP32x2
-// arithmetic; the in-range flags of a j-cluster's set i-clusters become per-lane
+// arithmetic; the in-range flags of a j-cluster's 8 i-clusters become per-lane
 // bit masks, ORed over the warp with one reduction per j-cluster.
 // Rolling pass: one warp per list entry; the few bits to re-test are numbered
 // over the warp and each lane tests whole bits (32 atom pairs).  Compiled with
@@ -46,10 +46,9 @@ __device__ __forceinline__ float2 p_sub(float2 a, float2 b)
 // own (no block barrier).  Lane (ip, jj), ip = lane & 3 and jj = lane >> 2, holds the shifted i-atoms
 // ip and ip + 4 of the entry's 8 i-clusters in registers as pairs {x_ip, x_ip+4}, ... and tests
 // both against j-atom jj of a j-cluster in one packed operation, so both results belong to the same
-// warp half (jj / 4) and the lane keeps their minimum.  An i-cluster with no bit in either half of a
-// j-cluster is skipped (a warp-uniform branch); the in-range flags of the others are collected as
-// per-lane bit masks, inner and outer, placed by warp half in one word and ORed over the warp with
-// one reduction per j-cluster.
+// warp half (jj / 4) and the lane keeps their minimum.  The in-range flags of the 8 i-clusters are
+// collected as per-lane bit masks, inner and outer, placed by warp half in one word and ORed over the
+// warp with one reduction per j-cluster; j-clusters without bits are skipped.
 template<int kPruneWarps>
 __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_outer, const float4* xq,
                                   const float* shiftvec, float outer2, float inner2)
@@ -59,14 +58,25 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
     const int      ip   = lane & 3;
     const int      jj   = lane >> 2;
     const unsigned full = 0xffffffffu;
+    // the next group's record is loaded while the current one is tested
+    Cj4 c4n{};
+    if (s.cj4_start + warp < s.cj4_end)
+    {
+        c4n = cj4[s.cj4_start + warp];
+    }
+    const float sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
+    // the j-atoms of the entry's j-clusters are fetched into L2 by the whole block (thread t: group
+    // t / 4, j-cluster t % 4), so that only each warp's first group waits for device memory
+    for (int q = threadIdx.x; q < (s.cj4_end - s.cj4_start) * kJg; q += blockDim.x)
+    {
+        const int cj = cj4[s.cj4_start + q / kJg].cj[q % kJg];
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(xq + (size_t)cj * kCl)));
+    }
     if (s.cj4_start + warp >= s.cj4_end)
     {
         return;
     }
-    // the next group's record is loaded while the current one is tested
-    Cj4 c4n = cj4[s.cj4_start + warp];
-    const float sx = shiftvec[3 * s.shift], sy = shiftvec[3 * s.shift + 1], sz = shiftvec[3 * s.shift + 2];
-    float2      xi[kNcl], yi[kNcl], zi[kNcl];
+    float2 xi[kNcl], yi[kNcl], zi[kNcl];
 #pragma unroll
     for (int c = 0; c < kNcl; c++)
     {
@@ -77,7 +87,8 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
         zi[c]          = make_float2(a.z + sz, b.z + sz);
     }
     // this lane's flags go to bits 0-15 (half 0) or 16-31 (half 1) of the reduced word
-    const int hshift = 16 * (jj >> 2);
+    const int    hshift   = 16 * (jj >> 2);
+    const float2 inner2x2 = make_float2(inner2, inner2), outer2x2 = make_float2(outer2, outer2);
     for (int j4 = s.cj4_start + warp; j4 < s.cj4_end; j4 += kPruneWarps)
     {
         const Cj4 c4 = c4n;
@@ -118,27 +129,32 @@ __device__ void prune_entry_fresh(const Sci& s, const Cj4* cj4, unsigned* imask_
             const float2 yjj = make_float2(xj[jm].y, xj[jm].y);
             const float2 zjj = make_float2(xj[jm].z, xj[jm].z);
             // per lane: bit i set when one of this lane's two pairs with i-cluster i is in range,
-            // shifted in from the top i-cluster down.  The flag is the sign of r^2 - cutoff^2 for
-            // the smaller r^2 of the two (the difference of two floats is negative exactly when the
-            // first is smaller); skipped i-clusters shift in a clear flag.  r^2 = fma(dz, dz,
-            // fma(dy, dy, dx dx)), the contraction of the reference's norm2 in its prune kernel.
+            // shifted in from the top i-cluster down.  All 8 i-clusters are tested (no per-cluster
+            // branch); the flag is the sign of r^2 - cutoff^2 for the smaller r^2 of the two (the
+            // difference of two floats is negative exactly when the first is smaller), taken for
+            // two i-clusters at once in packed arithmetic.  r^2 = fma(dz, dz, fma(dy, dy, dx dx)),
+            // the contraction of the reference's norm2 in its prune kernel.
             unsigned fin = 0u, fout = 0u;
 #pragma unroll
-            for (int i = kNcl - 1; i >= 0; i--)
+            for (int i = kNcl - 1; i >= 0; i -= 2)
             {
-                float din = 1.0f, dout = 1.0f;
-                if ((sel >> i) & 1u)
+                float mm[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++)
                 {
-                    const float2   dx = p_sub(xi[i], xjj);
-                    const float2   dy = p_sub(yi[i], yjj);
-                    const float2   dz = p_sub(zi[i], zjj);
+                    const float2   dx = p_sub(xi[i - u], xjj);
+                    const float2   dy = p_sub(yi[i - u], yjj);
+                    const float2   dz = p_sub(zi[i - u], zjj);
                     const float2   r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-                    const unsigned m  = min(__float_as_uint(r2.x), __float_as_uint(r2.y));
-                    din               = __fsub_rn(__uint_as_float(m), inner2);
-                    dout              = __fsub_rn(__uint_as_float(m), outer2);
+                    mm[u]             = __uint_as_float(min(__float_as_uint(r2.x), __float_as_uint(r2.y)));
                 }
-                fin  = __funnelshift_l(__float_as_uint(din), fin, 1);
-                fout = __funnelshift_l(__float_as_uint(dout), fout, 1);
+                const float2 m2   = make_float2(mm[0], mm[1]);
+                const float2 din  = p_sub(m2, inner2x2);
+                const float2 dout = p_sub(m2, outer2x2);
+                fin               = __funnelshift_l(__float_as_uint(din.x), fin, 1);
+                fin               = __funnelshift_l(__float_as_uint(din.y), fin, 1);
+                fout              = __funnelshift_l(__float_as_uint(dout.x), fout, 1);
+                fout              = __funnelshift_l(__float_as_uint(dout.y), fout, 1);
             }
             // any pair of the (i-cluster, half) within range: one OR over the lanes of
             // {inner half 0, outer half 0, inner half 1, outer half 1}, 8 bits each
@@ -315,7 +331,7 @@ __device__ void prune_entry_rolling(const Sci& s, const Cj4* cj4, const unsigned
 // Fresh prune: a block per list entry, its warps over the entry's groups.  Rolling prune: a warp
 // per list entry.
 template<int kPruneWarps, bool kFresh>
-__global__ void __launch_bounds__(32 * kPruneWarps, kFresh ? 5 : 6) k_prune(DeviceView v, int part, int nparts)
+__global__ void __launch_bounds__(32 * kPruneWarps, kFresh ? 4 : 6) k_prune(DeviceView v, int part, int nparts)
 {
     __shared__ RollSmem rsm[kFresh ? 1 : kPruneWarps];
     const int           numSci = v.hdr->num_sci;
@@ -325,10 +341,20 @@ __global__ void __launch_bounds__(32 * kPruneWarps, kFresh ? 5 : 6) k_prune(Devi
     }
     if constexpr (kFresh)
     {
+        // the next entry's record is loaded while the current entry is pruned
+        Sci sn{};
+        if (blockIdx.x < numSci)
+        {
+            sn = v.sci[blockIdx.x];
+        }
         for (int e = blockIdx.x; e < numSci; e += gridDim.x)
         {
-            prune_entry_fresh<kPruneWarps>(v.sci[e], v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2,
-                                           v.rlist_inner2);
+            const Sci s = sn;
+            if (e + gridDim.x < numSci)
+            {
+                sn = v.sci[e + gridDim.x];
+            }
+            prune_entry_fresh<kPruneWarps>(s, v.cj4, v.imask_outer, v.xq, v.shiftvec, v.rlist2, v.rlist_inner2);
         }
     }
     else

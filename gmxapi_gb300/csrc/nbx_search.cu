@@ -90,7 +90,8 @@ constexpr int kEmitStage = 512;  // j-lists up to this length are staged in shar
 
 struct CountSmem
 {
-    float4 bbi_lo[kNcl], bbi_hi[kNcl];  // shifted i-cluster bounding boxes
+    float4 bbc_lo[kNcl], bbc_hi[kNcl];  // the i-cell's cluster bounding boxes
+    float4 bbi_lo[kNcl], bbi_hi[kNcl];  // and shifted for the current entry
 };
 
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceView v)
@@ -128,6 +129,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceV
     const float* box  = v.g.box;
     const float2 bbcz_i = v.bbcz[ci];
     const int    ncl_i  = v.nclusters[ci];
+    // the cell's i-cluster bounding boxes, shifted per entry below
+    if (lane < kNcl)
+    {
+        sm.bbc_lo[lane] = v.bb[2 * (ci * kNcl + lane)];
+        sm.bbc_hi[lane] = v.bb[2 * (ci * kNcl + lane) + 1];
+    }
     int          shp_x  = (box[0] < rlist) ? 2 : 1;
 
     int            num_entries = 0, num_cj4 = 0;
@@ -210,8 +217,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceV
                 __syncwarp();
                 if (lane < kNcl)
                 {
-                    const float4 l = v.bb[2 * (ci * kNcl + lane)];
-                    const float4 h = v.bb[2 * (ci * kNcl + lane) + 1];
+                    const float4 l  = sm.bbc_lo[lane];
+                    const float4 h  = sm.bbc_hi[lane];
                     sm.bbi_lo[lane] = make_float4(l.x + shx, l.y + shy, l.z + shz, 0.0f);
                     sm.bbi_hi[lane] = make_float4(h.x + shx, h.y + shy, h.z + shz, 0.0f);
                 }
@@ -243,6 +250,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_search_count(DeviceV
                         const int cyf_x = (cx == 0 && shift == kCentral && cyf < ci_y) ? ci_y : cyf;
                         const int columnStart = v.cxy_ind[cx * v.g.ncy + cy];
                         const int columnEnd   = v.cxy_ind[cx * v.g.ncy + cy + 1];
+                        // the column's cell z-bounds into L1 ahead of the walks below
+                        for (int c = columnStart; c < columnEnd; c += 16)
+                        {
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(v.bbcz + c)));
+                        }
                         const float cy_real   = (float)cy;
                         float       d2zxy     = d2zx;
                         if (0.0f + cy_real * v.g.cs[1] > by1)
