@@ -252,10 +252,23 @@ def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
 
     seq_ms = timed(b.sequential_md_step_device)
     bat_ms = timed(b.md_step_device)
+    # the list search of the whole ensemble (one per system, each reading its list sizes back to the
+    # host), wall clock; the timed steps above hold none, so it is amortized over nstlist steps below
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(3):
+        b.search_device(frames[k].data_ptr())
+    torch.cuda.synchronize()
+    search_ms = (time.perf_counter() - t0) * 1e3 / 3
     b.close()
     return {"workload": "256 SPC water boxes, 500..20000 atoms log-uniform (seed 3)", "atoms": n,
             "steps": steps, "batched_ms_per_step": bat_ms, "sequential_ms_per_step": seq_ms,
-            "speedup": seq_ms / bat_ms, "force_evals_per_s_batched": len(ens) / (bat_ms * 1e-3),
+            "speedup": seq_ms / bat_ms,
+            "search_ms": search_ms, "search_atoms_per_s": n / (search_ms * 1e-3),
+            "batched_ms_per_step_with_search": bat_ms + search_ms / NSTLIST,
+            "sequential_ms_per_step_with_search": seq_ms + search_ms / NSTLIST,
+            "speedup_with_search": (seq_ms + search_ms / NSTLIST) / (bat_ms + search_ms / NSTLIST),
+            "force_evals_per_s_batched": len(ens) / (bat_ms * 1e-3),
             "force_evals_per_s_sequential": len(ens) / (seq_ms * 1e-3),
             "autotuned": best,
             "search_space": {"tile_stage_depth": space["tiles"], "launch_shape": "0: 256x2, 1: 128x4, 2: 512x1, "
@@ -263,7 +276,8 @@ def measure_ensemble(dev: int, steps: int = 30, warmup: int = 3) -> dict:
                              "tile": "0: one atom pair per lane (8x4 atoms per warp instruction), 1: two pairs per "
                                      "lane (8x8, packed FP32x2)", "candidates": len(tune),
                              "best_ms_per_step": min(tune.values()), "worst_ms_per_step": max(tune.values())},
-            "note": "each step: F+E+virial of all systems; search every 100 steps, rolling prune as autotuned"}
+            "note": "each step: F+E+virial of all systems; search every 100 steps (none inside the timed steps; "
+                    "the _with_search figures add one search per 100 steps), rolling prune as autotuned"}
 
 
 def measure_adjoint(dev: int, steps: int = 20, warmup: int = 3) -> dict:
