@@ -335,8 +335,8 @@ cudaError_t alloc_search_records(nbx_handle* h, int per_cell)
     return e;
 }
 
-// Grid + count, size the list, write, prune: the synchronous search.
-int search_sync(nbx_handle* h, float* d_x, int write_back)
+// Grid + count (and the prefix sum of the counts) of a search, without host synchronisation.
+cudaError_t search_launch_count(nbx_handle* h, float* d_x, int write_back)
 {
     DeviceView& v = h->v;
     cudaError_t e = cudaMemsetAsync(&v.hdr->status, 0, sizeof(unsigned), h->stream);
@@ -349,20 +349,22 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
         if (e == cudaSuccess) e = launch_search_count(v, h->stream);
     }
     h->launches += 7;  // 5 grid kernels, count, scan
-    int rc = cuda_check(h, e, "grid/search count");
+    return e;
+}
+
+// With the count pass's list header on the host (h_hdr): its status, the record regrowth (counting
+// again, synchronously) and the list capacity; then the write pass, balancing and the fresh prune,
+// without host synchronisation.
+int search_launch_write(nbx_handle* h)
+{
+    DeviceView& v  = h->v;
+    unsigned    st = h->h_hdr->status & ~(unsigned)(kStatusListOverflow | kStatusRecordOverflow);
+    int         rc = status_to_error(h, st);
     if (rc != NBX_OK)
     {
         return rc;
     }
-    if ((rc = read_header(h)) != NBX_OK)
-    {
-        return rc;
-    }
-    unsigned st = h->h_hdr->status & ~(unsigned)(kStatusListOverflow | kStatusRecordOverflow);
-    if ((rc = status_to_error(h, st)) != NBX_OK)
-    {
-        return rc;
-    }
+    cudaError_t e = cudaSuccess;
     if (h->h_hdr->status & kStatusRecordOverflow)
     {
         // a cell found more j-clusters than its records hold: grow them and count again
@@ -399,21 +401,30 @@ int search_sync(nbx_handle* h, float* d_x, int write_back)
         e = launch_prune(v, 1, 0, 1, h->stream);
     }
     h->launches += 5 + (h->use_prune ? 1 : 0);  // emit, 4 balancing kernels, prune
-    if ((rc = cuda_check(h, e, "search write")) != NBX_OK)
-    {
-        return rc;
-    }
-    if ((rc = read_header(h)) != NBX_OK)
-    {
-        return rc;
-    }
-    if ((rc = status_to_error(h, h->h_hdr->status)) != NBX_OK)
+    return cuda_check(h, e, "search write");
+}
+
+// With the write pass's list header on the host: its status; the list is in place.
+int search_finish(nbx_handle* h)
+{
+    const int rc = status_to_error(h, h->h_hdr->status);
+    if (rc != NBX_OK)
     {
         return rc;
     }
     h->have_list  = true;
     h->prune_part = 0;
     return NBX_OK;
+}
+
+// Grid + count, size the list, write, prune: the synchronous search.
+int search_sync(nbx_handle* h, float* d_x, int write_back)
+{
+    int rc = cuda_check(h, search_launch_count(h, d_x, write_back), "grid/search count");
+    if (rc == NBX_OK) rc = read_header(h);
+    if (rc == NBX_OK) rc = search_launch_write(h);
+    if (rc == NBX_OK) rc = read_header(h);
+    return rc == NBX_OK ? search_finish(h) : rc;
 }
 
 // Accumulates the finished event pairs into their phases.
@@ -1781,6 +1792,7 @@ struct nbx_batch
     cudaGraphExec_t          graph      = nullptr;
     cudaStream_t             capture_stream = nullptr;  // private: capture is not allowed on legacy streams
     const void*              graph_key[4] = { nullptr, nullptr, nullptr, nullptr };
+    std::vector<cudaStream_t> search_streams;  // the systems' searches run concurrently on these
     // adjoint / force matching
     double*                  d_gnbfp_pad = nullptr;  // (nt+1)^2 * 2 FP64 type-pair sums
     int*                     d_adj_counter = nullptr;
@@ -1880,11 +1892,95 @@ int batch_refresh(nbx_batch* b)
     return NBX_OK;
 }
 
+constexpr int kSearchStreams = 8;
+
+// The systems' searches, spread over kSearchStreams streams so that the small grid, search, balance
+// and prune launches of different systems run concurrently, in two rounds: every system's grid +
+// count, one host synchronisation for all their list headers, every system's write + balancing +
+// fresh prune, one more synchronisation (a system whose records overflow counts again synchronously
+// in between).  The batch's stream is synchronised first (the coordinates come from it) and the
+// systems use it again afterwards.
 int batch_search(nbx_batch* b, const float* d_x)
 {
-    for (size_t i = 0; i < b->sys.size(); i++)
+    const size_t nsys = b->sys.size();
+    cudaError_t  e    = cudaStreamSynchronize(b->stream);
+    while (e == cudaSuccess && b->search_streams.size() < (size_t)kSearchStreams)
     {
-        int rc = search_sync(b->sys[i], const_cast<float*>(d_x) + 3 * (size_t)b->offsets[i], 0);
+        cudaStream_t s = nullptr;
+        e              = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+        {
+            b->search_streams.push_back(s);
+        }
+    }
+    if (e != cudaSuccess)
+    {
+        return batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (size_t i = 0; i < nsys; i++)
+    {
+        b->sys[i]->stream = b->search_streams[i % kSearchStreams];
+    }
+    auto sync_all = [&]() {
+        cudaError_t r = cudaSuccess;
+        for (cudaStream_t s : b->search_streams)
+        {
+            const cudaError_t q = cudaStreamSynchronize(s);
+            r                   = r == cudaSuccess ? q : r;
+        }
+        return r;
+    };
+    auto restore = [&]() {
+        sync_all();
+        for (nbx_handle* h : b->sys)
+        {
+            h->stream = b->stream;
+        }
+    };
+    auto fail = [&](size_t i, int rc) {
+        restore();
+        return batch_error(b, rc, "system " + std::to_string(i) + ": " + b->sys[i]->err);
+    };
+    auto headers = [&](size_t i) {
+        nbx_handle* h = b->sys[i];
+        return cuda_check(h, cudaMemcpyAsync(h->h_hdr, h->v.hdr, sizeof(ListHeader), cudaMemcpyDeviceToHost,
+                                             h->stream),
+                          "read list header");
+    };
+    for (size_t i = 0; i < nsys; i++)
+    {
+        nbx_handle* h  = b->sys[i];
+        int         rc = cuda_check(h, search_launch_count(h, const_cast<float*>(d_x) + 3 * (size_t)b->offsets[i], 0),
+                                    "grid/search count");
+        if (rc == NBX_OK) rc = headers(i);
+        if (rc != NBX_OK)
+        {
+            return fail(i, rc);
+        }
+    }
+    if ((e = sync_all()) != cudaSuccess)
+    {
+        restore();
+        return batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (size_t i = 0; i < nsys; i++)
+    {
+        int rc = search_launch_write(b->sys[i]);
+        if (rc == NBX_OK) rc = headers(i);
+        if (rc != NBX_OK)
+        {
+            return fail(i, rc);
+        }
+    }
+    e = sync_all();
+    restore();
+    if (e != cudaSuccess)
+    {
+        return batch_error(b, NBX_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (size_t i = 0; i < nsys; i++)
+    {
+        const int rc = search_finish(b->sys[i]);
         if (rc != NBX_OK)
         {
             return batch_error(b, rc, "system " + std::to_string(i) + ": " + b->sys[i]->err);
@@ -2240,6 +2336,11 @@ int nbx_batch_destroy(nbx_batch* b)
     if (b->stream)
     {
         cudaStreamSynchronize(b->stream);
+    }
+    for (cudaStream_t s : b->search_streams)
+    {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
     }
     drop_graph(b);
     if (b->fm_graph)
