@@ -56,6 +56,34 @@ def test_batch_matches_single_systems(graph, variant, tile, depth):
     b.close()
 
 
+def test_batched_search_grows_records():
+    """Long-list systems (water at rlist 2.0 nm, cells beyond their initial 512 search records)
+    through the batched search, whose systems search concurrently on several streams and grow
+    their records between the two rounds: forces and energies equal the single-system path."""
+    torch = pytest.importorskip("torch")
+    ens = [systems.spc_water(m, (m * 0.0299) ** (1 / 3), seed=11 + k) for k, m in enumerate((3000, 2500, 400))]
+    opts = nblib.NBKernelOptions(coulomb_type=nblib.CoulombType.Pme, pairlist_cutoff=2.0, rcoulomb=0.9,
+                                 nstlist=10, compute_virial_and_energy=True)
+    b = BatchForceCalculator(ens, opts)
+    dev = torch.device("cuda:0")
+    x = torch.from_numpy(np.concatenate([s.x.reshape(-1) for s in ens])).to(dev)
+    f = torch.empty_like(x)
+    e = torch.zeros(2 * len(ens), dtype=torch.float64, device=dev)
+    b.search_device(x.data_ptr())  # the batched search (creation searched each system on its own)
+    b.compute_device(x.data_ptr(), f.data_ptr(), e.data_ptr(), None)
+    torch.cuda.synchronize()
+    fb = f.cpu().numpy()
+    eb = e.cpu().numpy().reshape(-1, 2)
+    for i, s in enumerate(ens):
+        calc = nblib.ForceCalculator(s, opts)
+        fs = calc.compute(s.x)
+        o = b.offsets[i]
+        assert rel_rms(fb[3 * o:3 * (o + s.n)].reshape(-1, 3), fs) <= FORCE_RTOL, (i, s.n)
+        assert np.all(np.abs(eb[i] - calc.energies) <= ENERGY_RTOL * np.abs(calc.energies)), (i, eb[i])
+        calc.close()
+    b.close()
+
+
 def test_batched_schedule_matches_sequential():
     """The scheduled batch step (search, batched rolling prune, compute) equals the per-system steps."""
     torch = pytest.importorskip("torch")

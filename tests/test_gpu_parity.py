@@ -102,6 +102,27 @@ def test_balanced_list_entries_match_oracle_in_order(name):
     assert (np.diff(cls) <= 0).all()
 
 
+def _long_list_water(n_molecules=3000, seed=11):
+    # water at rlist 2.0 nm: its cells find up to ~780 j-clusters (9,000 atoms), more than the 512
+    # search records a cell starts with
+    return systems.spc_water(n_molecules, (n_molecules * 0.0299) ** (1 / 3), seed=seed)
+
+
+def test_search_records_grow_for_long_lists():
+    """A cell that finds more j-clusters than its search records hold makes the search grow them and
+    count again: the list and the forces still match the oracle."""
+    s = _long_list_water()
+    calc, o = _pair(s, rlist=2.0)
+    pg, po = calc.pairlist(), o.pairlist()
+    a = canonical_pairs(pg["sci"], pg["cj4"], pg["excl"])
+    b = canonical_pairs(po["sci"], po["cj4"], po["excl"])
+    assert len(a) == len(b) and np.array_equal(a, b)
+    f = calc.compute(s.x)
+    o.force(True)
+    assert rel_rms(f, o.forces()) <= FORCE_RTOL
+    calc.close()
+
+
 def test_balancing_leaves_forces_unchanged():
     s = systems.water_small()
     calc, _o = _pair(s)
