@@ -139,10 +139,12 @@ class _NonbondedFunction(torch.autograd.Function):
         nbfp32 = nbfp.to(torch.float32).contiguous()
         engine._upload(q, nbfp32)
         f = torch.empty_like(x)
-        e = torch.zeros(2, dtype=torch.float64, device=x.device)
+        e = torch.empty(2, dtype=torch.float64, device=x.device)  # written by the call, not added to
         calc.compute_device(x.data_ptr(), f.data_ptr(), e.data_ptr(), None)
         ctx.engine = engine
         ctx.save_for_backward(x, q, nbfp, nbfp32)
+        # an unused output's gradient arrives as None instead of a zero-filled tensor
+        ctx.set_materialize_grads(False)
         return f, e
 
     @staticmethod
