@@ -285,12 +285,17 @@ __device__ void bitonic_sort_smem(unsigned long long* keys, int P)
                     const unsigned long long y0      = __shfl_xor_sync(full, e0, j >> 1);
                     const unsigned long long y1      = __shfl_xor_sync(full, e1, j >> 1);
                     const bool               takeMin = ((p0 & j) == 0) == up;
-                    e0                               = takeMin ? min(e0, y0) : max(e0, y0);
-                    e1                               = takeMin ? min(e1, y1) : max(e1, y1);
+                    // keep the smaller key when takeMin, else the larger: take the partner's key
+                    // when the comparison says so (keys are distinct)
+                    e0 = ((e0 > y0) == takeMin) ? y0 : e0;
+                    e1 = ((e1 > y1) == takeMin) ? y1 : e1;
                 }
-                const unsigned long long lo = min(e0, e1), hi = max(e0, e1);
-                e0                          = up ? lo : hi;
-                e1                          = up ? hi : lo;
+                if ((e0 > e1) == up)
+                {
+                    const unsigned long long t = e0;
+                    e0                         = e1;
+                    e1                         = t;
+                }
             }
             keys[p0]     = e0;
             keys[p0 + 1] = e1;
